@@ -1,0 +1,436 @@
+"""Benchmark of the GB300 PIMC sweep engine (bead-updates per second).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload c4|c1|c2|c3|c5]
+                    [--impl ours|reference]
+
+A step is one sweep (every particle's staging windows, N permutation swaps,
+one centre-of-mass phase) of every chain of the workload; a bead-update is
+one proposed bead position (staging m-1, swap 2(m-1), centre of mass M per
+attempt).  Default workload: 4096 independent trapped-gas chains of uneven
+size (N in [8, 512], M in {16, 32, 64, 128}, beta in [0.5, 4], Gaussian pair
+g in [0, 2], sigma 0.5, trap omega 1; seeds per chain), run by the persistent
+batched kernel under a CUDA graph.  The JSON line adds the plain per-chain
+launch path on the same chains, the CPU oracle on the machine's host cores, the
+end-to-end rate through host buffers, the roofline of the sweep kernel and
+the SM clocks seen during the timed region.
+
+--impl reference times the CPU restatement of the reference's own sweep
+(reference semantics, run!-style random move selection, one chain per host
+thread) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "pimc.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = ("bead-updates/sec/GB300: batched+adjoint vs plain GPU vs CPU, at E within 2σ "
+          "of reference")
+UNIT = "bead-updates/s"
+SEED = 20261203
+
+
+# --------------------------------------------------------------------- workloads
+def c4_chain_list(n=4096):
+    """4096 trapped-gas chains drawn from numpy default_rng(4096)"""
+    rng = np.random.default_rng(4096)
+    N = rng.integers(8, 513, size=n)
+    M = rng.choice([16, 32, 64, 128], size=n)
+    beta = rng.uniform(0.5, 4.0, size=n)
+    g = rng.uniform(0.0, 2.0, size=n)
+    return [dict(N=int(N[i]), M=int(M[i]), beta=float(beta[i]), g=float(g[i])) for i in range(n)]
+
+
+def workload(name, semantics):
+    """(chain params list, mix list, description) of a named workload"""
+    from pimc.engine import ChainParams, Mix
+    chains, mixes = [], []
+
+    def mix_for(N, M, ell, L, measure_every):
+        return Mix(stage_slices=ell, stage_min=2, stage_max=ell, stage_minacc=0.0, stage_maxacc=1.0,
+                   swaps_per_sweep=N if N > 1 else 0, swap_slices=ell, swap_min=2, swap_max=ell,
+                   swap_minacc=0.0, swap_maxacc=1.0, com_phases=1, com_step=1.0, com_minstep=0.1,
+                   com_maxstep=L / 2, adapt=1, measure_every=measure_every)
+
+    if name == "c4":
+        for i, c in enumerate(c4_chain_list()):
+            ell = min(16, c["M"] // 2)
+            chains.append(ChainParams(dim=2, N=c["N"], M=c["M"], L=8.0, T=1.0 / c["beta"], lam=0.5,
+                                      harmonic_omega=1.0, interactions=True, pair_g=c["g"],
+                                      pair_sigma=0.5, r_a=1.5, semantics=semantics, seed=SEED + i,
+                                      energy_capacity=0))
+            mixes.append(mix_for(c["N"], c["M"], ell, 8.0, 10))
+        desc = ("C4 batched: 4096 trapped-gas chains, N~U{8..512}, M~U{16,32,64,128}, "
+                "beta~U[0.5,4], Gaussian pair g~U[0,2] sigma=0.5 (cutoff 3 sigma, cell 1.6), "
+                "omega=1, L=8, staging l=min(16,M/2), N swaps + 1 CoM phase per sweep")
+    elif name == "c1":
+        chains.append(ChainParams(dim=2, N=10, M=20, L=5.0, T=1.0, lam=0.5, harmonic_omega=1.0,
+                                  semantics=semantics, seed=SEED, density_nbins=64,
+                                  energy_capacity=0))
+        mixes.append(mix_for(10, 20, 8, 5.0, 1))
+        desc = "C1 plain: 2D trapped ideal bosons N=10, beta=1, M=20, l=8, 64x64 density"
+    elif name == "c2":
+        chains.append(ChainParams(dim=2, N=64, M=32, L=10.0, T=0.5, lam=0.5, semantics=semantics,
+                                  seed=SEED, energy_capacity=0))
+        mixes.append(mix_for(64, 32, 16, 10.0, 1))
+        desc = "C2 plain: 2D free bosons N=64, beta=2, M=32, periodic [-10,10)^2, l=16"
+    elif name == "c3":
+        chains.append(ChainParams(dim=2, N=256, M=64, L=8.0, T=0.5, lam=0.5, harmonic_omega=1.0,
+                                  interactions=True, pair_g=1.0, pair_sigma=0.5, r_a=1.5,
+                                  semantics=semantics, seed=SEED, density_nbins=128,
+                                  energy_capacity=0))
+        mixes.append(mix_for(256, 64, 16, 8.0, 1))
+        desc = "C3 plain: 2D trapped bosons, Gaussian pair g=1 sigma=0.5, N=256, beta=2, M=64"
+    elif name == "c5":
+        chains.append(ChainParams(dim=2, N=1024, M=64, L=16.0, T=0.25, lam=0.5, harmonic_omega=0.1,
+                                  lattice_V0=4.0, lattice_a=1.0, interactions=True, pair_g=1.0,
+                                  pair_sigma=0.3, r_a=0.9, semantics=semantics, seed=SEED,
+                                  energy_capacity=0))
+        mixes.append(mix_for(1024, 64, 16, 16.0, 1))
+        desc = ("C5 plain + adjoint: lattice V0=4 a=1 + trap omega=0.1 + Gaussian pair g=1 "
+                "sigma=0.3, N=1024, beta=4, M=64")
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return chains, mixes, desc
+
+
+# --------------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi samples of the SM clock and throttle reasons while running"""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return ws, rank, local, pg
+
+
+def reduce_max_sum(pg, tmax, tsum):
+    """max of elapsed time and sum of work over ranks (host scalars)"""
+    if pg is None:
+        return tmax, tsum
+    import torch
+    dev = "cuda" if torch.cuda.is_available() and pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([tmax], dtype=torch.float64, device=dev)
+    s = torch.tensor([tsum], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    pg.all_reduce(s, op=pg.ReduceOp.SUM)
+    return float(t.item()), float(s.item())
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def pinned_empty(n):
+    """page-locked host buffer (torch only allocates it; numpy views it)"""
+    try:
+        import torch
+        t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        return t.numpy(), t
+    except Exception:
+        return np.empty(n), None
+
+
+# --------------------------------------------------------------------- CPU legs
+def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, threads=None):
+    """the CPU oracle (C restatement of the reference's sweep) on a bounded
+    sample of the workload's chains, one chain per host thread"""
+    import concurrent.futures as cf
+    from oracle import oracle as O
+    O.build()
+    threads = threads or os.cpu_count() or 1
+    n = len(chains)
+    take = max_chains or min(n, 4 * threads)
+    idx = np.linspace(0, n - 1, take).astype(int) if n > take else np.arange(n)
+
+    def one(i, attempts):
+        c, m = chains[i], mixes[i]
+        p = O.make_params(dim=c.dim, N=c.N, M=c.M, L=c.L, T=c.T, lam=c.lam,
+                          hcoef=0.5 * c.harmonic_omega ** 2, V0=c.lattice_V0, lat_a=c.lattice_a,
+                          pair_g=c.pair_g, pair_sigma=c.pair_sigma, interactions=c.interactions,
+                          r_a=c.r_a, semantics=semantics)
+        return O.bench_chains(p, 1, 1, attempts, m.stage_slices, 1.0, SEED + int(i))
+
+    # calibrate: one sweep's worth of attempts (N(k+2)) on each sampled chain
+    def sweep_attempts(i):
+        c, m = chains[i], mixes[i]
+        k = -(-c.M // m.stage_slices)
+        return c.N * (k + 2)
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        res = list(ex.map(lambda i: one(i, sweep_attempts(i)), idx))
+    t1 = time.perf_counter()
+    beads = sum(r[1] for r in res)
+    wall = t1 - t0
+    # scale the number of sweeps to fill about budget_s of wall time
+    reps = max(1, int(budget_s / max(wall, 1e-3)))
+    if reps > 1:
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            res = list(ex.map(lambda i: one(i, reps * sweep_attempts(i)), idx))
+        wall = time.perf_counter() - t0
+        beads = sum(r[1] for r in res)
+    sample = (f"{len(idx)} of {n} chains (evenly spaced), {reps} sweep(s) of run! attempts each "
+              f"(N(k+2) per sweep), {threads} host threads, {wall:.1f} s wall")
+    return beads / wall, threads, sample
+
+
+# --------------------------------------------------------------------- arms
+def run_reference(args):
+    ws, rank, local, pg = dist_setup()
+    if rank != 0:
+        return 0
+    chains, mixes, desc = workload(args.workload, 0)
+    rates = []
+    cores = os.cpu_count() or 1
+    sample = ""
+    for _ in range(args.warmup):
+        cpu_oracle_rate(chains, mixes, 0, budget_s=2.0)
+    for _ in range(args.steps):
+        r, cores, sample = cpu_oracle_rate(chains, mixes, 0, budget_s=args.ref_budget)
+        rates.append(r)
+    v = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "semantics": "reference (bug-compatible)"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "C restatement of PIMC.jl's sweep, not Julia (no Julia "
+                                   "toolchain on the box); " + sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import pimc
+    from pimc.engine import Engine
+    ws, rank, local, pg = dist_setup()
+    pimc.load()
+    sem = 1 if args.semantics == "physical" else 0
+    chains, mixes, desc = workload(args.workload, sem)
+    if ws > 1:  # weak scaling: every rank runs the full workload with its own seeds
+        for c in chains:
+            c.seed = c.seed + 1000003 * rank
+    eng = Engine(chains)
+    for i, m in enumerate(mixes):
+        eng.set_mix(m, chain=i)
+    batched = len(chains) > 1
+    run = eng.run_batched if batched else eng.run
+    if batched and args.tune:
+        eng.tune(sweeps_per_trial=1)
+    for _ in range(args.warmup):
+        run(1)
+    s0 = eng.total_stats()
+    barrier(pg)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        run(args.steps)
+        wall = time.perf_counter() - t0
+    ms = eng.last_run_ms()
+    launches = eng.last_run_launches()
+    s1 = eng.total_stats()
+    beads = s1.bead_updates - s0.bead_updates
+    tmax, beads_all = reduce_max_sum(pg, ms / 1e3, beads)
+    value = beads_all / tmax
+    ms_step = tmax * 1e3 / args.steps
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "gpu_launches": int(launches)}
+    state_bytes = sum(8 * (c.dim + 1) * c.N * c.M for c in chains)
+    cfg = {"workload": desc, "chains": len(chains), "semantics": args.semantics,
+           "parallelism": f"dp{ws} (independent chains per GPU)",
+           "l2": (f"chain state {state_bytes / 1e9:.2f} GB > 129 MB L2"
+                  if state_bytes > 129e6 else f"chain state {state_bytes / 1e6:.1f} MB (L2/shared resident)"),
+           "bead_updates_per_step": beads / args.steps}
+    if batched:
+        st = eng.total_stats()
+        cfg["launch"] = {"block": None, "sweeps_per_launch": None}
+    out["config"] = cfg
+    # roofline of the sweep kernel: algorithmic bytes per bead-update (48 B
+    # pair-free, 64 B with the pair interaction) over its measured duration
+    bpb = np.array([64.0 if c.interactions else 48.0 for c in chains])
+    w = np.array([c.N * c.M for c in chains], dtype=float)
+    bytes_per_bead = float((bpb * w).sum() / w.sum())
+    launch_s = (ms / 1e3) / max(launches, 1)
+    beads_per_launch = beads / max(launches, 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = beads_per_launch * bytes_per_bead / launch_s / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                       "frac": achieved / hbm, "traffic": args.traffic,
+                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                       "bytes_per_bead_update": bytes_per_bead,
+                       "note": "the sweep is FP64-pipe and latency bound (chain state is "
+                               "shared-memory/L2 resident within a sweep); see fp64 below"}
+    fp64_peak = args.fp64_peak
+    flops = beads_per_launch * args.fp64_flops_per_bead / launch_s / 1e12
+    out["roofline_fp64"] = {"bound": "fp64", "achieved": flops, "peak": fp64_peak,
+                            "unit": "TFLOP/s", "frac": flops / fp64_peak if fp64_peak else None,
+                            "flops_per_bead_update": args.fp64_flops_per_bead,
+                            "peak_source": "own DFMA probe (profiles/fp64_peak.md)"}
+    out["clocks"] = clk.summary()
+    # plain path: the same chains, one launch per chain per sweep
+    if batched and not args.no_plain:
+        p0 = eng.total_stats()
+        eng.run_plain(1)
+        pms = eng.last_run_ms()
+        p1 = eng.total_stats()
+        out["plain"] = {"value": (p1.bead_updates - p0.bead_updates) / (pms / 1e3),
+                        "unit": UNIT, "launches": eng.last_run_launches(),
+                        "ms_per_step": pms,
+                        "path": "one launch per chain per sweep (no queue, no graph)"}
+    # end to end through the C ABI with host buffers: upload the state, sweep,
+    # read back the state and the energy sums
+    if not args.no_e2e:
+        xh, keep = pinned_empty(eng.beads_all_size())
+        eng.get_beads_all(xh)
+        e0 = eng.total_stats()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.set_beads_all(xh)
+            run(1)
+            eng.get_beads_all(xh)
+            eng.energy_sums_all()
+        et = time.perf_counter() - t0
+        e1 = eng.total_stats()
+        emax, ebeads = reduce_max_sum(pg, et, e1.bead_updates - e0.bead_updates)
+        nb = 8 * eng.beads_all_size()
+        out["e2e"] = {"value": ebeads / emax, "unit": UNIT, "h2d_bytes_per_step": nb,
+                      "d2h_bytes_per_step": nb + 8 * 9 * len(chains),
+                      "path": "pimc_batch_set_beads_all (pinned host) -> pimc_run -> "
+                              "pimc_batch_get_beads_all + pimc_batch_energy_sums_all"}
+    if args.workload == "c5" or args.adjoint:
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            eng.adjoint(0, want_beads=True)
+        at = (time.perf_counter() - t0) / reps
+        c = chains[0]
+        out["adjoint"] = {"beads": c.N * c.M, "ms_per_call": at * 1e3,
+                          "bead_gradients_per_s": c.N * c.M / at}
+    if rank == 0 and not args.no_cpu:
+        r, cores, sample = cpu_oracle_rate(chains, mixes, sem, budget_s=args.cpu_budget)
+        out["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": "C restatement of PIMC.jl's sweep (same semantics), "
+                                         + sample}
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--semantics", default="physical", choices=["physical", "reference"])
+    ap.add_argument("--tune", type=int, default=1)
+    ap.add_argument("--adjoint", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--ref-budget", type=float, default=8.0)
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per sweep-kernel launch from an ncu capture")
+    ap.add_argument("--fp64-peak", type=float, default=None, help="TFLOP/s")
+    ap.add_argument("--fp64-flops-per-bead", type=float, default=25.0)
+    args = ap.parse_args()
+    if args.steps < 1 or args.warmup < 0:
+        raise SystemExit("steps >= 1 and warmup >= 0")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

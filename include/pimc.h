@@ -1,0 +1,232 @@
+/*
+ * pimc.h -- C ABI of the GB300 engine for the PIMC.jl Monte Carlo sweep.
+ *
+ * The reference package (oameye/PIMC.jl) has no FFI; its boundary is the
+ * Julia API: System(...), the update callables, run!, and the Density/Energy
+ * measurements.  Each entry point below names the reference interface it
+ * stands in for (file:line within the reference project).  A host wrapper
+ * (Julia via ccall, Python via ctypes) reproduces that API on top of it.
+ *
+ * Conventions
+ *   - Every call returns 0 on success or a negative PIMC_E* code; the text of
+ *     the last error on the calling host thread is pimc_last_error().
+ *   - Positions are caller-owned host buffers in structure-of-arrays order
+ *     x[d][n][j] (d < dim, n < N particles, j < M slices, slice 0-based);
+ *     they are copied in and out.  Device memory belongs to the handle.
+ *   - A handle holds one or more independent chains (a batch).  The
+ *     single-chain calls act on chain 0; the pimc_batch_* calls take a chain
+ *     index.  A handle is not re-entrant; distinct handles may be used from
+ *     distinct host threads.  Each handle owns one CUDA stream.
+ */
+#ifndef PIMC_H
+#define PIMC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PIMC_ABI_VERSION 1
+
+enum {
+  PIMC_OK = 0,
+  PIMC_EARG = -1,     /* invalid argument */
+  PIMC_ECUDA = -2,    /* CUDA runtime error */
+  PIMC_ESTATE = -3,   /* invalid state (e.g. next is not a permutation) */
+  PIMC_EDEVICE = -4,  /* device-side error flag (capacity, retry cap, ...) */
+  PIMC_EDRAWS = -5,   /* injected draw arrays ran out */
+  PIMC_ENOMEM = -6
+};
+
+/* acceptance semantics */
+enum {
+  PIMC_SEM_REFERENCE = 0, /* bug-compatible with the reference's updates */
+  PIMC_SEM_PHYSICAL = 1   /* same action, applied consistently (detailed balance) */
+};
+
+/* outcome of one attempted move */
+enum { PIMC_REJECT = 0, PIMC_ACCEPT = 1, PIMC_SKIP = 2, PIMC_HARDCORE = 3 };
+
+/* System(potential; dV, dim, M, N, mu, L, T, lambda, interactions, propint,
+ *        g, r_a, length_measurement_cycle, measure_scheme)
+ * (src/system.jl:129-167).  Closures cannot cross the ABI, so the potential
+ * and the pair propagator are engine-known forms:
+ *   V(r)  = 1/2 omega^2 |r|^2 + V0 sum_d sin^2(pi r_d / a)
+ *   lnU   = -tau/2 (v(|r1|) + v(|r2|)),  v(r) = g exp(-r^2 / (2 sigma^2))
+ * The hard-core radius is the reference's a = exp(-2 pi / g_contact) when
+ * interacting (src/system.jl:151), passed explicitly here. */
+typedef struct pimc_params {
+  int dim;               /* 1 or 2 */
+  int N;                 /* particles */
+  int M;                 /* imaginary-time slices */
+  double L;              /* half-width: box [-L, L)^dim */
+  double T;              /* temperature, beta = 1/T, tau = beta/M */
+  double lambda;         /* hbar^2 / 2m */
+  double mu;             /* chemical potential (used by lnU when propint < 0) */
+  double harmonic_omega; /* 0 = no trap */
+  double lattice_V0;     /* 0 = no lattice */
+  double lattice_a;
+  int interactions;      /* pair propagator on */
+  double pair_g, pair_sigma;
+  double r_a;            /* neighbour range; 0 -> L/4 (src/system.jl:18-24) */
+  double hardcore_a;     /* 0 = off */
+  int semantics;         /* PIMC_SEM_* */
+  uint64_t seed;         /* Philox key */
+  int density_nbins;     /* Density(s; nbins); 0 = no histogram */
+  int energy_capacity;   /* Energy(s, n): stored measurements per chain */
+  int retry_cap;         /* hard-core retries (s.ctr); 0 -> 10000 */
+} pimc_params;
+
+/* The update list of run!(s, n, updates) (src/simulation.jl:29-42) mapped
+ * onto a sweep.  One sweep = staging_phases staging phases (every particle's
+ * imaginary-time circle cut into windows of up to stage_slices slices,
+ * ReshapeLinear, src/updates/reshape.jl:31-91), swaps_per_sweep swap attempts
+ * (ReshapeSwapLinear, reshape.jl:123-283), com_phases single-path
+ * centre-of-mass phases (SingleCenterOfMass, src/updates/com.jl:136-224) and
+ * polymer_com_phases cycle centre-of-mass phases (PolymerCenterOfMass,
+ * com.jl:31-104).  Adaptation follows adjust! (src/updates/helper.jl:22-52)
+ * once per sweep when adapt != 0. */
+typedef struct pimc_move_mix {
+  int staging_phases;
+  int stage_slices, stage_min, stage_max;
+  double stage_minacc, stage_maxacc;
+  int swaps_per_sweep;
+  int swap_slices, swap_min, swap_max;
+  double swap_minacc, swap_maxacc;
+  int com_phases;
+  double com_step, com_minstep, com_maxstep, com_minacc, com_maxacc;
+  int polymer_com_phases;
+  double pcom_step, pcom_minstep, pcom_maxstep, pcom_minacc, pcom_maxacc;
+  int adapt;
+  int measure_every;     /* sweeps between measurements (measurement_Z_sector,
+                            src/measurement.jl:1-17); 0 = none */
+} pimc_move_mix;
+
+typedef struct pimc_stats {
+  unsigned long long attempts[4];  /* staging, swap, com, polymer com */
+  unsigned long long accepts[4];
+  unsigned long long skips;        /* swap with n1 == n2 */
+  double bead_updates;             /* proposed bead positions */
+  unsigned long long sweeps;
+  unsigned long long measurements;
+  int stage_slices, swap_slices;   /* current adaptive var.m */
+  double com_step, pcom_step;      /* current adaptive step */
+} pimc_stats;
+
+/* ---------------- lifecycle: System constructor (src/system.jl:129-167) */
+int pimc_create(const pimc_params *p, void **handle);
+/* one handle with nchains independent chains (params[c], mix[c]) */
+int pimc_batch_create(const pimc_params *params, int nchains, void **handle);
+int pimc_destroy(void *handle);
+int pimc_num_chains(void *handle, int *nchains);
+
+/* ---------------- state I/O: s.world[n].r / .next (src/system.jl:1-6) */
+/* set positions; recomputes the cached link actions (Particle.V) and grids */
+int pimc_set_beads(void *handle, const double *x);
+int pimc_get_beads(void *handle, double *x);
+int pimc_set_next(void *handle, const int *next);
+int pimc_get_next(void *handle, int *next);
+/* positions, cached link actions V[n][j] and next verbatim */
+int pimc_set_raw(void *handle, const double *x, const double *V, const int *next);
+int pimc_get_links(void *handle, double *V);
+/* init_world (src/system.jl:36-78) on the device: uniform start + Levy loop */
+int pimc_init_world(void *handle);
+int pimc_batch_set_beads(void *handle, int chain, const double *x);
+int pimc_batch_get_beads(void *handle, int chain, double *x);
+int pimc_batch_get_next(void *handle, int chain, int *next);
+/* every chain at once: x_all is the concatenation of each chain's
+ * x[d][n][j] in chain order (one host<->device copy per call) */
+int pimc_batch_set_beads_all(void *handle, const double *x_all);
+int pimc_batch_get_beads_all(void *handle, double *x_all);
+/* running energy sums of every chain: sum[c][4], sumsq[c][4], count[c] */
+int pimc_batch_energy_sums_all(void *handle, double *sum, double *sumsq,
+                               unsigned long long *count);
+
+/* ---------------- sweep: run!(s, n, updates) (src/simulation.jl:29-42) */
+int pimc_set_move_mix(void *handle, int chain, const pimc_move_mix *mix); /* chain<0: all */
+int pimc_run(void *handle, long long n_sweeps);
+/* all chains, one persistent launch per sweep block from a device work
+ * queue, captured in a CUDA graph */
+int pimc_batch_run(void *handle, long long n_sweeps);
+/* the same sweeps issued as one plain launch per chain (no queue, no graph) */
+int pimc_batch_run_plain(void *handle, long long n_sweeps);
+/* time candidate launch shapes on the handle's own chains and keep the best */
+int pimc_batch_tune(void *handle, int sweeps_per_trial, int *block_out, int *spl_out);
+int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch);
+
+/* ---------------- single moves with injected draws (parity level b) */
+/* (u::ReshapeLinear)(s) with n, j0, m given (reshape.jl:31-91).  normals are
+ * consumed d per interior bead in order; uniforms[0] is the Metropolis
+ * uniform, read only when delta < 1.  proposal (optional) receives the
+ * teleported window (m+1)*dim, bead-major. */
+int pimc_attempt_staging(void *handle, int n, int j0, int m, const double *normals,
+                         int n_normals, const double *uniforms, int n_uniforms, int *result,
+                         double *proposal);
+/* (u::ReshapeSwapLinear)(s) with j0, m, n1 and the partner-selection uniform
+ * given (reshape.jl:123-283, helper.jl:224-267) */
+int pimc_attempt_swap(void *handle, int j0, int m, int n1, double u_pick, const double *normals,
+                      int n_normals, const double *uniforms, int n_uniforms, int *result,
+                      int *n2, double *proposal);
+/* (u::SingleCenterOfMass)(s) on particle n (com.jl:136-224); uniforms: dim
+ * shift uniforms then the Metropolis uniform */
+int pimc_attempt_com(void *handle, int n, double step, const double *uniforms, int n_uniforms,
+                     int *result);
+/* PolymerCenterOfMass on the cycle containing n (com.jl:31-104, working) */
+int pimc_attempt_polymer_com(void *handle, int n, double step, const double *uniforms,
+                             int n_uniforms, int *result);
+
+/* ---------------- action evaluation (parity level a) */
+/* out[0] = sum lnK, out[1] = sum lnV (recomputed), out[2] = pair sum lnU
+ * (each unordered pair once), out[3] = sum of cached V
+ * (src/propagator.jl:16-28, src/system.jl:26-28) */
+int pimc_eval_action(void *handle, double out[4]);
+/* w_initial / w_updated of a staging move for a given proposed window
+ * rp[(m+1)*dim] (reshape.jl:66-77) */
+int pimc_eval_staging_weights(void *handle, int n, int j0, int m, const double *rp,
+                              double *w_init, double *w_upd);
+
+/* ---------------- estimators (src/measurement.jl) */
+int pimc_measure(void *handle);  /* one measurement of every chain now */
+/* Energy (measurement.jl:92-122): rows of 4: E_th, E_v (reference
+ * formulas), pair energy term, pair virial term */
+int pimc_get_energies(void *handle, int chain, double *out, int cap, int *count);
+/* running sums per chain: sum[4], sumsq[4], count */
+int pimc_get_energy_sums(void *handle, int chain, double *sum, double *sumsq,
+                         unsigned long long *count);
+/* Density (measurement.jl:45-55): nb^dim counts (column-major) and ndata */
+int pimc_get_density(void *handle, int chain, double *hist, unsigned long long *ndata);
+int pimc_reset_measurements(void *handle);
+
+/* ---------------- adjoint: per-bead dS_pot/dr and dS/d(V0, omega, g) */
+/* dSdr [dim][N][M] (optional), dSdtheta[3] = d/dV0, d/domega, d/dg,
+ * extra[4] = S_ext, S_pair, virial energy (external + pair), sum r.dS/dr */
+int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double *extra);
+/* change (V0, omega, g) in place; cached links are recomputed */
+int pimc_set_potential(void *handle, int chain, double V0, double omega, double g);
+
+/* ---------------- diagnostics, checkpoint */
+int pimc_get_stats(void *handle, int chain, pimc_stats *out);
+/* aggregate over chains */
+int pimc_get_total_stats(void *handle, pimc_stats *out);
+/* opaque, versioned snapshot of every chain: beads, links, next, counters,
+ * adaptive variables, generator position; restoring it reproduces the
+ * following sweeps bit for bit */
+int pimc_state_size(void *handle, size_t *bytes);
+int pimc_get_state(void *handle, void *buf, size_t bytes);
+int pimc_set_state(void *handle, const void *buf, size_t bytes);
+/* device time of the last run call (CUDA events on the handle's stream) */
+int pimc_last_run_ms(void *handle, double *ms);
+/* kernel launches issued by the last run call */
+int pimc_last_run_launches(void *handle, long long *launches);
+/* engine options: PIMC_OPT_FORCE_WARP_WINDOW routes pair-free staging
+ * attempts through the warp-cooperative window as well (parity coverage) */
+enum { PIMC_OPT_FORCE_WARP_WINDOW = 1 };
+int pimc_set_option(void *handle, int key, long long value);
+const char *pimc_last_error(void);
+int pimc_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1232 @@
+// pimc_api.cu -- extern "C" boundary of the engine (include/pimc.h).
+//
+// Host side of the System / run! / Density / Energy API: parameter checks,
+// device pools, state I/O, the plain and batched sweep drivers (work queue,
+// LPT chain order, CUDA graph of a sweep block, launch-shape tuner),
+// injected-draw attempts, estimators, adjoint and checkpoints.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pimc.h"
+#include "pimc_launch.h"
+#include "pimc_types.h"
+
+using namespace pimc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(PIMC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+constexpr int kWarpScratchMin = 5 * (64 + 1);  // doubles, window_warp
+constexpr unsigned kStateMagic = 0x50494D43u;   // "PIMC"
+
+struct Handle {
+  int nchains = 0;
+  std::vector<pimc_params> params;
+  std::vector<ChainDesc> desc;
+  std::vector<MixDev> mix;
+  std::vector<pimc_move_mix> umix;
+  ChainDesc *d_desc = nullptr;
+  ChainVar *d_var = nullptr;
+  MixDev *d_mix = nullptr;
+  double *d_dpool = nullptr;
+  size_t n_dpool = 0;
+  int *d_ipool = nullptr;
+  size_t n_ipool = 0;
+  unsigned long long *d_upool = nullptr;
+  size_t n_upool = 0;
+  int *d_queue = nullptr;
+  int *d_order = nullptr;
+  int *d_iout = nullptr;
+  double *d_buf = nullptr;
+  size_t n_buf = 0;
+  double *d_adj = nullptr;
+  size_t n_adj = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long last_launches = 0;
+  int maxN = 0, maxM = 0, maxNM = 0;
+  int block = 256;
+  int spl = 1;                 // sweeps per launch (batched)
+  int state_bytes = 0;         // shared bytes for staged chain state
+  int warp_scratch_d = 0;
+  size_t scratch_bytes = 0;
+  size_t dyn_smem = 0;
+  int num_sms = 0;
+  cudaGraphExec_t gexec = nullptr;
+  int g_spl = -1, g_block = -1;
+  int force_warp = 0;
+};
+
+int check_params(const pimc_params &p) {
+  if (p.dim < 1 || p.dim > 2) return fail(PIMC_EARG, "dim must be 1 or 2");
+  if (p.N < 1 || p.N > 8192) return fail(PIMC_EARG, "N must be in [1, 8192]");
+  if (p.M < 4 || p.M > 4096) return fail(PIMC_EARG, "M must be in [4, 4096]");
+  if (!(p.L > 0.0)) return fail(PIMC_EARG, "L must be positive");
+  if (!(p.T > 0.0)) return fail(PIMC_EARG, "T must be positive");
+  if (!(p.lambda > 0.0)) return fail(PIMC_EARG, "lambda must be positive");
+  if (p.lattice_V0 != 0.0 && !(p.lattice_a > 0.0)) return fail(PIMC_EARG, "lattice_a must be positive");
+  if (p.interactions && !(p.pair_sigma > 0.0)) return fail(PIMC_EARG, "pair_sigma must be positive");
+  if (p.interactions && !(p.r_a > 0.0))
+    return fail(PIMC_EARG, "interactions need r_a > 0 (the neighbour range is not searched for)");
+  if (p.semantics != PIMC_SEM_REFERENCE && p.semantics != PIMC_SEM_PHYSICAL)
+    return fail(PIMC_EARG, "semantics must be PIMC_SEM_REFERENCE or PIMC_SEM_PHYSICAL");
+  if (p.density_nbins < 0 || p.energy_capacity < 0) return fail(PIMC_EARG, "negative capacity");
+  if (p.hardcore_a < 0.0) return fail(PIMC_EARG, "hardcore_a must be >= 0");
+  return PIMC_OK;
+}
+
+// System constructor's derived constants (src/system.jl:129-167)
+ChainDesc make_desc(const pimc_params &p, int chain) {
+  ChainDesc d;
+  memset(&d, 0, sizeof(d));
+  d.N = p.N;
+  d.M = p.M;
+  d.dim = p.dim;
+  d.ld = p.M;
+  d.L = p.L;
+  d.beta = 1.0 / p.T;
+  d.tau = d.beta / p.M;
+  d.lambda = p.lambda;
+  d.mu = p.mu;
+  d.hcoef = 0.5 * p.harmonic_omega * p.harmonic_omega;
+  d.V0 = p.lattice_V0;
+  d.lat_k = p.lattice_V0 != 0.0 ? 1.0 / p.lattice_a : 0.0;
+  d.g = p.pair_g;
+  d.inv2s2 = p.interactions ? 1.0 / (2.0 * p.pair_sigma * p.pair_sigma) : 0.0;
+  const double ra = p.r_a > 0.0 ? p.r_a : p.L / 4.0;
+  d.nbins = (int)std::floor((2.0 * p.L) / ra);
+  if (d.nbins < 1) d.nbins = 1;
+  d.rc = 2.0 * p.L / d.nbins;
+  d.ncell = p.dim == 2 ? d.nbins * d.nbins : d.nbins;
+  d.hard_a = p.hardcore_a;
+  d.ctr = p.retry_cap > 0 ? p.retry_cap : 10000;
+  d.flags = 0;
+  if (p.interactions) d.flags |= PF_PAIR;
+  if (p.semantics == PIMC_SEM_PHYSICAL) d.flags |= PF_PHYS;
+  if (p.hardcore_a > 0.0) d.flags |= PF_HARD;
+  if (p.lattice_V0 != 0.0) d.flags |= PF_LATT;
+  if (p.harmonic_omega != 0.0) d.flags |= PF_HARM;
+  d.dens_nb = p.density_nbins;
+  d.dens_bw = p.density_nbins > 0 ? (2.0 * p.L) / p.density_nbins : 0.0;
+  d.eser_cap = p.energy_capacity;
+  d.wtab = std::min(p.M - 1, 32) + 1;
+  d.key0 = (unsigned)(p.seed & 0xffffffffu);
+  d.key1 = (unsigned)(p.seed >> 32);
+  d.chain_tag = (unsigned)chain;
+  const int ldm = (p.M & 1) ? p.M : p.M + 1;
+  d.smem_bytes = (int)(8 * (size_t)(p.dim + 1) * p.N * ldm + 4 * (size_t)p.N);
+  return d;
+}
+
+pimc_move_mix default_mix(const pimc_params &p) {
+  pimc_move_mix m;
+  memset(&m, 0, sizeof(m));
+  m.staging_phases = 1;
+  m.stage_slices = std::min(16, p.M - 2);
+  m.stage_min = 2;
+  m.stage_max = p.M - 2;
+  m.stage_minacc = 0.6;
+  m.stage_maxacc = 0.8;
+  m.swaps_per_sweep = p.N > 1 ? p.N : 0;
+  m.swap_slices = std::min(16, p.M - 2);
+  m.swap_min = 2;
+  m.swap_max = p.M - 2;
+  m.swap_minacc = 0.6;
+  m.swap_maxacc = 0.8;
+  m.com_phases = 1;
+  m.com_step = 1.0;
+  m.com_minstep = 1e-1;
+  m.com_maxstep = p.L / 2;
+  m.com_minacc = 0.4;
+  m.com_maxacc = 0.6;
+  m.polymer_com_phases = 0;
+  m.pcom_step = 1.0;
+  m.pcom_minstep = 1e-1;
+  m.pcom_maxstep = p.L / 2;
+  m.pcom_minacc = 0.4;
+  m.pcom_maxacc = 0.6;
+  m.adapt = 1;
+  m.measure_every = 0;
+  return m;
+}
+
+int check_mix(const pimc_move_mix &m, const pimc_params &p) {
+  if (m.staging_phases < 0 || m.swaps_per_sweep < 0 || m.com_phases < 0 || m.polymer_com_phases < 0)
+    return fail(PIMC_EARG, "negative move counts");
+  if (m.stage_slices < 2 || m.stage_min < 2 || m.stage_max < m.stage_min || m.stage_max > p.M - 1)
+    return fail(PIMC_EARG, "staging slices must satisfy 2 <= min <= max <= M-1");
+  if (m.swap_slices < 2 || m.swap_min < 2 || m.swap_max < m.swap_min || m.swap_max > p.M - 1)
+    return fail(PIMC_EARG, "swap slices must satisfy 2 <= min <= max <= M-1");
+  if (m.stage_max > 64 || m.swap_max > 64)
+    return fail(PIMC_EARG, "windows longer than 64 slices are not supported on the device");
+  if (m.measure_every < 0) return fail(PIMC_EARG, "measure_every must be >= 0");
+  return PIMC_OK;
+}
+
+MixDev to_dev(const pimc_move_mix &m) {
+  MixDev d;
+  memset(&d, 0, sizeof(d));
+  d.staging_phases = m.staging_phases;
+  d.stage_min = m.stage_min;
+  d.stage_max = m.stage_max;
+  d.stage_minacc = m.stage_minacc;
+  d.stage_maxacc = m.stage_maxacc;
+  d.swaps_per_sweep = m.swaps_per_sweep;
+  d.swap_min = m.swap_min;
+  d.swap_max = m.swap_max;
+  d.swap_minacc = m.swap_minacc;
+  d.swap_maxacc = m.swap_maxacc;
+  d.com_phases = m.com_phases;
+  d.com_minstep = m.com_minstep;
+  d.com_maxstep = m.com_maxstep;
+  d.com_minacc = m.com_minacc;
+  d.com_maxacc = m.com_maxacc;
+  d.polymer_com_phases = m.polymer_com_phases;
+  d.pcom_minstep = m.pcom_minstep;
+  d.pcom_maxstep = m.pcom_maxstep;
+  d.pcom_minacc = m.pcom_minacc;
+  d.pcom_maxacc = m.pcom_maxacc;
+  d.adapt = m.adapt;
+  d.measure_every = m.measure_every;
+  return d;
+}
+
+Handle *H(void *h) { return reinterpret_cast<Handle *>(h); }
+
+int ensure_buf(Handle *h, size_t n) {
+  if (n <= h->n_buf) return PIMC_OK;
+  if (h->d_buf) cudaFree(h->d_buf);
+  h->d_buf = nullptr;
+  h->n_buf = 0;
+  CK(cudaMalloc(&h->d_buf, n * sizeof(double)));
+  h->n_buf = n;
+  return PIMC_OK;
+}
+
+int sync_check(Handle *h) {
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaGetLastError());
+  return PIMC_OK;
+}
+
+size_t swap_scratch_bytes(int N, int M) {
+  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64) + sizeof(int) * 4 * (size_t)M;
+}
+
+// choose the shared-memory plan for a block size
+void plan_smem(Handle *h, int block, int state_cap) {
+  const int nw = block / 32;
+  h->warp_scratch_d = std::max(kWarpScratchMin, 3 * h->maxM);
+  size_t scratch = std::max(swap_scratch_bytes(h->maxN, h->maxM),
+                            (size_t)nw * h->warp_scratch_d * sizeof(double));
+  scratch = std::max(scratch, (size_t)2 * h->maxN * sizeof(int));
+  scratch = (scratch + 15) & ~(size_t)15;
+  int need_state = 0;
+  for (const auto &d : h->desc)
+    if (d.smem_bytes <= state_cap) need_state = std::max(need_state, d.smem_bytes);
+  need_state = (need_state + 15) & ~15;
+  h->state_bytes = need_state;
+  h->scratch_bytes = scratch;
+  h->dyn_smem = (size_t)need_state + scratch;
+}
+
+int upload_desc(Handle *h) {
+  CK(cudaMemcpyAsync(h->d_desc, h->desc.data(), sizeof(ChainDesc) * h->nchains,
+                     cudaMemcpyHostToDevice, h->stream));
+  return PIMC_OK;
+}
+
+int refresh_links_cells(Handle *h, int chain0, int nch) {
+  CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, chain0, nch, h->maxNM, h->stream));
+  CK(launch_cells(h->d_desc, h->d_dpool, h->d_ipool, chain0, nch, h->maxM, h->stream));
+  return PIMC_OK;
+}
+
+int create_impl(const pimc_params *params, int nchains, void **out) {
+  if (!params || !out || nchains < 1) return fail(PIMC_EARG, "null argument or nchains < 1");
+  if (nchains > (1 << 24)) return fail(PIMC_EARG, "too many chains");
+  for (int c = 0; c < nchains; ++c) {
+    int rc = check_params(params[c]);
+    if (rc) return fail(rc, "chain " + std::to_string(c) + ": " + g_err);
+    if (params[c].interactions) {
+      const double ra = params[c].r_a;
+      const int nb = (int)std::floor((2.0 * params[c].L) / ra);
+      if (nb < 3) return fail(PIMC_EARG, "interactions need at least 3 neighbour cells per dimension");
+    }
+  }
+  Handle *h = new Handle();
+  h->nchains = nchains;
+  h->params.assign(params, params + nchains);
+  size_t dp = 0, ip = 0, up = 0;
+  for (int c = 0; c < nchains; ++c) {
+    const pimc_params &p = params[c];
+    ChainDesc d = make_desc(p, c);
+    const size_t NM = (size_t)p.N * p.M;
+    d.x_off = (long long)dp; dp += (size_t)p.dim * NM;
+    d.V_off = (long long)dp; dp += NM;
+    dp = (dp + 1) & ~(size_t)1;
+    d.tab_off = (long long)dp; dp += 2 * (size_t)d.wtab * d.wtab;
+    d.eser_off = p.energy_capacity > 0 ? (long long)dp : -1;
+    dp += 4 * (size_t)p.energy_capacity;
+    d.next_off = (long long)ip; ip += p.N;
+    if (p.interactions || p.hardcore_a > 0.0) {
+      d.cell_off = (long long)ip;
+      ip += (size_t)p.M * d.ncell + 2 * NM;
+    } else {
+      d.cell_off = -1;
+    }
+    if (p.density_nbins > 0) {
+      d.dens_off = (long long)up;
+      up += p.dim == 2 ? (size_t)p.density_nbins * p.density_nbins : (size_t)p.density_nbins;
+    } else {
+      d.dens_off = -1;
+    }
+    h->desc.push_back(d);
+    pimc_move_mix m = default_mix(p);
+    h->umix.push_back(m);
+    h->mix.push_back(to_dev(m));
+    h->maxN = std::max(h->maxN, p.N);
+    h->maxM = std::max(h->maxM, p.M);
+    h->maxNM = std::max(h->maxNM, (int)NM);
+  }
+  h->n_dpool = dp;
+  h->n_ipool = std::max<size_t>(ip, 1);
+  h->n_upool = std::max<size_t>(up, 1);
+  auto cleanup = [&](int rc) {
+    pimc_destroy(h);
+    return rc;
+  };
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cleanup(fail(PIMC_ECUDA, "no CUDA device"));
+  cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
+    return cleanup(fail(PIMC_ECUDA, "stream/event creation failed"));
+  if (cudaMalloc(&h->d_desc, sizeof(ChainDesc) * nchains) != cudaSuccess ||
+      cudaMalloc(&h->d_var, sizeof(ChainVar) * nchains) != cudaSuccess ||
+      cudaMalloc(&h->d_mix, sizeof(MixDev) * nchains) != cudaSuccess ||
+      cudaMalloc(&h->d_dpool, sizeof(double) * h->n_dpool) != cudaSuccess ||
+      cudaMalloc(&h->d_ipool, sizeof(int) * h->n_ipool) != cudaSuccess ||
+      cudaMalloc(&h->d_upool, sizeof(unsigned long long) * h->n_upool) != cudaSuccess ||
+      cudaMalloc(&h->d_queue, sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&h->d_order, sizeof(int) * nchains) != cudaSuccess ||
+      cudaMalloc(&h->d_iout, sizeof(int) * 16) != cudaSuccess)
+    return cleanup(fail(PIMC_ENOMEM, "device allocation failed"));
+  cudaMemsetAsync(h->d_dpool, 0, sizeof(double) * h->n_dpool, h->stream);
+  cudaMemsetAsync(h->d_upool, 0, sizeof(unsigned long long) * h->n_upool, h->stream);
+  // bridge coefficient tables: alpha = (m-t)/(m+1-t), sigma = sqrt(2 lambda alpha tau)
+  std::vector<double> tab;
+  for (int c = 0; c < nchains; ++c) {
+    const ChainDesc &d = h->desc[c];
+    tab.assign(2 * (size_t)d.wtab * d.wtab, 0.0);
+    for (int m = 2; m < d.wtab; ++m)
+      for (int t = 1; t < m; ++t) {
+        const double a = (double)(m - t) / (double)(m + 1 - t);
+        tab[2 * ((size_t)m * d.wtab + t)] = a;
+        tab[2 * ((size_t)m * d.wtab + t) + 1] = std::sqrt(2.0 * d.lambda * a * d.tau);
+      }
+    cudaMemcpyAsync(h->d_dpool + d.tab_off, tab.data(), sizeof(double) * tab.size(),
+                    cudaMemcpyHostToDevice, h->stream);
+  }
+  std::vector<ChainVar> vars(nchains);
+  for (int c = 0; c < nchains; ++c) {
+    memset(&vars[c], 0, sizeof(ChainVar));
+    vars[c].stage_m = std::min(h->umix[c].stage_slices, h->umix[c].stage_max);
+    vars[c].swap_m = std::min(h->umix[c].swap_slices, h->umix[c].swap_max);
+    vars[c].com_step = h->umix[c].com_step;
+    vars[c].pcom_step = h->umix[c].pcom_step;
+  }
+  cudaMemcpyAsync(h->d_var, vars.data(), sizeof(ChainVar) * nchains, cudaMemcpyHostToDevice, h->stream);
+  cudaMemcpyAsync(h->d_mix, h->mix.data(), sizeof(MixDev) * nchains, cudaMemcpyHostToDevice, h->stream);
+  // LPT order: most expensive chains first (staging/CoM ~ N M, swaps ~ N^2)
+  std::vector<int> order(nchains);
+  for (int c = 0; c < nchains; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    auto cost = [&](int c) {
+      const pimc_params &p = h->params[c];
+      return (double)p.N * p.M * (p.interactions ? 4.0 : 1.0) + 0.5 * (double)p.N * p.N;
+    };
+    return cost(a) > cost(b);
+  });
+  cudaMemcpyAsync(h->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, h->stream);
+  if (upload_desc(h)) return cleanup(PIMC_ECUDA);
+  // System(): init_world, cached links, neighbour grid
+  if (launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, nchains, h->maxN, h->stream) != cudaSuccess ||
+      refresh_links_cells(h, 0, nchains))
+    return cleanup(fail(PIMC_ECUDA, "initialisation launch failed"));
+  plan_smem(h, h->block, 48 * 1024);
+  if (sync_check(h)) return cleanup(PIMC_ECUDA);
+  *out = h;
+  return PIMC_OK;
+}
+
+int check_chain(Handle *h, int chain) {
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (chain < 0 || chain >= h->nchains) return fail(PIMC_EARG, "chain index out of range");
+  return PIMC_OK;
+}
+
+int set_beads_impl(Handle *h, int chain, const double *x) {
+  if (check_chain(h, chain)) return PIMC_EARG;
+  if (!x) return fail(PIMC_EARG, "null positions");
+  const ChainDesc &d = h->desc[chain];
+  for (size_t i = 0; i < (size_t)d.dim * d.N * d.M; ++i)
+    if (!std::isfinite(x[i])) return fail(PIMC_EARG, "non-finite position");
+  CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x, sizeof(double) * d.dim * d.N * d.M,
+                     cudaMemcpyHostToDevice, h->stream));
+  if (refresh_links_cells(h, chain, 1)) return PIMC_ECUDA;
+  return sync_check(h);
+}
+
+int get_beads_impl(Handle *h, int chain, double *x) {
+  if (check_chain(h, chain)) return PIMC_EARG;
+  if (!x) return fail(PIMC_EARG, "null output");
+  const ChainDesc &d = h->desc[chain];
+  CK(cudaMemcpyAsync(x, h->d_dpool + d.x_off, sizeof(double) * d.dim * d.N * d.M,
+                     cudaMemcpyDeviceToHost, h->stream));
+  return sync_check(h);
+}
+
+int check_perm(const int *next, int N) {
+  std::vector<char> seen(N, 0);
+  for (int i = 0; i < N; ++i) {
+    if (next[i] < 0 || next[i] >= N || seen[next[i]]) return fail(PIMC_ESTATE, "next is not a permutation");
+    seen[next[i]] = 1;
+  }
+  return PIMC_OK;
+}
+
+int read_var(Handle *h, int chain, ChainVar *v) {
+  CK(cudaMemcpyAsync(v, h->d_var + chain, sizeof(ChainVar), cudaMemcpyDeviceToHost, h->stream));
+  return sync_check(h);
+}
+
+void fill_stats(const ChainVar &v, pimc_stats *o) {
+  for (int q = 0; q < 4; ++q) {
+    o->attempts[q] = v.att[q];
+    o->accepts[q] = v.acc[q];
+  }
+  o->skips = v.skips;
+  o->bead_updates = v.bead_updates;
+  o->sweeps = v.sweep;
+  o->measurements = v.n_meas;
+  o->stage_slices = v.stage_m;
+  o->swap_slices = v.swap_m;
+  o->com_step = v.com_step;
+  o->pcom_step = v.pcom_step;
+}
+
+SweepArgs sweep_args(Handle *h) {
+  SweepArgs a;
+  a.desc = h->d_desc;
+  a.var = h->d_var;
+  a.mix = h->d_mix;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.upool = h->d_upool;
+  a.nchains = h->nchains;
+  a.chain0 = 0;
+  a.order = nullptr;
+  a.queue = nullptr;
+  a.sweeps = 1;
+  a.state_bytes = h->state_bytes;
+  a.warp_scratch_d = h->warp_scratch_d;
+  return a;
+}
+
+int prepare_launch(Handle *h) {
+  CK(sweep_set_smem(h->dyn_smem));
+  return PIMC_OK;
+}
+
+int run_plain(Handle *h, long long n) {
+  if (prepare_launch(h)) return PIMC_ECUDA;
+  SweepArgs a = sweep_args(h);
+  a.nchains = 1;
+  CK(cudaEventRecord(h->ev0, h->stream));
+  long long launches = 0;
+  for (long long s = 0; s < n; ++s)
+    for (int c = 0; c < h->nchains; ++c) {
+      a.chain0 = c;
+      CK(launch_sweep(a, 1, h->block, h->dyn_smem, h->stream));
+      ++launches;
+    }
+  CK(cudaEventRecord(h->ev1, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_launches = launches;
+  return PIMC_OK;
+}
+
+int grid_for(Handle *h) {
+  int per_sm = 0;
+  if (sweep_occupancy(h->block, h->dyn_smem, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+  return std::max(1, std::min(h->nchains, per_sm * h->num_sms));
+}
+
+int build_graph(Handle *h, int spl) {
+  if (h->gexec && h->g_spl == spl && h->g_block == h->block) return PIMC_OK;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  SweepArgs a = sweep_args(h);
+  a.order = h->d_order;
+  a.queue = h->d_queue;
+  a.sweeps = spl;
+  const int grid = grid_for(h);
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
+  launch_sweep(a, grid, h->block, h->dyn_smem, h->stream);
+  CK(cudaStreamEndCapture(h->stream, &g));
+  cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(PIMC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  h->g_spl = spl;
+  h->g_block = h->block;
+  return PIMC_OK;
+}
+
+int run_batched(Handle *h, long long n) {
+  if (prepare_launch(h)) return PIMC_ECUDA;
+  const int spl = std::max(1, h->spl);
+  int rc = build_graph(h, spl);
+  if (rc) return rc;
+  CK(cudaEventRecord(h->ev0, h->stream));
+  long long launches = 0;
+  const long long full = n / spl, rem = n % spl;
+  for (long long i = 0; i < full; ++i) {
+    CK(cudaGraphLaunch(h->gexec, h->stream));
+    ++launches;
+  }
+  if (rem) {
+    SweepArgs a = sweep_args(h);
+    a.order = h->d_order;
+    a.queue = h->d_queue;
+    a.sweeps = (int)rem;
+    CK(cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream));
+    CK(launch_sweep(a, grid_for(h), h->block, h->dyn_smem, h->stream));
+    ++launches;
+  }
+  CK(cudaEventRecord(h->ev1, h->stream));
+  rc = sync_check(h);
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_launches = launches;
+  return PIMC_OK;
+}
+
+int check_device_errors(Handle *h) {
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  for (int c = 0; c < h->nchains; ++c)
+    if (v[c].err) return fail(PIMC_EDEVICE, "device error " + std::to_string(v[c].err) + " on chain " + std::to_string(c));
+  return PIMC_OK;
+}
+
+// ---------------------------------------------------------------- attempts
+
+int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, double step,
+                 const double *normals, int n_normals, const double *uniforms, int n_uniforms,
+                 int *result, int *extra, double *proposal) {
+  if (!h) return fail(PIMC_EARG, "null handle");
+  const ChainDesc &d = h->desc[0];
+  if (n < 0 || n >= d.N) return fail(PIMC_EARG, "particle index out of range");
+  if (kind == MV_STAGE || kind == MV_SWAP) {
+    if (j0 < 0 || j0 >= d.M) return fail(PIMC_EARG, "slice index out of range");
+    if (m < 2 || m > d.M - 1 || m > 64) return fail(PIMC_EARG, "window m must be in [2, min(M-1, 64)]");
+  }
+  if (n_normals < 0 || n_uniforms < 0 || (n_normals && !normals) || (n_uniforms && !uniforms))
+    return fail(PIMC_EARG, "bad draw arrays");
+  if (!(d.flags & PF_HARD)) {
+    const int need = kind == MV_STAGE ? (m - 1) * d.dim : (kind == MV_SWAP ? 2 * (m - 1) * d.dim : 0);
+    if (n_normals < need) return fail(PIMC_EDRAWS, "not enough injected normals");
+  }
+  if (kind == MV_SWAP && d.N <= 1) {
+    if (result) *result = PIMC_SKIP;
+    return PIMC_OK;
+  }
+  if (kind == MV_COM) {
+    int nx = -1;
+    CK(cudaMemcpyAsync(&nx, h->d_ipool + d.next_off + n, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    if (sync_check(h)) return PIMC_ECUDA;
+    if (nx != n) return fail(PIMC_EARG, "SingleCenterOfMass needs a particle with next == itself");
+  }
+  // snapshot of the chain so that a run-out of injected draws leaves no trace
+  const size_t nx = (size_t)d.dim * d.N * d.M, nv = (size_t)d.N * d.M;
+  const size_t ncl = d.cell_off >= 0 ? (size_t)d.M * d.ncell + 2 * nv : 0;
+  std::vector<double> sx(nx), sv(nv);
+  std::vector<int> sn(d.N), scl(ncl);
+  CK(cudaMemcpyAsync(sx.data(), h->d_dpool + d.x_off, nx * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(sv.data(), h->d_dpool + d.V_off, nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(sn.data(), h->d_ipool + d.next_off, d.N * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (ncl) CK(cudaMemcpyAsync(scl.data(), h->d_ipool + d.cell_off, ncl * 4, cudaMemcpyDeviceToHost, h->stream));
+  const size_t nprop = (size_t)2 * (m + 1) * d.dim + 8;
+  if (ensure_buf(h, (size_t)n_normals + n_uniforms + nprop + 8)) return PIMC_ENOMEM;
+  double *dn = h->d_buf, *du = dn + n_normals, *dprop = du + n_uniforms;
+  if (n_normals) CK(cudaMemcpyAsync(dn, normals, 8 * (size_t)n_normals, cudaMemcpyHostToDevice, h->stream));
+  if (n_uniforms) CK(cudaMemcpyAsync(du, uniforms, 8 * (size_t)n_uniforms, cudaMemcpyHostToDevice, h->stream));
+  AttemptArgs a;
+  a.desc = h->d_desc;
+  a.var = h->d_var;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.upool = h->d_upool;
+  a.chain = 0;
+  a.kind = kind;
+  a.n = n;
+  a.j0 = j0;
+  a.m = m;
+  a.u_pick = u_pick;
+  a.step = step;
+  a.normals = dn;
+  a.n_normals = n_normals;
+  a.uniforms = du;
+  a.n_uniforms = n_uniforms;
+  a.prop = proposal ? dprop : nullptr;
+  a.out = h->d_iout;
+  a.force_warp = h->force_warp;
+  size_t smem = std::max(swap_scratch_bytes(d.N, d.M), (size_t)std::max(kWarpScratchMin, 3 * d.M) * 8);
+  smem = std::max(smem, (size_t)2 * d.N * sizeof(int));
+  CK(launch_attempt(a, smem, h->stream));
+  int out[5] = {0, 0, 0, 0, 0};
+  CK(cudaMemcpyAsync(out, h->d_iout, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+  if (proposal) {
+    const size_t np = (kind == MV_SWAP ? 2 : 1) * (size_t)(m + 1) * d.dim;
+    CK(cudaMemcpyAsync(proposal, dprop, np * 8, cudaMemcpyDeviceToHost, h->stream));
+  }
+  int rc = sync_check(h);
+  if (rc) return rc;
+  if (out[4]) {
+    CK(cudaMemcpyAsync(h->d_dpool + d.x_off, sx.data(), nx * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_dpool + d.V_off, sv.data(), nv * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_ipool + d.next_off, sn.data(), d.N * 4, cudaMemcpyHostToDevice, h->stream));
+    if (ncl) CK(cudaMemcpyAsync(h->d_ipool + d.cell_off, scl.data(), ncl * 4, cudaMemcpyHostToDevice, h->stream));
+    sync_check(h);
+    return fail(PIMC_EDRAWS, "injected draws ran out; state restored");
+  }
+  if (out[0] < 0) return fail(PIMC_ESTATE, "invalid cycle structure");
+  if (result) *result = out[0];
+  if (extra) *extra = out[1];
+  return PIMC_OK;
+}
+
+}  // namespace
+
+// ===================================================================== C ABI
+extern "C" {
+
+const char *pimc_last_error(void) { return g_err.c_str(); }
+int pimc_abi_version(void) { return PIMC_ABI_VERSION; }
+
+int pimc_create(const pimc_params *p, void **handle) { return create_impl(p, 1, handle); }
+
+int pimc_batch_create(const pimc_params *params, int nchains, void **handle) {
+  return create_impl(params, nchains, handle);
+}
+
+int pimc_destroy(void *handle) {
+  Handle *h = H(handle);
+  if (!h) return PIMC_OK;
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaFree(h->d_desc);
+  cudaFree(h->d_var);
+  cudaFree(h->d_mix);
+  cudaFree(h->d_dpool);
+  cudaFree(h->d_ipool);
+  cudaFree(h->d_upool);
+  cudaFree(h->d_queue);
+  cudaFree(h->d_order);
+  cudaFree(h->d_iout);
+  cudaFree(h->d_buf);
+  cudaFree(h->d_adj);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return PIMC_OK;
+}
+
+int pimc_num_chains(void *handle, int *n) {
+  if (!handle || !n) return fail(PIMC_EARG, "null argument");
+  *n = H(handle)->nchains;
+  return PIMC_OK;
+}
+
+int pimc_set_beads(void *handle, const double *x) { return set_beads_impl(H(handle), 0, x); }
+int pimc_get_beads(void *handle, double *x) { return get_beads_impl(H(handle), 0, x); }
+int pimc_batch_set_beads(void *handle, int chain, const double *x) {
+  return set_beads_impl(H(handle), chain, x);
+}
+int pimc_batch_get_beads(void *handle, int chain, double *x) {
+  return get_beads_impl(H(handle), chain, x);
+}
+
+// chains' positions are contiguous in the pool in chain order, each
+// followed by its link row, table and series; copy chain by chain into one
+// pinned-or-pageable host buffer with one async copy per chain and one
+// link/grid refresh for all chains
+int pimc_batch_set_beads_all(void *handle, const double *x_all) {
+  Handle *h = H(handle);
+  if (!h || !x_all) return fail(PIMC_EARG, "null argument");
+  size_t off = 0;
+  for (int c = 0; c < h->nchains; ++c) {
+    const ChainDesc &d = h->desc[c];
+    const size_t n = (size_t)d.dim * d.N * d.M;
+    CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x_all + off, n * 8, cudaMemcpyHostToDevice, h->stream));
+    off += n;
+  }
+  if (refresh_links_cells(h, 0, h->nchains)) return PIMC_ECUDA;
+  return sync_check(h);
+}
+
+int pimc_batch_get_beads_all(void *handle, double *x_all) {
+  Handle *h = H(handle);
+  if (!h || !x_all) return fail(PIMC_EARG, "null argument");
+  size_t off = 0;
+  for (int c = 0; c < h->nchains; ++c) {
+    const ChainDesc &d = h->desc[c];
+    const size_t n = (size_t)d.dim * d.N * d.M;
+    CK(cudaMemcpyAsync(x_all + off, h->d_dpool + d.x_off, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    off += n;
+  }
+  return sync_check(h);
+}
+
+int pimc_batch_energy_sums_all(void *handle, double *sum, double *sumsq, unsigned long long *count) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  for (int c = 0; c < h->nchains; ++c) {
+    for (int q = 0; q < 4; ++q) {
+      if (sum) sum[4 * c + q] = v[c].esum[q];
+      if (sumsq) sumsq[4 * c + q] = v[c].esum2[q];
+    }
+    if (count) count[c] = v[c].n_meas;
+  }
+  return PIMC_OK;
+}
+
+int pimc_set_next(void *handle, const int *next) {
+  Handle *h = H(handle);
+  if (!h || !next) return fail(PIMC_EARG, "null argument");
+  const ChainDesc &d = h->desc[0];
+  if (check_perm(next, d.N)) return PIMC_ESTATE;
+  CK(cudaMemcpyAsync(h->d_ipool + d.next_off, next, sizeof(int) * d.N, cudaMemcpyHostToDevice, h->stream));
+  if (refresh_links_cells(h, 0, 1)) return PIMC_ECUDA;
+  return sync_check(h);
+}
+
+int pimc_batch_get_next(void *handle, int chain, int *next) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain) || !next) return fail(PIMC_EARG, "bad argument");
+  const ChainDesc &d = h->desc[chain];
+  CK(cudaMemcpyAsync(next, h->d_ipool + d.next_off, sizeof(int) * d.N, cudaMemcpyDeviceToHost, h->stream));
+  return sync_check(h);
+}
+int pimc_get_next(void *handle, int *next) { return pimc_batch_get_next(handle, 0, next); }
+
+int pimc_set_raw(void *handle, const double *x, const double *V, const int *next) {
+  Handle *h = H(handle);
+  if (!h || !x || !V || !next) return fail(PIMC_EARG, "null argument");
+  const ChainDesc &d = h->desc[0];
+  if (check_perm(next, d.N)) return PIMC_ESTATE;
+  CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x, sizeof(double) * d.dim * d.N * d.M, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_dpool + d.V_off, V, sizeof(double) * d.N * d.M, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_ipool + d.next_off, next, sizeof(int) * d.N, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_cells(h->d_desc, h->d_dpool, h->d_ipool, 0, 1, h->maxM, h->stream));
+  return sync_check(h);
+}
+
+int pimc_get_links(void *handle, double *V) {
+  Handle *h = H(handle);
+  if (!h || !V) return fail(PIMC_EARG, "null argument");
+  const ChainDesc &d = h->desc[0];
+  CK(cudaMemcpyAsync(V, h->d_dpool + d.V_off, sizeof(double) * d.N * d.M, cudaMemcpyDeviceToHost, h->stream));
+  return sync_check(h);
+}
+
+int pimc_init_world(void *handle) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  CK(launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, h->nchains, h->maxN, h->stream));
+  if (refresh_links_cells(h, 0, h->nchains)) return PIMC_ECUDA;
+  return sync_check(h);
+}
+
+int pimc_set_move_mix(void *handle, int chain, const pimc_move_mix *mix) {
+  Handle *h = H(handle);
+  if (!h || !mix) return fail(PIMC_EARG, "null argument");
+  if (chain >= h->nchains) return fail(PIMC_EARG, "chain index out of range");
+  const int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->nchains : chain + 1;
+  for (int c = c0; c < c1; ++c)
+    if (check_mix(*mix, h->params[c])) return PIMC_EARG;
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  if (sync_check(h)) return PIMC_ECUDA;
+  for (int c = c0; c < c1; ++c) {
+    h->umix[c] = *mix;
+    h->mix[c] = to_dev(*mix);
+    v[c].stage_m = std::min(mix->stage_slices, mix->stage_max);
+    v[c].swap_m = std::min(mix->swap_slices, mix->swap_max);
+    v[c].com_step = mix->com_step;
+    v[c].pcom_step = mix->pcom_step;
+  }
+  CK(cudaMemcpyAsync(h->d_var, v.data(), sizeof(ChainVar) * h->nchains, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_mix, h->mix.data(), sizeof(MixDev) * h->nchains, cudaMemcpyHostToDevice, h->stream));
+  return sync_check(h);
+}
+
+int pimc_run(void *handle, long long n_sweeps) {
+  Handle *h = H(handle);
+  if (!h || n_sweeps < 0) return fail(PIMC_EARG, "bad argument");
+  int rc = h->nchains == 1 ? run_plain(h, n_sweeps) : run_batched(h, n_sweeps);
+  if (rc) return rc;
+  return check_device_errors(h);
+}
+
+int pimc_batch_run(void *handle, long long n_sweeps) {
+  Handle *h = H(handle);
+  if (!h || n_sweeps < 0) return fail(PIMC_EARG, "bad argument");
+  int rc = run_batched(h, n_sweeps);
+  if (rc) return rc;
+  return check_device_errors(h);
+}
+
+int pimc_batch_run_plain(void *handle, long long n_sweeps) {
+  Handle *h = H(handle);
+  if (!h || n_sweeps < 0) return fail(PIMC_EARG, "bad argument");
+  int rc = run_plain(h, n_sweeps);
+  if (rc) return rc;
+  return check_device_errors(h);
+}
+
+int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (block < 64 || block > 1024 || block % 32) return fail(PIMC_EARG, "block must be a multiple of 32 in [64, 1024]");
+  if (sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
+  h->block = block;
+  h->spl = sweeps_per_launch;
+  plan_smem(h, block, 48 * 1024);
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  return PIMC_OK;
+}
+
+int pimc_get_state(void *handle, void *buf, size_t bytes);
+int pimc_set_state(void *handle, const void *buf, size_t bytes);
+int pimc_state_size(void *handle, size_t *bytes);
+
+int pimc_batch_tune(void *handle, int sweeps_per_trial, int *block_out, int *spl_out) {
+  Handle *h = H(handle);
+  if (!h || sweeps_per_trial < 1) return fail(PIMC_EARG, "bad argument");
+  // trials advance the chains; the snapshot puts them back afterwards
+  size_t nb = 0;
+  int rc = pimc_state_size(h, &nb);
+  if (rc) return rc;
+  std::vector<char> snap(nb);
+  if ((rc = pimc_get_state(h, snap.data(), nb))) return rc;
+  const int blocks[] = {128, 256, 512};
+  const int spls[] = {1, 4};
+  double best = 1e300;
+  int bb = h->block, bs = h->spl;
+  for (int b : blocks)
+    for (int s : spls) {
+      if (s > sweeps_per_trial) continue;
+      if ((rc = pimc_batch_set_launch(h, b, s))) return rc;
+      if ((rc = run_batched(h, s))) return rc;  // warm (graph build)
+      if ((rc = run_batched(h, sweeps_per_trial))) return rc;
+      if (h->last_ms < best) {
+        best = h->last_ms;
+        bb = b;
+        bs = s;
+      }
+    }
+  if ((rc = pimc_batch_set_launch(h, bb, bs))) return rc;
+  if ((rc = pimc_set_state(h, snap.data(), nb))) return rc;
+  if (block_out) *block_out = bb;
+  if (spl_out) *spl_out = bs;
+  return PIMC_OK;
+}
+
+int pimc_attempt_staging(void *handle, int n, int j0, int m, const double *normals, int n_normals,
+                         const double *uniforms, int n_uniforms, int *result, double *proposal) {
+  return attempt_impl(H(handle), MV_STAGE, n, j0, m, 0.0, 0.0, normals, n_normals, uniforms,
+                      n_uniforms, result, nullptr, proposal);
+}
+
+int pimc_attempt_swap(void *handle, int j0, int m, int n1, double u_pick, const double *normals,
+                      int n_normals, const double *uniforms, int n_uniforms, int *result, int *n2,
+                      double *proposal) {
+  return attempt_impl(H(handle), MV_SWAP, n1, j0, m, u_pick, 0.0, normals, n_normals, uniforms,
+                      n_uniforms, result, n2, proposal);
+}
+
+int pimc_attempt_com(void *handle, int n, double step, const double *uniforms, int n_uniforms,
+                     int *result) {
+  return attempt_impl(H(handle), MV_COM, n, 0, 2, 0.0, step, nullptr, 0, uniforms, n_uniforms,
+                      result, nullptr, nullptr);
+}
+
+int pimc_attempt_polymer_com(void *handle, int n, double step, const double *uniforms,
+                             int n_uniforms, int *result) {
+  return attempt_impl(H(handle), MV_PCOM, n, 0, 2, 0.0, step, nullptr, 0, uniforms, n_uniforms,
+                      result, nullptr, nullptr);
+}
+
+int pimc_eval_action(void *handle, double out[4]) {
+  Handle *h = H(handle);
+  if (!h || !out) return fail(PIMC_EARG, "null argument");
+  if (ensure_buf(h, 8)) return PIMC_ENOMEM;
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  a.desc = h->d_desc;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.upool = h->d_upool;
+  a.chain = 0;
+  a.out = h->d_buf;
+  CK(launch_eval_action(a, h->stream));
+  CK(cudaMemcpyAsync(out, h->d_buf, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return sync_check(h);
+}
+
+int pimc_eval_staging_weights(void *handle, int n, int j0, int m, const double *rp, double *w_init,
+                              double *w_upd) {
+  Handle *h = H(handle);
+  if (!h || !rp || !w_init || !w_upd) return fail(PIMC_EARG, "null argument");
+  const ChainDesc &d = h->desc[0];
+  if (n < 0 || n >= d.N || j0 < 0 || j0 >= d.M || m < 2 || m > d.M - 1)
+    return fail(PIMC_EARG, "window out of range");
+  const size_t nrp = (size_t)(m + 1) * d.dim;
+  if (ensure_buf(h, nrp + 8)) return PIMC_ENOMEM;
+  CK(cudaMemcpyAsync(h->d_buf + 8, rp, nrp * 8, cudaMemcpyHostToDevice, h->stream));
+  EvalArgs a;
+  memset(&a, 0, sizeof(a));
+  a.desc = h->d_desc;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.upool = h->d_upool;
+  a.chain = 0;
+  a.n = n;
+  a.j0 = j0;
+  a.m = m;
+  a.rp = h->d_buf + 8;
+  a.out = h->d_buf;
+  CK(launch_eval_weights(a, h->stream));
+  double o[2];
+  CK(cudaMemcpyAsync(o, h->d_buf, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  *w_init = o[0];
+  *w_upd = o[1];
+  return PIMC_OK;
+}
+
+int pimc_measure(void *handle) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  CK(launch_measure(h->d_desc, h->d_var, h->d_dpool, h->d_ipool, h->d_upool, 0, h->nchains, h->stream));
+  return sync_check(h);
+}
+
+int pimc_get_energies(void *handle, int chain, double *out, int cap, int *count) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  ChainVar v;
+  int rc = read_var(h, chain, &v);
+  if (rc) return rc;
+  const ChainDesc &d = h->desc[chain];
+  const int have = (int)std::min<unsigned long long>(v.eser_count, (unsigned long long)d.eser_cap);
+  const int k = std::min(have, std::max(cap, 0));
+  if (k > 0 && out) {
+    CK(cudaMemcpyAsync(out, h->d_dpool + d.eser_off, sizeof(double) * 4 * k, cudaMemcpyDeviceToHost, h->stream));
+    rc = sync_check(h);
+    if (rc) return rc;
+  }
+  if (count) *count = have;
+  return PIMC_OK;
+}
+
+int pimc_get_energy_sums(void *handle, int chain, double *sum, double *sumsq,
+                         unsigned long long *count) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  ChainVar v;
+  int rc = read_var(h, chain, &v);
+  if (rc) return rc;
+  for (int q = 0; q < 4; ++q) {
+    if (sum) sum[q] = v.esum[q];
+    if (sumsq) sumsq[q] = v.esum2[q];
+  }
+  if (count) *count = v.n_meas;
+  return PIMC_OK;
+}
+
+int pimc_get_density(void *handle, int chain, double *hist, unsigned long long *ndata) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  const ChainDesc &d = h->desc[chain];
+  if (d.dens_off < 0) return fail(PIMC_EARG, "no density histogram (density_nbins == 0)");
+  const size_t nb = d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb;
+  std::vector<unsigned long long> u(nb);
+  CK(cudaMemcpyAsync(u.data(), h->d_upool + d.dens_off, nb * 8, cudaMemcpyDeviceToHost, h->stream));
+  ChainVar v;
+  CK(cudaMemcpyAsync(&v, h->d_var + chain, sizeof(ChainVar), cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  if (hist)
+    for (size_t i = 0; i < nb; ++i) hist[i] = (double)u[i];
+  if (ndata) *ndata = v.ndata;
+  return PIMC_OK;
+}
+
+int pimc_reset_measurements(void *handle) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  if (sync_check(h)) return PIMC_ECUDA;
+  for (auto &x : v) {
+    x.n_meas = x.ndata = x.eser_count = 0;
+    for (int q = 0; q < 4; ++q) x.esum[q] = x.esum2[q] = 0.0;
+  }
+  CK(cudaMemcpyAsync(h->d_var, v.data(), sizeof(ChainVar) * h->nchains, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemsetAsync(h->d_upool, 0, sizeof(unsigned long long) * h->n_upool, h->stream));
+  return sync_check(h);
+}
+
+int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double *extra) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  const ChainDesc &d = h->desc[chain];
+  const size_t nbd = (size_t)d.N * d.M;
+  const int nblocks = (int)((nbd + 255) / 256);
+  const size_t need = 4 * nbd + (size_t)d.N + 8 * (size_t)nblocks + 16 + (size_t)d.dim * nbd;
+  if (need > h->n_adj) {
+    if (h->d_adj) cudaFree(h->d_adj);
+    h->d_adj = nullptr;
+    h->n_adj = 0;
+    CK(cudaMalloc(&h->d_adj, need * sizeof(double)));
+    h->n_adj = need;
+  }
+  AdjArgs a;
+  a.desc = h->d_desc;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.chain = chain;
+  a.omega = h->params[chain].harmonic_omega;
+  a.gA = h->d_adj;
+  a.gB = a.gA + 2 * nbd;
+  a.part = a.gB + 2 * nbd;
+  a.nblocks = nblocks;
+  a.totals = a.part + 8 * (size_t)nblocks;
+  a.sum_rg = a.totals + 8;
+  a.dSdr = a.sum_rg + 8;
+  a.inv = (int *)(a.dSdr + (size_t)d.dim * nbd);
+  // inv needs N ints: the buffer has N doubles of room after dSdr
+  CK(cudaMemsetAsync(a.sum_rg, 0, sizeof(double), h->stream));
+  CK(launch_adjoint(a, (int)nbd, h->stream));
+  double tot[9];
+  CK(cudaMemcpyAsync(tot, a.totals, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(tot + 8, a.sum_rg, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (dSdr) CK(cudaMemcpyAsync(dSdr, a.dSdr, sizeof(double) * d.dim * nbd, cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  // totals: S_ext, dV0, domega, S_pair, dg, pair virial, r.g_ext
+  if (dSdtheta) {
+    dSdtheta[0] = tot[1];
+    dSdtheta[1] = tot[2];
+    dSdtheta[2] = tot[4];
+  }
+  if (extra) {
+    const double Mt = d.M * d.tau;
+    extra[0] = tot[0];
+    extra[1] = tot[3];
+    extra[2] = (tot[0] + 0.5 * tot[6]) / Mt + (tot[3] + 0.5 * tot[5]) / Mt;
+    extra[3] = tot[8];
+  }
+  return PIMC_OK;
+}
+
+int pimc_set_potential(void *handle, int chain, double V0, double omega, double g) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  pimc_params &p = h->params[chain];
+  if (V0 != 0.0 && !(p.lattice_a > 0.0)) return fail(PIMC_EARG, "lattice_a must be positive");
+  p.lattice_V0 = V0;
+  p.harmonic_omega = omega;
+  p.pair_g = g;
+  ChainDesc &d = h->desc[chain];
+  d.V0 = V0;
+  d.lat_k = V0 != 0.0 ? 1.0 / p.lattice_a : 0.0;
+  d.hcoef = 0.5 * omega * omega;
+  d.g = g;
+  d.flags &= ~(PF_LATT | PF_HARM);
+  if (V0 != 0.0) d.flags |= PF_LATT;
+  if (omega != 0.0) d.flags |= PF_HARM;
+  if (upload_desc(h)) return PIMC_ECUDA;
+  CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, chain, 1, h->maxNM, h->stream));
+  return sync_check(h);
+}
+
+int pimc_get_stats(void *handle, int chain, pimc_stats *out) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain) || !out) return fail(PIMC_EARG, "bad argument");
+  ChainVar v;
+  int rc = read_var(h, chain, &v);
+  if (rc) return rc;
+  fill_stats(v, out);
+  return PIMC_OK;
+}
+
+int pimc_get_total_stats(void *handle, pimc_stats *out) {
+  Handle *h = H(handle);
+  if (!h || !out) return fail(PIMC_EARG, "null argument");
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  memset(out, 0, sizeof(*out));
+  for (auto &x : v) {
+    for (int q = 0; q < 4; ++q) {
+      out->attempts[q] += x.att[q];
+      out->accepts[q] += x.acc[q];
+    }
+    out->skips += x.skips;
+    out->bead_updates += x.bead_updates;
+    out->sweeps += x.sweep;
+    out->measurements += x.n_meas;
+  }
+  if (!v.empty()) {
+    out->stage_slices = v[0].stage_m;
+    out->swap_slices = v[0].swap_m;
+    out->com_step = v[0].com_step;
+    out->pcom_step = v[0].pcom_step;
+  }
+  return PIMC_OK;
+}
+
+// checkpoint layout: magic, version, nchains, then per chain the raw device
+// regions (x, V, next, cells, density, energy series) and ChainVar
+int pimc_state_size(void *handle, size_t *bytes) {
+  Handle *h = H(handle);
+  if (!h || !bytes) return fail(PIMC_EARG, "null argument");
+  size_t b = 3 * sizeof(unsigned);
+  for (const auto &d : h->desc) {
+    const size_t nm = (size_t)d.N * d.M;
+    b += sizeof(ChainVar) + 8 * ((size_t)d.dim * nm + nm) + 4 * (size_t)d.N;
+    if (d.cell_off >= 0) b += 4 * ((size_t)d.M * d.ncell + 2 * nm);
+    if (d.dens_off >= 0) b += 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb);
+    if (d.eser_off >= 0) b += 8 * 4 * (size_t)d.eser_cap;
+  }
+  *bytes = b;
+  return PIMC_OK;
+}
+
+static int state_io(Handle *h, char *buf, size_t bytes, bool save) {
+  size_t need = 0;
+  pimc_state_size(h, &need);
+  if (!buf || bytes < need) return fail(PIMC_EARG, "state buffer too small");
+  char *p = buf;
+  unsigned hdr[3] = {kStateMagic, (unsigned)PIMC_ABI_VERSION, (unsigned)h->nchains};
+  if (save) {
+    memcpy(p, hdr, sizeof(hdr));
+  } else {
+    unsigned in[3];
+    memcpy(in, p, sizeof(in));
+    if (in[0] != hdr[0] || in[1] != hdr[1] || in[2] != hdr[2])
+      return fail(PIMC_ESTATE, "state does not belong to a handle of this shape");
+  }
+  p += sizeof(hdr);
+  const auto kind = save ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice;
+  auto io = [&](void *dev, size_t n) -> cudaError_t {
+    cudaError_t e = save ? cudaMemcpyAsync(p, dev, n, kind, h->stream) : cudaMemcpyAsync(dev, p, n, kind, h->stream);
+    p += n;
+    return e;
+  };
+  for (int c = 0; c < h->nchains; ++c) {
+    const ChainDesc &d = h->desc[c];
+    const size_t nm = (size_t)d.N * d.M;
+    CK(io(h->d_var + c, sizeof(ChainVar)));
+    CK(io(h->d_dpool + d.x_off, 8 * (size_t)d.dim * nm));
+    CK(io(h->d_dpool + d.V_off, 8 * nm));
+    CK(io(h->d_ipool + d.next_off, 4 * (size_t)d.N));
+    if (d.cell_off >= 0) CK(io(h->d_ipool + d.cell_off, 4 * ((size_t)d.M * d.ncell + 2 * nm)));
+    if (d.dens_off >= 0) CK(io(h->d_upool + d.dens_off, 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb)));
+    if (d.eser_off >= 0) CK(io(h->d_dpool + d.eser_off, 8 * 4 * (size_t)d.eser_cap));
+  }
+  return sync_check(h);
+}
+
+int pimc_get_state(void *handle, void *buf, size_t bytes) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  return state_io(h, (char *)buf, bytes, true);
+}
+
+int pimc_set_state(void *handle, const void *buf, size_t bytes) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  return state_io(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+int pimc_last_run_ms(void *handle, double *ms) {
+  if (!handle || !ms) return fail(PIMC_EARG, "null argument");
+  *ms = H(handle)->last_ms;
+  return PIMC_OK;
+}
+
+int pimc_last_run_launches(void *handle, long long *launches) {
+  if (!handle || !launches) return fail(PIMC_EARG, "null argument");
+  *launches = H(handle)->last_launches;
+  return PIMC_OK;
+}
+
+int pimc_set_option(void *handle, int key, long long value) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (key == PIMC_OPT_FORCE_WARP_WINDOW) {
+    h->force_warp = value != 0;
+    return PIMC_OK;
+  }
+  return fail(PIMC_EARG, "unknown option");
+}
+
+}  // extern "C"

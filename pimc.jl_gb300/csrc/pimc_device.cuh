@@ -1,0 +1,573 @@
+// pimc_device.cuh -- device building blocks of the sweep: counter-based
+// random numbers, the action pieces, the cell grid, and the moves
+// (Levy staging window, permutation swap, centre-of-mass shifts) written once
+// and shared by the sweep kernels and the injected-draw attempt kernels.
+//
+// Reference correspondence (oameye/PIMC.jl):
+//   distance / lnK / lnV / teleport      src/propagator.jl:6-32
+//   lnU (Gaussian propint)               src/system.jl:26-28
+//   cell grid                            src/nearest_neighbours.jl:26-209
+//   metropolis                           src/updates/helper.jl:3-5
+//   hardspherelevy!                      src/updates/helper.jl:141-222
+//   ReshapeLinear                        src/updates/reshape.jl:31-91
+//   ReshapeSwapLinear / sampleparticles  src/updates/reshape.jl:123-283, helper.jl:224-267
+//   SingleCenterOfMass / Polymer...      src/updates/com.jl:31-224
+//   Density / Energy                     src/measurement.jl:45-122
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pimc_types.h"
+
+namespace pimc {
+
+constexpr int WMAX = 64;     // largest staging / swap window m handled on the device
+constexpr int TWMAX = 32;    // thread-per-window variant handles m <= TWMAX
+
+// move outcomes (PIMC_REJECT / ACCEPT / SKIP / HARDCORE of pimc.h)
+constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and draws derived from it
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox10(uint4 c, uint2 k) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k.x += 0x9E3779B9u; k.y += 0xBB67AE85u; }
+    const unsigned hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const unsigned hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+  }
+  return c;
+}
+
+// 53-bit uniform in [0, 1)
+__device__ __forceinline__ double u53(unsigned a, unsigned b) {
+  const unsigned long long x = ((((unsigned long long)a) << 32) | b) >> 11;
+  return (double)x * 0x1.0p-53;
+}
+
+// Box-Muller pair in FP64 (CUDA's log / sincospi / sqrt as library calls)
+__device__ __forceinline__ void normal2(uint4 r, double &z0, double &z1) {
+  const double u1 = 1.0 - u53(r.x, r.y);  // (0, 1]
+  const double u2 = u53(r.z, r.w);
+  const double rad = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  z0 = rad * c;
+  z1 = rad * s;
+}
+
+struct Stream {
+  uint2 key;
+  unsigned item, sweep, tag;
+  __device__ __forceinline__ uint4 at(unsigned draw) const {
+    return philox10(make_uint4(draw, item, sweep, tag), key);
+  }
+  __device__ __forceinline__ double uni(unsigned draw) const {
+    const uint4 r = at(draw);
+    return u53(r.x, r.y);
+  }
+};
+
+__device__ __forceinline__ Stream make_stream(const ChainDesc &d, unsigned long long sweep,
+                                              unsigned phase, unsigned item) {
+  Stream s;
+  s.key = make_uint2(d.key0, d.key1);
+  s.item = item;
+  s.sweep = (unsigned)sweep;
+  s.tag = (phase << 24) | (d.chain_tag & 0xFFFFFFu);
+  return s;
+}
+
+// draw indices inside one move's stream
+constexpr unsigned DRAW_SEQ = 0x40000000u;     // sequential normals (hard-core retries)
+constexpr unsigned DRAW_UNI = 0x80000000u;     // sequential uniforms (CoM shifts)
+constexpr unsigned DRAW_CHOICE = 0xA0000000u;  // move choices (window, partner)
+constexpr unsigned DRAW_ACCEPT = 0xC0000000u;  // Metropolis uniform
+
+// Generator-backed draws for one move.  bead_normals(k) is a pure function of
+// the bead index so lanes may evaluate beads in parallel.
+struct GenDraws {
+  Stream s;
+  unsigned seq;
+  int have;
+  double spare;
+  __device__ __forceinline__ void bead_normals(int k, int dim, double *z) const {
+    double a, b;
+    normal2(s.at((unsigned)k), a, b);
+    z[0] = a;
+    if (dim > 1) z[1] = b;
+  }
+  __device__ __forceinline__ void consumed(int) {}
+  __device__ __forceinline__ double normal() {
+    if (have) { have = 0; return spare; }
+    double a, b;
+    normal2(s.at(DRAW_SEQ + seq++), a, b);
+    spare = b;
+    have = 1;
+    return a;
+  }
+  __device__ __forceinline__ double uniform() { return s.uni(DRAW_UNI + seq++); }
+  __device__ __forceinline__ double uniform_accept() { return s.uni(DRAW_ACCEPT); }
+};
+
+__device__ __forceinline__ GenDraws gen_draws(const Stream &s) {
+  GenDraws g;
+  g.s = s;
+  g.seq = 0;
+  g.have = 0;
+  g.spare = 0.0;
+  return g;
+}
+
+// Injected draws (parity level b): normals bead-major, d per bead, in the
+// order the reference draws them; uniforms consumed sequentially.
+struct InjDraws {
+  const double *nrm;
+  int n_nrm, pn;
+  const double *uni;
+  int n_uni, pu;
+  int exh;
+  __device__ __forceinline__ void bead_normals(int k, int dim, double *z) const {
+    for (int d = 0; d < dim; ++d) {
+      const int i = pn + k * dim + d;
+      z[d] = i < n_nrm ? nrm[i] : 0.0;
+    }
+  }
+  __device__ __forceinline__ void consumed(int cnt) { pn += cnt; }
+  __device__ __forceinline__ double normal() {
+    if (pn < n_nrm) return nrm[pn++];
+    exh = 1;
+    return 0.0;
+  }
+  __device__ __forceinline__ double uniform() {
+    if (pu < n_uni) return uni[pu++];
+    exh = 1;
+    return 0.5;
+  }
+  __device__ __forceinline__ double uniform_accept() { return uniform(); }
+};
+
+// ---------------------------------------------------------------------------
+// chain view: x/V/next may live in shared or global memory (generic pointers)
+// ---------------------------------------------------------------------------
+struct CV {
+  const ChainDesc *d;
+  double *x;          // x[(k*N + n)*ld + j]
+  double *V;          // V[n*ld + j]
+  int *next;
+  int *head, *cn, *cp;  // cell lists (global)
+  const double2 *tab;   // (alpha, sigma)[m*wtab + t]
+  unsigned long long *hist;
+  double *eser;
+  int N, M, dim, ld;
+  __device__ __forceinline__ double &X(int k, int n, int j) const {
+    return x[((size_t)k * N + n) * ld + j];
+  }
+  __device__ __forceinline__ double &Vl(int n, int j) const { return V[(size_t)n * ld + j]; }
+};
+
+// ---------------------------------------------------------------------------
+// action pieces (src/propagator.jl)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dist1(double a, double b, double L) {
+  const double dx = fabs(a - b);
+  const double o = (2.0 * L) - dx;
+  return o < dx ? o : dx;
+}
+
+// teleport(x, L) = (x+L) - floor(x/2L + 1/2) 2L - L (src/propagator.jl:30-32).
+// The quotient is formed by a multiplication; when it lands within 1e-9 of an
+// integer the IEEE division of the reference is used instead, so the floor is
+// always the reference's.
+__device__ __forceinline__ double teleport(double x, double L, double inv2L) {
+  const double q = x * inv2L + 0.5;
+  double f = floor(q);
+  const double fr = q - f;
+  if (fr < 1e-9 || fr > 1.0 - 1e-9) f = floor(x / (2.0 * L) + 0.5);
+  return (x + L) - f * (2.0 * L) - L;
+}
+
+__device__ __forceinline__ double sgn(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 0.0); }
+
+// engine-known external potential: hcoef |r|^2 + V0 sum sin^2(pi r_d / a)
+__device__ __forceinline__ double vext(const ChainDesc &d, double x, double y) {
+  double v = 0.0;
+  if (d.flags & PF_HARM) {
+    double s = x * x;
+    if (d.dim > 1) s += y * y;
+    v += d.hcoef * s;
+  }
+  if (d.flags & PF_LATT) {
+    const double a = sinpi(x * d.lat_k);
+    double s = a * a;
+    if (d.dim > 1) {
+      const double b = sinpi(y * d.lat_k);
+      s += b * b;
+    }
+    v += d.V0 * s;
+  }
+  return v;
+}
+
+// gradient of vext along one coordinate
+__device__ __forceinline__ double dvext(const ChainDesc &d, double x) {
+  double g = 0.0;
+  if (d.flags & PF_HARM) g += 2.0 * d.hcoef * x;
+  if (d.flags & PF_LATT) g += d.V0 * (d.lat_k * 3.141592653589793) * sinpi(2.0 * x * d.lat_k);
+  return g;
+}
+
+__device__ __forceinline__ double vpair(const ChainDesc &d, double r2) {
+  return d.g * exp(-r2 * d.inv2s2);
+}
+
+__device__ __forceinline__ double lnU2(const ChainDesc &d, double r2a, double r2b) {
+  return -0.5 * d.tau * (vpair(d, r2a) + vpair(d, r2b));
+}
+
+// bridge coefficients alpha_t = (m-t)/(m+1-t), sigma_t = sqrt(2 lambda alpha tau)
+// (src/updates/helper.jl:154,165); tabulated per chain with the same
+// expression for m < wtab
+__device__ __forceinline__ double2 bridge_coef(const CV &c, int m, int t) {
+  if (m < c.d->wtab) return c.tab[m * c.d->wtab + t];
+  const double a = (double)(m - t) / (double)(m + 1 - t);
+  return make_double2(a, sqrt(2.0 * c.d->lambda * a * c.d->tau));
+}
+
+// ---------------------------------------------------------------------------
+// cell grid (src/nearest_neighbours.jl)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int cell_of(const ChainDesc &d, double x, double y) {
+  const double w = 2.0 * d.L / d.nbins;
+  int ix = (int)floor((x + d.L) / w);
+  ix = ix < 0 ? 0 : (ix >= d.nbins ? d.nbins - 1 : ix);
+  if (d.dim == 1) return ix;
+  int iy = (int)floor((y + d.L) / w);
+  iy = iy < 0 ? 0 : (iy >= d.nbins ? d.nbins - 1 : iy);
+  return ix + d.nbins * iy;
+}
+
+// 3x3 stencil (bin_neighbors, nearest_neighbours.jl:55-65) without duplicates
+__device__ __forceinline__ int stencil(const ChainDesc &d, int c, int *out) {
+  const int nb = d.nbins;
+  int k = 0;
+  if (d.dim == 1) {
+    const int cand[3] = {c, (c - 1 + nb) % nb, (c + 1) % nb};
+    for (int i = 0; i < 3; ++i) {
+      bool dup = false;
+      for (int q = 0; q < k; ++q) dup |= out[q] == cand[i];
+      if (!dup) out[k++] = cand[i];
+    }
+    return k;
+  }
+  const int x = c % nb, y = c / nb;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      const int cc = ((x + dx + nb) % nb) + nb * ((y + dy + nb) % nb);
+      bool dup = false;
+      for (int q = 0; q < k; ++q) dup |= out[q] == cc;
+      if (!dup) out[k++] = cc;
+    }
+  return k;
+}
+
+__device__ __forceinline__ void cell_move(const CV &c, int n, int j, int c_old, int c_new) {
+  if (c_old == c_new) return;
+  const int N = c.N;
+  int *nx = c.cn + (size_t)j * N, *pv = c.cp + (size_t)j * N;
+  int *h = c.head + (size_t)j * c.d->ncell;
+  const int p = pv[n], q = nx[n];
+  if (p >= 0) nx[p] = q; else h[c_old] = q;
+  if (q >= 0) pv[q] = p;
+  const int hh = h[c_new];
+  nx[n] = hh;
+  pv[n] = -1;
+  if (hh >= 0) pv[hh] = n;
+  h[c_new] = n;
+}
+
+// rebuild the lists of one slice from positions (ascending particle order)
+__device__ __forceinline__ void cells_rebuild_slice(const CV &c, int j) {
+  const ChainDesc &d = *c.d;
+  int *h = c.head + (size_t)j * d.ncell;
+  int *nx = c.cn + (size_t)j * c.N, *pv = c.cp + (size_t)j * c.N;
+  for (int q = 0; q < d.ncell; ++q) h[q] = -1;
+  for (int n = c.N - 1; n >= 0; --n) {
+    const int cc = cell_of(d, c.X(0, n, j), c.dim > 1 ? c.X(1, n, j) : 0.0);
+    const int hh = h[cc];
+    nx[n] = hh;
+    pv[n] = -1;
+    if (hh >= 0) pv[hh] = n;
+    h[cc] = n;
+  }
+}
+
+__device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, double bx,
+                                      double by) {
+  const double dx = dist1(ax, bx, d.L);
+  double s = dx * dx;
+  if (d.dim > 1) {
+    const double dy = dist1(ay, by, d.L);
+    s += dy * dy;
+  }
+  return s;
+}
+
+// sum over neighbours b of the moving bead (a at slice j, an its next bead
+// along the moving path) of lnU(d(a,b_j), d(an, b_next)), neighbours within
+// 2L/nbins found through the 3x3 stencil (find_nns, nearest_neighbours.jl:131-154)
+__device__ double pair_link(const CV &c, double ax, double ay, double anx, double any, int j,
+                            int e1, int e2) {
+  const ChainDesc &d = *c.d;
+  const int M = c.M, N = c.N;
+  const int jn = (j + 1 == M) ? 0 : j + 1;
+  const double rc2 = d.rc * d.rc;
+  int cells[9];
+  const int nc = stencil(d, cell_of(d, ax, ay), cells);
+  double w = 0.0;
+  for (int ci = 0; ci < nc; ++ci) {
+    for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
+      if (b == e1 || b == e2) continue;
+      const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.dim > 1 ? c.X(1, b, j) : 0.0);
+      if (r2a > rc2) continue;
+      const int bn = (j == M - 1) ? c.next[b] : b;
+      const double r2b = mi2(d, anx, any, c.X(0, bn, jn), c.dim > 1 ? c.X(1, bn, jn) : 0.0);
+      w += lnU2(d, r2a, r2b);
+    }
+  }
+  return w;
+}
+
+__device__ __forceinline__ double pair_cross(const ChainDesc &d, double ax, double ay, double anx,
+                                             double any, double bx, double by, double bnx,
+                                             double bny) {
+  const double r2a = mi2(d, ax, ay, bx, by);
+  if (r2a > d.rc * d.rc) return 0.0;
+  return lnU2(d, r2a, mi2(d, anx, any, bnx, bny));
+}
+
+// hard-core test (find_nn + distance < a, src/updates/helper.jl:167-169)
+__device__ bool hard_hit(const CV &c, double x, double y, int j, int e1, int e2) {
+  const ChainDesc &d = *c.d;
+  const double a2 = d.hard_a * d.hard_a;
+  int cells[9];
+  const int nc = stencil(d, cell_of(d, x, y), cells);
+  for (int ci = 0; ci < nc; ++ci)
+    for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0;
+         b = c.cn[(size_t)j * c.N + b]) {
+      if (b == e1 || b == e2) continue;
+      if (mi2(d, x, y, c.X(0, b, j), c.dim > 1 ? c.X(1, b, j) : 0.0) < a2) return true;
+    }
+  return false;
+}
+
+// ---------------------------------------------------------------------------
+// warp helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Levy staging window, one thread (pair-free acceptance, no hard core)
+// ReshapeLinear (src/updates/reshape.jl:31-91) with hardspherelevy! for a = 0
+// ---------------------------------------------------------------------------
+template <class D>
+__device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
+                             double *prop) {
+  const ChainDesc &d = *c.d;
+  const int M = c.M, dim = c.dim;
+  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const int nx = c.next[n];
+  const int jend = j0 + m;
+  const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
+  double bx[TWMAX + 1], by[TWMAX + 1], vp[TWMAX];
+  const double sx = c.X(0, n, j0), sy = dim > 1 ? c.X(1, n, j0) : 0.0;
+  double ex = c.X(0, oe, je), ey = dim > 1 ? c.X(1, oe, je) : 0.0;
+  if (fabs(sx - ex) > L) ex += sgn(sx) * (2.0 * L);
+  if (dim > 1 && fabs(sy - ey) > L) ey += sgn(sy) * (2.0 * L);
+  double px = sx, py = sy;
+  bx[0] = sx;
+  by[0] = sy;
+  for (int t = 1; t < m; ++t) {
+    const double2 ab = bridge_coef(c, m, t);
+    double z[2];
+    dr.bead_normals(t - 1, dim, z);
+    px = ab.x * px + (1.0 - ab.x) * ex + z[0] * ab.y;
+    bx[t] = px;
+    if (dim > 1) {
+      py = ab.x * py + (1.0 - ab.x) * ey + z[1] * ab.y;
+      by[t] = py;
+    }
+  }
+  dr.consumed((m - 1) * dim);
+  bx[m] = ex;
+  by[m] = ey;
+  double wi = 0.0, wu = 0.0, vprev = 0.0;
+  for (int t = 0; t <= m; ++t) {
+    bx[t] = teleport(bx[t], L, inv2L);
+    if (dim > 1) by[t] = teleport(by[t], L, inv2L);
+    const double vb = vext(d, bx[t], by[t]);
+    if (t > 0) vp[t - 1] = mhtau * (vprev + vb);
+    vprev = vb;
+  }
+  for (int t = 0; t < m; ++t) {
+    const int a = j0 + t;
+    wi += c.Vl(a < M ? n : nx, a < M ? a : a - M);
+  }
+  for (int t = 0; t < m; ++t) wu += vp[t];
+  if (prop)
+    for (int t = 0; t <= m; ++t) {
+      prop[t * dim] = bx[t];
+      if (dim > 1) prop[t * dim + 1] = by[t];
+    }
+  const double delta = exp(wu - wi);
+  const bool acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  if (acc) {
+    for (int t = 0; t < m; ++t) {
+      const int a = j0 + t;
+      const int o = a < M ? n : nx, j = a < M ? a : a - M;
+      if (t > 0 || rewrite_start) {
+        c.X(0, o, j) = bx[t];
+        if (dim > 1) c.X(1, o, j) = by[t];
+      }
+      c.Vl(o, j) = vp[t];
+    }
+  }
+  return acc ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Levy staging window, one warp: pair terms (physical semantics) and the
+// hard-core retry loop.  sb: per-warp shared scratch of 5*(WMAX+1) doubles.
+// ---------------------------------------------------------------------------
+template <class D>
+__device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
+                           double *sb, double *prop, bool update_cells) {
+  const ChainDesc &d = *c.d;
+  const int lane = threadIdx.x & 31;
+  const int M = c.M, dim = c.dim;
+  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
+  const bool hard = (d.flags & PF_HARD) != 0;
+  double *sx_ = sb, *sy_ = sb + (WMAX + 1), *svb = sb + 2 * (WMAX + 1);
+  double *sz = sb + 3 * (WMAX + 1);  // 2*(WMAX+1): normals
+  const int nx = c.next[n];
+  const int jend = j0 + m;
+  const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
+  const double sx = c.X(0, n, j0), sy = dim > 1 ? c.X(1, n, j0) : 0.0;
+  double ex = c.X(0, oe, je), ey = dim > 1 ? c.X(1, oe, je) : 0.0;
+  if (fabs(sx - ex) > L) ex += sgn(sx) * (2.0 * L);
+  if (dim > 1 && fabs(sy - ey) > L) ey += sgn(sy) * (2.0 * L);
+  int fail = 0;
+  if (!hard) {
+    for (int t = 1 + lane; t < m; t += 32) {
+      double z[2];
+      dr.bead_normals(t - 1, dim, z);
+      sz[2 * t] = z[0];
+      sz[2 * t + 1] = dim > 1 ? z[1] : 0.0;
+    }
+    dr.consumed((m - 1) * dim);
+    __syncwarp();
+    if (lane < dim) {
+      double p = lane == 0 ? sx : sy;
+      const double e = lane == 0 ? ex : ey;
+      double *dst = lane == 0 ? sx_ : sy_;
+      for (int t = 1; t < m; ++t) {
+        const double2 ab = bridge_coef(c, m, t);
+        p = ab.x * p + (1.0 - ab.x) * e + sz[2 * t + lane] * ab.y;
+        dst[t] = p;
+      }
+    }
+  } else if (lane == 0) {
+    // sequential retries in the reference's draw order; the reference
+    // excludes the start particle (fpcycle of the wrapped slice) in its
+    // find_nn, the physical semantics excludes the bead's true owner
+    double px = sx, py = sy;
+    for (int t = 1; t < m && !fail; ++t) {
+      const double2 ab = bridge_coef(c, m, t);
+      const int a = j0 + t, j = a < M ? a : a - M;
+      const int exc = (d.flags & PF_PHYS) ? (a < M ? n : nx) : n;
+      int tries = 0;
+      while (true) {
+        if (++tries > d.ctr) { fail = 1; break; }
+        double z0 = dr.normal(), z1 = dim > 1 ? dr.normal() : 0.0;
+        const double qx = ab.x * px + (1.0 - ab.x) * ex + z0 * ab.y;
+        const double qy = dim > 1 ? ab.x * py + (1.0 - ab.x) * ey + z1 * ab.y : 0.0;
+        const double tx = teleport(qx, L, inv2L), ty = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
+        if (!hard_hit(c, tx, ty, j, exc, -1)) { px = qx; py = qy; break; }
+      }
+      sx_[t] = px;
+      sy_[t] = py;
+    }
+  }
+  fail = __shfl_sync(0xffffffffu, fail, 0);
+  __syncwarp();
+  if (fail) return RES_HARDCORE;
+  for (int t = lane; t <= m; t += 32) {
+    double qx = t == 0 ? sx : (t == m ? ex : sx_[t]);
+    double qy = t == 0 ? sy : (t == m ? ey : sy_[t]);
+    qx = teleport(qx, L, inv2L);
+    if (dim > 1) qy = teleport(qy, L, inv2L);
+    sx_[t] = qx;
+    sy_[t] = qy;
+    svb[t] = vext(d, qx, qy);
+  }
+  __syncwarp();
+  double wi = 0.0, wu = 0.0;
+  for (int t = lane; t < m; t += 32) {
+    const int a = j0 + t;
+    const int o = a < M ? n : nx, j = a < M ? a : a - M;
+    wi += c.Vl(o, j);
+    wu += mhtau * (svb[t] + svb[t + 1]);
+    if (phys_pair) {
+      const int a1 = a + 1;
+      const int o1 = a1 < M ? n : nx, j1 = a1 < M ? a1 : a1 - M;
+      wi += pair_link(c, c.X(0, o, j), dim > 1 ? c.X(1, o, j) : 0.0, c.X(0, o1, j1),
+                      dim > 1 ? c.X(1, o1, j1) : 0.0, j, o, -1);
+      wu += pair_link(c, sx_[t], sy_[t], sx_[t + 1], sy_[t + 1], j, o, -1);
+    }
+  }
+  wi = warp_sum(wi);
+  wu = warp_sum(wu);
+  if (prop)
+    for (int t = lane; t <= m; t += 32) {
+      prop[t * dim] = sx_[t];
+      if (dim > 1) prop[t * dim + 1] = sy_[t];
+    }
+  int acc = 0;
+  if (lane == 0) {
+    const double delta = exp(wu - wi);
+    acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  }
+  acc = __shfl_sync(0xffffffffu, acc, 0);
+  if (acc) {
+    for (int t = lane; t < m; t += 32) {
+      const int a = j0 + t;
+      const int o = a < M ? n : nx, j = a < M ? a : a - M;
+      if (t > 0 || rewrite_start) {
+        if (update_cells) {
+          const int co = cell_of(d, c.X(0, o, j), dim > 1 ? c.X(1, o, j) : 0.0);
+          const int cnw = cell_of(d, sx_[t], sy_[t]);
+          cell_move(c, o, j, co, cnw);
+        }
+        c.X(0, o, j) = sx_[t];
+        if (dim > 1) c.X(1, o, j) = sy_[t];
+      }
+      c.Vl(o, j) = mhtau * (svb[t] + svb[t + 1]);
+    }
+  }
+  __syncwarp();
+  return acc;
+}
+
+}  // namespace pimc

@@ -1,0 +1,83 @@
+// pimc_launch.h -- kernel argument blocks and host launchers of the engine.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pimc_types.h"
+
+namespace pimc {
+
+struct SweepArgs {
+  const ChainDesc *desc;
+  ChainVar *var;
+  const MixDev *mix;
+  double *dpool;
+  int *ipool;
+  unsigned long long *upool;
+  int nchains;        // chains in this launch
+  int chain0;         // first chain when no queue/order is used
+  const int *order;   // chain order (LPT), or null
+  int *queue;         // device work-queue head, or null (one chain per CTA)
+  int sweeps;         // sweeps per chain per launch
+  int state_bytes;    // shared bytes reserved for staging a chain's state
+  int warp_scratch_d; // doubles of scratch per warp
+};
+
+struct AttemptArgs {
+  const ChainDesc *desc;
+  ChainVar *var;
+  double *dpool;
+  int *ipool;
+  unsigned long long *upool;
+  int chain, kind, n, j0, m;
+  double u_pick, step;
+  const double *normals;
+  int n_normals;
+  const double *uniforms;
+  int n_uniforms;
+  double *prop;
+  int *out;           // result, extra, normals used, uniforms used, exhausted
+  int force_warp;
+};
+
+struct EvalArgs {
+  const ChainDesc *desc;
+  double *dpool;
+  int *ipool;
+  unsigned long long *upool;
+  int chain, n, j0, m;
+  const double *rp;
+  double *out;
+};
+
+struct AdjArgs {
+  const ChainDesc *desc;
+  double *dpool;
+  int *ipool;
+  int chain;
+  double omega;
+  double *gA, *gB;    // [N*M][2] scratch
+  int *inv;           // [N] scratch
+  double *part;       // [nblocks][8] scratch
+  int nblocks;
+  double *dSdr;       // [dim][N][M] or null
+  double *totals;     // [8]
+  double *sum_rg;     // [1], zeroed before the launch
+};
+
+cudaError_t launch_sweep(const SweepArgs &a, int grid, int block, size_t smem, cudaStream_t s);
+cudaError_t sweep_set_smem(size_t smem);
+cudaError_t sweep_occupancy(int block, size_t smem, int *blocks_per_sm);
+cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s);
+cudaError_t launch_eval_action(const EvalArgs &a, cudaStream_t s);
+cudaError_t launch_eval_weights(const EvalArgs &a, cudaStream_t s);
+cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0,
+                              int nchains, int maxN, cudaStream_t s);
+cudaError_t launch_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
+                         int maxNM, cudaStream_t s);
+cudaError_t launch_cells(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
+                         int maxM, cudaStream_t s);
+cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
+                           unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
+cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);
+
+}  // namespace pimc

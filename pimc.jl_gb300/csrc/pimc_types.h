@@ -1,0 +1,81 @@
+// pimc_types.h -- host/device shared descriptors of the GB300 sweep engine.
+#pragma once
+#include <stdint.h>
+
+namespace pimc {
+
+// chain flags
+enum : int {
+  PF_PAIR = 1,      // pair propagator on (System interactions=true)
+  PF_PHYS = 2,      // physical semantics (pair action in every move, swap ratio)
+  PF_HARD = 4,      // hard-core radius > 0
+  PF_LATT = 8,      // square lattice term in V
+  PF_HARM = 16,     // harmonic trap term in V
+};
+
+// move kinds for counters
+enum : int { MV_STAGE = 0, MV_SWAP = 1, MV_COM = 2, MV_PCOM = 3 };
+
+// stream phases (Philox counter word 3, high byte)
+enum : unsigned {
+  PH_STAGE = 1, PH_STAGE_OFF = 2, PH_SWAP = 3, PH_COM = 4, PH_PCOM = 5, PH_INIT = 6,
+  PH_ORDER = 7
+};
+
+// constant per chain
+struct ChainDesc {
+  int N, M, dim, nbins, ncell, flags, ctr, dens_nb;
+  int ld;           // row stride of x/V rows in global memory (== M)
+  int wtab;         // bridge-coefficient table covers windows m < wtab
+  double L, tau, lambda, beta;
+  double hcoef, V0, lat_k;
+  double g, inv2s2, rc, hard_a, mu;
+  double dens_bw;
+  long long x_off;      // doubles: x[d][n][j] at dpool + x_off
+  long long V_off;      // doubles: V[n][j]
+  long long tab_off;    // double2: bridge table (alpha, sigma)[m*wtab + t]
+  long long next_off;   // ints: next[n]
+  long long cell_off;   // ints: head[M][ncell], cnext[M][N], cprev[M][N]
+  long long dens_off;   // u64: hist[nb^dim]
+  long long eser_off;   // doubles: energy series [cap][4]
+  int eser_cap;
+  int smem_bytes;       // bytes to stage x,V,next in shared memory (0: stays global)
+  unsigned key0, key1;  // Philox key
+  unsigned chain_tag;   // chain id (low 24 bits of counter word 3)
+  int pad_;
+};
+
+// move mix as seen by the device
+struct MixDev {
+  int staging_phases;
+  int stage_min, stage_max;
+  double stage_minacc, stage_maxacc;
+  int swaps_per_sweep;
+  int swap_min, swap_max;
+  double swap_minacc, swap_maxacc;
+  int com_phases;
+  double com_minstep, com_maxstep, com_minacc, com_maxacc;
+  int polymer_com_phases;
+  double pcom_minstep, pcom_maxstep, pcom_minacc, pcom_maxacc;
+  int adapt;
+  int measure_every;
+};
+
+// mutable per chain
+struct ChainVar {
+  unsigned long long sweep;
+  int stage_m, swap_m;
+  double com_step, pcom_step;
+  unsigned long long att[4], acc[4];
+  unsigned long long skips;
+  double bead_updates;
+  unsigned long long n_meas, ndata, eser_count;
+  double esum[4], esum2[4];
+  int err;
+  int pad_;
+};
+
+// device error codes (ChainVar::err, first error wins)
+enum : int { DERR_NONE = 0, DERR_WINDOW = 1, DERR_STATE = 2, DERR_SCRATCH = 3 };
+
+}  // namespace pimc

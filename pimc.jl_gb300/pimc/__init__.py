@@ -1,0 +1,21 @@
+"""GB300 engine for the PIMC.jl Monte Carlo sweep.
+
+``pimc.api`` mirrors the reference package's Julia API (System, the update
+callables, run/apply, Density, Energy); ``pimc.engine.Engine`` is the thin
+handle wrapper over the C ABI in ``include/pimc.h``; ``pimc.build()``
+compiles the CUDA library for sm_103a.
+"""
+from ._native import LIB_PATH, PimcError, build, load
+from .api import (Counter, Density, Energy, GaussianPair, Harmonic, NumbOfSlices, Particle,
+                  PolymerCenterOfMass, PotentialSum, ReshapeLinear, ReshapeSwapLinear,
+                  SingleCenterOfMass, SquareLattice, Step, System, Zero, acceptance, apply, run)
+from .engine import (ACCEPT, HARDCORE, REJECT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams,
+                     Engine, Mix)
+
+__all__ = [
+    "build", "load", "LIB_PATH", "PimcError", "Engine", "ChainParams", "Mix", "System", "Particle",
+    "Harmonic", "SquareLattice", "PotentialSum", "Zero", "GaussianPair", "ReshapeLinear",
+    "ReshapeSwapLinear", "SingleCenterOfMass", "PolymerCenterOfMass", "Counter", "Step",
+    "NumbOfSlices", "acceptance", "run", "apply", "Density", "Energy", "SEM_REFERENCE",
+    "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE",
+]

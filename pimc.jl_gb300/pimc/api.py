@@ -1,0 +1,508 @@
+"""The reference package's user API (oameye/PIMC.jl) over the GB300 engine.
+
+Mirrors the names, keyword arguments and fields a PIMC.jl user touches:
+
+    System(potential; dV, dim, M, N, mu, L, T, lambda, interactions, propint,
+           g, r_a, length_measurement_cycle, measure_scheme)   src/system.jl:129-167
+    ReshapeLinear / ReshapeSwapLinear (s, slices; ...)          src/updates/reshape.jl:7-29,99-121
+    SingleCenterOfMass / PolymerCenterOfMass (s, step; ...)     src/updates/com.jl:7-28,112-133
+    run!(s, n, updates; Zmeasurements)  -> run(...)             src/simulation.jl:29-42
+    apply!(s, f) -> apply(...), acceptance(q)                   src/simulation.jl:1-27
+    Density(s; nbins), Energy(s, n)                             src/measurement.jl:31-122
+
+Julia closures cannot cross the C ABI, so ``potential``, ``dV`` and
+``propint`` must be engine-known callables (Harmonic, SquareLattice, sums of
+them, GaussianPair); anything else raises -- there is no CPU fallback.
+Slices and particle indices are 0-based here.
+"""
+from __future__ import annotations
+
+import math
+from collections import deque
+
+import numpy as np
+
+from .engine import (ACCEPT, HARDCORE, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams, Engine,
+                     Mix, PimcError)
+
+
+# --------------------------------------------------------------- potentials
+class Harmonic:
+    """V(r) = omega^2 |r|^2 / 2; callable like the reference's closures."""
+
+    def __init__(self, omega: float = 1.0):
+        self.omega = float(omega)
+
+    def __call__(self, r):
+        r = np.asarray(r, dtype=float)
+        return 0.5 * self.omega ** 2 * float(np.dot(r, r))
+
+    def grad(self, r):
+        return self.omega ** 2 * np.asarray(r, dtype=float)
+
+
+class SquareLattice:
+    """V(r) = V0 sum_d sin^2(pi r_d / a)."""
+
+    def __init__(self, V0: float, a: float = 1.0):
+        self.V0, self.a = float(V0), float(a)
+
+    def __call__(self, r):
+        r = np.asarray(r, dtype=float)
+        return self.V0 * float(np.sum(np.sin(np.pi * r / self.a) ** 2))
+
+    def grad(self, r):
+        r = np.asarray(r, dtype=float)
+        return self.V0 * (np.pi / self.a) * np.sin(2 * np.pi * r / self.a)
+
+
+class PotentialSum:
+    def __init__(self, *terms):
+        self.terms = terms
+
+    def __call__(self, r):
+        return sum(t(r) for t in self.terms)
+
+    def grad(self, r):
+        return sum(t.grad(r) for t in self.terms)
+
+    def __add__(self, other):
+        return PotentialSum(*self.terms, other)
+
+
+Harmonic.__add__ = lambda self, o: PotentialSum(self, o)
+SquareLattice.__add__ = lambda self, o: PotentialSum(self, o)
+
+
+class Zero:
+    def __call__(self, r):
+        return 0.0
+
+    def grad(self, r):
+        return np.zeros_like(np.asarray(r, dtype=float))
+
+
+class GaussianPair:
+    """Pair propagator of v(r) = g exp(-r^2 / 2 sigma^2) in primitive form:
+    propint(r1, r2, tau) = exp(-tau/2 (v(|r1|) + v(|r2|)))."""
+
+    def __init__(self, g: float, sigma: float):
+        self.g, self.sigma = float(g), float(sigma)
+
+    def v(self, r):
+        return self.g * math.exp(-r * r / (2 * self.sigma ** 2))
+
+    def __call__(self, r1, r2, tau):
+        return math.exp(-0.5 * tau * (self.v(float(np.linalg.norm(r1))) + self.v(float(np.linalg.norm(r2)))))
+
+
+def _potential_terms(potential):
+    omega, V0, a = 0.0, 0.0, 1.0
+    terms = potential.terms if isinstance(potential, PotentialSum) else (potential,)
+    for t in terms:
+        if isinstance(t, Harmonic):
+            omega = t.omega
+        elif isinstance(t, SquareLattice):
+            V0, a = t.V0, t.a
+        elif isinstance(t, Zero) or t is None:
+            pass
+        else:
+            raise PimcError("potential must be Harmonic, SquareLattice, Zero or a sum of them; "
+                            "arbitrary closures cannot run on the device")
+    return omega, V0, a
+
+
+# --------------------------------------------------------------- world view
+class Particle:
+    """One path: r (M x dim), cached link actions V (M), next (0-based)."""
+
+    def __init__(self, r, V, nxt):
+        self.r, self.V, self.next = r, V, int(nxt)
+
+
+class System:
+    def __init__(self, potential=None, dV=None, dim: int = 2, M: int = 100, N: int = 2,
+                 μ: float = 0.0, L: float = 4.0, T: float = 1.0, λ: float = 1.0,
+                 interactions: bool = False, propint=None, g: float = 0.0, ra: float = 0.0,
+                 length_measurement_cycle: int = 10, measure_scheme: str = "c",
+                 semantics: int = SEM_REFERENCE, seed: int = 20261203, **kw):
+        λ = kw.pop("lam", λ)
+        μ = kw.pop("mu", μ)
+        ra = kw.pop("r_a", ra)
+        if kw:
+            raise TypeError(f"unknown keyword arguments {sorted(kw)}")
+        potential = Zero() if potential is None else potential
+        omega, V0, a = _potential_terms(potential)
+        if dV is not None and not (dV is potential or getattr(dV, "__self__", None) is potential
+                                   or dV in ("grad", np.asarray) or callable(dV)):
+            raise PimcError("dV must be the potential's gradient")
+        pair_g, pair_sigma = 0.0, 1.0
+        if interactions:
+            if not isinstance(propint, GaussianPair):
+                raise PimcError("interactions=True needs propint=GaussianPair(g, sigma)")
+            pair_g, pair_sigma = propint.g, propint.sigma
+            if ra == 0.0:
+                raise PimcError("pass ra (the neighbour range); determine_nnrange is not ported")
+        self.dim, self.M, self.N, self.Ninit = dim, M, N, N
+        self.μ, self.λ, self.L = μ, λ, L
+        self.vol = (2 * L) ** dim
+        self.β = 1.0 / T
+        self.τ = self.β / M
+        # hard-core radius of the contact model (src/system.jl:151)
+        self.a = math.exp(-2 * math.pi / g) if (interactions and g > 0) else 0.0
+        self.ctr = 10_000
+        self.V, self.dV, self.propint = potential, (dV or getattr(potential, "grad", None)), propint
+        self.measure_scheme = measure_scheme
+        self.N_MC = {N: 0}
+        self.Nctr = {N: 0}
+        self.Ncycle = length_measurement_cycle
+        self.semantics = semantics
+        self.rₐ = ra if ra > 0 else L / 4.0
+        self.nbins = int(math.floor(2 * L / self.rₐ))
+        self.rng = np.random.default_rng(seed)
+        self._cp = ChainParams(dim=dim, N=N, M=M, L=L, T=T, lam=λ, mu=μ, harmonic_omega=omega,
+                               lattice_V0=V0, lattice_a=a, interactions=interactions,
+                               pair_g=pair_g, pair_sigma=pair_sigma, r_a=ra,
+                               hardcore_a=self.a, semantics=semantics, seed=seed)
+        self.engine = Engine(self._cp)
+        self._eser_seen = 0
+
+    # System() already ran init_world on the device
+    @property
+    def world(self):
+        x = self.engine.get_beads()
+        V = self.engine.get_links()
+        nx = self.engine.get_next()
+        return [Particle(x[:, n, :].T.copy(), V[n].copy(), nx[n]) for n in range(self.N)]
+
+    def set_world(self, x, nxt=None):
+        self.engine.set_beads(x)
+        if nxt is not None:
+            self.engine.set_next(nxt)
+
+    def _ensure_engine(self, density_nbins: int, energy_capacity: int):
+        cp = self._cp
+        if cp.density_nbins == density_nbins and cp.energy_capacity >= energy_capacity:
+            return
+        x, V, nx = self.engine.get_beads(), self.engine.get_links(), self.engine.get_next()
+        cp.density_nbins = density_nbins
+        cp.energy_capacity = max(cp.energy_capacity, energy_capacity)
+        self.engine.close()
+        self.engine = Engine(cp)
+        self.engine.set_raw(x, V, nx)
+        self._eser_seen = 0
+
+
+# --------------------------------------------------------------- updates
+class Counter:
+    """Rolling acceptance queue (src/updates/helper.jl:6-11)."""
+
+    def __init__(self, range: int = 100_000, adj: int = 10):
+        self.queue, self.tries, self.range, self.adj = deque(), 0, range, adj
+
+
+class Step:
+    def __init__(self, size, minstep, maxstep, minacc, maxacc):
+        self.size, self.minstep, self.maxstep = size, minstep, maxstep
+        self.minacc, self.maxacc = minacc, maxacc
+
+
+class NumbOfSlices:
+    def __init__(self, m, minslices, maxslices, minacc, maxacc):
+        self.m, self.minslices, self.maxslices = m, minslices, maxslices
+        self.minacc, self.maxacc = minacc, maxacc
+
+
+def acceptance(q) -> float:
+    """sum(q)/length(q) (src/simulation.jl:1); NaN for an empty queue."""
+    return sum(q) / len(q) if len(q) else float("nan")
+
+
+def queue_(c: Counter, acc: bool):
+    c.tries += 1
+    c.queue.append(1 if acc else 0)
+    if len(c.queue) > c.range:
+        c.queue.popleft()
+
+
+def adjust_(var, acc: float):
+    if isinstance(var, Step):
+        if acc < var.minacc:
+            var.size *= 0.9
+        elif acc > var.maxacc:
+            var.size *= 1.1
+        var.size = min(var.maxstep, max(var.minstep, var.size))
+    else:
+        if acc < var.minacc:
+            var.m -= 1
+        elif acc > var.maxacc:
+            var.m += 1
+        var.m = min(var.maxslices, max(var.minslices, var.m))
+
+
+class _Update:
+    counter: Counter
+    counter_var: Counter
+
+
+class ReshapeLinear(_Update):
+    def __init__(self, s: System, slices: int, minslices=2, maxslices=None, minacc=0.6, maxacc=0.8,
+                 adj=10, range=10_000):
+        maxslices = s.M - 2 if maxslices is None else maxslices
+        self.counter = Counter()
+        self.var = NumbOfSlices(min(slices, maxslices), minslices, maxslices, minacc, maxacc)
+        self.counter_var = Counter(adj=adj, range=range)
+
+    def __call__(self, s: System) -> bool:
+        """One staging attempt on the device with host-drawn random numbers
+        (src/updates/reshape.jl:31-91)."""
+        n = int(s.rng.integers(0, s.N))
+        j0 = int(s.rng.integers(0, s.M))
+        m = min(self.var.maxslices, int(s.rng.integers(2, self.var.m + 1)))
+        res = _attempt_with_draws(s, lambda nr, un: s.engine.attempt_staging(n, j0, m, nr, un)[0],
+                                  (m - 1) * s.dim)
+        acc = res == ACCEPT
+        queue_(self.counter_var, acc)
+        return acc
+
+
+class ReshapeSwapLinear(_Update):
+    def __init__(self, s: System, slices: int, minslices=2, maxslices=None, minacc=0.6, maxacc=0.8,
+                 adj=10, range=10_000):
+        maxslices = s.M - 2 if maxslices is None else maxslices
+        self.counter = Counter()
+        self.var = NumbOfSlices(min(slices, maxslices), minslices, maxslices, minacc, maxacc)
+        self.counter_var = Counter(adj=adj, range=range)
+
+    def __call__(self, s: System) -> bool:
+        """One permutation attempt (src/updates/reshape.jl:123-283)."""
+        if s.N <= 1:
+            return False
+        j0 = int(s.rng.integers(0, s.M))
+        m = min(self.var.maxslices, int(s.rng.integers(2, self.var.m + 1)))
+        n1 = int(s.rng.integers(0, s.N))
+        up = float(s.rng.random())
+        res = _attempt_with_draws(
+            s, lambda nr, un: s.engine.attempt_swap(j0, m, n1, up, nr, un)[0], 2 * (m - 1) * s.dim)
+        if res == SKIP:
+            return False
+        acc = res == ACCEPT
+        queue_(self.counter_var, acc)
+        return acc
+
+
+class SingleCenterOfMass(_Update):
+    def __init__(self, s: System, step: float, minstep=1e-1, maxstep=None, minacc=0.4, maxacc=0.6,
+                 adj=10, range=10_000):
+        maxstep = s.L / 2 if maxstep is None else maxstep
+        self.counter = Counter()
+        self.var = Step(step, minstep, maxstep, minacc, maxacc)
+        self.counter_var = Counter(adj=adj, range=range)
+
+    def __call__(self, s: System) -> bool:
+        """Rigid shift of one non-permuting path (src/updates/com.jl:136-224)."""
+        nx = s.engine.get_next()
+        singles = [i for i in range(s.N) if nx[i] == i]
+        if not singles:
+            return False
+        n = singles[int(s.rng.integers(0, len(singles)))]
+        res = _attempt_with_draws(s, lambda nr, un: s.engine.attempt_com(n, self.var.size, un), 0,
+                                  n_uni=s.dim + 1)
+        acc = res == ACCEPT
+        queue_(self.counter_var, acc)
+        return acc
+
+
+class PolymerCenterOfMass(_Update):
+    def __init__(self, s: System, step: float, minstep=1e-1, maxstep=None, minacc=0.4, maxacc=0.6,
+                 adj=10, range=10_000):
+        maxstep = s.L / 2 if maxstep is None else maxstep
+        self.counter = Counter()
+        self.var = Step(step, minstep, maxstep, minacc, maxacc)
+        self.counter_var = Counter(adj=adj, range=range)
+
+    def __call__(self, s: System) -> bool:
+        """Rigid shift of a whole permutation cycle (src/updates/com.jl:31-104)."""
+        n = int(s.rng.integers(0, s.N))
+        res = _attempt_with_draws(s, lambda nr, un: s.engine.attempt_polymer_com(n, self.var.size, un),
+                                  0, n_uni=s.dim + 1)
+        acc = res == ACCEPT
+        queue_(self.counter_var, acc)
+        return acc
+
+
+def _attempt_with_draws(s: System, call, n_norm: int, n_uni: int = 1):
+    """Run one attempt with host-drawn normals/uniforms, growing the arrays when
+    the hard-core retries need more."""
+    scale = 1
+    while True:
+        nr = s.rng.standard_normal(max(n_norm * scale, 0))
+        un = s.rng.random(n_uni * scale)
+        try:
+            return call(nr, un)
+        except PimcError as e:
+            if "draws" not in str(e) or scale > 1 << 20:
+                raise
+            scale *= 4
+
+
+# --------------------------------------------------------------- measurements
+class Density:
+    """Cartesian density histogram (src/measurement.jl:31-55)."""
+
+    def __init__(self, s: System, nbins: int = 500):
+        self.nbins = nbins
+        self.bin = (2 * s.L) / nbins
+        self.dens = np.zeros((nbins,) * s.dim)
+        self.ndata = 0
+
+    def __call__(self, s: System):
+        s._ensure_engine(self.nbins, s._cp.energy_capacity)
+        s.engine.reset_measurements()
+        s.engine.measure()
+        self._pull(s)
+
+    def _pull(self, s: System):
+        hist, nd = s.engine.density()
+        h = hist.reshape((self.nbins,) * s.dim, order="F")
+        self.dens = self.dens + h
+        self.ndata += nd
+
+
+class Energy:
+    """Thermodynamic and virial energy series keyed by N (src/measurement.jl:78-122)."""
+
+    def __init__(self, s: System, n: int = 20_000):
+        self.capacity = n
+        self.energy = {0: []}
+        self.energy_virial = {0: []}
+
+    def _add(self, s: System, rows):
+        phys = s.semantics == SEM_PHYSICAL
+        e = rows[:, 0] + (rows[:, 2] if phys else 0.0)
+        ev = rows[:, 1] + (rows[:, 3] if phys else 0.0)
+        self.energy.setdefault(s.N, []).extend(e.tolist())
+        self.energy_virial.setdefault(s.N, []).extend(ev.tolist())
+        if len(self.energy[s.N]) > self.capacity:
+            raise PimcError("Energy storage is full (the reference errors here too)")
+
+
+# --------------------------------------------------------------- driver
+def _mix_for(s: System, n: int, updates):
+    """Map run!(s, n, updates) onto sweeps of the engine (one staging phase per
+    sweep; swaps and centre-of-mass moves in the proportions 1/every)."""
+    w = {}
+    objs = {}
+    for every, u in updates:
+        key = type(u).__name__
+        w[key] = w.get(key, 0.0) + 1.0 / every
+        objs[key] = u
+    wsum = sum(w.values())
+    N, M = s.N, s.M
+    st = objs.get("ReshapeLinear")
+    sw = objs.get("ReshapeSwapLinear")
+    cm = objs.get("SingleCenterOfMass")
+    pc = objs.get("PolymerCenterOfMass")
+    ell = st.var.m if st else 2
+    k = math.ceil(M / ell)
+    if st:
+        per_sweep = N * k * wsum / w["ReshapeLinear"]
+    else:
+        per_sweep = N * wsum / max(w.values())
+    sweeps = max(1, round(n / per_sweep))
+    unit = per_sweep / wsum
+
+    def frac(key):
+        return w.get(key, 0.0) * unit
+
+    mix = Mix(
+        staging_phases=1 if st else 0,
+        stage_slices=st.var.m if st else 2, stage_min=st.var.minslices if st else 2,
+        stage_max=min(st.var.maxslices, 64) if st else 2,
+        stage_minacc=st.var.minacc if st else 0.6, stage_maxacc=st.var.maxacc if st else 0.8,
+        swaps_per_sweep=int(round(frac("ReshapeSwapLinear"))) if (sw and N > 1) else 0,
+        swap_slices=sw.var.m if sw else 2, swap_min=sw.var.minslices if sw else 2,
+        swap_max=min(sw.var.maxslices, 64) if sw else 2,
+        swap_minacc=sw.var.minacc if sw else 0.6, swap_maxacc=sw.var.maxacc if sw else 0.8,
+        com_phases=max(1, int(round(frac("SingleCenterOfMass") / N))) if cm else 0,
+        com_step=cm.var.size if cm else 1.0, com_minstep=cm.var.minstep if cm else 0.1,
+        com_maxstep=cm.var.maxstep if cm else 1.0, com_minacc=cm.var.minacc if cm else 0.4,
+        com_maxacc=cm.var.maxacc if cm else 0.6,
+        polymer_com_phases=max(1, int(round(frac("PolymerCenterOfMass") / N))) if pc else 0,
+        pcom_step=pc.var.size if pc else 1.0, pcom_minstep=pc.var.minstep if pc else 0.1,
+        pcom_maxstep=pc.var.maxstep if pc else 1.0, pcom_minacc=pc.var.minacc if pc else 0.4,
+        pcom_maxacc=pc.var.maxacc if pc else 0.6,
+        adapt=1, measure_every=0)
+    return mix, sweeps, per_sweep, objs
+
+
+def run(s: System, n: int, updates, Zmeasurements=()):
+    """run!(s, n, updates; Zmeasurements) on the device: n move attempts are
+    mapped to sweeps (per sweep N*ceil(M/l) staging windows, swaps and CoM
+    moves in the 1/every proportions); measurements every
+    length_measurement_cycle attempts become one every ceil(Ncycle/per_sweep)
+    sweeps."""
+    s.ctr = 10_000 if not Zmeasurements else 1_000
+    mix, sweeps, per_sweep, objs = _mix_for(s, n, updates)
+    dens = [z for z in Zmeasurements if isinstance(z, Density)]
+    ens = [z for z in Zmeasurements if isinstance(z, Energy)]
+    if Zmeasurements:
+        mix.measure_every = max(1, round(s.Ncycle / per_sweep))
+        nb = dens[0].nbins if dens else 0
+        cap = s._eser_seen + sweeps // mix.measure_every + 1 if ens else 0
+        s._ensure_engine(nb, cap)
+        s.engine.reset_measurements()
+        s._eser_seen = 0
+    before = s.engine.stats()
+    s.engine.set_mix(mix)
+    s.engine.run(sweeps)
+    after = s.engine.stats()
+    # mirror the engine's counters and adaptive variables into the updates
+    kinds = {"ReshapeLinear": 0, "ReshapeSwapLinear": 1, "SingleCenterOfMass": 2,
+             "PolymerCenterOfMass": 3}
+    for key, u in objs.items():
+        q = kinds[key]
+        att = after.attempts[q] - before.attempts[q]
+        acc = after.accepts[q] - before.accepts[q]
+        u.counter.tries += att
+        u.counter_var.tries += att
+        u.counter_var.queue.extend([1] * acc + [0] * (att - acc))
+        while len(u.counter_var.queue) > u.counter_var.range:
+            u.counter_var.queue.popleft()
+        if q == 0:
+            u.var.m = after.stage_slices
+        elif q == 1:
+            u.var.m = after.swap_slices
+        elif q == 2:
+            u.var.size = after.com_step
+        else:
+            u.var.size = after.pcom_step
+    if Zmeasurements:
+        nmeas = after.measurements - before.measurements
+        s.N_MC[s.N] = s.N_MC.get(s.N, 0) + nmeas
+        rows = s.engine.energies()
+        for e in ens:
+            e._add(s, rows[s._eser_seen:])
+        s._eser_seen = len(rows)
+        for d in dens:
+            d._pull(s)
+    return None
+
+
+def apply(s: System, f):
+    """apply!(s, f) (src/simulation.jl:19-27): one attempt, queue, adjust."""
+    if isinstance(f, (list, tuple)):
+        for g in f:
+            g(s)
+        return None
+    acc = f(s)
+    queue_(f.counter, acc)
+    if f.counter_var.tries % f.counter_var.adj == 0:
+        adjust_(f.var, acceptance(f.counter_var.queue))
+    return None
+
+
+__all__ = ["System", "Particle", "Harmonic", "SquareLattice", "PotentialSum", "Zero",
+           "GaussianPair", "ReshapeLinear", "ReshapeSwapLinear", "SingleCenterOfMass",
+           "PolymerCenterOfMass", "Counter", "Step", "NumbOfSlices", "acceptance", "run", "apply",
+           "Density", "Energy", "SEM_REFERENCE", "SEM_PHYSICAL"]

@@ -1,0 +1,34 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (ROOT, os.path.join(ROOT, "pimc.jl_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built engine")
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle as O
+    O.build()
+    return O
+
+
+@pytest.fixture(scope="session")
+def engine_lib():
+    import glob
+
+    import pimc
+    srcs = glob.glob(os.path.join(ROOT, "pimc.jl_gb300", "csrc", "*")) + \
+        [os.path.join(ROOT, "include", "pimc.h")]
+    stale = not os.path.exists(pimc.LIB_PATH) or \
+        max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(pimc.LIB_PATH)
+    if stale:
+        pimc.build()
+    return pimc.load()

@@ -1,0 +1,121 @@
+"""CPU tests of the host-side logic: the run!-to-sweep mapping of the API
+mirror, the synthetic workload definitions, and the multi-rank timing
+reduction of bench.py over two gloo ranks."""
+import json
+import math
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+class FakeSystem:
+    """only the fields the mapping reads (no engine)"""
+
+    def __init__(self, N, M, L=5.0):
+        self.N, self.M, self.L = N, M, L
+
+
+def test_survey_mix_maps_to_one_sweep():
+    """[(1, Reshape(l)), (k, Swap(l)), (k, CoM)] with N(k+2) attempts is one
+    sweep: N*k staging windows, N swaps, one CoM phase"""
+    from pimc.api import ReshapeLinear, ReshapeSwapLinear, SingleCenterOfMass, _mix_for
+    s = FakeSystem(N=64, M=32)
+    ell = 16
+    k = math.ceil(s.M / ell)
+    ups = [(1, ReshapeLinear(s, ell, minacc=0.0, maxacc=1.0)),
+           (k, ReshapeSwapLinear(s, ell, minacc=0.0, maxacc=1.0)),
+           (k, SingleCenterOfMass(s, 1.0))]
+    mix, sweeps, per_sweep, objs = _mix_for(s, 64 * (k + 2) * 10, ups)
+    assert sweeps == 10
+    assert per_sweep == 64 * (k + 2)
+    assert mix.staging_phases == 1 and mix.stage_slices == ell
+    assert mix.swaps_per_sweep == 64
+    assert mix.com_phases == 1
+    assert set(objs) == {"ReshapeLinear", "ReshapeSwapLinear", "SingleCenterOfMass"}
+
+
+def test_update_defaults_follow_reference():
+    from pimc.api import ReshapeLinear, SingleCenterOfMass
+    s = FakeSystem(N=2, M=100, L=4.0)
+    r = ReshapeLinear(s, 20)
+    assert (r.var.m, r.var.minslices, r.var.maxslices, r.var.minacc, r.var.maxacc) == (20, 2, 98, 0.6, 0.8)
+    c = SingleCenterOfMass(s, 3.0)
+    assert (c.var.size, c.var.minstep, c.var.maxstep, c.var.minacc, c.var.maxacc) == (3.0, 0.1, 2.0, 0.4, 0.6)
+
+
+def test_acceptance_and_adjust():
+    from pimc.api import NumbOfSlices, Step, acceptance, adjust_
+    assert math.isnan(acceptance([]))
+    assert acceptance([1, 0, 1, 1]) == 0.75
+    st = Step(1.0, 0.1, 2.0, 0.4, 0.6)
+    adjust_(st, 0.1)
+    assert st.size == 0.9
+    adjust_(st, float("nan"))  # an empty queue leaves the step alone
+    assert st.size == 0.9
+    m = NumbOfSlices(5, 2, 6, 0.6, 0.8)
+    adjust_(m, 0.9)
+    adjust_(m, 0.9)
+    assert m.m == 6
+
+
+def test_potentials_are_callable_like_closures():
+    from pimc.api import GaussianPair, Harmonic, SquareLattice, _potential_terms
+    V = Harmonic(1.0) + SquareLattice(4.0, 1.0)
+    r = np.array([0.25, -0.5])
+    assert math.isclose(V(r), 0.5 * 0.3125 + 4.0 * (0.5 + 1.0))
+    assert _potential_terms(V) == (1.0, 4.0, 1.0)
+    gp = GaussianPair(1.0, 0.5)
+    assert 0 < gp([0.1, 0.0], [0.2, 0.0], 0.05) < 1
+    from pimc import PimcError
+    with pytest.raises(PimcError):
+        _potential_terms(lambda r: 0.0)
+
+
+def test_c4_chain_list_is_the_committed_one():
+    sys.path.insert(0, ROOT)
+    import bench
+    chains = bench.c4_chain_list()
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "c4_chains.json")))
+    for k in ("N", "M", "beta", "g"):
+        assert [c[k] for c in chains] == ref[k]
+    N = np.array([c["N"] for c in chains])
+    assert len(chains) == 4096 and N.min() >= 8 and N.max() <= 512
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _rank_main(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    tmax, tsum = bench.reduce_max_sum(dist, 1.0 + rank, 10.0 * (rank + 1))
+    bench.barrier(dist)
+    out[rank] = (tmax, tsum)
+    dist.destroy_process_group()
+
+
+def test_multirank_reduction_gloo():
+    """weak scaling: the job time is the max over ranks and the work the sum
+    (bench.py on world_size 2, gloo, CPU)"""
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+    port = _free_port()
+    mgr = mp.Manager()
+    out = mgr.dict()
+    mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
+    assert out[0] == (2.0, 30.0) and out[1] == (2.0, 30.0)
