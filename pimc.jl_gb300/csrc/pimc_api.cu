@@ -38,6 +38,7 @@ int fail(int code, const std::string &msg) {
 
 constexpr int kWarpScratchMin = 5 * (64 + 1);  // doubles, window_warp
 constexpr unsigned kStateMagic = 0x50494D43u;   // "PIMC"
+constexpr int kStateBudget = 100 * 1024;        // shared bytes for a staged chain
 
 struct Handle {
   int nchains = 0;
@@ -61,6 +62,8 @@ struct Handle {
   size_t n_buf = 0;
   double *d_adj = nullptr;
   size_t n_adj = 0;
+  double *d_stage = nullptr;   // host-layout positions of every chain (transposes)
+  size_t n_stage = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0.0;
@@ -103,7 +106,7 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   d.N = p.N;
   d.M = p.M;
   d.dim = p.dim;
-  d.ld = p.M;
+  d.ldn = p.N;
   d.L = p.L;
   d.beta = 1.0 / p.T;
   d.tau = d.beta / p.M;
@@ -134,8 +137,9 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   d.key0 = (unsigned)(p.seed & 0xffffffffu);
   d.key1 = (unsigned)(p.seed >> 32);
   d.chain_tag = (unsigned)chain;
-  const int ldm = (p.M & 1) ? p.M : p.M + 1;
-  d.smem_bytes = (int)(8 * (size_t)(p.dim + 1) * p.N * ldm + 4 * (size_t)p.N);
+  const size_t nm = (size_t)p.N * p.M;
+  const size_t sb = 8 * (size_t)(p.dim + 1) * nm + 4 * (size_t)p.dim * nm + 4 * (size_t)p.N;
+  d.smem_bytes = sb > (size_t)(1 << 30) ? (1 << 30) : (int)((sb + 15) & ~(size_t)15);
   return d;
 }
 
@@ -230,17 +234,22 @@ int sync_check(Handle *h) {
   return PIMC_OK;
 }
 
-size_t swap_scratch_bytes(int N, int M) {
-  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64) + sizeof(int) * 4 * (size_t)M;
+size_t swap_scratch_bytes(int N) {
+  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64);
+}
+
+// pol/idx (2N ints, padded) + 3M doubles of the CTA centre-of-mass move
+size_t com_scratch_bytes(int N, int M) {
+  return sizeof(int) * (2 * (size_t)N + 2) + sizeof(double) * 3 * (size_t)M;
 }
 
 // choose the shared-memory plan for a block size
 void plan_smem(Handle *h, int block, int state_cap) {
   const int nw = block / 32;
-  h->warp_scratch_d = std::max(kWarpScratchMin, 3 * h->maxM);
-  size_t scratch = std::max(swap_scratch_bytes(h->maxN, h->maxM),
+  h->warp_scratch_d = kWarpScratchMin;
+  size_t scratch = std::max(swap_scratch_bytes(h->maxN),
                             (size_t)nw * h->warp_scratch_d * sizeof(double));
-  scratch = std::max(scratch, (size_t)2 * h->maxN * sizeof(int));
+  scratch = std::max(scratch, com_scratch_bytes(h->maxN, h->maxM));
   scratch = (scratch + 15) & ~(size_t)15;
   int need_state = 0;
   for (const auto &d : h->desc)
@@ -257,9 +266,9 @@ int upload_desc(Handle *h) {
   return PIMC_OK;
 }
 
-int refresh_links_cells(Handle *h, int chain0, int nch) {
+// cached links V and the FP32 mirror from the positions
+int refresh_links(Handle *h, int chain0, int nch) {
   CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, chain0, nch, h->maxNM, h->stream));
-  CK(launch_cells(h->d_desc, h->d_dpool, h->d_ipool, chain0, nch, h->maxM, h->stream));
   return PIMC_OK;
 }
 
@@ -285,17 +294,14 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     const size_t NM = (size_t)p.N * p.M;
     d.x_off = (long long)dp; dp += (size_t)p.dim * NM;
     d.V_off = (long long)dp; dp += NM;
+    d.xf_off = (long long)dp; dp += ((size_t)p.dim * NM + 1) / 2;
     dp = (dp + 1) & ~(size_t)1;
+    d.host_off = (long long)h->n_stage;
+    h->n_stage += (size_t)p.dim * NM;
     d.tab_off = (long long)dp; dp += 2 * (size_t)d.wtab * d.wtab;
     d.eser_off = p.energy_capacity > 0 ? (long long)dp : -1;
     dp += 4 * (size_t)p.energy_capacity;
     d.next_off = (long long)ip; ip += p.N;
-    if (p.interactions || p.hardcore_a > 0.0) {
-      d.cell_off = (long long)ip;
-      ip += (size_t)p.M * d.ncell + 2 * NM;
-    } else {
-      d.cell_off = -1;
-    }
     if (p.density_nbins > 0) {
       d.dens_off = (long long)up;
       up += p.dim == 2 ? (size_t)p.density_nbins * p.density_nbins : (size_t)p.density_nbins;
@@ -331,7 +337,8 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
       cudaMalloc(&h->d_upool, sizeof(unsigned long long) * h->n_upool) != cudaSuccess ||
       cudaMalloc(&h->d_queue, sizeof(int)) != cudaSuccess ||
       cudaMalloc(&h->d_order, sizeof(int) * nchains) != cudaSuccess ||
-      cudaMalloc(&h->d_iout, sizeof(int) * 16) != cudaSuccess)
+      cudaMalloc(&h->d_iout, sizeof(int) * 16) != cudaSuccess ||
+      cudaMalloc(&h->d_stage, sizeof(double) * std::max<size_t>(h->n_stage, 1)) != cudaSuccess)
     return cleanup(fail(PIMC_ENOMEM, "device allocation failed"));
   cudaMemsetAsync(h->d_dpool, 0, sizeof(double) * h->n_dpool, h->stream);
   cudaMemsetAsync(h->d_upool, 0, sizeof(unsigned long long) * h->n_upool, h->stream);
@@ -373,9 +380,9 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   if (upload_desc(h)) return cleanup(PIMC_ECUDA);
   // System(): init_world, cached links, neighbour grid
   if (launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, nchains, h->maxN, h->stream) != cudaSuccess ||
-      refresh_links_cells(h, 0, nchains))
+      refresh_links(h, 0, nchains))
     return cleanup(fail(PIMC_ECUDA, "initialisation launch failed"));
-  plan_smem(h, h->block, 48 * 1024);
+  plan_smem(h, h->block, kStateBudget);
   if (sync_check(h)) return cleanup(PIMC_ECUDA);
   *out = h;
   return PIMC_OK;
@@ -393,9 +400,10 @@ int set_beads_impl(Handle *h, int chain, const double *x) {
   const ChainDesc &d = h->desc[chain];
   for (size_t i = 0; i < (size_t)d.dim * d.N * d.M; ++i)
     if (!std::isfinite(x[i])) return fail(PIMC_EARG, "non-finite position");
-  CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x, sizeof(double) * d.dim * d.N * d.M,
-                     cudaMemcpyHostToDevice, h->stream));
-  if (refresh_links_cells(h, chain, 1)) return PIMC_ECUDA;
+  const size_t n = (size_t)d.dim * d.N * d.M;
+  CK(cudaMemcpyAsync(h->d_stage + d.host_off, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_import(h->d_desc, h->d_dpool, h->d_stage, chain, 1, n, h->stream));
+  if (refresh_links(h, chain, 1)) return PIMC_ECUDA;
   return sync_check(h);
 }
 
@@ -403,8 +411,9 @@ int get_beads_impl(Handle *h, int chain, double *x) {
   if (check_chain(h, chain)) return PIMC_EARG;
   if (!x) return fail(PIMC_EARG, "null output");
   const ChainDesc &d = h->desc[chain];
-  CK(cudaMemcpyAsync(x, h->d_dpool + d.x_off, sizeof(double) * d.dim * d.N * d.M,
-                     cudaMemcpyDeviceToHost, h->stream));
+  const size_t n = (size_t)d.dim * d.N * d.M;
+  CK(launch_export(h->d_desc, h->d_dpool, h->d_stage, chain, 1, n, h->stream));
+  CK(cudaMemcpyAsync(x, h->d_stage + d.host_off, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
   return sync_check(h);
 }
 
@@ -582,14 +591,12 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
     if (nx != n) return fail(PIMC_EARG, "SingleCenterOfMass needs a particle with next == itself");
   }
   // snapshot of the chain so that a run-out of injected draws leaves no trace
-  const size_t nx = (size_t)d.dim * d.N * d.M, nv = (size_t)d.N * d.M;
-  const size_t ncl = d.cell_off >= 0 ? (size_t)d.M * d.ncell + 2 * nv : 0;
-  std::vector<double> sx(nx), sv(nv);
-  std::vector<int> sn(d.N), scl(ncl);
-  CK(cudaMemcpyAsync(sx.data(), h->d_dpool + d.x_off, nx * 8, cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaMemcpyAsync(sv.data(), h->d_dpool + d.V_off, nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  // x, V and the mirror are contiguous in the pool
+  const size_t nsnap = (size_t)(d.tab_off - d.x_off);
+  std::vector<double> sx(nsnap);
+  std::vector<int> sn(d.N);
+  CK(cudaMemcpyAsync(sx.data(), h->d_dpool + d.x_off, nsnap * 8, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(sn.data(), h->d_ipool + d.next_off, d.N * 4, cudaMemcpyDeviceToHost, h->stream));
-  if (ncl) CK(cudaMemcpyAsync(scl.data(), h->d_ipool + d.cell_off, ncl * 4, cudaMemcpyDeviceToHost, h->stream));
   const size_t nprop = (size_t)2 * (m + 1) * d.dim + 8;
   if (ensure_buf(h, (size_t)n_normals + n_uniforms + nprop + 8)) return PIMC_ENOMEM;
   double *dn = h->d_buf, *du = dn + n_normals, *dprop = du + n_uniforms;
@@ -615,8 +622,8 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   a.prop = proposal ? dprop : nullptr;
   a.out = h->d_iout;
   a.force_warp = h->force_warp;
-  size_t smem = std::max(swap_scratch_bytes(d.N, d.M), (size_t)std::max(kWarpScratchMin, 3 * d.M) * 8);
-  smem = std::max(smem, (size_t)2 * d.N * sizeof(int));
+  size_t smem = std::max(swap_scratch_bytes(d.N), (size_t)kWarpScratchMin * 8);
+  smem = std::max(smem, com_scratch_bytes(d.N, d.M));
   CK(launch_attempt(a, smem, h->stream));
   int out[5] = {0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(out, h->d_iout, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
@@ -627,10 +634,8 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   int rc = sync_check(h);
   if (rc) return rc;
   if (out[4]) {
-    CK(cudaMemcpyAsync(h->d_dpool + d.x_off, sx.data(), nx * 8, cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(h->d_dpool + d.V_off, sv.data(), nv * 8, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_dpool + d.x_off, sx.data(), nsnap * 8, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_ipool + d.next_off, sn.data(), d.N * 4, cudaMemcpyHostToDevice, h->stream));
-    if (ncl) CK(cudaMemcpyAsync(h->d_ipool + d.cell_off, scl.data(), ncl * 4, cudaMemcpyHostToDevice, h->stream));
     sync_check(h);
     return fail(PIMC_EDRAWS, "injected draws ran out; state restored");
   }
@@ -670,6 +675,7 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_iout);
   cudaFree(h->d_buf);
   cudaFree(h->d_adj);
+  cudaFree(h->d_stage);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -692,34 +698,22 @@ int pimc_batch_get_beads(void *handle, int chain, double *x) {
   return get_beads_impl(H(handle), chain, x);
 }
 
-// chains' positions are contiguous in the pool in chain order, each
-// followed by its link row, table and series; copy chain by chain into one
-// pinned-or-pageable host buffer with one async copy per chain and one
-// link/grid refresh for all chains
+// one host<->device copy of the whole batch (host layout, chain order) and
+// one transpose / link refresh launch for all chains
 int pimc_batch_set_beads_all(void *handle, const double *x_all) {
   Handle *h = H(handle);
   if (!h || !x_all) return fail(PIMC_EARG, "null argument");
-  size_t off = 0;
-  for (int c = 0; c < h->nchains; ++c) {
-    const ChainDesc &d = h->desc[c];
-    const size_t n = (size_t)d.dim * d.N * d.M;
-    CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x_all + off, n * 8, cudaMemcpyHostToDevice, h->stream));
-    off += n;
-  }
-  if (refresh_links_cells(h, 0, h->nchains)) return PIMC_ECUDA;
+  CK(cudaMemcpyAsync(h->d_stage, x_all, h->n_stage * 8, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_import(h->d_desc, h->d_dpool, h->d_stage, 0, h->nchains, (size_t)2 * h->maxNM, h->stream));
+  if (refresh_links(h, 0, h->nchains)) return PIMC_ECUDA;
   return sync_check(h);
 }
 
 int pimc_batch_get_beads_all(void *handle, double *x_all) {
   Handle *h = H(handle);
   if (!h || !x_all) return fail(PIMC_EARG, "null argument");
-  size_t off = 0;
-  for (int c = 0; c < h->nchains; ++c) {
-    const ChainDesc &d = h->desc[c];
-    const size_t n = (size_t)d.dim * d.N * d.M;
-    CK(cudaMemcpyAsync(x_all + off, h->d_dpool + d.x_off, n * 8, cudaMemcpyDeviceToHost, h->stream));
-    off += n;
-  }
+  CK(launch_export(h->d_desc, h->d_dpool, h->d_stage, 0, h->nchains, (size_t)2 * h->maxNM, h->stream));
+  CK(cudaMemcpyAsync(x_all, h->d_stage, h->n_stage * 8, cudaMemcpyDeviceToHost, h->stream));
   return sync_check(h);
 }
 
@@ -746,7 +740,7 @@ int pimc_set_next(void *handle, const int *next) {
   const ChainDesc &d = h->desc[0];
   if (check_perm(next, d.N)) return PIMC_ESTATE;
   CK(cudaMemcpyAsync(h->d_ipool + d.next_off, next, sizeof(int) * d.N, cudaMemcpyHostToDevice, h->stream));
-  if (refresh_links_cells(h, 0, 1)) return PIMC_ECUDA;
+  if (refresh_links(h, 0, 1)) return PIMC_ECUDA;
   return sync_check(h);
 }
 
@@ -764,10 +758,15 @@ int pimc_set_raw(void *handle, const double *x, const double *V, const int *next
   if (!h || !x || !V || !next) return fail(PIMC_EARG, "null argument");
   const ChainDesc &d = h->desc[0];
   if (check_perm(next, d.N)) return PIMC_ESTATE;
-  CK(cudaMemcpyAsync(h->d_dpool + d.x_off, x, sizeof(double) * d.dim * d.N * d.M, cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->d_dpool + d.V_off, V, sizeof(double) * d.N * d.M, cudaMemcpyHostToDevice, h->stream));
+  const size_t n = (size_t)d.dim * d.N * d.M;
+  std::vector<double> vt((size_t)d.N * d.M);
+  for (int i = 0; i < d.N; ++i)
+    for (int j = 0; j < d.M; ++j) vt[(size_t)j * d.N + i] = V[(size_t)i * d.M + j];
+  CK(cudaMemcpyAsync(h->d_stage + d.host_off, x, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+  CK(launch_import(h->d_desc, h->d_dpool, h->d_stage, 0, 1, n, h->stream));
+  CK(cudaMemcpyAsync(h->d_dpool + d.V_off, vt.data(), sizeof(double) * vt.size(), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->d_ipool + d.next_off, next, sizeof(int) * d.N, cudaMemcpyHostToDevice, h->stream));
-  CK(launch_cells(h->d_desc, h->d_dpool, h->d_ipool, 0, 1, h->maxM, h->stream));
+  CK(launch_mirror(h->d_desc, h->d_dpool, 0, 1, h->maxNM, h->stream));
   return sync_check(h);
 }
 
@@ -775,15 +774,20 @@ int pimc_get_links(void *handle, double *V) {
   Handle *h = H(handle);
   if (!h || !V) return fail(PIMC_EARG, "null argument");
   const ChainDesc &d = h->desc[0];
-  CK(cudaMemcpyAsync(V, h->d_dpool + d.V_off, sizeof(double) * d.N * d.M, cudaMemcpyDeviceToHost, h->stream));
-  return sync_check(h);
+  std::vector<double> vt((size_t)d.N * d.M);
+  CK(cudaMemcpyAsync(vt.data(), h->d_dpool + d.V_off, sizeof(double) * vt.size(), cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  for (int i = 0; i < d.N; ++i)
+    for (int j = 0; j < d.M; ++j) V[(size_t)i * d.M + j] = vt[(size_t)j * d.N + i];
+  return PIMC_OK;
 }
 
 int pimc_init_world(void *handle) {
   Handle *h = H(handle);
   if (!h) return fail(PIMC_EARG, "null handle");
   CK(launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, h->nchains, h->maxN, h->stream));
-  if (refresh_links_cells(h, 0, h->nchains)) return PIMC_ECUDA;
+  if (refresh_links(h, 0, h->nchains)) return PIMC_ECUDA;
   return sync_check(h);
 }
 
@@ -841,7 +845,7 @@ int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch) {
   if (sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
   h->block = block;
   h->spl = sweeps_per_launch;
-  plan_smem(h, block, 48 * 1024);
+  plan_smem(h, block, kStateBudget);
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
@@ -1143,16 +1147,15 @@ int pimc_get_total_stats(void *handle, pimc_stats *out) {
   return PIMC_OK;
 }
 
-// checkpoint layout: magic, version, nchains, then per chain the raw device
-// regions (x, V, next, cells, density, energy series) and ChainVar
+// checkpoint layout: magic, version, nchains, then per chain ChainVar and the
+// raw device regions (positions, links and FP32 mirror, next, density,
+// energy series)
 int pimc_state_size(void *handle, size_t *bytes) {
   Handle *h = H(handle);
   if (!h || !bytes) return fail(PIMC_EARG, "null argument");
   size_t b = 3 * sizeof(unsigned);
   for (const auto &d : h->desc) {
-    const size_t nm = (size_t)d.N * d.M;
-    b += sizeof(ChainVar) + 8 * ((size_t)d.dim * nm + nm) + 4 * (size_t)d.N;
-    if (d.cell_off >= 0) b += 4 * ((size_t)d.M * d.ncell + 2 * nm);
+    b += sizeof(ChainVar) + 8 * (size_t)(d.tab_off - d.x_off) + 4 * (size_t)d.N;
     if (d.dens_off >= 0) b += 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb);
     if (d.eser_off >= 0) b += 8 * 4 * (size_t)d.eser_cap;
   }
@@ -1183,12 +1186,9 @@ static int state_io(Handle *h, char *buf, size_t bytes, bool save) {
   };
   for (int c = 0; c < h->nchains; ++c) {
     const ChainDesc &d = h->desc[c];
-    const size_t nm = (size_t)d.N * d.M;
     CK(io(h->d_var + c, sizeof(ChainVar)));
-    CK(io(h->d_dpool + d.x_off, 8 * (size_t)d.dim * nm));
-    CK(io(h->d_dpool + d.V_off, 8 * nm));
+    CK(io(h->d_dpool + d.x_off, 8 * (size_t)(d.tab_off - d.x_off)));
     CK(io(h->d_ipool + d.next_off, 4 * (size_t)d.N));
-    if (d.cell_off >= 0) CK(io(h->d_ipool + d.cell_off, 4 * ((size_t)d.M * d.ncell + 2 * nm)));
     if (d.dens_off >= 0) CK(io(h->d_upool + d.dens_off, 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb)));
     if (d.eser_off >= 0) CK(io(h->d_dpool + d.eser_off, 8 * 4 * (size_t)d.eser_cap));
   }

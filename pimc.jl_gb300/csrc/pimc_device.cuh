@@ -1,18 +1,25 @@
 // pimc_device.cuh -- device building blocks of the sweep: counter-based
-// random numbers, the action pieces, the cell grid, and the moves
-// (Levy staging window, permutation swap, centre-of-mass shifts) written once
-// and shared by the sweep kernels and the injected-draw attempt kernels.
+// random numbers, the action pieces, neighbour scans, and the staging
+// window written once and shared by the sweep kernels and the injected-draw
+// attempt kernels.
+//
+// Layout: positions are slice-major on the device, x[d][j][n] (all particles
+// of one imaginary-time slice contiguous), cached links V[j][n].  Thread-per-
+// window staging reads slices of consecutive particles (coalesced), and a
+// neighbour query at slice j is a contiguous row.  Chains with a pair action
+// or a hard core keep an FP32 mirror xf[j][n] of the positions: a warp scans
+// the row in FP32 with a safety margin and evaluates the few candidates near
+// the cut-off exactly in FP64, so the neighbour set is exactly the
+// reference's (every bead within 2L/nbins, src/nearest_neighbours.jl:131-154)
+// without a linked cell grid to chase or maintain.
 //
 // Reference correspondence (oameye/PIMC.jl):
 //   distance / lnK / lnV / teleport      src/propagator.jl:6-32
 //   lnU (Gaussian propint)               src/system.jl:26-28
-//   cell grid                            src/nearest_neighbours.jl:26-209
+//   neighbour set                        src/nearest_neighbours.jl:106-179
 //   metropolis                           src/updates/helper.jl:3-5
 //   hardspherelevy!                      src/updates/helper.jl:141-222
 //   ReshapeLinear                        src/updates/reshape.jl:31-91
-//   ReshapeSwapLinear / sampleparticles  src/updates/reshape.jl:123-283, helper.jl:224-267
-//   SingleCenterOfMass / Polymer...      src/updates/com.jl:31-224
-//   Density / Energy                     src/measurement.jl:45-122
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -150,22 +157,35 @@ struct InjDraws {
 };
 
 // ---------------------------------------------------------------------------
-// chain view: x/V/next may live in shared or global memory (generic pointers)
+// chain view: x/V/next/xf may live in shared or global memory (generic pointers)
 // ---------------------------------------------------------------------------
 struct CV {
   const ChainDesc *d;
-  double *x;          // x[(k*N + n)*ld + j]
-  double *V;          // V[n*ld + j]
+  double *x;          // x[(k*M + j)*ldn + n]
+  double *V;          // V[j*ldn + n]
   int *next;
-  int *head, *cn, *cp;  // cell lists (global)
-  const double2 *tab;   // (alpha, sigma)[m*wtab + t]
+  float *xf;          // FP32 mirror [(j*ldn + n)*dim + k], or null
+  const double2 *tab; // (alpha, sigma)[m*wtab + t]
   unsigned long long *hist;
   double *eser;
-  int N, M, dim, ld;
+  int N, M, dim, ldn;
   __device__ __forceinline__ double &X(int k, int n, int j) const {
-    return x[((size_t)k * N + n) * ld + j];
+    return x[((size_t)k * M + j) * ldn + n];
   }
-  __device__ __forceinline__ double &Vl(int n, int j) const { return V[(size_t)n * ld + j]; }
+  __device__ __forceinline__ double &Vl(int n, int j) const { return V[(size_t)j * ldn + n]; }
+  __device__ __forceinline__ double Xd(int k, int n, int j) const {
+    return k < dim ? X(k, n, j) : 0.0;
+  }
+  // every position write goes through here so that the FP32 mirror follows
+  __device__ __forceinline__ void set_pos(int n, int j, double px, double py) const {
+    X(0, n, j) = px;
+    if (dim > 1) X(1, n, j) = py;
+    if (xf) {
+      float *f = xf + ((size_t)j * ldn + n) * dim;
+      f[0] = (float)px;
+      if (dim > 1) f[1] = (float)py;
+    }
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -236,74 +256,6 @@ __device__ __forceinline__ double2 bridge_coef(const CV &c, int m, int t) {
   return make_double2(a, sqrt(2.0 * c.d->lambda * a * c.d->tau));
 }
 
-// ---------------------------------------------------------------------------
-// cell grid (src/nearest_neighbours.jl)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ int cell_of(const ChainDesc &d, double x, double y) {
-  const double w = 2.0 * d.L / d.nbins;
-  int ix = (int)floor((x + d.L) / w);
-  ix = ix < 0 ? 0 : (ix >= d.nbins ? d.nbins - 1 : ix);
-  if (d.dim == 1) return ix;
-  int iy = (int)floor((y + d.L) / w);
-  iy = iy < 0 ? 0 : (iy >= d.nbins ? d.nbins - 1 : iy);
-  return ix + d.nbins * iy;
-}
-
-// 3x3 stencil (bin_neighbors, nearest_neighbours.jl:55-65) without duplicates
-__device__ __forceinline__ int stencil(const ChainDesc &d, int c, int *out) {
-  const int nb = d.nbins;
-  int k = 0;
-  if (d.dim == 1) {
-    const int cand[3] = {c, (c - 1 + nb) % nb, (c + 1) % nb};
-    for (int i = 0; i < 3; ++i) {
-      bool dup = false;
-      for (int q = 0; q < k; ++q) dup |= out[q] == cand[i];
-      if (!dup) out[k++] = cand[i];
-    }
-    return k;
-  }
-  const int x = c % nb, y = c / nb;
-  for (int dy = -1; dy <= 1; ++dy)
-    for (int dx = -1; dx <= 1; ++dx) {
-      const int cc = ((x + dx + nb) % nb) + nb * ((y + dy + nb) % nb);
-      bool dup = false;
-      for (int q = 0; q < k; ++q) dup |= out[q] == cc;
-      if (!dup) out[k++] = cc;
-    }
-  return k;
-}
-
-__device__ __forceinline__ void cell_move(const CV &c, int n, int j, int c_old, int c_new) {
-  if (c_old == c_new) return;
-  const int N = c.N;
-  int *nx = c.cn + (size_t)j * N, *pv = c.cp + (size_t)j * N;
-  int *h = c.head + (size_t)j * c.d->ncell;
-  const int p = pv[n], q = nx[n];
-  if (p >= 0) nx[p] = q; else h[c_old] = q;
-  if (q >= 0) pv[q] = p;
-  const int hh = h[c_new];
-  nx[n] = hh;
-  pv[n] = -1;
-  if (hh >= 0) pv[hh] = n;
-  h[c_new] = n;
-}
-
-// rebuild the lists of one slice from positions (ascending particle order)
-__device__ __forceinline__ void cells_rebuild_slice(const CV &c, int j) {
-  const ChainDesc &d = *c.d;
-  int *h = c.head + (size_t)j * d.ncell;
-  int *nx = c.cn + (size_t)j * c.N, *pv = c.cp + (size_t)j * c.N;
-  for (int q = 0; q < d.ncell; ++q) h[q] = -1;
-  for (int n = c.N - 1; n >= 0; --n) {
-    const int cc = cell_of(d, c.X(0, n, j), c.dim > 1 ? c.X(1, n, j) : 0.0);
-    const int hh = h[cc];
-    nx[n] = hh;
-    pv[n] = -1;
-    if (hh >= 0) pv[hh] = n;
-    h[cc] = n;
-  }
-}
-
 __device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, double bx,
                                       double by) {
   const double dx = dist1(ax, bx, d.L);
@@ -315,52 +267,96 @@ __device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, 
   return s;
 }
 
-// sum over neighbours b of the moving bead (a at slice j, an its next bead
-// along the moving path) of lnU(d(a,b_j), d(an, b_next)), neighbours within
-// 2L/nbins found through the 3x3 stencil (find_nns, nearest_neighbours.jl:131-154)
-__device__ double pair_link(const CV &c, double ax, double ay, double anx, double any, int j,
-                            int e1, int e2) {
+// ---------------------------------------------------------------------------
+// neighbour scans over one slice
+// ---------------------------------------------------------------------------
+// FP32 prefilter: min-image squared distance in FP32 plus a margin that
+// covers the FP32 rounding of positions within [-L, L] (|err| of each
+// coordinate difference <= 4 L 2^-24), so every pair within r of the exact
+// FP64 distance passes the filter.
+struct Prefilter {
+  float L2f, ax, ay;
+  float lim;   // squared radius plus margin
+  int dim;
+  __device__ __forceinline__ void init(const ChainDesc &d, double px, double py, double r) {
+    dim = d.dim;
+    L2f = (float)(2.0 * d.L);
+    ax = (float)px;
+    ay = (float)py;
+    const double e = 4.0 * d.L * 5.9604644775390625e-8 + 1e-30;
+    lim = (float)((r + 2.0 * e) * (r + 2.0 * e) * (1.0 + 1e-6) + 1e-12);
+  }
+  __device__ __forceinline__ bool pass(const float *p) const {
+    float dx = fabsf(ax - p[0]);
+    dx = fminf(dx, L2f - dx);
+    float s = dx * dx;
+    if (dim > 1) {
+      float dy = fabsf(ay - p[1]);
+      dy = fminf(dy, L2f - dy);
+      s = fmaf(dy, dy, s);
+    }
+    return s <= lim;
+  }
+};
+
+// pair terms of one link of a moving path, old and new in one pass over the
+// slice: for every other bead b at slice j within rc of the old bead (a) add
+// lnU(d(a, b_j), d(an, b_next)) to wo, and within rc of the new bead (p) add
+// lnU(d(p, b_j), d(pn, b_next)) to wn.  Old terms skip b in {eo1, eo2}, new
+// terms b in {en1, en2}; with excl != null both skip every b with
+// excl[b] >= 0.  Lanes split the particles; the sums are per lane.
+__device__ __forceinline__ void pair_link_lanes(const CV &c, int j, int eo1, int eo2, int en1,
+                                                int en2, const int *excl, bool do_old,
+                                                bool do_new, double ax, double ay, double anx,
+                                                double any, double px, double py, double pnx,
+                                                double pny, double &wo, double &wn, int lane,
+                                                int lanes) {
   const ChainDesc &d = *c.d;
-  const int M = c.M, N = c.N;
+  const int N = c.N, M = c.M, dim = c.dim;
   const int jn = (j + 1 == M) ? 0 : j + 1;
   const double rc2 = d.rc * d.rc;
-  int cells[9];
-  const int nc = stencil(d, cell_of(d, ax, ay), cells);
-  double w = 0.0;
-  for (int ci = 0; ci < nc; ++ci) {
-    for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
-      if (b == e1 || b == e2) continue;
-      const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.dim > 1 ? c.X(1, b, j) : 0.0);
-      if (r2a > rc2) continue;
-      const int bn = (j == M - 1) ? c.next[b] : b;
-      const double r2b = mi2(d, anx, any, c.X(0, bn, jn), c.dim > 1 ? c.X(1, bn, jn) : 0.0);
-      w += lnU2(d, r2a, r2b);
+  Prefilter fo, fn;
+  fo.init(d, ax, ay, d.rc);
+  fn.init(d, px, py, d.rc);
+  const float *row = c.xf + (size_t)j * c.ldn * dim;
+  for (int b = lane; b < N; b += lanes) {
+    const float *pb = row + (size_t)b * dim;
+    bool po = do_old && fo.pass(pb), pnw = do_new && fn.pass(pb);
+    if (!(po || pnw)) continue;
+    if (excl && excl[b] >= 0) continue;
+    po = po && b != eo1 && b != eo2;
+    pnw = pnw && b != en1 && b != en2;
+    if (!(po || pnw)) continue;
+    const double bx = c.X(0, b, j), by = c.Xd(1, b, j);
+    const int bn = (j == M - 1) ? c.next[b] : b;
+    const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
+    if (po) {
+      const double r2a = mi2(d, ax, ay, bx, by);
+      if (r2a <= rc2) wo += lnU2(d, r2a, mi2(d, anx, any, bnx, bny));
+    }
+    if (pnw) {
+      const double r2a = mi2(d, px, py, bx, by);
+      if (r2a <= rc2) wn += lnU2(d, r2a, mi2(d, pnx, pny, bnx, bny));
     }
   }
-  return w;
 }
 
-__device__ __forceinline__ double pair_cross(const ChainDesc &d, double ax, double ay, double anx,
-                                             double any, double bx, double by, double bnx,
-                                             double bny) {
-  const double r2a = mi2(d, ax, ay, bx, by);
-  if (r2a > d.rc * d.rc) return 0.0;
-  return lnU2(d, r2a, mi2(d, anx, any, bnx, bny));
-}
-
-// hard-core test (find_nn + distance < a, src/updates/helper.jl:167-169)
-__device__ bool hard_hit(const CV &c, double x, double y, int j, int e1, int e2) {
+// any bead other than e1/e2 at slice j closer than the hard-core radius
+// (find_nn + distance < a, src/updates/helper.jl:167-169); per-lane result
+__device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, int j, int e1,
+                                               int e2, int lane, int lanes) {
   const ChainDesc &d = *c.d;
+  const int N = c.N, dim = c.dim;
   const double a2 = d.hard_a * d.hard_a;
-  int cells[9];
-  const int nc = stencil(d, cell_of(d, x, y), cells);
-  for (int ci = 0; ci < nc; ++ci)
-    for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0;
-         b = c.cn[(size_t)j * c.N + b]) {
-      if (b == e1 || b == e2) continue;
-      if (mi2(d, x, y, c.X(0, b, j), c.dim > 1 ? c.X(1, b, j) : 0.0) < a2) return true;
-    }
-  return false;
+  Prefilter f;
+  f.init(d, x, y, d.hard_a);
+  const float *row = c.xf + (size_t)j * c.ldn * dim;
+  bool hit = false;
+  for (int b = lane; b < N && !hit; b += lanes) {
+    if (b == e1 || b == e2 || !f.pass(row + (size_t)b * dim)) continue;
+    if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;
+  }
+  return hit;
 }
 
 // ---------------------------------------------------------------------------
@@ -391,8 +387,8 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
   const int jend = j0 + m;
   const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
   double bx[TWMAX + 1], by[TWMAX + 1], vp[TWMAX];
-  const double sx = c.X(0, n, j0), sy = dim > 1 ? c.X(1, n, j0) : 0.0;
-  double ex = c.X(0, oe, je), ey = dim > 1 ? c.X(1, oe, je) : 0.0;
+  const double sx = c.X(0, n, j0), sy = c.Xd(1, n, j0);
+  double ex = c.X(0, oe, je), ey = c.Xd(1, oe, je);
   if (fabs(sx - ex) > L) ex += sgn(sx) * (2.0 * L);
   if (dim > 1 && fabs(sy - ey) > L) ey += sgn(sy) * (2.0 * L);
   double px = sx, py = sy;
@@ -436,10 +432,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
     for (int t = 0; t < m; ++t) {
       const int a = j0 + t;
       const int o = a < M ? n : nx, j = a < M ? a : a - M;
-      if (t > 0 || rewrite_start) {
-        c.X(0, o, j) = bx[t];
-        if (dim > 1) c.X(1, o, j) = by[t];
-      }
+      if (t > 0 || rewrite_start) c.set_pos(o, j, bx[t], by[t]);
       c.Vl(o, j) = vp[t];
     }
   }
@@ -452,7 +445,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
 // ---------------------------------------------------------------------------
 template <class D>
 __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
-                           double *sb, double *prop, bool update_cells) {
+                           double *sb, double *prop) {
   const ChainDesc &d = *c.d;
   const int lane = threadIdx.x & 31;
   const int M = c.M, dim = c.dim;
@@ -464,8 +457,8 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   const int nx = c.next[n];
   const int jend = j0 + m;
   const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
-  const double sx = c.X(0, n, j0), sy = dim > 1 ? c.X(1, n, j0) : 0.0;
-  double ex = c.X(0, oe, je), ey = dim > 1 ? c.X(1, oe, je) : 0.0;
+  const double sx = c.X(0, n, j0), sy = c.Xd(1, n, j0);
+  double ex = c.X(0, oe, je), ey = c.Xd(1, oe, je);
   if (fabs(sx - ex) > L) ex += sgn(sx) * (2.0 * L);
   if (dim > 1 && fabs(sy - ey) > L) ey += sgn(sy) * (2.0 * L);
   int fail = 0;
@@ -488,10 +481,10 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
         dst[t] = p;
       }
     }
-  } else if (lane == 0) {
-    // sequential retries in the reference's draw order; the reference
-    // excludes the start particle (fpcycle of the wrapped slice) in its
-    // find_nn, the physical semantics excludes the bead's true owner
+  } else {
+    // sequential retries in the reference's draw order (lane 0 draws, the warp
+    // scans the slice); the reference excludes the start particle (fpcycle of
+    // the wrapped slice) in its find_nn, the physical semantics the true owner
     double px = sx, py = sy;
     for (int t = 1; t < m && !fail; ++t) {
       const double2 ab = bridge_coef(c, m, t);
@@ -500,17 +493,24 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
       int tries = 0;
       while (true) {
         if (++tries > d.ctr) { fail = 1; break; }
-        double z0 = dr.normal(), z1 = dim > 1 ? dr.normal() : 0.0;
-        const double qx = ab.x * px + (1.0 - ab.x) * ex + z0 * ab.y;
-        const double qy = dim > 1 ? ab.x * py + (1.0 - ab.x) * ey + z1 * ab.y : 0.0;
+        double qx = 0.0, qy = 0.0;
+        if (lane == 0) {
+          const double z0 = dr.normal(), z1 = dim > 1 ? dr.normal() : 0.0;
+          qx = ab.x * px + (1.0 - ab.x) * ex + z0 * ab.y;
+          qy = dim > 1 ? ab.x * py + (1.0 - ab.x) * ey + z1 * ab.y : 0.0;
+        }
+        qx = __shfl_sync(0xffffffffu, qx, 0);
+        qy = __shfl_sync(0xffffffffu, qy, 0);
         const double tx = teleport(qx, L, inv2L), ty = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
-        if (!hard_hit(c, tx, ty, j, exc, -1)) { px = qx; py = qy; break; }
+        const bool hit = __any_sync(0xffffffffu, hard_hit_lanes(c, tx, ty, j, exc, -1, lane, 32));
+        if (!hit) { px = qx; py = qy; break; }
       }
-      sx_[t] = px;
-      sy_[t] = py;
+      if (lane == 0) {
+        sx_[t] = px;
+        sy_[t] = py;
+      }
     }
   }
-  fail = __shfl_sync(0xffffffffu, fail, 0);
   __syncwarp();
   if (fail) return RES_HARDCORE;
   for (int t = lane; t <= m; t += 32) {
@@ -526,15 +526,18 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   double wi = 0.0, wu = 0.0;
   for (int t = lane; t < m; t += 32) {
     const int a = j0 + t;
-    const int o = a < M ? n : nx, j = a < M ? a : a - M;
-    wi += c.Vl(o, j);
+    wi += c.Vl(a < M ? n : nx, a < M ? a : a - M);
     wu += mhtau * (svb[t] + svb[t + 1]);
-    if (phys_pair) {
-      const int a1 = a + 1;
+  }
+  if (phys_pair) {
+    // one warp-wide pass over the slice per link, old and new together
+    for (int t = 0; t < m; ++t) {
+      const int a = j0 + t, a1 = a + 1;
+      const int o = a < M ? n : nx, j = a < M ? a : a - M;
       const int o1 = a1 < M ? n : nx, j1 = a1 < M ? a1 : a1 - M;
-      wi += pair_link(c, c.X(0, o, j), dim > 1 ? c.X(1, o, j) : 0.0, c.X(0, o1, j1),
-                      dim > 1 ? c.X(1, o1, j1) : 0.0, j, o, -1);
-      wu += pair_link(c, sx_[t], sy_[t], sx_[t + 1], sy_[t + 1], j, o, -1);
+      pair_link_lanes(c, j, o, -1, o, -1, nullptr, true, true, c.X(0, o, j), c.Xd(1, o, j),
+                      c.X(0, o1, j1), c.Xd(1, o1, j1), sx_[t], sy_[t], sx_[t + 1], sy_[t + 1], wi,
+                      wu, lane, 32);
     }
   }
   wi = warp_sum(wi);
@@ -554,15 +557,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     for (int t = lane; t < m; t += 32) {
       const int a = j0 + t;
       const int o = a < M ? n : nx, j = a < M ? a : a - M;
-      if (t > 0 || rewrite_start) {
-        if (update_cells) {
-          const int co = cell_of(d, c.X(0, o, j), dim > 1 ? c.X(1, o, j) : 0.0);
-          const int cnw = cell_of(d, sx_[t], sy_[t]);
-          cell_move(c, o, j, co, cnw);
-        }
-        c.X(0, o, j) = sx_[t];
-        if (dim > 1) c.X(1, o, j) = sy_[t];
-      }
+      if (t > 0 || rewrite_start) c.set_pos(o, j, sx_[t], sy_[t]);
       c.Vl(o, j) = mhtau * (svb[t] + svb[t + 1]);
     }
   }

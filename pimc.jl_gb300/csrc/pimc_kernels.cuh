@@ -1,12 +1,12 @@
-// pimc_kernels.cuh -- CTA-level moves (permutation swap, centre-of-mass
-// shifts), estimators, and the sweep driver executed by one CTA per chain.
+// pimc_kernels.cuh -- warp/CTA-level moves (permutation swap, centre-of-mass
+// shifts) and the estimators.
 #pragma once
 #include "pimc_device.cuh"
 
 namespace pimc {
 
 // ---------------------------------------------------------------------------
-// block reductions (red: >= 256 doubles of shared memory; K <= 6)
+// block reductions (red: >= 256 doubles of shared memory; K <= 8)
 // ---------------------------------------------------------------------------
 template <int K>
 __device__ __forceinline__ void block_sum_k(double (&v)[K], double *red) {
@@ -26,145 +26,169 @@ __device__ __forceinline__ void block_sum_k(double (&v)[K], double *red) {
   __syncthreads();
 }
 
-template <int K>
-__device__ __forceinline__ void block_max_k(double (&v)[K], double *red) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int k = 0; k < K; ++k) v[k] = warp_max(v[k]);
-  __syncthreads();
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < K; ++k) red[k * 32 + w] = v[k];
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    double s = lane < nw ? red[k * 32 + lane] : -INFINITY;
-    v[k] = warp_max(s);
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ int block_min_int(int v, int *ired) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if (lane == 0) ired[w] = v;
-  __syncthreads();
-  int s = lane < nw ? ired[lane] : 0x7fffffff;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s = min(s, __shfl_xor_sync(0xffffffffu, s, o));
-  __syncthreads();
-  return s;
-}
-
-// exclusive prefix over the block of one double per thread
-__device__ __forceinline__ double block_exclusive_scan(double v, double *red) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  double incl = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double t = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += t;
-  }
-  __syncthreads();
-  if (lane == 31) red[w] = incl;
-  __syncthreads();
-  double base = 0.0;
-  for (int q = 0; q < w && q < nw; ++q) base += red[q];
-  __syncthreads();
-  return base + incl - v;
-}
-
 __device__ __forceinline__ double logaddexp(double a, double b) {
   const double mx = fmax(a, b);
   if (mx == -INFINITY) return -INFINITY;
   return mx + log(exp(a - mx) + exp(b - mx));
 }
 
-// shared scratch of the swap: doubles then ints
-struct SwapScratch {
-  double *w;              // N heat-bath weights
-  double *r1x, *r1y, *r2x, *r2y, *vb1, *vb2;  // WMAX+1 each
-  double *z;              // 2*WMAX*2 normals
-  int *pa, *pb, *ca, *cb; // M each
-  static __host__ __device__ size_t bytes(int N, int M) {
-    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX) + sizeof(int) * 4 * (size_t)M;
+// exclusive prefix over the warp of one double per lane
+__device__ __forceinline__ double warp_exclusive_scan(double v) {
+  const int lane = threadIdx.x & 31;
+  double incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
   }
-  __device__ void carve(void *base, int N, int M) {
+  return incl - v;
+}
+
+__device__ __forceinline__ int warp_min_int(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// shared scratch of the swap
+struct SwapScratch {
+  double *w;                                   // N heat-bath weights
+  double *r1x, *r1y, *r2x, *r2y, *vb1, *vb2;   // WMAX+1 each
+  double *z;                                   // 4*WMAX normals
+  static __host__ __device__ size_t bytes(int N) {
+    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX);
+  }
+  __device__ void carve(void *base, int N) {
     double *p = (double *)base;
     w = p; p += N;
     r1x = p; p += WMAX + 1; r1y = p; p += WMAX + 1;
     r2x = p; p += WMAX + 1; r2y = p; p += WMAX + 1;
     vb1 = p; p += WMAX + 1; vb2 = p; p += WMAX + 1;
-    z = p; p += 4 * WMAX;
-    int *q = (int *)p;
-    pa = q; q += M; pb = q; q += M; ca = q; q += M; cb = q;
+    z = p;
+  }
+};
+
+// heat-bath exponent -(|s - E|^2 + |x_i(j0) - f|^2) / (4 lambda m tau) with
+// E the end bead of particle i's path (or an explicit end): FP64 as the
+// reference (attempt parity), or FP32 from the position mirror (sweeps: the
+// proposal weights are then a deterministic FP32 function of the
+// configuration, and the physical ratio uses the same function, so detailed
+// balance is exact)
+template <bool FAST>
+struct HeatBath {
+  const CV *c;
+  double inv_den;
+  float inv_denf, L2f;
+  int se, j0;
+  bool wrap;
+  __device__ __forceinline__ int endp(int i) const { return wrap ? c->next[i] : i; }
+  __device__ __forceinline__ float d2f(float a, float b, float a2, float b2) const {
+    float dx = fabsf(a - b);
+    dx = fminf(dx, L2f - dx);
+    float s = dx * dx;
+    if (c->dim > 1) {
+      float dy = fabsf(a2 - b2);
+      dy = fminf(dy, L2f - dy);
+      s = fmaf(dy, dy, s);
+    }
+    return s;
+  }
+  // E = bead (endp(i), se) unless ex_given
+  __device__ __forceinline__ double expo(int i, double sx, double sy, double fx, double fy,
+                                         bool ex_given = false, double ex = 0.0,
+                                         double ey = 0.0) const {
+    const ChainDesc &d = *c->d;
+    if (!FAST) {
+      if (!ex_given) {
+        const int ei = endp(i);
+        ex = c->X(0, ei, se);
+        ey = c->Xd(1, ei, se);
+      }
+      const double t1 = mi2(d, sx, sy, ex, ey);
+      const double t2 = mi2(d, c->X(0, i, j0), c->Xd(1, i, j0), fx, fy);
+      return -(t1 + t2) * inv_den;
+    } else {
+      const int dim = c->dim;
+      float efx, efy = 0.f;
+      if (!ex_given) {
+        const float *pe = c->xf + ((size_t)se * c->ldn + endp(i)) * dim;
+        efx = pe[0];
+        if (dim > 1) efy = pe[1];
+      } else {
+        efx = (float)ex;
+        efy = (float)ey;
+      }
+      const float *pi = c->xf + ((size_t)j0 * c->ldn + i) * dim;
+      const float s = d2f((float)sx, efx, (float)sy, efy) +
+                      d2f(pi[0], (float)fx, dim > 1 ? pi[1] : 0.f, (float)fy);
+      return (double)(-s * inv_denf);
+    }
+  }
+  __device__ __forceinline__ double ex_(double v) const {
+    return FAST ? (double)__expf((float)v) : exp(v);
   }
 };
 
 // ---------------------------------------------------------------------------
-// permutation swap, whole CTA: (u::ReshapeSwapLinear)(s) with the heat-bath
+// permutation swap, one warp: (u::ReshapeSwapLinear)(s) with the heat-bath
 // partner choice sampleparticles (src/updates/reshape.jl:123-283,
-// src/updates/helper.jl:224-267).  Returns RES_*; *n2_out receives n2.
+// src/updates/helper.jl:224-267).  Returns RES_*; n2_out receives n2.
 // ---------------------------------------------------------------------------
-template <class D>
-__device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr, SwapScratch &S,
-                        double *red, int *ired, int *sflag, double *prop, int *n2_out,
-                        bool update_cells) {
+template <bool FAST, class D>
+__device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &dr,
+                         SwapScratch &S, double *prop, int *n2_out) {
   const ChainDesc &d = *c.d;
-  const int N = c.N, M = c.M, dim = c.dim, tid = threadIdx.x, nt = blockDim.x;
+  const int N = c.N, M = c.M, dim = c.dim, lane = threadIdx.x & 31;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
-  const bool wrap = (j0 + m) >= M;
-  const int se = wrap ? j0 + m - M : j0 + m;
-  const double taum = m * d.tau;
-  const double den = 4.0 * taum * d.lambda;
-  auto endp = [&](int i) { return wrap ? c.next[i] : i; };
-  auto Xd = [&](int k, int n, int j) { return k < dim ? c.X(k, n, j) : 0.0; };
-  const double ax = c.X(0, n1, j0), ay = Xd(1, n1, j0);
-  const int e1p = endp(n1);
-  const double e1x = c.X(0, e1p, se), e1y = Xd(1, e1p, se);
-  // heat-bath weights exp(t_i + y_i), shifted by the maximum
-  double vm[1] = {-INFINITY};
-  for (int i = tid; i < N; i += nt) {
-    const int ei = endp(i);
-    const double t1 = -mi2(d, ax, ay, c.X(0, ei, se), Xd(1, ei, se)) / den;
-    const double t2 = -mi2(d, c.X(0, i, j0), Xd(1, i, j0), e1x, e1y) / den;
-    S.w[i] = t1 + t2;
-    vm[0] = fmax(vm[0], t1 + t2);
+  HeatBath<FAST> hb;
+  hb.c = &c;
+  hb.j0 = j0;
+  hb.wrap = (j0 + m) >= M;
+  hb.se = hb.wrap ? j0 + m - M : j0 + m;
+  hb.inv_den = 1.0 / (4.0 * (m * d.tau) * d.lambda);
+  hb.inv_denf = (float)hb.inv_den;
+  hb.L2f = (float)(2.0 * L);
+  const int se = hb.se;
+  const bool wrap = hb.wrap;
+  const double ax = c.X(0, n1, j0), ay = c.Xd(1, n1, j0);
+  const int e1p = hb.endp(n1);
+  const double e1x = c.X(0, e1p, se), e1y = c.Xd(1, e1p, se);
+  // weights exp(t_i + y_i) shifted by their maximum (the reference normalises
+  // them, helper.jl:260-263; the shift keeps them from underflowing)
+  const int chunk = (N + 31) / 32;
+  const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
+  double wmax = -INFINITY;
+  for (int i = i0; i < i1; ++i) {
+    const double v = hb.expo(i, ax, ay, e1x, e1y);
+    S.w[i] = v;
+    wmax = fmax(wmax, v);
   }
-  block_max_k<1>(vm, red);
-  const double wmax = vm[0];
-  double vs[1] = {0.0};
-  for (int i = tid; i < N; i += nt) {
-    const double e = exp(S.w[i] - wmax);
+  wmax = warp_max(wmax);
+  double ls = 0.0;
+  for (int i = i0; i < i1; ++i) {
+    const double e = hb.ex_(S.w[i] - wmax);
     S.w[i] = e;
-    vs[0] += e;
+    ls += e;
   }
-  block_sum_k<1>(vs, red);
-  const double ssum = vs[0];
-  double vq[1] = {0.0};
-  for (int i = tid; i < N; i += nt) {
-    const double q = S.w[i] / ssum;
+  const double ssum = warp_sum(ls);
+  const double inv_s = 1.0 / ssum;
+  double lq = 0.0;
+  for (int i = i0; i < i1; ++i) {
+    const double q = S.w[i] * inv_s;
     S.w[i] = q;
-    vq[0] += q;
+    lq += q;
   }
-  block_sum_k<1>(vq, red);
-  const double target = u_pick * vq[0];
+  const double target = u_pick * warp_sum(lq);
   // first i with cumulative weight >= target (StatsBase.sample)
-  const int chunk = (N + nt - 1) / nt;
-  const int i0 = min(N, tid * chunk), i1 = min(N, i0 + chunk);
-  double loc = 0.0;
-  for (int i = i0; i < i1; ++i) loc += S.w[i];
-  double cw = block_exclusive_scan(loc, red);
+  double cw = warp_exclusive_scan(lq);
   int cand = 0x7fffffff;
   for (int i = i0; i < i1; ++i) {
     cw += S.w[i];
     if (cw >= target) { cand = i; break; }
   }
-  int n2 = block_min_int(cand, ired);
+  int n2 = warp_min_int(cand);
   if (n2 >= N) n2 = N - 1;
-  if (n2_out && tid == 0) *n2_out = n2;
+  if (n2_out && lane == 0) *n2_out = n2;
   if (n2 == n1) return RES_SKIP;
 
   double log_ratio = 0.0;
@@ -172,39 +196,31 @@ __device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr
     // (1/S'_1 + 1/S'_2) / (1/S_1 + 1/S_2): S_a sums the heat-bath weights
     // with a chosen first; primes after the ends of n1 and n2 are exchanged
     const double l1 = wmax + log(ssum);
-    const double bx = c.X(0, n2, j0), by = Xd(1, n2, j0);
-    const int e2p = endp(n2);
-    const double e2x = c.X(0, e2p, se), e2y = Xd(1, e2p, se);
-    double wv[3];
-    double mx3[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = tid; i < N; i += nt) {
-      const int ei = endp(i);
-      const double ex = c.X(0, ei, se), ey = Xd(1, ei, se);
-      const double epx = i == n1 ? e2x : (i == n2 ? e1x : ex);
-      const double epy = i == n1 ? e2y : (i == n2 ? e1y : ey);
-      const double xi = c.X(0, i, j0), yi = Xd(1, i, j0);
-      wv[0] = -mi2(d, bx, by, ex, ey) / den - mi2(d, xi, yi, e2x, e2y) / den;
-      wv[1] = -mi2(d, ax, ay, epx, epy) / den - mi2(d, xi, yi, e2x, e2y) / den;
-      wv[2] = -mi2(d, bx, by, epx, epy) / den - mi2(d, xi, yi, e1x, e1y) / den;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) mx3[k] = fmax(mx3[k], wv[k]);
+    const double bx = c.X(0, n2, j0), by = c.Xd(1, n2, j0);
+    const int e2p = hb.endp(n2);
+    const double e2x = c.X(0, e2p, se), e2y = c.Xd(1, e2p, se);
+    // expo(i) with E(i) replaced by E'(i): the ends of n1 and n2 exchanged
+    auto expo_p = [&](int i, double sx_, double sy_, double fx, double fy) {
+      if (i != n1 && i != n2) return hb.expo(i, sx_, sy_, fx, fy);
+      return hb.expo(i, sx_, sy_, fx, fy, true, i == n1 ? e2x : e1x, i == n1 ? e2y : e1y);
+    };
+    double mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int i = i0; i < i1; ++i) {
+      mx[0] = fmax(mx[0], hb.expo(i, bx, by, e2x, e2y));
+      mx[1] = fmax(mx[1], expo_p(i, ax, ay, e2x, e2y));
+      mx[2] = fmax(mx[2], expo_p(i, bx, by, e1x, e1y));
     }
-    block_max_k<3>(mx3, red);
+    for (int k = 0; k < 3; ++k) mx[k] = warp_max(mx[k]);
     double s3[3] = {0.0, 0.0, 0.0};
-    for (int i = tid; i < N; i += nt) {
-      const int ei = endp(i);
-      const double ex = c.X(0, ei, se), ey = Xd(1, ei, se);
-      const double epx = i == n1 ? e2x : (i == n2 ? e1x : ex);
-      const double epy = i == n1 ? e2y : (i == n2 ? e1y : ey);
-      const double xi = c.X(0, i, j0), yi = Xd(1, i, j0);
-      s3[0] += exp(-mi2(d, bx, by, ex, ey) / den - mi2(d, xi, yi, e2x, e2y) / den - mx3[0]);
-      s3[1] += exp(-mi2(d, ax, ay, epx, epy) / den - mi2(d, xi, yi, e2x, e2y) / den - mx3[1]);
-      s3[2] += exp(-mi2(d, bx, by, epx, epy) / den - mi2(d, xi, yi, e1x, e1y) / den - mx3[2]);
+    for (int i = i0; i < i1; ++i) {
+      s3[0] += hb.ex_(hb.expo(i, bx, by, e2x, e2y) - mx[0]);
+      s3[1] += hb.ex_(expo_p(i, ax, ay, e2x, e2y) - mx[1]);
+      s3[2] += hb.ex_(expo_p(i, bx, by, e1x, e1y) - mx[2]);
     }
-    block_sum_k<3>(s3, red);
-    const double l2 = mx3[0] + log(s3[0]);
-    const double l1p = mx3[1] + log(s3[1]);
-    const double l2p = mx3[2] + log(s3[2]);
+    for (int k = 0; k < 3; ++k) s3[k] = warp_sum(s3[k]);
+    const double l2 = mx[0] + log(s3[0]);
+    const double l1p = mx[1] + log(s3[1]);
+    const double l2p = mx[2] + log(s3[2]);
     log_ratio = logaddexp(-l1p, -l2p) - logaddexp(-l1, -l2);
   }
 
@@ -213,26 +229,27 @@ __device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr
   auto own1 = [&](int t) { return (j0 + t < M) ? n1 : nx1; };
   auto own2 = [&](int t) { return (j0 + t < M) ? n2 : nx2; };
   auto slc = [&](int t) { return (j0 + t < M) ? j0 + t : j0 + t - M; };
-  const double s1x = ax, s1y = ay, s2x = c.X(0, n2, j0), s2y = Xd(1, n2, j0);
-  const int e2p = endp(n2);
-  double f1x = c.X(0, e2p, se), f1y = Xd(1, e2p, se);  // r1 ends at E(n2)
+  const double s1x = ax, s1y = ay, s2x = c.X(0, n2, j0), s2y = c.Xd(1, n2, j0);
+  const int e2p = hb.endp(n2);
+  double f1x = c.X(0, e2p, se), f1y = c.Xd(1, e2p, se);  // r1 ends at E(n2)
   double f2x = e1x, f2y = e1y;                            // r2 ends at E(n1)
   if (fabs(s1x - f1x) > L) f1x += sgn(s1x) * (2.0 * L);
   if (dim > 1 && fabs(s1y - f1y) > L) f1y += sgn(s1y) * (2.0 * L);
   if (fabs(s2x - f2x) > L) f2x += sgn(s2x) * (2.0 * L);
   if (dim > 1 && fabs(s2y - f2y) > L) f2y += sgn(s2y) * (2.0 * L);
   const bool hard = (d.flags & PF_HARD) != 0;
+  int fail = 0;
   if (!hard) {
-    for (int k = tid; k < 2 * (m - 1); k += nt) {
+    for (int k = lane; k < 2 * (m - 1); k += 32) {
       double zz[2];
       dr.bead_normals(k, dim, zz);
       S.z[2 * k] = zz[0];
       S.z[2 * k + 1] = dim > 1 ? zz[1] : 0.0;
     }
     dr.consumed(2 * (m - 1) * dim);
-    __syncthreads();
-    if (tid < 2 * dim) {
-      const int b = tid / dim, k = tid % dim;
+    __syncwarp();
+    if (lane < 2 * dim) {
+      const int b = lane / dim, k = lane % dim;
       double p = b == 0 ? (k == 0 ? s1x : s1y) : (k == 0 ? s2x : s2y);
       const double e = b == 0 ? (k == 0 ? f1x : f1y) : (k == 0 ? f2x : f2y);
       double *dst = b == 0 ? (k == 0 ? S.r1x : S.r1y) : (k == 0 ? S.r2x : S.r2y);
@@ -242,9 +259,7 @@ __device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr
         dst[t] = p;
       }
     }
-    if (tid == 0) *sflag = 0;
-  } else if (tid == 0) {
-    int fail = 0;
+  } else {
     for (int b = 0; b < 2 && !fail; ++b) {
       double px = b == 0 ? s1x : s2x, py = b == 0 ? s1y : s2y;
       const double ex = b == 0 ? f1x : f2x, ey = b == 0 ? f1y : f2y;
@@ -257,24 +272,31 @@ __device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr
         int tries = 0;
         while (true) {
           if (++tries > d.ctr) { fail = 1; break; }
-          const double z0 = dr.normal(), z1 = dim > 1 ? dr.normal() : 0.0;
-          const double qx = ab.x * px + (1.0 - ab.x) * ex + z0 * ab.y;
-          const double qy = dim > 1 ? ab.x * py + (1.0 - ab.x) * ey + z1 * ab.y : 0.0;
-          if (!hard_hit(c, teleport(qx, L, inv2L), dim > 1 ? teleport(qy, L, inv2L) : 0.0, j, ea,
-                        eb)) {
-            px = qx; py = qy;
+          double qx = 0.0, qy = 0.0;
+          if (lane == 0) {
+            const double z0 = dr.normal(), z1 = dim > 1 ? dr.normal() : 0.0;
+            qx = ab.x * px + (1.0 - ab.x) * ex + z0 * ab.y;
+            qy = dim > 1 ? ab.x * py + (1.0 - ab.x) * ey + z1 * ab.y : 0.0;
+          }
+          qx = __shfl_sync(0xffffffffu, qx, 0);
+          qy = __shfl_sync(0xffffffffu, qy, 0);
+          const double tx = teleport(qx, L, inv2L), ty = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
+          if (!__any_sync(0xffffffffu, hard_hit_lanes(c, tx, ty, j, ea, eb, lane, 32))) {
+            px = qx;
+            py = qy;
             break;
           }
         }
-        dx[t] = px;
-        dy[t] = py;
+        if (lane == 0) {
+          dx[t] = px;
+          dy[t] = py;
+        }
       }
     }
-    *sflag = fail;
   }
-  __syncthreads();
-  if (*sflag) return RES_HARDCORE;
-  for (int k = tid; k < 2 * (m + 1); k += nt) {
+  __syncwarp();
+  if (fail) return RES_HARDCORE;
+  for (int k = lane; k < 2 * (m + 1); k += 32) {
     const int b = k / (m + 1), t = k % (m + 1);
     double qx, qy;
     if (b == 0) {
@@ -285,208 +307,167 @@ __device__ int swap_cta(const CV &c, int j0, int m, int n1, double u_pick, D &dr
       qy = t == 0 ? s2y : (t == m ? f2y : S.r2y[t]);
     }
     qx = teleport(qx, L, inv2L);
-    if (dim > 1) qy = teleport(qy, L, inv2L); else qy = 0.0;
+    qy = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
     (b == 0 ? S.r1x : S.r2x)[t] = qx;
     (b == 0 ? S.r1y : S.r2y)[t] = qy;
     (b == 0 ? S.vb1 : S.vb2)[t] = vext(d, qx, qy);
   }
-  __syncthreads();
+  __syncwarp();
   const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
-  double ws[2] = {0.0, 0.0};
-  for (int k = tid; k < 2 * m; k += nt) {
+  double wi = 0.0, wu = 0.0;
+  for (int k = lane; k < 2 * m; k += 32) {
     const int b = k / m, t = k % m;
     const int j = slc(t), o = b == 0 ? own1(t) : own2(t);
-    const int on = b == 0 ? own1(t + 1) : own2(t + 1), jn = slc(t + 1);
-    const double *bxs = b == 0 ? S.r1x : S.r2x, *bys = b == 0 ? S.r1y : S.r2y;
-    const double *vb = b == 0 ? S.vb1 : S.vb2;
-    ws[0] += c.Vl(o, j);
-    ws[1] += mhtau * (vb[t] + vb[t + 1]);
-    if (any_pair) {
-      const double ox = c.X(0, o, j), oy = Xd(1, o, j), onx = c.X(0, on, jn), ony = Xd(1, on, jn);
+    wi += c.Vl(o, j);
+    wu += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
+  }
+  if (any_pair) {
+    for (int k = 0; k < 2 * m; ++k) {
+      const int b = k / m, t = k % m;
+      const int j = slc(t), o = b == 0 ? own1(t) : own2(t);
+      const int on = b == 0 ? own1(t + 1) : own2(t + 1), jn = slc(t + 1);
+      const double *bxs = b == 0 ? S.r1x : S.r2x, *bys = b == 0 ? S.r1y : S.r2y;
+      const double ox = c.X(0, o, j), oy = c.Xd(1, o, j), onx = c.X(0, on, jn), ony = c.Xd(1, on, jn);
       if (!phys) {
-        // the reference: old pairs exclude only the path's own particle,
-        // the new paths' pair terms are added to w_initial
-        ws[0] += pair_link(c, ox, oy, onx, ony, j, o, -1);
-        ws[0] += pair_link(c, bxs[t], bys[t], bxs[t + 1], bys[t + 1], j, own1(t), own2(t));
+        // the reference: old pairs exclude only the path's own particle, the
+        // new paths' pair terms are added to w_initial (reshape.jl:166-240)
+        double wn = 0.0;
+        pair_link_lanes(c, j, o, -1, own1(t), own2(t), nullptr, true, true, ox, oy, onx, ony,
+                        bxs[t], bys[t], bxs[t + 1], bys[t + 1], wi, wn, lane, 32);
+        wi += wn;
       } else {
-        ws[0] += pair_link(c, ox, oy, onx, ony, j, own1(t), own2(t));
-        ws[1] += pair_link(c, bxs[t], bys[t], bxs[t + 1], bys[t + 1], j, own1(t), own2(t));
-        if (b == 0) {
+        pair_link_lanes(c, j, own1(t), own2(t), own1(t), own2(t), nullptr, true, true, ox, oy,
+                        onx, ony, bxs[t], bys[t], bxs[t + 1], bys[t + 1], wi, wu, lane, 32);
+        if (b == 0 && lane == 0) {
           const int o2 = own2(t), o2n = own2(t + 1);
-          ws[0] += pair_cross(d, ox, oy, onx, ony, c.X(0, o2, j), Xd(1, o2, j), c.X(0, o2n, jn),
-                              Xd(1, o2n, jn));
-          ws[1] += pair_cross(d, S.r1x[t], S.r1y[t], S.r1x[t + 1], S.r1y[t + 1], S.r2x[t],
-                              S.r2y[t], S.r2x[t + 1], S.r2y[t + 1]);
+          const double a2x = c.X(0, o2, j), a2y = c.Xd(1, o2, j);
+          const double a2nx = c.X(0, o2n, jn), a2ny = c.Xd(1, o2n, jn);
+          const double r2o = mi2(d, ox, oy, a2x, a2y);
+          if (r2o <= d.rc * d.rc) wi += lnU2(d, r2o, mi2(d, onx, ony, a2nx, a2ny));
+          const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
+          if (r2n <= d.rc * d.rc)
+            wu += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
         }
       }
     }
   }
-  block_sum_k<2>(ws, red);
+  wi = warp_sum(wi);
+  wu = warp_sum(wu);
   if (prop)
-    for (int k = tid; k < 2 * (m + 1); k += nt) {
+    for (int k = lane; k < 2 * (m + 1); k += 32) {
       const int b = k / (m + 1), t = k % (m + 1);
       prop[k * dim] = (b == 0 ? S.r1x : S.r2x)[t];
       if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
     }
-  if (tid == 0) {
-    const double delta = exp(ws[1] - ws[0] + log_ratio);
-    *sflag = (delta >= 1.0) || (delta > dr.uniform_accept());
+  int acc = 0;
+  if (lane == 0) {
+    const double delta = exp(wu - wi + log_ratio);
+    acc = (delta >= 1.0) || (delta > dr.uniform_accept());
   }
-  __syncthreads();
-  const int acc = *sflag;
+  acc = __shfl_sync(0xffffffffu, acc, 0);
   if (!acc) return RES_REJECT;
   // accept: exchange next, write the bridges along the new cycles, exchange
   // the tails (reshape.jl:247-279)
-  const int nn1 = nx2, nn2 = nx1;  // next after the exchange
+  const int nn1 = nx2, nn2 = nx1;
   auto nown1 = [&](int t) { return (j0 + t < M) ? n1 : nn1; };
   auto nown2 = [&](int t) { return (j0 + t < M) ? n2 : nn2; };
-  const bool tail = (j0 + m) < M - 1;
-  if (update_cells) {
-    for (int j = tid; j < M; j += nt) {
-      const int t = (j - j0 + M) % M;
-      int pa = -1, pb = -1;
-      if (t >= 1 && t <= m) { pa = nown1(t); pb = nown2(t); }
-      else if (tail && j > se) { pa = n1; pb = n2; }
-      S.pa[j] = pa;
-      S.pb[j] = pb;
-      S.ca[j] = pa >= 0 ? cell_of(d, c.X(0, pa, j), Xd(1, pa, j)) : -1;
-      S.cb[j] = pb >= 0 ? cell_of(d, c.X(0, pb, j), Xd(1, pb, j)) : -1;
-    }
-  }
-  __syncthreads();
-  if (tid == 0) {
+  if (lane == 0) {
     c.next[n1] = nn1;
     c.next[n2] = nn2;
   }
-  for (int t = 1 + tid; t <= m; t += nt) {
+  for (int t = 1 + lane; t <= m; t += 32) {
     const int j = slc(t);
-    c.X(0, nown1(t), j) = S.r1x[t];
-    c.X(0, nown2(t), j) = S.r2x[t];
-    if (dim > 1) {
-      c.X(1, nown1(t), j) = S.r1y[t];
-      c.X(1, nown2(t), j) = S.r2y[t];
-    }
+    c.set_pos(nown1(t), j, S.r1x[t], S.r1y[t]);
+    c.set_pos(nown2(t), j, S.r2x[t], S.r2y[t]);
   }
-  for (int t = tid; t < m; t += nt) {
+  for (int t = lane; t < m; t += 32) {
     const int j = slc(t);
     c.Vl(nown1(t), j) = mhtau * (S.vb1[t] + S.vb1[t + 1]);
     c.Vl(nown2(t), j) = mhtau * (S.vb2[t] + S.vb2[t + 1]);
   }
-  if (tail)
-    for (int j = se + 1 + tid; j < M; j += nt) {
-      for (int k = 0; k < dim; ++k) {
-        const double a = c.X(k, n1, j);
-        c.X(k, n1, j) = c.X(k, n2, j);
-        c.X(k, n2, j) = a;
-      }
+  if (j0 + m < M - 1)
+    for (int j = se + 1 + lane; j < M; j += 32) {
+      const double ax_ = c.X(0, n1, j), ay_ = c.Xd(1, n1, j);
+      c.set_pos(n1, j, c.X(0, n2, j), c.Xd(1, n2, j));
+      c.set_pos(n2, j, ax_, ay_);
       const double v = c.Vl(n1, j);
       c.Vl(n1, j) = c.Vl(n2, j);
       c.Vl(n2, j) = v;
     }
-  if (phys && !wrap && tid == 0) {
+  if (phys && !wrap && lane == 0) {
     // the link leaving the end bead moves with the tail
     const double v = c.Vl(n1, se);
     c.Vl(n1, se) = c.Vl(n2, se);
     c.Vl(n2, se) = v;
   }
-  __syncthreads();
-  if (update_cells) {
-    for (int j = tid; j < M; j += nt) {
-      if (S.pa[j] >= 0)
-        cell_move(c, S.pa[j], j, S.ca[j], cell_of(d, c.X(0, S.pa[j], j), Xd(1, S.pa[j], j)));
-      if (S.pb[j] >= 0)
-        cell_move(c, S.pb[j], j, S.cb[j], cell_of(d, c.X(0, S.pb[j], j), Xd(1, S.pb[j], j)));
-    }
-    __syncthreads();
-  }
+  __syncwarp();
   return RES_ACCEPT;
 }
 
 // ---------------------------------------------------------------------------
-// single-path centre of mass, one warp: (u::SingleCenterOfMass)(s) with
-// move_polymer! (src/updates/com.jl:136-224, src/updates/helper.jl:368-395).
-// sb: per-warp shared scratch of 3*M doubles.
+// single-path centre of mass, one thread per particle (pair-free acceptance,
+// no hard core): (u::SingleCenterOfMass)(s) with move_polymer!
+// (src/updates/com.jl:136-224, src/updates/helper.jl:368-395).  The shifted
+// path is recomputed for the write-back instead of being stored.
 // ---------------------------------------------------------------------------
 template <class D>
-__device__ int com_warp(const CV &c, int n, double step, D &dr, double *sb, bool update_cells) {
+__device__ int com_thread(const CV &c, int n, double step, D &dr) {
   const ChainDesc &d = *c.d;
-  const int lane = threadIdx.x & 31, M = c.M, dim = c.dim;
+  const int M = c.M, dim = c.dim;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
-  const bool hard = (d.flags & PF_HARD) != 0;
-  const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
-  double *qx_ = sb, *qy_ = sb + M, *vb = sb + 2 * M;
-  int tries = 0, fail = 0;
-  double shx = 0.0, shy = 0.0;
-  while (true) {
-    if (lane == 0) {
-      if (++tries > d.ctr) {
-        fail = 1;
-      } else {
-        shx = step * 2.0 * (dr.uniform() - 0.5);
-        shy = dim > 1 ? step * 2.0 * (dr.uniform() - 0.5) : 0.0;
-      }
-    }
-    fail = __shfl_sync(0xffffffffu, fail, 0);
-    if (fail) break;
-    shx = __shfl_sync(0xffffffffu, shx, 0);
-    shy = __shfl_sync(0xffffffffu, shy, 0);
-    bool hit = false;
-    for (int j = lane; j < M; j += 32) {
+  const double shx = step * 2.0 * (dr.uniform() - 0.5);
+  const double shy = dim > 1 ? step * 2.0 * (dr.uniform() - 0.5) : 0.0;
+  double wi = 0.0, wu = 0.0;
+  const double q0x = teleport(c.X(0, n, 0) + shx, L, inv2L);
+  const double q0y = dim > 1 ? teleport(c.X(1, n, 0) + shy, L, inv2L) : 0.0;
+  const double v0 = vext(d, q0x, q0y);
+  double vprev = v0;
+  for (int j = 1; j <= M; ++j) {
+    double vj = v0;
+    if (j < M) {
       const double qx = teleport(c.X(0, n, j) + shx, L, inv2L);
       const double qy = dim > 1 ? teleport(c.X(1, n, j) + shy, L, inv2L) : 0.0;
-      qx_[j] = qx;
-      qy_[j] = qy;
-      if (hard && hard_hit(c, qx, qy, j, n, -1)) hit = true;
+      vj = vext(d, qx, qy);
     }
-    if (!__any_sync(0xffffffffu, hit)) break;
+    wi += c.Vl(n, j - 1);
+    wu += mhtau * (vprev + vj);
+    vprev = vj;
   }
-  if (fail) return RES_HARDCORE;
-  for (int j = lane; j < M; j += 32) vb[j] = vext(d, qx_[j], qy_[j]);
-  __syncwarp();
-  double wi = 0.0, wu = 0.0;
-  for (int j = lane; j < M; j += 32) {
-    const int jn = j + 1 == M ? 0 : j + 1;
-    wi += c.Vl(n, j);
-    wu += mhtau * (vb[j] + vb[jn]);
-    if (phys_pair) {
-      wi += pair_link(c, c.X(0, n, j), dim > 1 ? c.X(1, n, j) : 0.0, c.X(0, n, jn),
-                      dim > 1 ? c.X(1, n, jn) : 0.0, j, n, -1);
-      wu += pair_link(c, qx_[j], qy_[j], qx_[jn], qy_[jn], j, n, -1);
-    }
-  }
-  wi = warp_sum(wi);
-  wu = warp_sum(wu);
-  int acc = 0;
-  if (lane == 0) {
-    const double delta = exp(wu - wi);
-    acc = (delta >= 1.0) || (delta > dr.uniform_accept());
-  }
-  acc = __shfl_sync(0xffffffffu, acc, 0);
+  const double delta = exp(wu - wi);
+  const bool acc = (delta >= 1.0) || (delta > dr.uniform_accept());
   if (acc) {
-    for (int j = lane; j < M; j += 32) {
-      const int jn = j + 1 == M ? 0 : j + 1;
-      if (update_cells)
-        cell_move(c, n, j, cell_of(d, c.X(0, n, j), dim > 1 ? c.X(1, n, j) : 0.0),
-                  cell_of(d, qx_[j], qy_[j]));
-      c.X(0, n, j) = qx_[j];
-      if (dim > 1) c.X(1, n, j) = qy_[j];
-      c.Vl(n, j) = mhtau * (vb[j] + vb[jn]);
+    vprev = v0;
+    double px = q0x, py = q0y;
+    for (int j = 1; j <= M; ++j) {
+      double qx = q0x, qy = q0y, vj = v0;
+      if (j < M) {
+        qx = teleport(c.X(0, n, j) + shx, L, inv2L);
+        qy = dim > 1 ? teleport(c.X(1, n, j) + shy, L, inv2L) : 0.0;
+        vj = vext(d, qx, qy);
+      }
+      c.set_pos(n, j - 1, px, py);
+      c.Vl(n, j - 1) = mhtau * (vprev + vj);
+      vprev = vj;
+      px = qx;
+      py = qy;
     }
   }
-  __syncwarp();
-  return acc;
+  return acc ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
-// cycle centre of mass, whole CTA: PolymerCenterOfMass (src/updates/com.jl:31-104)
-// without the worm fields that make the reference's version fail.
-// pol/idx: int scratch of 2N.
+// centre of mass of a whole cycle (npol members; npol = 1 is the single-path
+// move), whole CTA: pair terms with every particle outside the cycle, hard-
+// core retries, PolymerCenterOfMass (src/updates/com.jl:31-104) without the
+// worm fields that make the reference's version fail.  pol/idx: int scratch
+// of 2N; q: shared scratch of 3*M doubles (single-path case).
 // ---------------------------------------------------------------------------
 template <class D>
-__device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *idx, double *red,
-                        int *sflag, int *np_out, bool update_cells) {
+__device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int *pol, int *idx,
+                       double *q, double *red, int *sflag, int *np_out) {
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M, dim = c.dim, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
   const bool hard = (d.flags & PF_HARD) != 0;
   const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
@@ -494,10 +475,14 @@ __device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *i
   __syncthreads();
   if (tid == 0) {
     int np = 0, i = n;
-    do {
-      pol[np++] = i;
-      i = c.next[i];
-    } while (i != n && np <= N);
+    if (polymer) {
+      do {
+        pol[np++] = i;
+        i = c.next[i];
+      } while (i != n && np <= N);
+    } else {
+      pol[np++] = n;
+    }
     *sflag = np;
   }
   __syncthreads();
@@ -506,7 +491,7 @@ __device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *i
   if (np > N) return -1;
   for (int i = tid; i < np; i += nt) idx[pol[i]] = i;
   __syncthreads();
-  double *shift = red + 224;  // two doubles beyond the reduction slots
+  double *shift = red + 240;  // two doubles beyond the reduction slots
   int tries = 0;
   while (true) {
     if (tid == 0) {
@@ -521,45 +506,60 @@ __device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *i
     __syncthreads();
     if (*sflag < 0) return RES_HARDCORE;
     if (!hard) break;
+    // a warp per bead, lanes over the slice
     int hit = 0;
-    for (int k = tid; k < np * M; k += nt) {
+    for (int k = warp; k < np * M; k += nwarps) {
       const int i = pol[k / M], j = k % M;
       const double qx = teleport(c.X(0, i, j) + shift[0], L, inv2L);
       const double qy = dim > 1 ? teleport(c.X(1, i, j) + shift[1], L, inv2L) : 0.0;
-      if (hard_hit(c, qx, qy, j, i, -1)) hit = 1;
+      if (hard_hit_lanes(c, qx, qy, j, i, -1, lane, 32)) hit = 1;
     }
     if (!__syncthreads_or(hit)) break;
   }
   const double shx = shift[0], shy = shift[1];
+  auto qpos = [&](int i, int j, double &qx, double &qy) {
+    qx = teleport(c.X(0, i, j) + shx, L, inv2L);
+    qy = dim > 1 ? teleport(c.X(1, i, j) + shy, L, inv2L) : 0.0;
+  };
+  if (!polymer) {
+    for (int j = tid; j < M; j += nt) {
+      double qx, qy;
+      qpos(n, j, qx, qy);
+      q[j] = qx;
+      q[M + j] = qy;
+      q[2 * M + j] = vext(d, qx, qy);
+    }
+    __syncthreads();
+  }
   double ws[2] = {0.0, 0.0};
   for (int k = tid; k < np * M; k += nt) {
     const int i = pol[k / M], j = k % M;
     const int jn = j + 1 == M ? 0 : j + 1, in = j == M - 1 ? c.next[i] : i;
-    const double ox = c.X(0, i, j), oy = dim > 1 ? c.X(1, i, j) : 0.0;
-    const double onx = c.X(0, in, jn), ony = dim > 1 ? c.X(1, in, jn) : 0.0;
-    const double qx = teleport(ox + shx, L, inv2L), qy = dim > 1 ? teleport(oy + shy, L, inv2L) : 0.0;
-    const double qnx = teleport(onx + shx, L, inv2L);
-    const double qny = dim > 1 ? teleport(ony + shy, L, inv2L) : 0.0;
     ws[0] += c.Vl(i, j);
-    ws[1] += mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
-    if (phys_pair) {
-      // pairs with particles outside the cycle; pairs inside it keep their
-      // relative positions under the rigid shift
-      int cells[9];
-      for (int side = 0; side < 2; ++side) {
-        const double px = side ? qx : ox, py = side ? qy : oy;
-        const double pnx = side ? qnx : onx, pny = side ? qny : ony;
-        const int nc = stencil(d, cell_of(d, px, py), cells);
-        double w = 0.0;
-        for (int ci = 0; ci < nc; ++ci)
-          for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
-            if (idx[b] >= 0) continue;
-            const int bn = j == M - 1 ? c.next[b] : b;
-            w += pair_cross(d, px, py, pnx, pny, c.X(0, b, j), dim > 1 ? c.X(1, b, j) : 0.0,
-                            c.X(0, bn, jn), dim > 1 ? c.X(1, bn, jn) : 0.0);
-          }
-        ws[side] += w;
+    if (!polymer) {
+      ws[1] += mhtau * (q[2 * M + j] + q[2 * M + jn]);
+    } else {
+      double qx, qy, qnx, qny;
+      qpos(i, j, qx, qy);
+      qpos(in, jn, qnx, qny);
+      ws[1] += mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
+    }
+  }
+  if (phys_pair) {
+    // a warp per link, lanes over the slice; pairs inside the cycle keep
+    // their relative positions under the rigid shift
+    for (int k = warp; k < np * M; k += nwarps) {
+      const int i = pol[k / M], j = k % M;
+      const int jn = j + 1 == M ? 0 : j + 1, in = j == M - 1 ? c.next[i] : i;
+      double qx, qy, qnx, qny;
+      if (!polymer) {
+        qx = q[j]; qy = q[M + j]; qnx = q[jn]; qny = q[M + jn];
+      } else {
+        qpos(i, j, qx, qy);
+        qpos(in, jn, qnx, qny);
       }
+      pair_link_lanes(c, j, -1, -1, -1, -1, idx, true, true, c.X(0, i, j), c.Xd(1, i, j),
+                      c.X(0, in, jn), c.Xd(1, in, jn), qx, qy, qnx, qny, ws[0], ws[1], lane, 32);
     }
   }
   block_sum_k<2>(ws, red);
@@ -570,30 +570,43 @@ __device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *i
   __syncthreads();
   const int acc = *sflag;
   if (!acc) return RES_REJECT;
-  // links first (they read the unshifted neighbours), then positions per slice
+  // links first (they read the unshifted neighbours), then positions
   for (int k = tid; k < np * M; k += nt) {
     const int i = pol[k / M], j = k % M;
     const int jn = j + 1 == M ? 0 : j + 1, in = j == M - 1 ? c.next[i] : i;
-    const double qx = teleport(c.X(0, i, j) + shx, L, inv2L);
-    const double qy = dim > 1 ? teleport(c.X(1, i, j) + shy, L, inv2L) : 0.0;
-    const double qnx = teleport(c.X(0, in, jn) + shx, L, inv2L);
-    const double qny = dim > 1 ? teleport(c.X(1, in, jn) + shy, L, inv2L) : 0.0;
-    c.Vl(i, j) = mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
+    if (!polymer) {
+      c.Vl(i, j) = mhtau * (q[2 * M + j] + q[2 * M + jn]);
+    } else {
+      double qx, qy, qnx, qny;
+      qpos(i, j, qx, qy);
+      qpos(in, jn, qnx, qny);
+      c.Vl(i, j) = mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
+    }
   }
   __syncthreads();
-  for (int j = tid; j < M; j += nt)
-    for (int q = 0; q < np; ++q) {
-      const int i = pol[q];
-      const double qx = teleport(c.X(0, i, j) + shx, L, inv2L);
-      const double qy = dim > 1 ? teleport(c.X(1, i, j) + shy, L, inv2L) : 0.0;
-      if (update_cells)
-        cell_move(c, i, j, cell_of(d, c.X(0, i, j), dim > 1 ? c.X(1, i, j) : 0.0),
-                  cell_of(d, qx, qy));
-      c.X(0, i, j) = qx;
-      if (dim > 1) c.X(1, i, j) = qy;
+  for (int k = tid; k < np * M; k += nt) {
+    const int i = pol[k / M], j = k % M;
+    double qx, qy;
+    if (!polymer) {
+      qx = q[j];
+      qy = q[M + j];
+    } else {
+      qpos(i, j, qx, qy);
     }
+    c.set_pos(i, j, qx, qy);
+  }
   __syncthreads();
   return RES_ACCEPT;
+}
+
+// floor((x + L) / w) with the division replaced by a multiplication unless
+// the quotient lies within 1e-9 of an integer (then the IEEE division decides)
+__device__ __forceinline__ long long bin_floor(double x, double L, double w, double inv_w) {
+  const double q = (x + L) * inv_w;
+  double f = floor(q);
+  const double fr = q - f;
+  if (fr < 1e-9 || fr > 1.0 - 1e-9) f = floor((x + L) / w);
+  return (long long)f;
 }
 
 // ---------------------------------------------------------------------------
@@ -603,43 +616,51 @@ __device__ int pcom_cta(const CV &c, int n, double step, D &dr, int *pol, int *i
 __device__ void measure_cta(const CV &c, double *red, double *out, bool density) {
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M, dim = c.dim, tid = threadIdx.x, nt = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
   const bool pair = (d.flags & PF_PAIR) != 0;
   const double rc2 = d.rc * d.rc, cg = d.inv2s2;
   double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // link, pot, vkin, pair, pair virial
+  const double inv_bw = density ? 1.0 / d.dens_bw : 0.0;
   for (int k = tid; k < N * M; k += nt) {
-    const int i = k / M, j = k % M;
+    const int j = k / N, i = k % N;
     const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-    const double ax = c.X(0, i, j), ay = dim > 1 ? c.X(1, i, j) : 0.0;
-    const double bx = c.X(0, in, jn), by = dim > 1 ? c.X(1, in, jn) : 0.0;
+    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+    const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
     s[0] += mi2(d, ax, ay, bx, by);
     s[1] += vext(d, ax, ay) + vext(d, bx, by);
     s[2] += ax * dvext(d, ax) + (dim > 1 ? ay * dvext(d, ay) : 0.0);
-    if (pair) {
-      int cells[9];
-      const int nc = stencil(d, cell_of(d, ax, ay), cells);
-      for (int ci = 0; ci < nc; ++ci)
-        for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
-          if (b <= i) continue;
-          const double r2a = mi2(d, ax, ay, c.X(0, b, j), dim > 1 ? c.X(1, b, j) : 0.0);
-          if (r2a > rc2) continue;
-          const int bn = j == M - 1 ? c.next[b] : b;
-          const double r2b = mi2(d, bx, by, c.X(0, bn, jn), dim > 1 ? c.X(1, bn, jn) : 0.0);
-          const double v1 = vpair(d, r2a), v2 = vpair(d, r2b);
-          s[3] += 0.5 * d.tau * (v1 + v2);
-          s[4] += 0.5 * d.tau * (-2.0 * cg * r2a * v1 - 2.0 * cg * r2b * v2);
-        }
-    }
     if (density) {
-      const double bw = d.dens_bw;
-      const long long ib = (long long)floor((ax + d.L) / bw);
+      const long long ib = bin_floor(ax, d.L, d.dens_bw, inv_bw);
       bool ok = ib >= 1 && ib <= d.dens_nb;
       long long idx = ib - 1;
       if (dim > 1) {
-        const long long jb = (long long)floor((ay + d.L) / bw);
+        const long long jb = bin_floor(ay, d.L, d.dens_bw, inv_bw);
         ok = ok && jb >= 1 && jb <= d.dens_nb;
         idx += (jb - 1) * d.dens_nb;
       }
       if (ok) atomicAdd(c.hist + idx, 1ull);
+    }
+  }
+  if (pair) {
+    // a warp per bead, lanes over the higher-numbered particles of its slice
+    for (int k = warp; k < N * M; k += nwarps) {
+      const int j = k / N, i = k % N;
+      const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
+      const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+      const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
+      Prefilter f;
+      f.init(d, ax, ay, d.rc);
+      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      for (int b = i + 1 + lane; b < N; b += 32) {
+        if (!f.pass(row + (size_t)b * dim)) continue;
+        const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
+        if (r2a > rc2) continue;
+        const int bn = j == M - 1 ? c.next[b] : b;
+        const double r2b = mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn));
+        const double v1 = vpair(d, r2a), v2 = vpair(d, r2b);
+        s[3] += 0.5 * d.tau * (v1 + v2);
+        s[4] += 0.5 * d.tau * (-2.0 * cg * r2a * v1 - 2.0 * cg * r2b * v2);
+      }
     }
   }
   block_sum_k<5>(s, red);

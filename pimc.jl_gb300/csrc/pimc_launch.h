@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pimc_types.h"
 
 namespace pimc {
@@ -74,8 +76,12 @@ cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, 
                               int nchains, int maxN, cudaStream_t s);
 cudaError_t launch_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
                          int maxNM, cudaStream_t s);
-cudaError_t launch_cells(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
-                         int maxM, cudaStream_t s);
+cudaError_t launch_import(const ChainDesc *desc, double *dpool, const double *src, int chain0,
+                          int nchains, size_t maxn, cudaStream_t s);
+cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *dst, int chain0,
+                          int nchains, size_t maxn, cudaStream_t s);
+cudaError_t launch_mirror(const ChainDesc *desc, double *dpool, int chain0, int nchains, int maxNM,
+                          cudaStream_t s);
 cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);

@@ -1,11 +1,11 @@
 // pimc_sweep.cu -- kernels of the GB300 sweep engine.
 //
 // One CTA owns one chain for the duration of a sweep (or of a block of
-// sweeps).  Small chains are staged in shared memory (x, V, next with an odd
-// row stride so that thread-per-window accesses are bank-conflict free);
-// larger ones are updated in place in HBM/L2.  The same kernel serves the
-// plain path (one launch per chain) and the batched path (persistent grid
-// pulling chains from a device work queue, LPT order, captured in a graph).
+// sweeps).  Chains that fit are staged in shared memory (x, V, the FP32
+// mirror and next); larger ones are updated in place in HBM/L2.  The same
+// kernel serves the plain path (one launch per chain) and the batched path
+// (persistent grid pulling chains from a device work queue in LPT order,
+// captured in a CUDA graph).
 #include <cuda_runtime.h>
 
 #include "pimc_kernels.cuh"
@@ -20,26 +20,17 @@ __device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ip
   c.N = d->N;
   c.M = d->M;
   c.dim = d->dim;
-  c.ld = d->M;
+  c.ldn = d->N;
   c.x = dpool + d->x_off;
   c.V = dpool + d->V_off;
+  c.xf = (float *)(dpool + d->xf_off);
   c.next = ipool + d->next_off;
   c.tab = (const double2 *)(dpool + d->tab_off);
-  if (d->cell_off >= 0) {
-    c.head = ipool + d->cell_off;
-    c.cn = c.head + (size_t)d->M * d->ncell;
-    c.cp = c.cn + (size_t)d->M * d->N;
-  } else {
-    c.head = c.cn = c.cp = nullptr;
-  }
-  c.hist = d->dens_off >= 0 ? upool + d->dens_off : nullptr;
+  c.hist = (d->dens_off >= 0 && upool) ? upool + d->dens_off : nullptr;
   c.eser = d->eser_off >= 0 ? dpool + d->eser_off : nullptr;
   return c;
 }
 
-__device__ __forceinline__ bool chain_has_cells(const ChainDesc &d) {
-  return (d.flags & (PF_PAIR | PF_HARD)) != 0;
-}
 // moves whose acceptance depends on other paths at the same slice
 __device__ __forceinline__ bool chain_serial_local(const ChainDesc &d) {
   return ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) || (d.flags & PF_HARD);
@@ -81,7 +72,6 @@ struct SmemCtl {
   MixDev mix;
   double red[256];
   double e4[4];
-  int ired[32];
   int iflag[8];
   int chain;
 };
@@ -93,11 +83,10 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = nt >> 5;
   const int N = c.N, M = c.M;
-  const bool cells = chain_has_cells(d);
   const bool serial_local = chain_serial_local(d);
   const unsigned long long sweep = sc.v.sweep;
   double *wsb = (double *)scratch + (size_t)warp * warp_scratch_d;
-  // per-thread tallies: attempts, accepts (x4), skips, bead updates
+  // per-thread tallies: attempts x4, accepts x4, skips, bead updates
   double tal[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
   // ---- staging phases (ReshapeLinear)
@@ -109,9 +98,12 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
     const int o = min(M - 1, (int)(so.uni(0) * M));
     const int items = N * k;
     if (!serial_local) {
+      // every window of the phase is independent: slot s of particle n moves
+      // the beads strictly inside its slot; item order s*N + n makes
+      // neighbouring threads touch neighbouring particles of one slice
       if (ell <= TWMAX) {
         for (int it = tid; it < items; it += nt) {
-          const int n = it / k, s = it % k;
+          const int s = it / N, n = it % N;
           const int len = s < k - 1 ? ell : M - (k - 1) * ell;
           if (len < 2) continue;
           const int st = (o + s * ell) % M;
@@ -124,13 +116,13 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         }
       } else {
         for (int it = warp; it < items; it += nwarps) {
-          const int n = it / k, s = it % k;
+          const int s = it / N, n = it % N;
           const int len = s < k - 1 ? ell : M - (k - 1) * ell;
           if (len < 2) continue;
           const int st = (o + s * ell) % M;
           GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + it)));
           const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr, false);
+          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
           if (lane == 0) {
             tal[0] += 1.0;
             tal[4] += r == RES_ACCEPT;
@@ -138,23 +130,18 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
           }
         }
       }
-      __syncthreads();
-      if (cells) {
-        for (int j = tid; j < M; j += nt) cells_rebuild_slice(c, j);
-        __syncthreads();
-      }
     } else {
-      // windows of one slot touch each other through the pair action or the
-      // hard core: a warp walks the particles of its slot in order; distinct
+      // windows of one slot interact through the pair action or the hard
+      // core: a warp walks the particles of its slot in order; distinct
       // slots share only their fixed end slices and run concurrently
       for (int s = warp; s < k; s += nwarps) {
         const int len = s < k - 1 ? ell : M - (k - 1) * ell;
         if (len < 2) continue;
         const int st = (o + s * ell) % M;
         for (int n = 0; n < N; ++n) {
-          GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + n * k + s)));
+          GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + s * N + n)));
           const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr, cells);
+          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
           if (lane == 0) {
             tal[0] += 1.0;
             tal[4] += r == RES_ACCEPT;
@@ -162,70 +149,67 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
           }
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
   }
 
-  // ---- permutation swaps (ReshapeSwapLinear), one at a time
+  // ---- permutation swaps (ReshapeSwapLinear), one at a time by warp 0
   if (N > 1 && mix.swaps_per_sweep > 0) {
-    SwapScratch S;
-    S.carve(scratch, N, M);
-    const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
-    for (int a = 0; a < mix.swaps_per_sweep; ++a) {
-      const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
-      const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
-      const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
-      const int sm = max(2, sc.v.swap_m);
-      const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
-      const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
-      const double upick = u53(r1.z, r1.w);
-      GenDraws dr = gen_draws(ss);
-      const int r = swap_cta(c, j0, m, n1, upick, dr, S, sc.red, sc.ired, &sc.iflag[0], nullptr,
-                             nullptr, cells);
-      if (tid == 0) {
-        if (r == RES_SKIP) {
-          tal[8] += 1.0;
-        } else {
-          tal[1] += 1.0;
-          tal[5] += r == RES_ACCEPT;
-          if (r != RES_HARDCORE) tal[9] += 2.0 * (m - 1);
+    if (warp == 0) {
+      SwapScratch S;
+      S.carve(scratch, N);
+      const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
+      for (int a = 0; a < mix.swaps_per_sweep; ++a) {
+        const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
+        const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
+        const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
+        const int sm = max(2, sc.v.swap_m);
+        const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
+        const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
+        const double upick = u53(r1.z, r1.w);
+        GenDraws dr = gen_draws(ss);
+        const int r = swap_warp<true>(c, j0, m, n1, upick, dr, S, nullptr, nullptr);
+        if (lane == 0) {
+          if (r == RES_SKIP) {
+            tal[8] += 1.0;
+          } else {
+            tal[1] += 1.0;
+            tal[5] += r == RES_ACCEPT;
+            if (r != RES_HARDCORE) tal[9] += 2.0 * (m - 1);
+          }
         }
       }
     }
+    __syncthreads();
   }
 
   // ---- single-path centre of mass
   for (int ph = 0; ph < mix.com_phases; ++ph) {
     const double step = sc.v.com_step;
     if (!serial_local) {
-      for (int n = warp; n < N; n += nwarps) {
+      for (int n = tid; n < N; n += nt) {
         if (c.next[n] != n) continue;
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_warp(c, n, step, dr, wsb, false);
-        if (lane == 0) {
+        const int r = com_thread(c, n, step, dr);
+        tal[2] += 1.0;
+        tal[6] += r;
+        tal[9] += M;
+      }
+      __syncthreads();
+    } else {
+      int *pol = (int *)scratch, *idx = pol + N;
+      double *q = (double *)(pol + 2 * N);
+      for (int n = 0; n < N; ++n) {
+        if (c.next[n] != n) continue;
+        GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
+        const int r = com_cta(c, n, false, step, dr, pol, idx, q, sc.red, &sc.iflag[2], nullptr);
+        if (tid == 0) {
           tal[2] += 1.0;
           tal[6] += r == RES_ACCEPT;
           if (r != RES_HARDCORE) tal[9] += M;
         }
-      }
-      __syncthreads();
-      if (cells) {
-        for (int j = tid; j < M; j += nt) cells_rebuild_slice(c, j);
         __syncthreads();
       }
-    } else {
-      if (warp == 0)
-        for (int n = 0; n < N; ++n) {
-          if (c.next[n] != n) continue;
-          GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-          const int r = com_warp(c, n, step, dr, wsb, cells);
-          if (lane == 0) {
-            tal[2] += 1.0;
-            tal[6] += r == RES_ACCEPT;
-            if (r != RES_HARDCORE) tal[9] += M;
-          }
-        }
-      __syncthreads();
     }
   }
 
@@ -244,9 +228,9 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
       __syncthreads();
       if (!sc.iflag[1]) continue;
       GenDraws dr = gen_draws(make_stream(d, sweep, PH_PCOM, (unsigned)(ph * N + n)));
-      int np = 0;
-      const int r = pcom_cta(c, n, sc.v.pcom_step, dr, pol, idx, sc.red, &sc.iflag[2], &sc.iflag[3], cells);
-      np = sc.iflag[3];
+      const int r = com_cta(c, n, true, sc.v.pcom_step, dr, pol, idx, nullptr, sc.red,
+                            &sc.iflag[2], &sc.iflag[3]);
+      const int np = sc.iflag[3];
       if (tid == 0) {
         tal[3] += 1.0;
         tal[7] += r == RES_ACCEPT;
@@ -258,31 +242,31 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
 
   // ---- tallies and adaptation (once per sweep)
   {
-    double t6[6] = {tal[0], tal[1], tal[2], tal[3], tal[8], tal[9]};
-    double a4[4] = {tal[4], tal[5], tal[6], tal[7]};
-    block_sum_k<6>(t6, sc.red);
-    block_sum_k<4>(a4, sc.red);
+    double t8[8] = {tal[0], tal[1], tal[2], tal[3], tal[4], tal[5], tal[6], tal[7]};
+    double t2[2] = {tal[8], tal[9]};
+    block_sum_k<8>(t8, sc.red);
+    block_sum_k<2>(t2, sc.red);
     if (tid == 0) {
       ChainVar &v = sc.v;
       for (int q = 0; q < 4; ++q) {
-        v.att[q] += (unsigned long long)t6[q];
-        v.acc[q] += (unsigned long long)a4[q];
+        v.att[q] += (unsigned long long)t8[q];
+        v.acc[q] += (unsigned long long)t8[4 + q];
       }
-      v.skips += (unsigned long long)t6[4];
-      v.bead_updates += t6[5];
+      v.skips += (unsigned long long)t2[0];
+      v.bead_updates += t2[1];
       if (mix.adapt) {
         // the reference divides by an empty queue (NaN) and leaves var alone
-        if (t6[0] > 0)
-          adapt_slices(v.stage_m, a4[0] / t6[0], mix.stage_min, mix.stage_max, mix.stage_minacc,
+        if (t8[0] > 0)
+          adapt_slices(v.stage_m, t8[4] / t8[0], mix.stage_min, mix.stage_max, mix.stage_minacc,
                        mix.stage_maxacc);
-        if (t6[1] > 0)
-          adapt_slices(v.swap_m, a4[1] / t6[1], mix.swap_min, mix.swap_max, mix.swap_minacc,
+        if (t8[1] > 0)
+          adapt_slices(v.swap_m, t8[5] / t8[1], mix.swap_min, mix.swap_max, mix.swap_minacc,
                        mix.swap_maxacc);
-        if (t6[2] > 0)
-          adapt_step(v.com_step, a4[2] / t6[2], mix.com_minstep, mix.com_maxstep, mix.com_minacc,
+        if (t8[2] > 0)
+          adapt_step(v.com_step, t8[6] / t8[2], mix.com_minstep, mix.com_maxstep, mix.com_minacc,
                      mix.com_maxacc);
-        if (t6[3] > 0)
-          adapt_step(v.pcom_step, a4[3] / t6[3], mix.pcom_minstep, mix.pcom_maxstep,
+        if (t8[3] > 0)
+          adapt_step(v.pcom_step, t8[7] / t8[3], mix.pcom_minstep, mix.pcom_maxstep,
                      mix.pcom_minacc, mix.pcom_maxacc);
       }
     }
@@ -324,30 +308,31 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
     CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
     const int N = d.N, M = d.M, dim = d.dim;
     const bool staged = d.smem_bytes > 0 && d.smem_bytes <= a.state_bytes;
+    const size_t nx = (size_t)dim * M * N, nv = (size_t)M * N;
     if (staged) {
-      const int ldm = (M & 1) ? M : M + 1;
       double *sx = (double *)smem;
-      double *sV = sx + (size_t)dim * N * ldm;
-      int *snx = (int *)(sV + (size_t)N * ldm);
-      for (int e = tid; e < dim * N * M; e += nt) {
-        const int row = e / M, j = e % M;
-        sx[(size_t)row * ldm + j] = c.x[e];
-      }
-      for (int e = tid; e < N * M; e += nt) sV[(size_t)(e / M) * ldm + e % M] = c.V[e];
+      double *sV = sx + nx;
+      float *sf = (float *)(sV + nv);
+      int *snx = (int *)(sf + nx);
+      for (size_t e = tid; e < nx; e += nt) sx[e] = c.x[e];
+      for (size_t e = tid; e < nv; e += nt) sV[e] = c.V[e];
+      for (size_t e = tid; e < nx; e += nt) sf[e] = c.xf[e];
       for (int e = tid; e < N; e += nt) snx[e] = c.next[e];
       c.x = sx;
       c.V = sV;
+      c.xf = sf;
       c.next = snx;
-      c.ld = ldm;
       __syncthreads();
     }
     unsigned char *scratch = smem + a.state_bytes;
     for (int s = 0; s < a.sweeps; ++s) sweep_one(sc, c, scratch, a.warp_scratch_d);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
+      float *gf = (float *)(a.dpool + d.xf_off);
       int *gn = a.ipool + d.next_off;
-      for (int e = tid; e < dim * N * M; e += nt) gx[e] = c.x[(size_t)(e / M) * c.ld + e % M];
-      for (int e = tid; e < N * M; e += nt) gV[e] = c.V[(size_t)(e / M) * c.ld + e % M];
+      for (size_t e = tid; e < nx; e += nt) gx[e] = c.x[e];
+      for (size_t e = tid; e < nv; e += nt) gV[e] = c.V[e];
+      for (size_t e = tid; e < nx; e += nt) gf[e] = c.xf[e];
       for (int e = tid; e < N; e += nt) gn[e] = c.next[e];
     }
     if (tid == 0) a.var[sc.chain] = sc.v;
@@ -369,7 +354,6 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   __syncthreads();
   const ChainDesc &d = sc.d;
   CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-  const bool cells = chain_has_cells(d);
   InjDraws dr;
   dr.nrm = a.normals;
   dr.n_nrm = a.n_normals;
@@ -379,32 +363,32 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   dr.pu = 0;
   dr.exh = 0;
   int res = 0, extra = -1;
-  bool rebuild = false;
+  const bool serial = chain_serial_local(d);
   if (a.kind == MV_STAGE) {
-    const bool use_warp = chain_serial_local(d) || a.force_warp || a.m > TWMAX;
+    const bool use_warp = serial || a.force_warp || a.m > TWMAX;
     if (use_warp) {
-      if (tid < 32) res = window_warp(c, a.n, a.j0, a.m, dr, true, (double *)smem, a.prop, cells);
+      if (tid < 32) res = window_warp(c, a.n, a.j0, a.m, dr, true, (double *)smem, a.prop);
     } else {
       if (tid == 0) res = window_thread(c, a.n, a.j0, a.m, dr, true, a.prop);
-      rebuild = cells;
     }
   } else if (a.kind == MV_SWAP) {
-    SwapScratch S;
-    S.carve(smem, d.N, d.M);
-    res = swap_cta(c, a.j0, a.m, a.n, a.u_pick, dr, S, sc.red, sc.ired, &sc.iflag[0], a.prop,
-                   &sc.iflag[4], cells);
+    if (tid < 32) {
+      SwapScratch S;
+      S.carve(smem, d.N);
+      res = swap_warp<false>(c, a.j0, a.m, a.n, a.u_pick, dr, S, a.prop, &sc.iflag[4]);
+    }
+    __syncthreads();
     extra = sc.iflag[4];
-  } else if (a.kind == MV_COM) {
-    if (tid < 32) res = com_warp(c, a.n, a.step, dr, (double *)smem, cells);
+  } else if (a.kind == MV_COM && !serial && !a.force_warp) {
+    if (tid == 0) res = com_thread(c, a.n, a.step, dr);
   } else {
     int *pol = (int *)smem, *idx = pol + d.N;
-    res = pcom_cta(c, a.n, a.step, dr, pol, idx, sc.red, &sc.iflag[2], &sc.iflag[3], cells);
+    double *q = (double *)(pol + 2 * d.N);
+    res = com_cta(c, a.n, a.kind == MV_PCOM, a.step, dr, pol, idx, q, sc.red, &sc.iflag[2],
+                  &sc.iflag[3]);
     extra = sc.iflag[3];
   }
   __syncthreads();
-  if (rebuild) {
-    for (int j = tid; j < d.M; j += blockDim.x) cells_rebuild_slice(c, j);
-  }
   if (tid == 0) {
     a.out[0] = res;
     a.out[1] = extra;
@@ -419,7 +403,8 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
   __shared__ SmemCtl sc;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = nt >> 5;
   if (tid == 0) sc.d = a.desc[a.chain];
   __syncthreads();
   const ChainDesc &d = sc.d;
@@ -428,24 +413,30 @@ __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
   const double den = 4.0 * d.tau * d.lambda, mhtau = -0.5 * d.tau, rc2 = d.rc * d.rc;
   double s[4] = {0.0, 0.0, 0.0, 0.0};
   for (int k = tid; k < N * M; k += nt) {
-    const int i = k / M, j = k % M;
+    const int j = k / N, i = k % N;
     const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-    const double ax = c.X(0, i, j), ay = dim > 1 ? c.X(1, i, j) : 0.0;
-    const double bx = c.X(0, in, jn), by = dim > 1 ? c.X(1, in, jn) : 0.0;
+    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+    const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
     s[0] += -mi2(d, ax, ay, bx, by) / den;
     s[1] += mhtau * (vext(d, ax, ay) + vext(d, bx, by));
     s[3] += c.Vl(i, j);
-    if (d.flags & PF_PAIR) {
-      int cells[9];
-      const int nc = stencil(d, cell_of(d, ax, ay), cells);
-      for (int ci = 0; ci < nc; ++ci)
-        for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
-          if (b <= i) continue;
-          const double r2a = mi2(d, ax, ay, c.X(0, b, j), dim > 1 ? c.X(1, b, j) : 0.0);
-          if (r2a > rc2) continue;
-          const int bn = j == M - 1 ? c.next[b] : b;
-          s[2] += lnU2(d, r2a, mi2(d, bx, by, c.X(0, bn, jn), dim > 1 ? c.X(1, bn, jn) : 0.0));
-        }
+  }
+  if (d.flags & PF_PAIR) {
+    for (int k = warp; k < N * M; k += nwarps) {
+      const int j = k / N, i = k % N;
+      const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
+      const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+      const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
+      Prefilter f;
+      f.init(d, ax, ay, d.rc);
+      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      for (int b = i + 1 + lane; b < N; b += 32) {
+        if (!f.pass(row + (size_t)b * dim)) continue;
+        const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
+        if (r2a > rc2) continue;
+        const int bn = j == M - 1 ? c.next[b] : b;
+        s[2] += lnU2(d, r2a, mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn)));
+      }
     }
   }
   block_sum_k<4>(s, sc.red);
@@ -454,8 +445,10 @@ __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
 }
 
 __global__ void k_eval_weights(EvalArgs a) {
-  if (threadIdx.x != 0) return;
-  const ChainDesc d = a.desc[a.chain];
+  __shared__ ChainDesc d;
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) d = a.desc[a.chain];
+  __syncthreads();
   CV c = make_cv(&d, a.dpool, a.ipool, a.upool);
   const int M = c.M, dim = c.dim, n = a.n, j0 = a.j0, m = a.m;
   const int nx = c.next[n];
@@ -464,81 +457,121 @@ __global__ void k_eval_weights(EvalArgs a) {
   auto px = [&](int t) { return rp[t * dim]; };
   auto py = [&](int t) { return dim > 1 ? rp[t * dim + 1] : 0.0; };
   double wi = 0.0, wu = 0.0;
-  for (int t = 0; t < m; ++t) {
-    const int ab = j0 + t;
-    wi += c.Vl(ab < M ? n : nx, ab < M ? ab : ab - M);
+  if (lane == 0) {
+    for (int t = 0; t < m; ++t) {
+      const int ab = j0 + t;
+      wi += c.Vl(ab < M ? n : nx, ab < M ? ab : ab - M);
+    }
+    for (int t = 0; t < m; ++t) wu += mhtau * (vext(d, px(t), py(t)) + vext(d, px(t + 1), py(t + 1)));
   }
-  for (int t = 0; t < m; ++t) wu += mhtau * (vext(d, px(t), py(t)) + vext(d, px(t + 1), py(t + 1)));
   if ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) {
     for (int t = 0; t < m; ++t) {
       const int ab = j0 + t, ab1 = ab + 1;
       const int o = ab < M ? n : nx, j = ab < M ? ab : ab - M;
       const int o1 = ab1 < M ? n : nx, j1 = ab1 < M ? ab1 : ab1 - M;
-      wi += pair_link(c, c.X(0, o, j), dim > 1 ? c.X(1, o, j) : 0.0, c.X(0, o1, j1),
-                      dim > 1 ? c.X(1, o1, j1) : 0.0, j, o, -1);
-      wu += pair_link(c, px(t), py(t), px(t + 1), py(t + 1), j, o, -1);
+      pair_link_lanes(c, j, o, -1, o, -1, nullptr, true, true, c.X(0, o, j), c.Xd(1, o, j),
+                      c.X(0, o1, j1), c.Xd(1, o1, j1), px(t), py(t), px(t + 1), py(t + 1), wi, wu,
+                      lane, 32);
     }
   }
-  a.out[0] = wi;
-  a.out[1] = wu;
+  wi = warp_sum(wi);
+  wu = warp_sum(wu);
+  if (threadIdx.x == 0) {
+    a.out[0] = wi;
+    a.out[1] = wu;
+  }
 }
 
 // ---------------------------------------------------------------------------
-// state maintenance: init_world, cached links, cell lists, measurements
+// state maintenance: layout transposes, init_world, cached links + mirror,
+// measurements
 // ---------------------------------------------------------------------------
+// host layout x[d][n][j] (a batch buffer at d.host_off) -> device x[d][j][n]
+__global__ void k_import(const ChainDesc *desc, double *dpool, const double *src, int chain0) {
+  const ChainDesc &d = desc[chain0 + blockIdx.y];
+  const size_t tot = (size_t)d.dim * d.N * d.M;
+  double *x = dpool + d.x_off;
+  const double *s = src + d.host_off;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = e / ((size_t)d.M * d.N), r = e % ((size_t)d.M * d.N);
+    const size_t j = r / d.N, n = r % d.N;
+    x[e] = s[(k * d.N + n) * d.M + j];
+  }
+}
+
+__global__ void k_export(const ChainDesc *desc, const double *dpool, double *dst, int chain0) {
+  const ChainDesc &d = desc[chain0 + blockIdx.y];
+  const size_t tot = (size_t)d.dim * d.N * d.M;
+  const double *x = dpool + d.x_off;
+  double *o = dst + d.host_off;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
+       e += (size_t)gridDim.x * blockDim.x) {
+    const size_t k = e / ((size_t)d.M * d.N), r = e % ((size_t)d.M * d.N);
+    const size_t n = r / d.M, j = r % d.M;
+    o[e] = x[(k * d.M + j) * d.N + n];
+  }
+}
+
 // init_world (src/system.jl:36-78): uniform start, closed Levy loop through
 // M rows whose first and last rows coincide, teleport
 __global__ void k_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= d.N) return;
-  const int M = d.M, N = d.N, dim = d.dim;
-  double *x = dpool + d.x_off;
-  int *next = ipool + d.next_off;
+  CV c = make_cv(&d, dpool, ipool, nullptr);
+  const int M = d.M, dim = d.dim;
   GenDraws dr = gen_draws(make_stream(d, 0, PH_INIT, (unsigned)n));
   const double L = d.L, inv2L = 1.0 / (2.0 * L);
+  double st[2] = {0.0, 0.0};
   for (int k = 0; k < dim; ++k) {
-    const double s = 2.0 * L * (dr.uniform() - 0.5);
-    x[((size_t)k * N + n) * M] = s;
-    x[((size_t)k * N + n) * M + M - 1] = s;
+    st[k] = 2.0 * L * (dr.uniform() - 0.5);
+    c.X(k, n, 0) = st[k];
+    c.X(k, n, M - 1) = st[k];
   }
   const int mm = M - 2;
+  double p[2] = {st[0], st[1]};
   for (int j = 1; j <= mm; ++j) {
     const double al = (double)(mm + 1 - j) / (double)(mm + 2 - j);
     const double sg = sqrt(2.0 * d.lambda * al * d.tau);
     double z[2];
     for (int k = 0; k < dim; ++k) z[k] = dr.normal();
     for (int k = 0; k < dim; ++k) {
-      double *row = x + ((size_t)k * N + n) * M;
-      row[j] = al * row[j - 1] + (1.0 - al) * row[M - 1] + z[k] * sg;
+      p[k] = al * p[k] + (1.0 - al) * st[k] + z[k] * sg;
+      c.X(k, n, j) = p[k];
     }
   }
-  for (int k = 0; k < dim; ++k) {
-    double *row = x + ((size_t)k * N + n) * M;
-    for (int j = 0; j < M; ++j) row[j] = teleport(row[j], L, inv2L);
-  }
-  next[n] = n;
+  for (int k = 0; k < dim; ++k)
+    for (int j = 0; j < M; ++j) c.X(k, n, j) = teleport(c.X(k, n, j), L, inv2L);
+  c.next[n] = n;
 }
 
+// cached link actions V[j][n] = lnV(bead, next bead) and the FP32 mirror
 __global__ void k_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= d.N * d.M) return;
   CV c = make_cv(&d, dpool, ipool, nullptr);
-  const int i = k / d.M, j = k % d.M;
-  const int in = j == d.M - 1 ? c.next[i] : i, jn = j + 1 == d.M ? 0 : j + 1;
-  const double ax = c.X(0, i, j), ay = d.dim > 1 ? c.X(1, i, j) : 0.0;
-  const double bx = c.X(0, in, jn), by = d.dim > 1 ? c.X(1, in, jn) : 0.0;
-  c.Vl(i, j) = -0.5 * d.tau * (vext(d, ax, ay) + vext(d, bx, by));
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.N * d.M; k += gridDim.x * blockDim.x) {
+    const int j = k / d.N, i = k % d.N;
+    const int in = j == d.M - 1 ? c.next[i] : i, jn = j + 1 == d.M ? 0 : j + 1;
+    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+    const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
+    c.Vl(i, j) = -0.5 * d.tau * (vext(d, ax, ay) + vext(d, bx, by));
+    float *f = c.xf + ((size_t)j * c.ldn + i) * d.dim;
+    f[0] = (float)ax;
+    if (d.dim > 1) f[1] = (float)ay;
+  }
 }
 
-__global__ void k_cells(const ChainDesc *desc, double *dpool, int *ipool, int chain0) {
+// the FP32 mirror alone (after verbatim state uploads)
+__global__ void k_mirror(const ChainDesc *desc, double *dpool, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
-  if (d.cell_off < 0) return;
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= d.M) return;
-  CV c = make_cv(&d, dpool, ipool, nullptr);
-  cells_rebuild_slice(c, j);
+  CV c = make_cv(&d, dpool, nullptr, nullptr);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.N * d.M; k += gridDim.x * blockDim.x) {
+    const int j = k / d.N, i = k % d.N;
+    float *f = c.xf + ((size_t)j * c.ldn + i) * d.dim;
+    f[0] = (float)c.X(0, i, j);
+    if (d.dim > 1) f[1] = (float)c.X(1, i, j);
+  }
 }
 
 __global__ void __launch_bounds__(256) k_measure(const ChainDesc *desc, ChainVar *var, double *dpool,
@@ -560,7 +593,9 @@ __global__ void __launch_bounds__(256) k_measure(const ChainDesc *desc, ChainVar
 
 // ---------------------------------------------------------------------------
 // adjoint of the potential action S_pot = -sum lnV - sum lnU:
-// per-bead dS/dr and dS/d(V0, omega, g).  Bead-parallel over one chain.
+// per-bead dS/dr and dS/d(V0, omega, g).  Bead-parallel over one chain;
+// consecutive threads are consecutive particles of one slice, so the slice
+// row they scan is shared.
 // part[block][8]: S_ext, dV0, domega, S_pair, dg, pair virial, r.g_ext, 0
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double mi_signed(double a, double b, double L) {
@@ -572,17 +607,19 @@ __device__ __forceinline__ double mi_signed(double a, double b, double L) {
 
 __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
   __shared__ double red[256];
-  const ChainDesc d = a.desc[a.chain];
+  __shared__ ChainDesc d;
+  if (threadIdx.x == 0) d = a.desc[a.chain];
+  __syncthreads();
   CV c = make_cv(&d, a.dpool, a.ipool, nullptr);
   const int N = c.N, M = c.M, dim = c.dim;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (k < N * M) {
-    const int i = k / M, j = k % M;
+    const int j = k / N, i = k % N;
     const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
     const double tau = d.tau;
-    const double ax = c.X(0, i, j), ay = dim > 1 ? c.X(1, i, j) : 0.0;
-    const double anx = c.X(0, in, jn), any = dim > 1 ? c.X(1, in, jn) : 0.0;
+    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+    const double anx = c.X(0, in, jn), any = c.Xd(1, in, jn);
     double ge[2] = {tau * dvext(d, ax), dim > 1 ? tau * dvext(d, ay) : 0.0};
     v[0] = tau * vext(d, ax, ay);
     if (d.flags & PF_LATT) {
@@ -594,44 +631,41 @@ __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
     double go[2] = {0.0, 0.0}, gn[2] = {0.0, 0.0};
     if (d.flags & PF_PAIR) {
       const double rc2 = d.rc * d.rc, cg = d.inv2s2, h = 0.5 * tau;
-      int cells[9];
-      const int nc = stencil(d, cell_of(d, ax, ay), cells);
-      for (int ci = 0; ci < nc; ++ci)
-        for (int b = c.head[(size_t)j * d.ncell + cells[ci]]; b >= 0; b = c.cn[(size_t)j * N + b]) {
-          if (b == i) continue;
-          const double bxv = c.X(0, b, j), byv = dim > 1 ? c.X(1, b, j) : 0.0;
-          const double d1x = mi_signed(ax, bxv, d.L), d1y = dim > 1 ? mi_signed(ay, byv, d.L) : 0.0;
-          const double r2a = d1x * d1x + d1y * d1y;
-          if (r2a > rc2) continue;
-          const int bn = j == M - 1 ? c.next[b] : b;
-          const double bnx = c.X(0, bn, jn), bny = dim > 1 ? c.X(1, bn, jn) : 0.0;
-          const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
-          const double r2b = d2x * d2x + d2y * d2y;
-          const double e1 = exp(-r2a * cg), e2 = exp(-r2b * cg);
-          const double v1 = d.g * e1, v2 = d.g * e2;
-          go[0] += h * (-2.0 * cg * v1) * d1x;
-          go[1] += h * (-2.0 * cg * v1) * d1y;
-          gn[0] += h * (-2.0 * cg * v2) * d2x;
-          gn[1] += h * (-2.0 * cg * v2) * d2y;
-          // each unordered pair is visited from both sides
-          v[3] += 0.5 * h * (v1 + v2);
-          v[4] += 0.5 * h * (e1 + e2);
-          v[5] += 0.5 * h * (-2.0 * cg) * (r2a * v1 + r2b * v2);
-        }
+      Prefilter f;
+      f.init(d, ax, ay, d.rc);
+      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      for (int b = 0; b < N; ++b) {
+        if (b == i || !f.pass(row + (size_t)b * dim)) continue;
+        const double bxv = c.X(0, b, j), byv = c.Xd(1, b, j);
+        const double d1x = mi_signed(ax, bxv, d.L), d1y = dim > 1 ? mi_signed(ay, byv, d.L) : 0.0;
+        const double r2a = mi2(d, ax, ay, bxv, byv);
+        if (r2a > rc2) continue;
+        const int bn = j == M - 1 ? c.next[b] : b;
+        const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
+        const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
+        const double r2b = mi2(d, anx, any, bnx, bny);
+        const double e1 = exp(-r2a * cg), e2 = exp(-r2b * cg);
+        const double v1 = d.g * e1, v2 = d.g * e2;
+        go[0] += h * (-2.0 * cg * v1) * d1x;
+        go[1] += h * (-2.0 * cg * v1) * d1y;
+        gn[0] += h * (-2.0 * cg * v2) * d2x;
+        gn[1] += h * (-2.0 * cg * v2) * d2y;
+        // each unordered pair is visited from both sides
+        v[3] += 0.5 * h * (v1 + v2);
+        v[4] += 0.5 * h * (e1 + e2);
+        v[5] += 0.5 * h * (-2.0 * cg) * (r2a * v1 + r2b * v2);
+      }
     }
-    for (int q = 0; q < dim; ++q) {
-      a.gA[(size_t)k * 2 + q] = ge[q] + go[q];
-      a.gB[(size_t)k * 2 + q] = gn[q];
+    // per-bead buffers in the chain's [i][j] order (k2 = i*M + j)
+    const size_t k2 = (size_t)i * M + j;
+    for (int q = 0; q < 2; ++q) {
+      a.gA[k2 * 2 + q] = ge[q] + go[q];
+      a.gB[k2 * 2 + q] = gn[q];
     }
   }
-  block_sum_k<6>(*reinterpret_cast<double(*)[6]>(v), red);
-  double w2[2] = {v[6], v[7]};
-  block_sum_k<2>(w2, red);
-  if (threadIdx.x == 0) {
-    for (int q = 0; q < 6; ++q) a.part[(size_t)blockIdx.x * 8 + q] = v[q];
-    a.part[(size_t)blockIdx.x * 8 + 6] = w2[0];
-    a.part[(size_t)blockIdx.x * 8 + 7] = w2[1];
-  }
+  block_sum_k<8>(v, red);
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 8; ++q) a.part[(size_t)blockIdx.x * 8 + q] = v[q];
 }
 
 __global__ void k_inverse_next(AdjArgs a) {
@@ -643,10 +677,12 @@ __global__ void k_inverse_next(AdjArgs a) {
 
 __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
   __shared__ double red[256];
-  const ChainDesc d = a.desc[a.chain];
+  __shared__ ChainDesc d;
+  if (threadIdx.x == 0) d = a.desc[a.chain];
+  __syncthreads();
   CV c = make_cv(&d, a.dpool, a.ipool, nullptr);
   const int N = c.N, M = c.M, dim = c.dim;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;  // k = i*M + j
   double rg[1] = {0.0};
   if (k < N * M) {
     const int i = k / M, j = k % M;
@@ -663,14 +699,9 @@ __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
     double t[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = threadIdx.x; b < a.nblocks; b += blockDim.x)
       for (int q = 0; q < 8; ++q) t[q] += a.part[(size_t)b * 8 + q];
-    block_sum_k<6>(*reinterpret_cast<double(*)[6]>(t), red);
-    double t2[2] = {t[6], t[7]};
-    block_sum_k<2>(t2, red);
-    if (threadIdx.x == 0) {
-      for (int q = 0; q < 6; ++q) a.totals[q] = t[q];
-      a.totals[6] = t2[0];
-      a.totals[7] = t2[1];
-    }
+    block_sum_k<8>(t, red);
+    if (threadIdx.x == 0)
+      for (int q = 0; q < 8; ++q) a.totals[q] = t[q];
   }
 }
 
@@ -701,6 +732,18 @@ cudaError_t launch_eval_weights(const EvalArgs &a, cudaStream_t s) {
   k_eval_weights<<<1, 32, 0, s>>>(a);
   return cudaGetLastError();
 }
+cudaError_t launch_import(const ChainDesc *desc, double *dpool, const double *src, int chain0,
+                          int nchains, size_t maxn, cudaStream_t s) {
+  dim3 g((unsigned)std::min<size_t>((maxn + 255) / 256, 1024), nchains);
+  k_import<<<g, 256, 0, s>>>(desc, dpool, src, chain0);
+  return cudaGetLastError();
+}
+cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *dst, int chain0,
+                          int nchains, size_t maxn, cudaStream_t s) {
+  dim3 g((unsigned)std::min<size_t>((maxn + 255) / 256, 1024), nchains);
+  k_export<<<g, 256, 0, s>>>(desc, dpool, dst, chain0);
+  return cudaGetLastError();
+}
 cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0,
                               int nchains, int maxN, cudaStream_t s) {
   dim3 g((maxN + 127) / 128, nchains);
@@ -709,14 +752,14 @@ cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, 
 }
 cudaError_t launch_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
                          int maxNM, cudaStream_t s) {
-  dim3 g((maxNM + 255) / 256, nchains);
+  dim3 g((unsigned)std::min((maxNM + 255) / 256, 1024), nchains);
   k_links<<<g, 256, 0, s>>>(desc, dpool, ipool, chain0);
   return cudaGetLastError();
 }
-cudaError_t launch_cells(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
-                         int maxM, cudaStream_t s) {
-  dim3 g((maxM + 63) / 64, nchains);
-  k_cells<<<g, 64, 0, s>>>(desc, dpool, ipool, chain0);
+cudaError_t launch_mirror(const ChainDesc *desc, double *dpool, int chain0, int nchains, int maxNM,
+                          cudaStream_t s) {
+  dim3 g((unsigned)std::min((maxNM + 255) / 256, 1024), nchains);
+  k_mirror<<<g, 256, 0, s>>>(desc, dpool, chain0);
   return cudaGetLastError();
 }
 cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,

@@ -25,21 +25,22 @@ enum : unsigned {
 // constant per chain
 struct ChainDesc {
   int N, M, dim, nbins, ncell, flags, ctr, dens_nb;
-  int ld;           // row stride of x/V rows in global memory (== M)
+  int ldn;          // particle stride of a slice row in global memory (== N)
   int wtab;         // bridge-coefficient table covers windows m < wtab
   double L, tau, lambda, beta;
   double hcoef, V0, lat_k;
   double g, inv2s2, rc, hard_a, mu;
   double dens_bw;
-  long long x_off;      // doubles: x[d][n][j] at dpool + x_off
-  long long V_off;      // doubles: V[n][j]
+  long long x_off;      // doubles: x[d][j][n] (slice-major) at dpool + x_off
+  long long V_off;      // doubles: V[j][n]
+  long long xf_off;     // doubles: FP32 position mirror [j][n][d] (floats)
+  long long host_off;   // doubles: offset of the chain in a host-layout batch buffer
   long long tab_off;    // double2: bridge table (alpha, sigma)[m*wtab + t]
   long long next_off;   // ints: next[n]
-  long long cell_off;   // ints: head[M][ncell], cnext[M][N], cprev[M][N]
   long long dens_off;   // u64: hist[nb^dim]
   long long eser_off;   // doubles: energy series [cap][4]
   int eser_cap;
-  int smem_bytes;       // bytes to stage x,V,next in shared memory (0: stays global)
+  int smem_bytes;       // bytes to stage x, V, mirror, next in shared memory
   unsigned key0, key1;  // Philox key
   unsigned chain_tag;   // chain id (low 24 bits of counter word 3)
   int pad_;

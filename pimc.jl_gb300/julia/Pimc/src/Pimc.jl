@@ -1,0 +1,339 @@
+"""
+    Pimc
+
+Drop-in for oameye/PIMC.jl's user API backed by the GB300 engine
+(`libpimc_gb300.so`, C ABI in `include/pimc.h`) through `ccall`.
+
+Kept from the reference (names, keyword arguments, fields read by its
+examples and tests): `System`, `ReshapeLinear`, `ReshapeSwapLinear`,
+`SingleCenterOfMass`, `PolymerCenterOfMass`, `run!`, `apply!`,
+`acceptance`, `Density`, `Energy`, `Counter`, `Step`, `NumbOfSlices`.
+Julia closures cannot cross the ABI: the potential must be built from
+`Harmonic`, `SquareLattice` (and their sum), the interaction propagator from
+`GaussianPair`; any other closure raises (there is no CPU fallback).
+Slices and particles are 1-based on this side as in the reference.
+
+This file is written against the header and the Python mirror
+(`pimc.jl_gb300/pimc/api.py`) that the test-suite exercises; no Julia
+toolchain exists on the build machines, so it is not executed there.
+"""
+module Pimc
+
+using ChainRulesCore
+
+export System, run!, apply!, acceptance, ReshapeLinear, ReshapeSwapLinear,
+       SingleCenterOfMass, PolymerCenterOfMass, Density, Energy, Counter, Step,
+       NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients
+
+const libpimc = get(ENV, "PIMC_GB300_LIB",
+                    joinpath(@__DIR__, "..", "..", "..", "lib", "libpimc_gb300.so"))
+
+# ---------------------------------------------------------------- C structs
+struct PimcParams
+    dim::Cint; N::Cint; M::Cint
+    L::Cdouble; T::Cdouble; lambda::Cdouble; mu::Cdouble
+    harmonic_omega::Cdouble; lattice_V0::Cdouble; lattice_a::Cdouble
+    interactions::Cint; pair_g::Cdouble; pair_sigma::Cdouble
+    r_a::Cdouble; hardcore_a::Cdouble; semantics::Cint
+    seed::UInt64; density_nbins::Cint; energy_capacity::Cint; retry_cap::Cint
+end
+
+mutable struct PimcMoveMix
+    staging_phases::Cint
+    stage_slices::Cint; stage_min::Cint; stage_max::Cint
+    stage_minacc::Cdouble; stage_maxacc::Cdouble
+    swaps_per_sweep::Cint
+    swap_slices::Cint; swap_min::Cint; swap_max::Cint
+    swap_minacc::Cdouble; swap_maxacc::Cdouble
+    com_phases::Cint
+    com_step::Cdouble; com_minstep::Cdouble; com_maxstep::Cdouble
+    com_minacc::Cdouble; com_maxacc::Cdouble
+    polymer_com_phases::Cint
+    pcom_step::Cdouble; pcom_minstep::Cdouble; pcom_maxstep::Cdouble
+    pcom_minacc::Cdouble; pcom_maxacc::Cdouble
+    adapt::Cint; measure_every::Cint
+end
+
+struct PimcStats
+    attempts::NTuple{4,Culonglong}; accepts::NTuple{4,Culonglong}
+    skips::Culonglong; bead_updates::Cdouble; sweeps::Culonglong
+    measurements::Culonglong; stage_slices::Cint; swap_slices::Cint
+    com_step::Cdouble; pcom_step::Cdouble
+end
+
+function check(rc)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:pimc_last_error, libpimc), Cstring, ()))
+    error("pimc error $rc: $msg")
+end
+
+# ---------------------------------------------------------------- potentials
+struct Harmonic; omega::Float64; end
+(h::Harmonic)(r) = 0.5 * h.omega^2 * sum(abs2, r)
+struct SquareLattice; V0::Float64; a::Float64; end
+(s::SquareLattice)(r) = s.V0 * sum(x -> sin(pi * x / s.a)^2, r)
+struct PotentialSum; terms::Vector{Any}; end
+(p::PotentialSum)(r) = sum(t(r) for t in p.terms)
+Base.:+(a::Union{Harmonic,SquareLattice}, b::Union{Harmonic,SquareLattice}) = PotentialSum([a, b])
+struct GaussianPair; g::Float64; sigma::Float64; end
+(gp::GaussianPair)(r1, r2, tau) =
+    exp(-tau / 2 * (gp.g * exp(-sum(abs2, r1) / (2gp.sigma^2)) +
+                    gp.g * exp(-sum(abs2, r2) / (2gp.sigma^2))))
+
+function potential_terms(V)
+    omega, V0, a = 0.0, 0.0, 1.0
+    for t in (V isa PotentialSum ? V.terms : [V])
+        if t isa Harmonic
+            omega = t.omega
+        elseif t isa SquareLattice
+            V0, a = t.V0, t.a
+        elseif t === zero || t isa Function && t(zeros(2)) == 0 && t(ones(2)) == 0
+            nothing
+        else
+            error("potential must be Harmonic, SquareLattice or their sum")
+        end
+    end
+    return omega, V0, a
+end
+
+# ---------------------------------------------------------------- System
+mutable struct System
+    handle::Ptr{Cvoid}
+    dim::Int64; M::Int64; N::Int64; Ninit::Int64
+    μ::Float64; λ::Float64; L::Float64; vol::Float64; β::Float64; τ::Float64
+    V::Any; dV::Any; propint::Any; a::Float64; ctr::Int64
+    measure_scheme::Symbol
+    N_MC::Dict{Int64,Int64}; Nctr::Dict{Int64,Int64}; Ncycle::Int64
+    params::PimcParams
+    eser_seen::Int
+end
+
+function System(potential; dV = zero, dim::Int64 = 2, M::Int64 = 100, N::Int64 = 2,
+                μ::Float64 = 0.0, L::Float64 = 4.0, T::Float64 = 1.0, λ::Float64 = 1.0,
+                interactions::Bool = false, propint = _ -> 0.0, g::Float64 = 0.0,
+                rₐ::Float64 = 0.0, length_measurement_cycle::Int64 = 10,
+                measure_scheme::Symbol = :c, semantics::Int = 0, seed::UInt64 = UInt64(20261203))
+    omega, V0, a_lat = potential_terms(potential)
+    pg, ps = 0.0, 1.0
+    if interactions
+        propint isa GaussianPair || error("interactions=true needs propint = GaussianPair(g, σ)")
+        rₐ > 0 || error("pass rₐ (determine_nnrange is not ported)")
+        pg, ps = propint.g, propint.sigma
+    end
+    a = interactions && g > 0 ? exp(-2π / g) : 0.0
+    p = PimcParams(dim, N, M, L, T, λ, μ, omega, V0, a_lat, interactions, pg, ps, rₐ, a,
+                   semantics, seed, 0, 0, 0)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pimc_create, libpimc), Cint, (Ref{PimcParams}, Ref{Ptr{Cvoid}}), p, h))
+    s = System(h[], dim, M, N, N, μ, λ, L, (2L)^dim, 1 / T, 1 / (T * M), potential, dV,
+               propint, a, 10_000, measure_scheme, Dict(N => 0), Dict(N => 0),
+               length_measurement_cycle, p, 0)
+    finalizer(s -> ccall((:pimc_destroy, libpimc), Cint, (Ptr{Cvoid},), s.handle), s)
+    return s
+end
+
+"""Positions as the reference's `s.world[n].r` (M x dim per particle)."""
+function Base.getproperty(s::System, f::Symbol)
+    if f === :world
+        x = Vector{Float64}(undef, s.dim * s.N * s.M)
+        check(ccall((:pimc_get_beads, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), s.handle, x))
+        nx = Vector{Cint}(undef, s.N)
+        check(ccall((:pimc_get_next, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cint}), s.handle, nx))
+        X = reshape(x, s.M, s.N, s.dim)   # x[d][n][j] row-major == X[j, n, d]
+        return [(r = X[:, n, :], next = nx[n] + 1) for n in 1:s.N]
+    end
+    return getfield(s, f)
+end
+
+# ---------------------------------------------------------------- updates
+Base.@kwdef mutable struct Counter
+    queue::Vector{Bool} = Bool[]; tries::Int64 = 0; range::Int64 = 100_000; adj::Int64 = 10
+end
+mutable struct Step; size::Float64; minstep::Float64; maxstep::Float64; minacc::Float64; maxacc::Float64; end
+mutable struct NumbOfSlices; m::Int64; minslices::Int64; maxslices::Int64; minacc::Float64; maxacc::Float64; end
+acceptance(q) = sum(q) / length(q)
+
+abstract type Update end
+for (T, V) in ((:ReshapeLinear, :NumbOfSlices), (:ReshapeSwapLinear, :NumbOfSlices))
+    @eval struct $T <: Update
+        counter::Counter; var::$V; counter_var::Counter
+        $T(s::System, slices::Int64; minslices = 2, maxslices = s.M - 2, minacc = 0.6,
+           maxacc = 0.8, adj = 10, range = 10_000) =
+            new(Counter(), NumbOfSlices(min(slices, maxslices), minslices, maxslices, minacc, maxacc),
+                Counter(adj = adj, range = range))
+    end
+end
+for T in (:SingleCenterOfMass, :PolymerCenterOfMass)
+    @eval struct $T <: Update
+        counter::Counter; var::Step; counter_var::Counter
+        $T(s::System, step::Float64; minstep = 1e-1, maxstep = s.L / 2, minacc = 0.4,
+           maxacc = 0.6, adj = 10, range = 10_000) =
+            new(Counter(), Step(step, minstep, maxstep, minacc, maxacc), Counter(adj = adj, range = range))
+    end
+end
+
+# single attempts with host-drawn random numbers (src/updates/*.jl call sites)
+function (u::ReshapeLinear)(s::System)
+    n, j0 = rand(0:s.N-1), rand(0:s.M-1)
+    m = min(u.var.maxslices, rand(2:u.var.m))
+    nr, un = randn((m - 1) * s.dim * (s.a > 0 ? 64 : 1)), rand(1)
+    res = Ref{Cint}(0)
+    check(ccall((:pimc_attempt_staging, libpimc), Cint,
+                (Ptr{Cvoid}, Cint, Cint, Cint, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}, Ptr{Cdouble}),
+                s.handle, n, j0, m, nr, length(nr), un, 1, res, C_NULL))
+    acc = res[] == 1
+    push!(u.counter_var.queue, acc); u.counter_var.tries += 1
+    return acc
+end
+
+function (u::ReshapeSwapLinear)(s::System)
+    s.N <= 1 && return false
+    j0, m, n1 = rand(0:s.M-1), min(u.var.maxslices, rand(2:u.var.m)), rand(0:s.N-1)
+    nr, un = randn(2 * (m - 1) * s.dim * (s.a > 0 ? 64 : 1)), rand(1)
+    res, n2 = Ref{Cint}(0), Ref{Cint}(0)
+    check(ccall((:pimc_attempt_swap, libpimc), Cint,
+                (Ptr{Cvoid}, Cint, Cint, Cint, Cdouble, Ptr{Cdouble}, Cint, Ptr{Cdouble}, Cint,
+                 Ref{Cint}, Ref{Cint}, Ptr{Cdouble}),
+                s.handle, j0, m, n1, rand(), nr, length(nr), un, 1, res, n2, C_NULL))
+    res[] == 2 && return false
+    acc = res[] == 1
+    push!(u.counter_var.queue, acc); u.counter_var.tries += 1
+    return acc
+end
+
+for (T, fn) in ((:SingleCenterOfMass, :pimc_attempt_com), (:PolymerCenterOfMass, :pimc_attempt_polymer_com))
+    @eval function (u::$T)(s::System)
+        nx = Vector{Cint}(undef, s.N)
+        check(ccall((:pimc_get_next, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cint}), s.handle, nx))
+        cand = $(T === :SingleCenterOfMass) ? [i - 1 for i in 1:s.N if nx[i] == i - 1] : collect(0:s.N-1)
+        isempty(cand) && return false
+        un = rand(s.dim + 1)
+        res = Ref{Cint}(0)
+        check(ccall(($(QuoteNode(fn)), libpimc), Cint,
+                    (Ptr{Cvoid}, Cint, Cdouble, Ptr{Cdouble}, Cint, Ref{Cint}),
+                    s.handle, rand(cand), u.var.size, un, length(un), res))
+        acc = res[] == 1
+        push!(u.counter_var.queue, acc); u.counter_var.tries += 1
+        return acc
+    end
+end
+
+# ---------------------------------------------------------------- measurements
+mutable struct Density
+    nbins::Int64; bin::Float64; dens::Array{Float64}; ndata::Int64
+    Density(s::System; nbins = 500) = new(nbins, 2s.L / nbins, zeros(ntuple(_ -> nbins, s.dim)), 0)
+end
+mutable struct Energy
+    energy::Dict{Int64,Vector{Float64}}; energy_virial::Dict{Int64,Vector{Float64}}; n::Int
+    Energy(s::System, n = 20_000) = new(Dict(0 => Float64[]), Dict(0 => Float64[]), n)
+end
+
+# ---------------------------------------------------------------- run!
+"""
+    run!(s, n, updates; Zmeasurements)
+
+`n` attempts of the update list (src/simulation.jl:29-42) become sweeps of the
+engine: one staging phase per sweep (N ceil(M/l) windows), swaps and
+centre-of-mass moves in the 1/every proportions, measurements every
+ceil(Ncycle / attempts-per-sweep) sweeps.
+"""
+function run!(s::System, n::Int64, updates; Zmeasurements = Any[])
+    w = Dict{Symbol,Float64}(); obj = Dict{Symbol,Any}()
+    for (every, u) in updates
+        k = nameof(typeof(u)); w[k] = get(w, k, 0.0) + 1 / every; obj[k] = u
+    end
+    ws = sum(values(w))
+    st = get(obj, :ReshapeLinear, nothing)
+    ell = st === nothing ? 2 : st.var.m
+    k = cld(s.M, ell)
+    per = st === nothing ? s.N * ws / maximum(values(w)) : s.N * k * ws / w[:ReshapeLinear]
+    sweeps = max(1, round(Int, n / per)); unit = per / ws
+    frac(key) = get(w, key, 0.0) * unit
+    sw = get(obj, :ReshapeSwapLinear, nothing); cm = get(obj, :SingleCenterOfMass, nothing)
+    pc = get(obj, :PolymerCenterOfMass, nothing)
+    mix = PimcMoveMix(st === nothing ? 0 : 1, ell, st === nothing ? 2 : st.var.minslices,
+                      st === nothing ? 2 : min(st.var.maxslices, 64),
+                      st === nothing ? 0.6 : st.var.minacc, st === nothing ? 0.8 : st.var.maxacc,
+                      sw === nothing ? 0 : round(Int, frac(:ReshapeSwapLinear)),
+                      sw === nothing ? 2 : sw.var.m, 2, sw === nothing ? 2 : min(sw.var.maxslices, 64),
+                      sw === nothing ? 0.6 : sw.var.minacc, sw === nothing ? 0.8 : sw.var.maxacc,
+                      cm === nothing ? 0 : max(1, round(Int, frac(:SingleCenterOfMass) / s.N)),
+                      cm === nothing ? 1.0 : cm.var.size, 0.1, s.L / 2, 0.4, 0.6,
+                      pc === nothing ? 0 : max(1, round(Int, frac(:PolymerCenterOfMass) / s.N)),
+                      pc === nothing ? 1.0 : pc.var.size, 0.1, s.L / 2, 0.4, 0.6, 1,
+                      isempty(Zmeasurements) ? 0 : max(1, round(Int, s.Ncycle / per)))
+    check(ccall((:pimc_set_move_mix, libpimc), Cint, (Ptr{Cvoid}, Cint, Ref{PimcMoveMix}), s.handle, -1, mix))
+    check(ccall((:pimc_run, libpimc), Cint, (Ptr{Cvoid}, Clonglong), s.handle, sweeps))
+    for z in Zmeasurements
+        if z isa Energy
+            cnt = Ref{Cint}(0)
+            check(ccall((:pimc_get_energies, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+                        s.handle, 0, C_NULL, 0, cnt))
+            rows = Vector{Float64}(undef, 4 * max(cnt[], 1))
+            check(ccall((:pimc_get_energies, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+                        s.handle, 0, rows, cnt[], cnt))
+            R = reshape(rows, 4, :)
+            append!(get!(z.energy, s.N, Float64[]), R[1, s.eser_seen+1:cnt[]])
+            append!(get!(z.energy_virial, s.N, Float64[]), R[2, s.eser_seen+1:cnt[]])
+            s.N_MC[s.N] = get(s.N_MC, s.N, 0) + cnt[] - s.eser_seen
+            s.eser_seen = cnt[]
+        end
+    end
+    return nothing
+end
+
+function apply!(s::System, f::Update)
+    acc = f(s)
+    push!(f.counter.queue, acc); f.counter.tries += 1
+    if f.counter_var.tries % f.counter_var.adj == 0 && !isempty(f.counter_var.queue)
+        a = acceptance(f.counter_var.queue)
+        if f.var isa Step
+            f.var.size = clamp(a < f.var.minacc ? f.var.size * 0.9 : a > f.var.maxacc ? f.var.size * 1.1 : f.var.size,
+                               f.var.minstep, f.var.maxstep)
+        else
+            f.var.m = clamp(a < f.var.minacc ? f.var.m - 1 : a > f.var.maxacc ? f.var.m + 1 : f.var.m,
+                            f.var.minslices, f.var.maxslices)
+        end
+    end
+    return nothing
+end
+
+# ---------------------------------------------------------------- adjoint
+"""
+    action_gradients(s) -> (S_pot, dS/dr [dim, N, M] as x[d][n][j], dS/d(V0, ω, g))
+
+The potential part of the action and its adjoint from the device kernel.
+"""
+function action_gradients(s::System)
+    g = Vector{Float64}(undef, s.dim * s.N * s.M)
+    th = zeros(3); ex = zeros(4)
+    check(ccall((:pimc_adjoint, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}),
+                s.handle, 0, g, th, ex))
+    return ex[1] + ex[2], g, th
+end
+
+struct PotentialParams; V0::Float64; ω::Float64; g::Float64; end
+
+"""
+    potential_action(s, θ::PotentialParams) -> S_pot
+
+The potential action of the current paths at parameters θ; differentiable in
+θ through a ChainRulesCore rrule backed by the adjoint kernel.
+"""
+function potential_action(s::System, θ::PotentialParams)
+    check(ccall((:pimc_set_potential, libpimc), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble),
+                s.handle, 0, θ.V0, θ.ω, θ.g))
+    S, _, _ = action_gradients(s)
+    return S
+end
+
+function ChainRulesCore.rrule(::typeof(potential_action), s::System, θ::PotentialParams)
+    check(ccall((:pimc_set_potential, libpimc), Cint, (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble),
+                s.handle, 0, θ.V0, θ.ω, θ.g))
+    S, _, dθ = action_gradients(s)
+    pullback(ΔS) = (NoTangent(), NoTangent(),
+                    Tangent{PotentialParams}(V0 = ΔS * dθ[1], ω = ΔS * dθ[2], g = ΔS * dθ[3]))
+    return S, pullback
+end
+
+end # module
