@@ -290,6 +290,9 @@ def run_ours(args):
     pimc.load()
     sem = 1 if args.semantics == "physical" else 0
     chains, mixes, desc = workload(args.workload, sem)
+    if args.chains > 0:
+        chains, mixes = chains[:args.chains], mixes[:args.chains]
+        desc += f" (first {len(chains)} chains)"
     if ws > 1:  # weak scaling: every rank runs the full workload with its own seeds
         for c in chains:
             c.seed = c.seed + 1000003 * rank
@@ -298,8 +301,15 @@ def run_ours(args):
         eng.set_mix(m, chain=i)
     batched = len(chains) > 1
     run = eng.run_batched if batched else eng.run
-    if batched and args.tune:
-        eng.tune(sweeps_per_trial=1)
+    launch = None
+    if batched and args.launch:
+        f = args.launch.split(":")
+        eng.set_launch(block=int(f[1]), sweeps_per_launch=int(f[2]),
+                       state_smem_bytes=int(f[3]) if len(f) > 3 else 0,
+                       warp_per_chain=f[0] == "warp")
+        launch = dict(eng.launch, tuned=False)
+    elif batched and args.tune:
+        launch = eng.tune(sweeps_per_trial=1)
     for _ in range(args.warmup):
         run(1)
     s0 = eng.total_stats()
@@ -325,9 +335,8 @@ def run_ours(args):
            "l2": (f"chain state {state_bytes / 1e9:.2f} GB > 129 MB L2"
                   if state_bytes > 129e6 else f"chain state {state_bytes / 1e6:.1f} MB (L2/shared resident)"),
            "bead_updates_per_step": beads / args.steps}
-    if batched:
-        st = eng.total_stats()
-        cfg["launch"] = {"block": None, "sweeps_per_launch": None}
+    if batched and launch:
+        cfg["launch"] = dict({"tuned": True}, **launch)
     out["config"] = cfg
     # roofline of the sweep kernel: algorithmic bytes per bead-update (48 B
     # pair-free, 64 B with the pair interaction) over its measured duration
@@ -414,6 +423,11 @@ def main():
     ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--semantics", default="physical", choices=["physical", "reference"])
     ap.add_argument("--tune", type=int, default=1)
+    ap.add_argument("--chains", type=int, default=0,
+                    help="keep only the first K chains of the workload (small profiling cases)")
+    ap.add_argument("--launch", default=None,
+                    help="fixed batched launch shape instead of tuning: cta:BLOCK:SPL:STATE_BYTES "
+                         "or warp:BLOCK:SPL")
     ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -151,9 +151,22 @@ int pimc_run(void *handle, long long n_sweeps);
 int pimc_batch_run(void *handle, long long n_sweeps);
 /* the same sweeps issued as one plain launch per chain (no queue, no graph) */
 int pimc_batch_run_plain(void *handle, long long n_sweeps);
-/* time candidate launch shapes on the handle's own chains and keep the best */
-int pimc_batch_tune(void *handle, int sweeps_per_trial, int *block_out, int *spl_out);
-int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch);
+/* launch shape of pimc_batch_run.  warp_per_chain = 0: one CTA of `block`
+ * threads per chain, the chain's state staged in shared memory when it fits
+ * state_smem_bytes.  warp_per_chain = 1: every warp of a `block`-thread CTA
+ * runs its own chain (block <= 256, state_smem_bytes ignored).  Both shapes
+ * give the same chains bit for bit; they differ in speed only. */
+typedef struct {
+  int warp_per_chain;
+  int block;
+  int sweeps_per_launch;
+  int state_smem_bytes;
+} pimc_launch;
+/* time candidate launch shapes on the handle's own chains and keep the
+ * fastest; the chains are restored afterwards.  chosen may be NULL. */
+int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen);
+int pimc_batch_set_launch(void *handle, const pimc_launch *launch);
+int pimc_batch_get_launch(void *handle, pimc_launch *launch);
 
 /* ---------------- single moves with injected draws (parity level b) */
 /* (u::ReshapeLinear)(s) with n, j0, m given (reshape.jl:31-91).  normals are

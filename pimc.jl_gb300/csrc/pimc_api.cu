@@ -36,9 +36,22 @@ int fail(int code, const std::string &msg) {
       return fail(PIMC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
-constexpr int kWarpScratchMin = 5 * (64 + 1);  // doubles, window_warp
+constexpr int kWarpScratchMin = 5 * (64 + 1) + 96;  // doubles, window_warp + its queue
+constexpr int kQueueBytes = 96 * 8;                  // one warp's neighbour queue
 constexpr unsigned kStateMagic = 0x50494D43u;   // "PIMC"
 constexpr int kStateBudget = 100 * 1024;        // shared bytes for a staged chain
+
+// one launch shape of the sweep kernel and its shared-memory layout
+struct Plan {
+  int mode = 0;                // 0: one CTA per chain, 1: one warp per chain
+  int block = 256;
+  int spl = 1;                 // sweeps per launch
+  int state_cap = kStateBudget;
+  int state_bytes = 0;         // shared bytes for a staged chain (CTA mode)
+  int warp_scratch_d = kWarpScratchMin;
+  int warp_bytes = 0;          // scratch bytes of one warp's chain (warp mode)
+  size_t dyn_smem = 0;
+};
 
 struct Handle {
   int nchains = 0;
@@ -69,15 +82,11 @@ struct Handle {
   double last_ms = 0.0;
   long long last_launches = 0;
   int maxN = 0, maxM = 0, maxNM = 0;
-  int block = 256;
-  int spl = 1;                 // sweeps per launch (batched)
-  int state_bytes = 0;         // shared bytes for staged chain state
-  int warp_scratch_d = 0;
-  size_t scratch_bytes = 0;
-  size_t dyn_smem = 0;
+  Plan bat;                    // batched launch shape (tuned or set)
+  Plan one;                    // plain per-chain launches: one CTA each
   int num_sms = 0;
+  int max_dyn_smem = 0;         // opt-in shared bytes per CTA, less static use
   cudaGraphExec_t gexec = nullptr;
-  int g_spl = -1, g_block = -1;
   int force_warp = 0;
 };
 
@@ -235,29 +244,49 @@ int sync_check(Handle *h) {
 }
 
 size_t swap_scratch_bytes(int N) {
-  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64);
+  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64) + kQueueBytes;
 }
 
-// pol/idx (2N ints, padded) + 3M doubles of the CTA centre-of-mass move
-size_t com_scratch_bytes(int N, int M) {
-  return sizeof(int) * (2 * (size_t)N + 2) + sizeof(double) * 3 * (size_t)M;
+// pol/idx (2N ints) + 3M doubles + one neighbour queue per warp of the CTA
+// centre-of-mass move
+size_t com_scratch_bytes(int N, int M, int nwarps) {
+  return sizeof(int) * 2 * (size_t)N + sizeof(double) * 3 * (size_t)M +
+         (size_t)nwarps * kQueueBytes;
 }
 
-// choose the shared-memory plan for a block size
-void plan_smem(Handle *h, int block, int state_cap) {
+// shared-memory layout of a launch shape.  CTA mode: staged chain state (the
+// largest chain that fits state_cap) followed by the CTA's scratch.  Warp
+// mode: per warp, its chain's control block and the scratch of a one-warp
+// group; chain state stays in global memory.
+Plan plan_smem(const Handle *h, int mode, int block, int spl, int state_cap) {
+  Plan p;
+  p.mode = mode;
+  p.block = block;
+  p.spl = spl;
+  p.state_cap = state_cap;
+  p.warp_scratch_d = kWarpScratchMin;
+  if (mode == 1) {
+    size_t w = std::max(swap_scratch_bytes(h->maxN), (size_t)kWarpScratchMin * sizeof(double));
+    w = std::max(w, com_scratch_bytes(h->maxN, h->maxM, 1));
+    w = (w + 15) & ~(size_t)15;
+    p.state_bytes = 0;
+    p.state_cap = 0;
+    p.warp_bytes = (int)w;
+    p.dyn_smem = (size_t)(block / 32) * (sweep_ctl_bytes() + w);
+    return p;
+  }
   const int nw = block / 32;
-  h->warp_scratch_d = kWarpScratchMin;
   size_t scratch = std::max(swap_scratch_bytes(h->maxN),
-                            (size_t)nw * h->warp_scratch_d * sizeof(double));
-  scratch = std::max(scratch, com_scratch_bytes(h->maxN, h->maxM));
+                            (size_t)nw * p.warp_scratch_d * sizeof(double));
+  scratch = std::max(scratch, com_scratch_bytes(h->maxN, h->maxM, nw));
   scratch = (scratch + 15) & ~(size_t)15;
   int need_state = 0;
   for (const auto &d : h->desc)
     if (d.smem_bytes <= state_cap) need_state = std::max(need_state, d.smem_bytes);
   need_state = (need_state + 15) & ~15;
-  h->state_bytes = need_state;
-  h->scratch_bytes = scratch;
-  h->dyn_smem = (size_t)need_state + scratch;
+  p.state_bytes = need_state;
+  p.dyn_smem = (size_t)need_state + scratch;
+  return p;
 }
 
 int upload_desc(Handle *h) {
@@ -326,6 +355,8 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cleanup(fail(PIMC_ECUDA, "no CUDA device"));
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&h->max_dyn_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  h->max_dyn_smem -= 4096;  // the CTA kernel's static control block and reduction buffer
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess)
     return cleanup(fail(PIMC_ECUDA, "stream/event creation failed"));
@@ -378,11 +409,13 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   });
   cudaMemcpyAsync(h->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, h->stream);
   if (upload_desc(h)) return cleanup(PIMC_ECUDA);
+  if (upload_exp_table() != cudaSuccess) return cleanup(fail(PIMC_ECUDA, "exp table upload failed"));
   // System(): init_world, cached links, neighbour grid
   if (launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, nchains, h->maxN, h->stream) != cudaSuccess ||
       refresh_links(h, 0, nchains))
     return cleanup(fail(PIMC_ECUDA, "initialisation launch failed"));
-  plan_smem(h, h->block, kStateBudget);
+  h->bat = plan_smem(h, 0, 256, 1, kStateBudget);
+  h->one = h->bat;
   if (sync_check(h)) return cleanup(PIMC_ECUDA);
   *out = h;
   return PIMC_OK;
@@ -446,7 +479,7 @@ void fill_stats(const ChainVar &v, pimc_stats *o) {
   o->pcom_step = v.pcom_step;
 }
 
-SweepArgs sweep_args(Handle *h) {
+SweepArgs sweep_args(Handle *h, const Plan &p) {
   SweepArgs a;
   a.desc = h->d_desc;
   a.var = h->d_var;
@@ -459,26 +492,24 @@ SweepArgs sweep_args(Handle *h) {
   a.order = nullptr;
   a.queue = nullptr;
   a.sweeps = 1;
-  a.state_bytes = h->state_bytes;
-  a.warp_scratch_d = h->warp_scratch_d;
+  a.state_bytes = p.state_bytes;
+  a.warp_scratch_d = p.warp_scratch_d;
+  a.warp_bytes = p.warp_bytes;
   return a;
 }
 
-int prepare_launch(Handle *h) {
-  CK(sweep_set_smem(h->dyn_smem));
-  return PIMC_OK;
-}
-
+// plain path: one launch of one CTA per chain per sweep, no queue, no graph
 int run_plain(Handle *h, long long n) {
-  if (prepare_launch(h)) return PIMC_ECUDA;
-  SweepArgs a = sweep_args(h);
+  const Plan &p = h->one;
+  CK(sweep_set_smem(p.mode, p.dyn_smem));
+  SweepArgs a = sweep_args(h, p);
   a.nchains = 1;
   CK(cudaEventRecord(h->ev0, h->stream));
   long long launches = 0;
   for (long long s = 0; s < n; ++s)
     for (int c = 0; c < h->nchains; ++c) {
       a.chain0 = c;
-      CK(launch_sweep(a, 1, h->block, h->dyn_smem, h->stream));
+      CK(launch_sweep(a, p.mode, 1, p.block, p.dyn_smem, h->stream));
       ++launches;
     }
   CK(cudaEventRecord(h->ev1, h->stream));
@@ -491,40 +522,40 @@ int run_plain(Handle *h, long long n) {
   return PIMC_OK;
 }
 
-int grid_for(Handle *h) {
+// persistent grid: every resident CTA (CTA mode) or resident warp (warp mode)
+// pulls chains from the work queue
+int grid_for(Handle *h, const Plan &p) {
   int per_sm = 0;
-  if (sweep_occupancy(h->block, h->dyn_smem, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
-  return std::max(1, std::min(h->nchains, per_sm * h->num_sms));
+  if (sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+  const int units_per_cta = p.mode == 1 ? p.block / 32 : 1;
+  const int need = (h->nchains + units_per_cta - 1) / units_per_cta;
+  return std::max(1, std::min(need, per_sm * h->num_sms));
 }
 
-int build_graph(Handle *h, int spl) {
-  if (h->gexec && h->g_spl == spl && h->g_block == h->block) return PIMC_OK;
-  if (h->gexec) {
-    cudaGraphExecDestroy(h->gexec);
-    h->gexec = nullptr;
-  }
-  SweepArgs a = sweep_args(h);
+int build_graph(Handle *h) {
+  if (h->gexec) return PIMC_OK;
+  const Plan &p = h->bat;
+  SweepArgs a = sweep_args(h, p);
   a.order = h->d_order;
   a.queue = h->d_queue;
-  a.sweeps = spl;
-  const int grid = grid_for(h);
+  a.sweeps = p.spl;
+  const int grid = grid_for(h, p);
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
-  launch_sweep(a, grid, h->block, h->dyn_smem, h->stream);
+  launch_sweep(a, p.mode, grid, p.block, p.dyn_smem, h->stream);
   CK(cudaStreamEndCapture(h->stream, &g));
   cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(PIMC_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  h->g_spl = spl;
-  h->g_block = h->block;
   return PIMC_OK;
 }
 
 int run_batched(Handle *h, long long n) {
-  if (prepare_launch(h)) return PIMC_ECUDA;
-  const int spl = std::max(1, h->spl);
-  int rc = build_graph(h, spl);
+  const Plan &p = h->bat;
+  CK(sweep_set_smem(p.mode, p.dyn_smem));
+  const int spl = std::max(1, p.spl);
+  int rc = build_graph(h);
   if (rc) return rc;
   CK(cudaEventRecord(h->ev0, h->stream));
   long long launches = 0;
@@ -534,12 +565,12 @@ int run_batched(Handle *h, long long n) {
     ++launches;
   }
   if (rem) {
-    SweepArgs a = sweep_args(h);
+    SweepArgs a = sweep_args(h, p);
     a.order = h->d_order;
     a.queue = h->d_queue;
     a.sweeps = (int)rem;
     CK(cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream));
-    CK(launch_sweep(a, grid_for(h), h->block, h->dyn_smem, h->stream));
+    CK(launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream));
     ++launches;
   }
   CK(cudaEventRecord(h->ev1, h->stream));
@@ -623,7 +654,7 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   a.out = h->d_iout;
   a.force_warp = h->force_warp;
   size_t smem = std::max(swap_scratch_bytes(d.N), (size_t)kWarpScratchMin * 8);
-  smem = std::max(smem, com_scratch_bytes(d.N, d.M));
+  smem = std::max(smem, com_scratch_bytes(d.N, d.M, 4));
   CK(launch_attempt(a, smem, h->stream));
   int out[5] = {0, 0, 0, 0, 0};
   CK(cudaMemcpyAsync(out, h->d_iout, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
@@ -838,14 +869,31 @@ int pimc_batch_run_plain(void *handle, long long n_sweeps) {
   return check_device_errors(h);
 }
 
-int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch) {
+int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
+  if (l.warp_per_chain != 0 && l.warp_per_chain != 1)
+    return fail(PIMC_EARG, "warp_per_chain must be 0 or 1");
+  const int bmax = l.warp_per_chain ? 256 : 512;
+  if (l.block < 32 * (1 + !l.warp_per_chain) || l.block > bmax || l.block % 32)
+    return fail(PIMC_EARG, l.warp_per_chain ? "block must be a multiple of 32 in [32, 256]"
+                                            : "block must be a multiple of 32 in [64, 512]");
+  if (l.sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
+  if (l.state_smem_bytes < 0 || l.state_smem_bytes > 160 * 1024)
+    return fail(PIMC_EARG, "state_smem_bytes must be in [0, 160 KiB]");
+  Plan p = plan_smem(h, l.warp_per_chain, l.block, l.sweeps_per_launch, l.state_smem_bytes);
+  if (h->max_dyn_smem > 0 && p.dyn_smem > (size_t)h->max_dyn_smem)
+    return fail(PIMC_EARG, "launch shape needs " + std::to_string(p.dyn_smem) +
+                               " shared bytes per CTA, more than the device offers");
+  *out = p;
+  return PIMC_OK;
+}
+
+int pimc_batch_set_launch(void *handle, const pimc_launch *launch) {
   Handle *h = H(handle);
-  if (!h) return fail(PIMC_EARG, "null handle");
-  if (block < 64 || block > 1024 || block % 32) return fail(PIMC_EARG, "block must be a multiple of 32 in [64, 1024]");
-  if (sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
-  h->block = block;
-  h->spl = sweeps_per_launch;
-  plan_smem(h, block, kStateBudget);
+  if (!h || !launch) return fail(PIMC_EARG, "null argument");
+  Plan p;
+  int rc = check_launch(h, *launch, &p);
+  if (rc) return rc;
+  h->bat = p;
   if (h->gexec) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
@@ -853,11 +901,27 @@ int pimc_batch_set_launch(void *handle, int block, int sweeps_per_launch) {
   return PIMC_OK;
 }
 
+int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
+  Handle *h = H(handle);
+  if (!h || !launch) return fail(PIMC_EARG, "null argument");
+  launch->warp_per_chain = h->bat.mode;
+  launch->block = h->bat.block;
+  launch->sweeps_per_launch = h->bat.spl;
+  launch->state_smem_bytes = h->bat.state_cap;
+  return PIMC_OK;
+}
+
 int pimc_get_state(void *handle, void *buf, size_t bytes);
 int pimc_set_state(void *handle, const void *buf, size_t bytes);
 int pimc_state_size(void *handle, size_t *bytes);
 
-int pimc_batch_tune(void *handle, int sweeps_per_trial, int *block_out, int *spl_out) {
+// project-written tuner: time every launch shape -- one CTA per chain with
+// (threads, sweeps per launch, shared-memory staging budget), or one warp per
+// chain with (warps per CTA, sweeps per launch) -- on the handle's own chains
+// and keep the fastest.  Smaller staging budgets trade shared-memory residency
+// of small chains for more resident CTAs per SM; warp mode trades threads per
+// chain for chains in flight.
+int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
   Handle *h = H(handle);
   if (!h || sweeps_per_trial < 1) return fail(PIMC_EARG, "bad argument");
   // trials advance the chains; the snapshot puts them back afterwards
@@ -866,26 +930,30 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, int *block_out, int *spl
   if (rc) return rc;
   std::vector<char> snap(nb);
   if ((rc = pimc_get_state(h, snap.data(), nb))) return rc;
-  const int blocks[] = {128, 256, 512};
-  const int spls[] = {1, 4};
+  std::vector<pimc_launch> cand;
+  for (int s : {1, 2}) {
+    if (s > sweeps_per_trial) continue;
+    for (int b : {64, 128, 256})
+      for (int m : {0, 32 * 1024, kStateBudget}) cand.push_back({0, b, s, m});
+    for (int b : {64, 128, 256}) cand.push_back({1, b, s, 0});
+  }
   double best = 1e300;
-  int bb = h->block, bs = h->spl;
-  for (int b : blocks)
-    for (int s : spls) {
-      if (s > sweeps_per_trial) continue;
-      if ((rc = pimc_batch_set_launch(h, b, s))) return rc;
-      if ((rc = run_batched(h, s))) return rc;  // warm (graph build)
-      if ((rc = run_batched(h, sweeps_per_trial))) return rc;
-      if (h->last_ms < best) {
-        best = h->last_ms;
-        bb = b;
-        bs = s;
-      }
+  pimc_launch keep;
+  pimc_batch_get_launch(h, &keep);
+  for (const pimc_launch &l : cand) {
+    Plan p;
+    if (check_launch(h, l, &p)) continue;  // does not fit this device
+    if ((rc = pimc_batch_set_launch(h, &l))) return rc;
+    if ((rc = run_batched(h, l.sweeps_per_launch))) return rc;  // warm (graph build)
+    if ((rc = run_batched(h, sweeps_per_trial))) return rc;
+    if (h->last_ms < best) {
+      best = h->last_ms;
+      keep = l;
     }
-  if ((rc = pimc_batch_set_launch(h, bb, bs))) return rc;
+  }
+  if ((rc = pimc_batch_set_launch(h, &keep))) return rc;
   if ((rc = pimc_set_state(h, snap.data(), nb))) return rc;
-  if (block_out) *block_out = bb;
-  if (spl_out) *spl_out = bs;
+  if (chosen) *chosen = keep;
   return PIMC_OK;
 }
 

@@ -30,6 +30,7 @@ namespace pimc {
 
 constexpr int WMAX = 64;     // largest staging / swap window m handled on the device
 constexpr int TWMAX = 32;    // thread-per-window variant handles m <= TWMAX
+constexpr int WARP_SCRATCH_D = 5 * (WMAX + 1) + 96;  // doubles of per-warp scratch
 
 // move outcomes (PIMC_REJECT / ACCEPT / SKIP / HARDCORE of pimc.h)
 constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
@@ -239,8 +240,30 @@ __device__ __forceinline__ double dvext(const ChainDesc &d, double x) {
   return g;
 }
 
+// exp(x) for x <= 0 by a table of exp(-k/64), k = 0..2560 (filled from the
+// host's libm at handle creation), times the degree-5 Taylor polynomial of
+// exp(f) on |f| <= 1/128 (Tang's table-driven method, ACM TOMS 15, 1989):
+// truncation <= (1/128)^6/720 = 3.2e-16 relative, about 9 FP64 operations
+// against the library's longer range reduction and polynomial.  Arguments
+// below -40 (pair terms of far-away next beads) go to the library exp.
+constexpr int EXPTAB_N = 2560;
+// defined here: only the kernel translation unit includes this header
+__device__ double g_exptab[EXPTAB_N + 1];
+
+__device__ __forceinline__ double exp_neg(double x) {
+  if (!(x >= -40.0)) return exp(x);
+  const int k = __double2int_rn(x * -64.0);
+  const double f = fma((double)k, 0.015625, x);
+  double p = fma(f, 1.0 / 120.0, 1.0 / 24.0);
+  p = fma(p, f, 1.0 / 6.0);
+  p = fma(p, f, 0.5);
+  p = fma(p, f, 1.0);
+  p = fma(p, f, 1.0);
+  return __ldg(&g_exptab[k]) * p;
+}
+
 __device__ __forceinline__ double vpair(const ChainDesc &d, double r2) {
-  return d.g * exp(-r2 * d.inv2s2);
+  return d.g * exp_neg(-r2 * d.inv2s2);
 }
 
 __device__ __forceinline__ double lnU2(const ChainDesc &d, double r2a, double r2b) {
@@ -299,47 +322,112 @@ struct Prefilter {
   }
 };
 
-// pair terms of one link of a moving path, old and new in one pass over the
-// slice: for every other bead b at slice j within rc of the old bead (a) add
-// lnU(d(a, b_j), d(an, b_next)) to wo, and within rc of the new bead (p) add
-// lnU(d(p, b_j), d(pn, b_next)) to wn.  Old terms skip b in {eo1, eo2}, new
-// terms b in {en1, en2}; with excl != null both skip every b with
-// excl[b] >= 0.  Lanes split the particles; the sums are per lane.
-__device__ __forceinline__ void pair_link_lanes(const CV &c, int j, int eo1, int eo2, int en1,
-                                                int en2, const int *excl, bool do_old,
-                                                bool do_new, double ax, double ay, double anx,
-                                                double any, double px, double py, double pnx,
-                                                double pny, double &wo, double &wn, int lane,
-                                                int lanes) {
+// ---------------------------------------------------------------------------
+// pair terms of a moving path segment, old and new configurations, with
+// every lane busy.  A segment is a list of links t: bead t at slice(t) and
+// the next bead along the path (at slice(t)+1).  Pass 1: lanes test the
+// particles of the slice against the old and the new bead in FP32 and push
+// the survivors (b, t, side) onto a warp-private queue in shared memory
+// (ballot + popc).  Pass 2: whenever 32 entries are queued, each lane takes
+// one and evaluates it exactly in FP64.  The warp's divergent FP64 work is
+// then proportional to the neighbours found, not to the particles scanned.
+//
+// Seg provides: links(), slice(t), cur(side, t, &x, &y), nxt(side, t, &x, &y),
+// skip(side, t, b).  side 0 = old configuration, 1 = new.
+// ---------------------------------------------------------------------------
+constexpr int PQ_CAP = 96;  // queue entries per warp (64-bit)
+
+template <class Seg>
+__device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long long e,
+                                        double &wo, double &wn) {
   const ChainDesc &d = *c.d;
-  const int N = c.N, M = c.M, dim = c.dim;
-  const int jn = (j + 1 == M) ? 0 : j + 1;
-  const double rc2 = d.rc * d.rc;
-  Prefilter fo, fn;
-  fo.init(d, ax, ay, d.rc);
-  fn.init(d, px, py, d.rc);
-  const float *row = c.xf + (size_t)j * c.ldn * dim;
-  for (int b = lane; b < N; b += lanes) {
-    const float *pb = row + (size_t)b * dim;
-    bool po = do_old && fo.pass(pb), pnw = do_new && fn.pass(pb);
-    if (!(po || pnw)) continue;
-    if (excl && excl[b] >= 0) continue;
-    po = po && b != eo1 && b != eo2;
-    pnw = pnw && b != en1 && b != en2;
-    if (!(po || pnw)) continue;
-    const double bx = c.X(0, b, j), by = c.Xd(1, b, j);
-    const int bn = (j == M - 1) ? c.next[b] : b;
-    const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
-    if (po) {
-      const double r2a = mi2(d, ax, ay, bx, by);
-      if (r2a <= rc2) wo += lnU2(d, r2a, mi2(d, anx, any, bnx, bny));
-    }
-    if (pnw) {
-      const double r2a = mi2(d, px, py, bx, by);
-      if (r2a <= rc2) wn += lnU2(d, r2a, mi2(d, pnx, pny, bnx, bny));
+  const int M = c.M;
+  const int b = (int)(e >> 32), t = (int)((e >> 1) & 0x7fffffffu), side = (int)(e & 1u);
+  const int j = s.slice(t), jn = j + 1 == M ? 0 : j + 1;
+  double ax, ay, anx, any;
+  s.cur(side, t, ax, ay);
+  const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
+  if (r2a > d.rc * d.rc) return;
+  s.nxt(side, t, anx, any);
+  const int bn = j == M - 1 ? c.next[b] : b;
+  const double w = lnU2(d, r2a, mi2(d, anx, any, c.X(0, bn, jn), c.Xd(1, bn, jn)));
+  if (side) wn += w; else wo += w;
+}
+
+// evaluate the first min(qn, 32) queued entries and move the rest up
+template <class Seg>
+__device__ __forceinline__ void pq_flush(const CV &c, const Seg &s, unsigned long long *q, int &qn,
+                                         double &wo, double &wn, int lane) {
+  const int k = qn < 32 ? qn : 32;
+  if (lane < k) pq_eval(c, s, q[lane], wo, wn);
+  __syncwarp();
+  unsigned long long rest[3];
+  const int nr = qn - k;
+  for (int r = 0; r < 3; ++r) {
+    const int i = 32 + lane + 32 * r;
+    rest[r] = (lane + 32 * r < nr) ? q[i] : 0ull;
+  }
+  __syncwarp();
+  for (int r = 0; r < 3; ++r)
+    if (lane + 32 * r < nr) q[lane + 32 * r] = rest[r];
+  __syncwarp();
+  qn = nr;
+}
+
+template <class Seg>
+__device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
+                              unsigned long long *q, double &wo, double &wn, int lane) {
+  const ChainDesc &d = *c.d;
+  const int N = c.N, dim = c.dim;
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  for (int t = t0; t < t1; ++t) {
+    const int j = s.slice(t);
+    Prefilter fo, fn;
+    double ax, ay, px, py;
+    s.cur(0, t, ax, ay);
+    s.cur(1, t, px, py);
+    fo.init(d, ax, ay, d.rc);
+    fn.init(d, px, py, d.rc);
+    const float *row = c.xf + (size_t)j * c.ldn * dim;
+    for (int b0 = 0; b0 < N; b0 += 32) {
+      const int b = b0 + lane;
+      bool po = false, pn = false;
+      if (b < N) {
+        const float *pb = row + (size_t)b * dim;
+        po = do_old && fo.pass(pb) && !s.skip(0, t, b);
+        pn = do_new && fn.pass(pb) && !s.skip(1, t, b);
+      }
+      const unsigned mo = __ballot_sync(0xffffffffu, po), mn = __ballot_sync(0xffffffffu, pn);
+      const unsigned long long base = ((unsigned long long)(unsigned)b << 32) | ((unsigned)t << 1);
+      if (po) q[qn + __popc(mo & lt)] = base;
+      qn += __popc(mo);
+      if (pn) q[qn + __popc(mn & lt)] = base | 1ull;
+      qn += __popc(mn);
+      __syncwarp();
+      if (qn >= 32) pq_flush(c, s, q, qn, wo, wn, lane);
     }
   }
+  while (qn > 0) pq_flush(c, s, q, qn, wo, wn, lane);
 }
+
+// a staging window: bead t at absolute slice j0+t of particle n (next(n)
+// past slice M); new beads in shared arrays; the moving path is excluded
+struct WindowSeg {
+  const CV *c;
+  int n, nx, j0, M;
+  const double *px, *py;
+  __device__ __forceinline__ int own(int t) const { return j0 + t < M ? n : nx; }
+  __device__ __forceinline__ int slice(int t) const { return j0 + t < M ? j0 + t : j0 + t - M; }
+  __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
+    if (side) { x = px[t]; y = py[t]; }
+    else { x = c->X(0, own(t), slice(t)); y = c->Xd(1, own(t), slice(t)); }
+  }
+  __device__ __forceinline__ void nxt(int side, int t, double &x, double &y) const {
+    cur(side, t + 1, x, y);
+  }
+  __device__ __forceinline__ bool skip(int, int t, int b) const { return b == own(t); }
+};
 
 // any bead other than e1/e2 at slice j closer than the hard-core radius
 // (find_nn + distance < a, src/updates/helper.jl:167-169); per-lane result
@@ -441,7 +529,8 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
 
 // ---------------------------------------------------------------------------
 // Levy staging window, one warp: pair terms (physical semantics) and the
-// hard-core retry loop.  sb: per-warp shared scratch of 5*(WMAX+1) doubles.
+// hard-core retry loop.  sb: per-warp shared scratch of 5*(WMAX+1) doubles
+// followed by a PQ_CAP-entry neighbour queue.
 // ---------------------------------------------------------------------------
 template <class D>
 __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
@@ -530,15 +619,9 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     wu += mhtau * (svb[t] + svb[t + 1]);
   }
   if (phys_pair) {
-    // one warp-wide pass over the slice per link, old and new together
-    for (int t = 0; t < m; ++t) {
-      const int a = j0 + t, a1 = a + 1;
-      const int o = a < M ? n : nx, j = a < M ? a : a - M;
-      const int o1 = a1 < M ? n : nx, j1 = a1 < M ? a1 : a1 - M;
-      pair_link_lanes(c, j, o, -1, o, -1, nullptr, true, true, c.X(0, o, j), c.Xd(1, o, j),
-                      c.X(0, o1, j1), c.Xd(1, o1, j1), sx_[t], sy_[t], sx_[t + 1], sy_[t + 1], wi,
-                      wu, lane, 32);
-    }
+    WindowSeg seg{&c, n, nx, j0, M, sx_, sy_};
+    segment_pairs(c, seg, 0, m, true, true, (unsigned long long *)(sb + 5 * (WMAX + 1)), wi, wu,
+                  lane);
   }
   wi = warp_sum(wi);
   wu = warp_sum(wu);

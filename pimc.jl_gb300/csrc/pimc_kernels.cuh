@@ -55,8 +55,9 @@ struct SwapScratch {
   double *w;                                   // N heat-bath weights
   double *r1x, *r1y, *r2x, *r2y, *vb1, *vb2;   // WMAX+1 each
   double *z;                                   // 4*WMAX normals
+  unsigned long long *q;                       // PQ_CAP neighbour queue
   static __host__ __device__ size_t bytes(int N) {
-    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX);
+    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX + PQ_CAP);
   }
   __device__ void carve(void *base, int N) {
     double *p = (double *)base;
@@ -64,8 +65,60 @@ struct SwapScratch {
     r1x = p; p += WMAX + 1; r1y = p; p += WMAX + 1;
     r2x = p; p += WMAX + 1; r2y = p; p += WMAX + 1;
     vb1 = p; p += WMAX + 1; vb2 = p; p += WMAX + 1;
-    z = p;
+    z = p; p += 4 * WMAX;
+    q = (unsigned long long *)p;
   }
+};
+
+// one bridge of a swap: old path (start particle na, next nxa) and its new
+// beads; old terms of the reference see the other moving path
+struct SwapSeg {
+  const CV *c;
+  int j0, M, na, nxa, n1, nx1, n2, nx2;
+  const double *px, *py;
+  bool ref;
+  __device__ __forceinline__ int slice(int t) const { return j0 + t < M ? j0 + t : j0 + t - M; }
+  __device__ __forceinline__ int own(int t) const { return j0 + t < M ? na : nxa; }
+  __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
+    if (side) { x = px[t]; y = py[t]; }
+    else { x = c->X(0, own(t), slice(t)); y = c->Xd(1, own(t), slice(t)); }
+  }
+  __device__ __forceinline__ void nxt(int side, int t, double &x, double &y) const {
+    cur(side, t + 1, x, y);
+  }
+  __device__ __forceinline__ bool skip(int side, int t, int b) const {
+    if (ref && side == 0) return b == own(t);
+    const bool w = j0 + t >= M;
+    return b == (w ? nx1 : n1) || b == (w ? nx2 : n2);
+  }
+};
+
+// links of particles moved by a rigid shift: link t is slice t % M of member
+// pol[t / M] (a single path when np == 1); new beads are the shifted old
+// beads (precomputed for a single path, recomputed for a cycle); particles
+// of the moved cycle are excluded
+struct ComSeg {
+  const CV *c;
+  const int *pol, *idx;
+  int M;
+  const double *q;   // single path: new x[M], y[M]; null for a cycle
+  double shx, shy, L, inv2L;
+  __device__ __forceinline__ int slice(int t) const { return t % M; }
+  __device__ __forceinline__ void bead(int side, int i, int j, double &x, double &y) const {
+    if (!side) { x = c->X(0, i, j); y = c->Xd(1, i, j); return; }
+    if (q) { x = q[j]; y = q[M + j]; return; }
+    x = teleport(c->X(0, i, j) + shx, L, inv2L);
+    y = c->dim > 1 ? teleport(c->X(1, i, j) + shy, L, inv2L) : 0.0;
+  }
+  __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
+    bead(side, pol[t / M], t % M, x, y);
+  }
+  __device__ __forceinline__ void nxt(int side, int t, double &x, double &y) const {
+    const int i = pol[t / M], j = t % M;
+    if (j + 1 < M) bead(side, i, j + 1, x, y);
+    else bead(side, c->next[i], 0, x, y);
+  }
+  __device__ __forceinline__ bool skip(int, int, int b) const { return idx[b] >= 0; }
 };
 
 // heat-bath exponent -(|s - E|^2 + |x_i(j0) - f|^2) / (4 lambda m tau) with
@@ -322,34 +375,29 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
     wu += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
   }
   if (any_pair) {
-    for (int k = 0; k < 2 * m; ++k) {
-      const int b = k / m, t = k % m;
-      const int j = slc(t), o = b == 0 ? own1(t) : own2(t);
-      const int on = b == 0 ? own1(t + 1) : own2(t + 1), jn = slc(t + 1);
-      const double *bxs = b == 0 ? S.r1x : S.r2x, *bys = b == 0 ? S.r1y : S.r2y;
-      const double ox = c.X(0, o, j), oy = c.Xd(1, o, j), onx = c.X(0, on, jn), ony = c.Xd(1, on, jn);
-      if (!phys) {
-        // the reference: old pairs exclude only the path's own particle, the
-        // new paths' pair terms are added to w_initial (reshape.jl:166-240)
-        double wn = 0.0;
-        pair_link_lanes(c, j, o, -1, own1(t), own2(t), nullptr, true, true, ox, oy, onx, ony,
-                        bxs[t], bys[t], bxs[t + 1], bys[t + 1], wi, wn, lane, 32);
-        wi += wn;
-      } else {
-        pair_link_lanes(c, j, own1(t), own2(t), own1(t), own2(t), nullptr, true, true, ox, oy,
-                        onx, ony, bxs[t], bys[t], bxs[t + 1], bys[t + 1], wi, wu, lane, 32);
-        if (b == 0 && lane == 0) {
-          const int o2 = own2(t), o2n = own2(t + 1);
-          const double a2x = c.X(0, o2, j), a2y = c.Xd(1, o2, j);
-          const double a2nx = c.X(0, o2n, jn), a2ny = c.Xd(1, o2n, jn);
-          const double r2o = mi2(d, ox, oy, a2x, a2y);
-          if (r2o <= d.rc * d.rc) wi += lnU2(d, r2o, mi2(d, onx, ony, a2nx, a2ny));
-          const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
-          if (r2n <= d.rc * d.rc)
-            wu += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
-        }
-      }
+    for (int b = 0; b < 2; ++b) {
+      SwapSeg seg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
+                  b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys};
+      double wo = 0.0, wn = 0.0;
+      segment_pairs(c, seg, 0, m, true, true, S.q, wo, wn, lane);
+      // the reference adds the new paths' pair terms to w_initial and lets
+      // the old ones see the other moving path (reshape.jl:166-240)
+      wi += wo;
+      if (phys) wu += wn; else wi += wn;
     }
+    if (phys)
+      for (int t = lane; t < m; t += 32) {
+        // the pair of the two moving paths, old and new
+        const int j = slc(t), jn = slc(t + 1);
+        const int o1 = own1(t), o1n = own1(t + 1), o2 = own2(t), o2n = own2(t + 1);
+        const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
+        const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
+        if (r2o <= d.rc * d.rc)
+          wi += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
+        const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
+        if (r2n <= d.rc * d.rc)
+          wu += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+      }
   }
   wi = warp_sum(wi);
   wu = warp_sum(wu);
@@ -460,19 +508,45 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
 // move), whole CTA: pair terms with every particle outside the cycle, hard-
 // core retries, PolymerCenterOfMass (src/updates/com.jl:31-104) without the
 // worm fields that make the reference's version fail.  pol/idx: int scratch
-// of 2N; q: shared scratch of 3*M doubles (single-path case).
+// of 2N; q: shared scratch of 3*M doubles (single-path case); qbuf: one
+// PQ_CAP-entry neighbour queue per warp.
 // ---------------------------------------------------------------------------
-template <class D>
-__device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int *pol, int *idx,
-                       double *q, double *red, int *sflag, int *np_out) {
+// the threads that run a move: a whole CTA, or one warp on its own
+template <bool WARP>
+struct Group {
+  __device__ __forceinline__ static int rank() { return WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+  __device__ __forceinline__ static int size() { return WARP ? 32 : (int)blockDim.x; }
+  __device__ __forceinline__ static void sync() {
+    if (WARP) __syncwarp(); else __syncthreads();
+  }
+  __device__ __forceinline__ static int any(int p) {
+    return WARP ? __any_sync(0xffffffffu, p) : __syncthreads_or(p);
+  }
+  template <int K>
+  __device__ __forceinline__ static void sum(double (&v)[K], double *red) {
+    if (WARP) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    } else {
+      block_sum_k<K>(v, red);
+    }
+  }
+};
+
+template <bool WARP, class D>
+__device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, int *pol, int *idx,
+                         double *q, unsigned long long *qbuf, double *red, double *shift,
+                         int *sflag, int *np_out) {
+  using G = Group<WARP>;
   const ChainDesc &d = *c.d;
-  const int N = c.N, M = c.M, dim = c.dim, tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int N = c.N, M = c.M, dim = c.dim, tid = G::rank(), nt = G::size();
+  const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
+  const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
   const bool hard = (d.flags & PF_HARD) != 0;
   const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
   for (int i = tid; i < N; i += nt) idx[i] = -1;
-  __syncthreads();
+  G::sync();
   if (tid == 0) {
     int np = 0, i = n;
     if (polymer) {
@@ -485,13 +559,13 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
     }
     *sflag = np;
   }
-  __syncthreads();
+  G::sync();
   const int np = *sflag;
+  G::sync();
   if (np_out && tid == 0) *np_out = np;
   if (np > N) return -1;
   for (int i = tid; i < np; i += nt) idx[pol[i]] = i;
-  __syncthreads();
-  double *shift = red + 240;  // two doubles beyond the reduction slots
+  G::sync();
   int tries = 0;
   while (true) {
     if (tid == 0) {
@@ -503,8 +577,10 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
         *sflag = 0;
       }
     }
-    __syncthreads();
-    if (*sflag < 0) return RES_HARDCORE;
+    G::sync();
+    const int fl = *sflag;
+    G::sync();
+    if (fl < 0) return RES_HARDCORE;
     if (!hard) break;
     // a warp per bead, lanes over the slice
     int hit = 0;
@@ -514,7 +590,7 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
       const double qy = dim > 1 ? teleport(c.X(1, i, j) + shift[1], L, inv2L) : 0.0;
       if (hard_hit_lanes(c, qx, qy, j, i, -1, lane, 32)) hit = 1;
     }
-    if (!__syncthreads_or(hit)) break;
+    if (!G::any(hit)) break;
   }
   const double shx = shift[0], shy = shift[1];
   auto qpos = [&](int i, int j, double &qx, double &qy) {
@@ -529,7 +605,7 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
       q[M + j] = qy;
       q[2 * M + j] = vext(d, qx, qy);
     }
-    __syncthreads();
+    G::sync();
   }
   double ws[2] = {0.0, 0.0};
   for (int k = tid; k < np * M; k += nt) {
@@ -546,29 +622,21 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
     }
   }
   if (phys_pair) {
-    // a warp per link, lanes over the slice; pairs inside the cycle keep
-    // their relative positions under the rigid shift
-    for (int k = warp; k < np * M; k += nwarps) {
-      const int i = pol[k / M], j = k % M;
-      const int jn = j + 1 == M ? 0 : j + 1, in = j == M - 1 ? c.next[i] : i;
-      double qx, qy, qnx, qny;
-      if (!polymer) {
-        qx = q[j]; qy = q[M + j]; qnx = q[jn]; qny = q[M + jn];
-      } else {
-        qpos(i, j, qx, qy);
-        qpos(in, jn, qnx, qny);
-      }
-      pair_link_lanes(c, j, -1, -1, -1, -1, idx, true, true, c.X(0, i, j), c.Xd(1, i, j),
-                      c.X(0, in, jn), c.Xd(1, in, jn), qx, qy, qnx, qny, ws[0], ws[1], lane, 32);
-    }
+    // warps split the links, lanes the particles of each slice; pairs inside
+    // the cycle keep their relative positions under the rigid shift
+    ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L};
+    const int tot = np * M, per = (tot + nwarps - 1) / nwarps;
+    const int t0 = min(tot, warp * per), t1 = min(tot, t0 + per);
+    segment_pairs(c, seg, t0, t1, true, true, qbuf + (size_t)warp * PQ_CAP, ws[0], ws[1], lane);
   }
-  block_sum_k<2>(ws, red);
+  G::template sum<2>(ws, red);
   if (tid == 0) {
     const double delta = exp(ws[1] - ws[0]);
     *sflag = (delta >= 1.0) || (delta > dr.uniform_accept());
   }
-  __syncthreads();
+  G::sync();
   const int acc = *sflag;
+  G::sync();
   if (!acc) return RES_REJECT;
   // links first (they read the unshifted neighbours), then positions
   for (int k = tid; k < np * M; k += nt) {
@@ -583,7 +651,7 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
       c.Vl(i, j) = mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
     }
   }
-  __syncthreads();
+  G::sync();
   for (int k = tid; k < np * M; k += nt) {
     const int i = pol[k / M], j = k % M;
     double qx, qy;
@@ -595,7 +663,7 @@ __device__ int com_cta(const CV &c, int n, bool polymer, double step, D &dr, int
     }
     c.set_pos(i, j, qx, qy);
   }
-  __syncthreads();
+  G::sync();
   return RES_ACCEPT;
 }
 
@@ -611,12 +679,17 @@ __device__ __forceinline__ long long bin_floor(double x, double L, double w, dou
 
 // ---------------------------------------------------------------------------
 // estimators, whole CTA (src/measurement.jl:45-55, 92-122)
-// out[0] E_th, out[1] E_v, out[2] pair energy, out[3] pair virial energy
+// out[0] E_th, out[1] E_v, out[2] pair energy, out[3] pair virial energy;
+// qbuf: one PQ_CAP-entry queue per warp (pair chains)
 // ---------------------------------------------------------------------------
-__device__ void measure_cta(const CV &c, double *red, double *out, bool density) {
+template <bool WARP>
+__device__ void measure_group(const CV &c, double *red, double *out, bool density,
+                              unsigned long long *qbuf) {
+  using G = Group<WARP>;
   const ChainDesc &d = *c.d;
-  const int N = c.N, M = c.M, dim = c.dim, tid = threadIdx.x, nt = blockDim.x;
-  const int lane = tid & 31, warp = tid >> 5, nwarps = nt >> 5;
+  const int N = c.N, M = c.M, dim = c.dim, tid = G::rank(), nt = G::size();
+  const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
+  const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
   const bool pair = (d.flags & PF_PAIR) != 0;
   const double rc2 = d.rc * d.rc, cg = d.inv2s2;
   double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // link, pot, vkin, pair, pair virial
@@ -641,29 +714,58 @@ __device__ void measure_cta(const CV &c, double *red, double *out, bool density)
       if (ok) atomicAdd(c.hist + idx, 1ull);
     }
   }
-  if (pair) {
-    // a warp per bead, lanes over the higher-numbered particles of its slice
-    for (int k = warp; k < N * M; k += nwarps) {
-      const int j = k / N, i = k % N;
-      const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-      const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
-      const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
+  if (pair && qbuf) {
+    // warps split the beads; lanes test the higher-numbered particles of the
+    // slice in FP32 and queue the survivors, evaluated 32 at a time in FP64
+    unsigned long long *q = qbuf + (size_t)warp * PQ_CAP;
+    const unsigned lt = (1u << lane) - 1u;
+    const int tot = N * M, per = (tot + nwarps - 1) / nwarps;
+    const int k0 = min(tot, warp * per), k1 = min(tot, k0 + per);
+    int qn = 0;
+    auto flush = [&]() {
+      const int k = qn < 32 ? qn : 32;
+      if (lane < k) {
+        const unsigned long long e = q[lane];
+        const int b = (int)(e >> 32), kk = (int)(e & 0xffffffffu);
+        const int j = kk / N, i = kk % N;
+        const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
+        const double r2a = mi2(d, c.X(0, i, j), c.Xd(1, i, j), c.X(0, b, j), c.Xd(1, b, j));
+        if (r2a <= rc2) {
+          const int bn = j == M - 1 ? c.next[b] : b;
+          const double r2b = mi2(d, c.X(0, in, jn), c.Xd(1, in, jn), c.X(0, bn, jn), c.Xd(1, bn, jn));
+          const double v1 = vpair(d, r2a), v2 = vpair(d, r2b);
+          s[3] += 0.5 * d.tau * (v1 + v2);
+          s[4] += 0.5 * d.tau * (-2.0 * cg * r2a * v1 - 2.0 * cg * r2b * v2);
+        }
+      }
+      __syncwarp();
+      unsigned long long rest[3];
+      const int nr = qn - k;
+      for (int r = 0; r < 3; ++r) rest[r] = (lane + 32 * r < nr) ? q[32 + lane + 32 * r] : 0ull;
+      __syncwarp();
+      for (int r = 0; r < 3; ++r)
+        if (lane + 32 * r < nr) q[lane + 32 * r] = rest[r];
+      __syncwarp();
+      qn = nr;
+    };
+    for (int kk = k0; kk < k1; ++kk) {
+      const int j = kk / N, i = kk % N;
       Prefilter f;
-      f.init(d, ax, ay, d.rc);
+      f.init(d, c.X(0, i, j), c.Xd(1, i, j), d.rc);
       const float *row = c.xf + (size_t)j * c.ldn * dim;
-      for (int b = i + 1 + lane; b < N; b += 32) {
-        if (!f.pass(row + (size_t)b * dim)) continue;
-        const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
-        if (r2a > rc2) continue;
-        const int bn = j == M - 1 ? c.next[b] : b;
-        const double r2b = mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn));
-        const double v1 = vpair(d, r2a), v2 = vpair(d, r2b);
-        s[3] += 0.5 * d.tau * (v1 + v2);
-        s[4] += 0.5 * d.tau * (-2.0 * cg * r2a * v1 - 2.0 * cg * r2b * v2);
+      for (int b0 = i + 1; b0 < N; b0 += 32) {
+        const int b = b0 + lane;
+        const bool p = b < N && f.pass(row + (size_t)b * dim);
+        const unsigned mk = __ballot_sync(0xffffffffu, p);
+        if (p) q[qn + __popc(mk & lt)] = ((unsigned long long)(unsigned)b << 32) | (unsigned)kk;
+        qn += __popc(mk);
+        __syncwarp();
+        if (qn >= 32) flush();
       }
     }
+    while (qn > 0) flush();
   }
-  block_sum_k<5>(s, red);
+  G::template sum<5>(s, red);
   if (tid == 0) {
     const double tau = d.tau;
     out[0] = (double)(dim * N) / (2.0 * tau) - 1.0 / (4.0 * d.lambda * (tau * tau) * M) * s[0] +

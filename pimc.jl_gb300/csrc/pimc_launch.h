@@ -22,6 +22,7 @@ struct SweepArgs {
   int sweeps;         // sweeps per chain per launch
   int state_bytes;    // shared bytes reserved for staging a chain's state
   int warp_scratch_d; // doubles of scratch per warp
+  int warp_bytes;     // warp-per-chain mode: scratch bytes of each warp
 };
 
 struct AttemptArgs {
@@ -66,9 +67,12 @@ struct AdjArgs {
   double *sum_rg;     // [1], zeroed before the launch
 };
 
-cudaError_t launch_sweep(const SweepArgs &a, int grid, int block, size_t smem, cudaStream_t s);
-cudaError_t sweep_set_smem(size_t smem);
-cudaError_t sweep_occupancy(int block, size_t smem, int *blocks_per_sm);
+// mode 0: one CTA per chain (k_sweep); mode 1: one warp per chain (k_sweep_warp)
+cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size_t smem,
+                         cudaStream_t s);
+cudaError_t sweep_set_smem(int mode, size_t smem);
+size_t sweep_ctl_bytes();
+cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm);
 cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s);
 cudaError_t launch_eval_action(const EvalArgs &a, cudaStream_t s);
 cudaError_t launch_eval_weights(const EvalArgs &a, cudaStream_t s);
@@ -85,5 +89,6 @@ cudaError_t launch_mirror(const ChainDesc *desc, double *dpool, int chain0, int 
 cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);
+cudaError_t upload_exp_table();
 
 }  // namespace pimc

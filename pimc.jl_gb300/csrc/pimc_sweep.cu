@@ -8,6 +8,8 @@
 // captured in a CUDA graph).
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "pimc_kernels.cuh"
 #include "pimc_launch.h"
 
@@ -70,18 +72,21 @@ struct SmemCtl {
   ChainDesc d;
   ChainVar v;
   MixDev mix;
-  double red[256];
+  double shift[2];
   double e4[4];
   int iflag[8];
   int chain;
 };
 
-// one sweep of one chain by the whole CTA
-__device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int warp_scratch_d) {
+// one sweep of one chain by a group: the whole CTA, or one warp on its own
+template <bool WARP>
+__device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *scratch,
+                          int warp_scratch_d) {
+  using G = Group<WARP>;
   const ChainDesc &d = sc.d;
   const MixDev &mix = sc.mix;
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = nt >> 5;
+  const int tid = G::rank(), nt = G::size(), lane = threadIdx.x & 31;
+  const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
   const int N = c.N, M = c.M;
   const bool serial_local = chain_serial_local(d);
   const unsigned long long sweep = sc.v.sweep;
@@ -150,7 +155,7 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         }
       }
     }
-    __syncthreads();
+    G::sync();
   }
 
   // ---- permutation swaps (ReshapeSwapLinear), one at a time by warp 0
@@ -180,7 +185,7 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         }
       }
     }
-    __syncthreads();
+    G::sync();
   }
 
   // ---- single-path centre of mass
@@ -195,20 +200,21 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         tal[6] += r;
         tal[9] += M;
       }
-      __syncthreads();
+      G::sync();
     } else {
       int *pol = (int *)scratch, *idx = pol + N;
       double *q = (double *)(pol + 2 * N);
+      unsigned long long *qbuf = (unsigned long long *)(q + 3 * M);
       for (int n = 0; n < N; ++n) {
         if (c.next[n] != n) continue;
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_cta(c, n, false, step, dr, pol, idx, q, sc.red, &sc.iflag[2], nullptr);
+        const int r = com_group<WARP>(c, n, false, step, dr, pol, idx, q, qbuf, red, sc.shift, &sc.iflag[2], nullptr);
         if (tid == 0) {
           tal[2] += 1.0;
           tal[6] += r == RES_ACCEPT;
           if (r != RES_HARDCORE) tal[9] += M;
         }
-        __syncthreads();
+        G::sync();
       }
     }
   }
@@ -216,6 +222,7 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
   // ---- cycle centre of mass, one attempt per cycle (led by its lowest index)
   for (int ph = 0; ph < mix.polymer_com_phases; ++ph) {
     int *pol = (int *)scratch, *idx = pol + N;
+    unsigned long long *qbuf = (unsigned long long *)((double *)(pol + 2 * N) + 3 * M);
     for (int n = 0; n < N; ++n) {
       if (tid == 0) {
         int lead = 1, i = c.next[n], guard = 0;
@@ -225,10 +232,10 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         }
         sc.iflag[1] = lead;
       }
-      __syncthreads();
+      G::sync();
       if (!sc.iflag[1]) continue;
       GenDraws dr = gen_draws(make_stream(d, sweep, PH_PCOM, (unsigned)(ph * N + n)));
-      const int r = com_cta(c, n, true, sc.v.pcom_step, dr, pol, idx, nullptr, sc.red,
+      const int r = com_group<WARP>(c, n, true, sc.v.pcom_step, dr, pol, idx, nullptr, qbuf, red, sc.shift,
                             &sc.iflag[2], &sc.iflag[3]);
       const int np = sc.iflag[3];
       if (tid == 0) {
@@ -236,7 +243,7 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
         tal[7] += r == RES_ACCEPT;
         if (r != RES_HARDCORE) tal[9] += (double)M * np;
       }
-      __syncthreads();
+      G::sync();
     }
   }
 
@@ -244,8 +251,8 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
   {
     double t8[8] = {tal[0], tal[1], tal[2], tal[3], tal[4], tal[5], tal[6], tal[7]};
     double t2[2] = {tal[8], tal[9]};
-    block_sum_k<8>(t8, sc.red);
-    block_sum_k<2>(t2, sc.red);
+    G::template sum<8>(t8, red);
+    G::template sum<2>(t2, red);
     if (tid == 0) {
       ChainVar &v = sc.v;
       for (int q = 0; q < 4; ++q) {
@@ -274,16 +281,53 @@ __device__ void sweep_one(SmemCtl &sc, const CV &c, unsigned char *scratch, int 
 
   // ---- measurement cadence (measurement_Z_sector)
   if (mix.measure_every > 0 && ((sweep + 1) % (unsigned long long)mix.measure_every) == 0) {
-    measure_cta(c, sc.red, sc.e4, c.hist != nullptr);
+    measure_group<WARP>(c, red, sc.e4, c.hist != nullptr, (unsigned long long *)scratch);
     if (tid == 0) record_measurement(d, sc.v, c, sc.e4, c.hist != nullptr);
   }
   if (tid == 0) sc.v.sweep++;
-  __syncthreads();
+  G::sync();
+}
+
+// warp per chain: every warp of the grid pulls chains from the queue (or
+// takes chain0 + its global warp index once) and sweeps them alone; its
+// control block and scratch live in its own slice of dynamic shared memory
+__global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const size_t ctl = (sizeof(SmemCtl) + 15) & ~(size_t)15;
+  unsigned char *mine = smem + (size_t)w * (ctl + a.warp_bytes);
+  SmemCtl &sc = *reinterpret_cast<SmemCtl *>(mine);
+  unsigned char *scratch = mine + ctl;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + w;
+  int iter = 0;
+  while (true) {
+    int ci = a.nchains;
+    if (lane == 0) {
+      if (a.queue) ci = atomicAdd(a.queue, 1);
+      else ci = iter == 0 ? gw : a.nchains;
+      if (ci < a.nchains) {
+        const int ch = a.order ? a.order[ci] : a.chain0 + ci;
+        sc.chain = ch;
+        sc.d = a.desc[ch];
+        sc.v = a.var[ch];
+        sc.mix = a.mix[ch];
+      }
+    }
+    ci = __shfl_sync(0xffffffffu, ci, 0);
+    __syncwarp();
+    ++iter;
+    if (ci >= a.nchains) break;
+    CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<true>(sc, nullptr, c, scratch, a.warp_scratch_d);
+    if (lane == 0) a.var[sc.chain] = sc.v;
+    __syncwarp();
+  }
 }
 
 __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SmemCtl sc;
+  __shared__ double red[256];
   const int tid = threadIdx.x, nt = blockDim.x;
   int iter = 0;
   while (true) {
@@ -325,7 +369,7 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
       __syncthreads();
     }
     unsigned char *scratch = smem + a.state_bytes;
-    for (int s = 0; s < a.sweeps; ++s) sweep_one(sc, c, scratch, a.warp_scratch_d);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<false>(sc, red, c, scratch, a.warp_scratch_d);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
       float *gf = (float *)(a.dpool + d.xf_off);
@@ -346,6 +390,7 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
 __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SmemCtl sc;
+  __shared__ double red[256];
   const int tid = threadIdx.x;
   if (tid == 0) {
     sc.d = a.desc[a.chain];
@@ -384,7 +429,8 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   } else {
     int *pol = (int *)smem, *idx = pol + d.N;
     double *q = (double *)(pol + 2 * d.N);
-    res = com_cta(c, a.n, a.kind == MV_PCOM, a.step, dr, pol, idx, q, sc.red, &sc.iflag[2],
+    unsigned long long *qbuf = (unsigned long long *)(q + 3 * d.M);
+    res = com_group<false>(c, a.n, a.kind == MV_PCOM, a.step, dr, pol, idx, q, qbuf, red, sc.shift, &sc.iflag[2],
                   &sc.iflag[3]);
     extra = sc.iflag[3];
   }
@@ -403,6 +449,7 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
   __shared__ SmemCtl sc;
+  __shared__ double red[256];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = nt >> 5;
   if (tid == 0) sc.d = a.desc[a.chain];
@@ -439,7 +486,7 @@ __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
       }
     }
   }
-  block_sum_k<4>(s, sc.red);
+  block_sum_k<4>(s, red);
   if (tid == 0)
     for (int q = 0; q < 4; ++q) a.out[q] = s[q];
 }
@@ -465,14 +512,15 @@ __global__ void k_eval_weights(EvalArgs a) {
     for (int t = 0; t < m; ++t) wu += mhtau * (vext(d, px(t), py(t)) + vext(d, px(t + 1), py(t + 1)));
   }
   if ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) {
-    for (int t = 0; t < m; ++t) {
-      const int ab = j0 + t, ab1 = ab + 1;
-      const int o = ab < M ? n : nx, j = ab < M ? ab : ab - M;
-      const int o1 = ab1 < M ? n : nx, j1 = ab1 < M ? ab1 : ab1 - M;
-      pair_link_lanes(c, j, o, -1, o, -1, nullptr, true, true, c.X(0, o, j), c.Xd(1, o, j),
-                      c.X(0, o1, j1), c.Xd(1, o1, j1), px(t), py(t), px(t + 1), py(t + 1), wi, wu,
-                      lane, 32);
+    __shared__ double wx[WMAX + 1], wy[WMAX + 1];
+    __shared__ unsigned long long q[PQ_CAP];
+    for (int t = lane; t <= m; t += 32) {
+      wx[t] = px(t);
+      wy[t] = py(t);
     }
+    __syncwarp();
+    WindowSeg seg{&c, n, nx, j0, M, wx, wy};
+    segment_pairs(c, seg, 0, m, true, true, q, wi, wu, lane);
   }
   wi = warp_sum(wi);
   wu = warp_sum(wu);
@@ -577,6 +625,7 @@ __global__ void k_mirror(const ChainDesc *desc, double *dpool, int chain0) {
 __global__ void __launch_bounds__(256) k_measure(const ChainDesc *desc, ChainVar *var, double *dpool,
                                                  int *ipool, unsigned long long *upool, int chain0) {
   __shared__ SmemCtl sc;
+  __shared__ double red[256];
   const int ch = chain0 + blockIdx.x;
   if (threadIdx.x == 0) {
     sc.d = desc[ch];
@@ -584,7 +633,8 @@ __global__ void __launch_bounds__(256) k_measure(const ChainDesc *desc, ChainVar
   }
   __syncthreads();
   CV c = make_cv(&sc.d, dpool, ipool, upool);
-  measure_cta(c, sc.red, sc.e4, c.hist != nullptr);
+  __shared__ unsigned long long qbuf[8 * PQ_CAP];
+  measure_group<false>(c, red, sc.e4, c.hist != nullptr, qbuf);
   if (threadIdx.x == 0) {
     record_measurement(sc.d, sc.v, c, sc.e4, c.hist != nullptr);
     var[ch] = sc.v;
@@ -644,7 +694,7 @@ __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
         const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
         const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
         const double r2b = mi2(d, anx, any, bnx, bny);
-        const double e1 = exp(-r2a * cg), e2 = exp(-r2b * cg);
+        const double e1 = exp_neg(-r2a * cg), e2 = exp_neg(-r2b * cg);
         const double v1 = d.g * e1, v2 = d.g * e2;
         go[0] += h * (-2.0 * cg * v1) * d1x;
         go[1] += h * (-2.0 * cg * v1) * d1y;
@@ -708,14 +758,29 @@ __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_sweep(const SweepArgs &a, int grid, int block, size_t smem, cudaStream_t s) {
-  k_sweep<<<grid, block, smem, s>>>(a);
+
+// the exp table of exp_neg for the current device
+cudaError_t upload_exp_table() {
+  static double tab[EXPTAB_N + 1];
+  for (int k = 0; k <= EXPTAB_N; ++k) tab[k] = std::exp(-k / 64.0);
+  return cudaMemcpyToSymbol(g_exptab, tab, sizeof(tab));
+}
+
+cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size_t smem,
+                         cudaStream_t s) {
+  if (mode == 1) k_sweep_warp<<<grid, block, smem, s>>>(a);
+  else k_sweep<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
-cudaError_t sweep_set_smem(size_t smem) {
+cudaError_t sweep_set_smem(int mode, size_t smem) {
+  if (mode == 1)
+    return cudaFuncSetAttribute(k_sweep_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   return cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
-cudaError_t sweep_occupancy(int block, size_t smem, int *blocks_per_sm) {
+size_t sweep_ctl_bytes() { return (sizeof(SmemCtl) + 15) & ~(size_t)15; }
+cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm) {
+  if (mode == 1)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_warp, block, smem);
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep, block, smem);
 }
 cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s) {

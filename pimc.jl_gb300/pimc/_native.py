@@ -102,6 +102,11 @@ class Stats(C.Structure):
     ]
 
 
+class Launch(C.Structure):
+    _fields_ = [("warp_per_chain", C.c_int), ("block", C.c_int),
+                ("sweeps_per_launch", C.c_int), ("state_smem_bytes", C.c_int)]
+
+
 # every symbol include/pimc.h declares, with its argument types
 _vp, _dp, _ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
 _ull = C.POINTER(C.c_ulonglong)
@@ -127,8 +132,9 @@ SIGNATURES = {
     "pimc_run": [_vp, C.c_longlong],
     "pimc_batch_run": [_vp, C.c_longlong],
     "pimc_batch_run_plain": [_vp, C.c_longlong],
-    "pimc_batch_tune": [_vp, C.c_int, _ip, _ip],
-    "pimc_batch_set_launch": [_vp, C.c_int, C.c_int],
+    "pimc_batch_tune": [_vp, C.c_int, C.POINTER(Launch)],
+    "pimc_batch_set_launch": [_vp, C.POINTER(Launch)],
+    "pimc_batch_get_launch": [_vp, C.POINTER(Launch)],
     "pimc_attempt_staging": [_vp, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, C.c_int, _ip, _dp],
     "pimc_attempt_swap": [_vp, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp, C.c_int,
                           _ip, _ip, _dp],

@@ -11,7 +11,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from ._native import MoveMix, Params, PimcError, Stats, check, load
+from ._native import Launch, MoveMix, Params, PimcError, Stats, check, load
 
 SEM_REFERENCE = 0
 SEM_PHYSICAL = 1
@@ -214,13 +214,24 @@ class Engine:
     def run_plain(self, n_sweeps: int):
         check(self.L.pimc_batch_run_plain(self.h, int(n_sweeps)))
 
-    def tune(self, sweeps_per_trial: int = 2):
-        b, s = C.c_int(), C.c_int()
-        check(self.L.pimc_batch_tune(self.h, sweeps_per_trial, C.byref(b), C.byref(s)))
-        return b.value, s.value
+    def tune(self, sweeps_per_trial: int = 2) -> dict:
+        """time the candidate launch shapes and keep the fastest (chains restored)"""
+        l = Launch()
+        check(self.L.pimc_batch_tune(self.h, sweeps_per_trial, C.byref(l)))
+        return self.launch
 
-    def set_launch(self, block: int, sweeps_per_launch: int):
-        check(self.L.pimc_batch_set_launch(self.h, block, sweeps_per_launch))
+    def set_launch(self, block: int, sweeps_per_launch: int = 1,
+                   state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False):
+        l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes)
+        check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
+
+    @property
+    def launch(self) -> dict:
+        """the batched launch shape in use"""
+        l = Launch()
+        check(self.L.pimc_batch_get_launch(self.h, C.byref(l)))
+        return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
+                "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes}
 
     def last_run_ms(self) -> float:
         v = C.c_double()

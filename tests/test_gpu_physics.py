@@ -157,8 +157,10 @@ def test_checkpoint_resume_bit_exact():
 
 
 def test_batched_equals_plain_and_tuner_is_transparent():
-    """the persistent/queue/graph path and one launch per chain produce the
-    same chains bit for bit; the tuner restores the state it advances"""
+    """the persistent/queue/graph path, in every launch shape (one CTA per
+    chain with and without shared-memory staging, one warp per chain), and
+    one launch per chain produce the same chains bit for bit; the tuner
+    restores the state it advances"""
     from pimc.engine import ChainParams, Engine
     rng = np.random.default_rng(7)
     ps = []
@@ -169,21 +171,46 @@ def test_batched_equals_plain_and_tuner_is_transparent():
                               harmonic_omega=1.0, interactions=bool(i % 2), pair_g=float(rng.uniform(0, 2)),
                               pair_sigma=0.5, r_a=1.5, semantics=int(i % 3 == 0), seed=1000 + i,
                               energy_capacity=8))
-    a, b = Engine(ps), Engine(ps)
+    shapes = [None, dict(block=64, sweeps_per_launch=2, warp_per_chain=True),
+              dict(block=256, sweeps_per_launch=1, warp_per_chain=True),
+              dict(block=128, sweeps_per_launch=3, state_smem_bytes=0),
+              dict(block=256, sweeps_per_launch=1, state_smem_bytes=100 * 1024)]
+    b = Engine(ps)
     for i, p in enumerate(ps):
-        m = mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3)
-        a.set_mix(m, chain=i)
-        b.set_mix(m, chain=i)
-    a.tune(sweeps_per_trial=2)
-    a.run_batched(6)
+        b.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
     b.run_plain(6)
-    for c in range(len(ps)):
-        np.testing.assert_array_equal(a.get_beads(c), b.get_beads(c))
-        np.testing.assert_array_equal(a.get_next(c), b.get_next(c))
-        # the estimator's block reduction order follows the tuned block size
-        np.testing.assert_allclose(a.energies(c), b.energies(c), rtol=1e-13, atol=1e-13)
-    sa, sb = a.total_stats(), b.total_stats()
-    assert sa.bead_updates == sb.bead_updates and sa.sweeps == sb.sweeps == 6 * len(ps)
+    sb = b.total_stats()
+    for shape in shapes:
+        a = Engine(ps)
+        for i, p in enumerate(ps):
+            a.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
+        if shape is None:
+            a.tune(sweeps_per_trial=2)
+        else:
+            a.set_launch(**shape)
+            got = a.launch
+            for k, v in shape.items():
+                assert got[k] == v
+        a.run_batched(6)
+        for c in range(len(ps)):
+            np.testing.assert_array_equal(a.get_beads(c), b.get_beads(c))
+            np.testing.assert_array_equal(a.get_next(c), b.get_next(c))
+            # the estimator's reduction order follows the threads per chain
+            np.testing.assert_allclose(a.energies(c), b.energies(c), rtol=1e-13, atol=1e-13)
+        sa = a.total_stats()
+        assert sa.bead_updates == sb.bead_updates and sa.sweeps == sb.sweeps == 6 * len(ps)
+        a.close()
+
+
+def test_launch_shape_rejects_bad_values():
+    from pimc.engine import ChainParams, Engine
+    from pimc._native import PimcError
+    e = Engine([ChainParams(dim=2, N=4, M=8, L=6.0, T=1.0, lam=0.5, harmonic_omega=1.0, seed=1)] * 2)
+    for bad in [dict(block=48), dict(block=512, warp_per_chain=True), dict(block=16, warp_per_chain=True),
+                dict(block=128, sweeps_per_launch=0), dict(block=128, state_smem_bytes=-1)]:
+        with pytest.raises(PimcError):
+            e.set_launch(**bad)
+    e.close()
 
 
 def _fd_action(e, oracle_free=None):
