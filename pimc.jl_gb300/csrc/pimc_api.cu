@@ -36,8 +36,6 @@ int fail(int code, const std::string &msg) {
       return fail(PIMC_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
-constexpr int kWarpScratchMin = 5 * (64 + 1) + 96;  // doubles, window_warp + its queue
-constexpr int kQueueBytes = 96 * 8;                  // one warp's neighbour queue
 constexpr unsigned kStateMagic = 0x50494D43u;   // "PIMC"
 constexpr int kStateBudget = 100 * 1024;        // shared bytes for a staged chain
 
@@ -48,7 +46,7 @@ struct Plan {
   int spl = 1;                 // sweeps per launch
   int state_cap = kStateBudget;
   int state_bytes = 0;         // shared bytes for a staged chain (CTA mode)
-  int warp_scratch_d = kWarpScratchMin;
+  int warp_scratch_d = window_scratch_doubles();
   int warp_bytes = 0;          // scratch bytes of one warp's chain (warp mode)
   size_t dyn_smem = 0;
 };
@@ -131,6 +129,21 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   if (d.nbins < 1) d.nbins = 1;
   d.rc = 2.0 * p.L / d.nbins;
   d.ncell = p.dim == 2 ? d.nbins * d.nbins : d.nbins;
+  // 16-bit fixed-point mirror of the positions on the periodic box: a pair
+  // within R of each other has mirror coordinates within R/u + 1 (u the unit)
+  // per axis; the bound adds 4 units so that a shifted mirror centre (one
+  // more rounding) is covered as well
+  {
+    const double u = 2.0 * p.L / 65536.0;
+    d.q_scale = 65536.0 / (2.0 * p.L);
+    d.q_unit2 = (float)(u * u);
+    auto lim = [&](double R) {
+      const double v = std::ceil((R / u + 4.0) * (R / u + 4.0));
+      return v >= 4294967295.0 ? 0xffffffffu : (unsigned)v;  // squares stay <= 2^31
+    };
+    d.q_lim_rc = lim(d.rc);
+    d.q_lim_hard = lim(p.hardcore_a);
+  }
   d.hard_a = p.hardcore_a;
   d.ctr = p.retry_cap > 0 ? p.retry_cap : 10000;
   d.flags = 0;
@@ -147,7 +160,7 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   d.key1 = (unsigned)(p.seed >> 32);
   d.chain_tag = (unsigned)chain;
   const size_t nm = (size_t)p.N * p.M;
-  const size_t sb = 8 * (size_t)(p.dim + 1) * nm + 4 * (size_t)p.dim * nm + 4 * (size_t)p.N;
+  const size_t sb = 8 * (size_t)(p.dim + 1) * nm + 4 * nm + 4 * (size_t)p.N;
   d.smem_bytes = sb > (size_t)(1 << 30) ? (1 << 30) : (int)((sb + 15) & ~(size_t)15);
   return d;
 }
@@ -243,17 +256,6 @@ int sync_check(Handle *h) {
   return PIMC_OK;
 }
 
-size_t swap_scratch_bytes(int N) {
-  return sizeof(double) * ((size_t)N + 6 * (64 + 1) + 4 * 64) + kQueueBytes;
-}
-
-// pol/idx (2N ints) + 3M doubles + one neighbour queue per warp of the CTA
-// centre-of-mass move
-size_t com_scratch_bytes(int N, int M, int nwarps) {
-  return sizeof(int) * 2 * (size_t)N + sizeof(double) * 3 * (size_t)M +
-         (size_t)nwarps * kQueueBytes;
-}
-
 // shared-memory layout of a launch shape.  CTA mode: staged chain state (the
 // largest chain that fits state_cap) followed by the CTA's scratch.  Warp
 // mode: per warp, its chain's control block and the scratch of a one-warp
@@ -264,9 +266,9 @@ Plan plan_smem(const Handle *h, int mode, int block, int spl, int state_cap) {
   p.block = block;
   p.spl = spl;
   p.state_cap = state_cap;
-  p.warp_scratch_d = kWarpScratchMin;
+  p.warp_scratch_d = window_scratch_doubles();
   if (mode == 1) {
-    size_t w = std::max(swap_scratch_bytes(h->maxN), (size_t)kWarpScratchMin * sizeof(double));
+    size_t w = std::max(swap_scratch_bytes(h->maxN), (size_t)window_scratch_doubles() * sizeof(double));
     w = std::max(w, com_scratch_bytes(h->maxN, h->maxM, 1));
     w = (w + 15) & ~(size_t)15;
     p.state_bytes = 0;
@@ -323,7 +325,7 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     const size_t NM = (size_t)p.N * p.M;
     d.x_off = (long long)dp; dp += (size_t)p.dim * NM;
     d.V_off = (long long)dp; dp += NM;
-    d.xf_off = (long long)dp; dp += ((size_t)p.dim * NM + 1) / 2;
+    d.xq_off = (long long)dp; dp += (NM + 1) / 2;
     dp = (dp + 1) & ~(size_t)1;
     d.host_off = (long long)h->n_stage;
     h->n_stage += (size_t)p.dim * NM;
@@ -653,7 +655,7 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   a.prop = proposal ? dprop : nullptr;
   a.out = h->d_iout;
   a.force_warp = h->force_warp;
-  size_t smem = std::max(swap_scratch_bytes(d.N), (size_t)kWarpScratchMin * 8);
+  size_t smem = std::max(swap_scratch_bytes(d.N), (size_t)window_scratch_doubles() * 8);
   smem = std::max(smem, com_scratch_bytes(d.N, d.M, 4));
   CK(launch_attempt(a, smem, h->stream));
   int out[5] = {0, 0, 0, 0, 0};
@@ -1004,8 +1006,8 @@ int pimc_eval_staging_weights(void *handle, int n, int j0, int m, const double *
   Handle *h = H(handle);
   if (!h || !rp || !w_init || !w_upd) return fail(PIMC_EARG, "null argument");
   const ChainDesc &d = h->desc[0];
-  if (n < 0 || n >= d.N || j0 < 0 || j0 >= d.M || m < 2 || m > d.M - 1)
-    return fail(PIMC_EARG, "window out of range");
+  if (n < 0 || n >= d.N || j0 < 0 || j0 >= d.M || m < 2 || m > d.M - 1 || m > 64)
+    return fail(PIMC_EARG, "window out of range (m must be in [2, min(M-1, 64)])");
   const size_t nrp = (size_t)(m + 1) * d.dim;
   if (ensure_buf(h, nrp + 8)) return PIMC_ENOMEM;
   CK(cudaMemcpyAsync(h->d_buf + 8, rp, nrp * 8, cudaMemcpyHostToDevice, h->stream));

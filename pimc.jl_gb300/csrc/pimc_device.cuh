@@ -6,12 +6,13 @@
 // Layout: positions are slice-major on the device, x[d][j][n] (all particles
 // of one imaginary-time slice contiguous), cached links V[j][n].  Thread-per-
 // window staging reads slices of consecutive particles (coalesced), and a
-// neighbour query at slice j is a contiguous row.  Chains with a pair action
-// or a hard core keep an FP32 mirror xf[j][n] of the positions: a warp scans
-// the row in FP32 with a safety margin and evaluates the few candidates near
-// the cut-off exactly in FP64, so the neighbour set is exactly the
-// reference's (every bead within 2L/nbins, src/nearest_neighbours.jl:131-154)
-// without a linked cell grid to chase or maintain.
+// neighbour query at slice j is a contiguous row.  Every chain keeps a
+// 16-bit fixed-point mirror xq[j][n] of the positions (one 32-bit word per
+// bead): a warp scans the row with integer arithmetic and a bound that
+// covers the rounding, and evaluates the few candidates exactly in FP64, so
+// the neighbour set is exactly the reference's (every bead within 2L/nbins,
+// src/nearest_neighbours.jl:131-154) without a linked cell grid to chase or
+// maintain.
 //
 // Reference correspondence (oameye/PIMC.jl):
 //   distance / lnK / lnV / teleport      src/propagator.jl:6-32
@@ -30,7 +31,10 @@ namespace pimc {
 
 constexpr int WMAX = 64;     // largest staging / swap window m handled on the device
 constexpr int TWMAX = 32;    // thread-per-window variant handles m <= TWMAX
-constexpr int WARP_SCRATCH_D = 5 * (WMAX + 1) + 96;  // doubles of per-warp scratch
+// doubles of per-warp scratch of window_warp: new beads x, y, their external
+// potential, normals (2 per bead), the neighbour queue (96 entries), and the
+// new beads' mirror words
+constexpr int WARP_SCRATCH_D = 5 * (WMAX + 1) + 96 + (WMAX + 2) / 2;
 
 // move outcomes (PIMC_REJECT / ACCEPT / SKIP / HARDCORE of pimc.h)
 constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
@@ -158,14 +162,34 @@ struct InjDraws {
 };
 
 // ---------------------------------------------------------------------------
-// chain view: x/V/next/xf may live in shared or global memory (generic pointers)
+// 16-bit fixed-point mirror of the positions: a coordinate x of the periodic
+// box [-L, L) is stored as round((x + L) 65536 / 2L) mod 65536, x in the low
+// and y in the high half of a 32-bit word.  A wrapped 16-bit difference is
+// the minimum-image separation in mirror units, so a neighbour prefilter is
+// integer arithmetic on one word per bead (half the bytes of an FP32 copy).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned qcoord(const ChainDesc &d, double x) {
+  return (unsigned)__double2ll_rn((x + d.L) * d.q_scale) & 0xffffu;
+}
+__device__ __forceinline__ unsigned qpos(const ChainDesc &d, double x, double y) {
+  return qcoord(d, x) | (d.dim > 1 ? qcoord(d, y) << 16 : 0u);
+}
+// squared minimum-image separation of two mirror words, in squared units
+__device__ __forceinline__ unsigned qdist2(unsigned a, unsigned b) {
+  const unsigned dd = __vsub2(a, b);
+  const int dx = ((int)(dd << 16)) >> 16, dy = ((int)dd) >> 16;
+  return (unsigned)(dx * dx) + (unsigned)(dy * dy);
+}
+
+// ---------------------------------------------------------------------------
+// chain view: x/V/next/xq may live in shared or global memory (generic pointers)
 // ---------------------------------------------------------------------------
 struct CV {
   const ChainDesc *d;
   double *x;          // x[(k*M + j)*ldn + n]
   double *V;          // V[j*ldn + n]
   int *next;
-  float *xf;          // FP32 mirror [(j*ldn + n)*dim + k], or null
+  unsigned *xq;       // fixed-point mirror [j*ldn + n]
   const double2 *tab; // (alpha, sigma)[m*wtab + t]
   unsigned long long *hist;
   double *eser;
@@ -177,15 +201,24 @@ struct CV {
   __device__ __forceinline__ double Xd(int k, int n, int j) const {
     return k < dim ? X(k, n, j) : 0.0;
   }
-  // every position write goes through here so that the FP32 mirror follows
+  __device__ __forceinline__ unsigned Q(int n, int j) const { return xq[(size_t)j * ldn + n]; }
+  // every position write goes through here so that the mirror follows
   __device__ __forceinline__ void set_pos(int n, int j, double px, double py) const {
     X(0, n, j) = px;
     if (dim > 1) X(1, n, j) = py;
-    if (xf) {
-      float *f = xf + ((size_t)j * ldn + n) * dim;
-      f[0] = (float)px;
-      if (dim > 1) f[1] = (float)py;
+    xq[(size_t)j * ldn + n] = qpos(*d, px, py);
+  }
+  // exchange the beads of particles a and b at slice j, mirror included
+  __device__ __forceinline__ void exchange(int a, int b, int j) const {
+    for (int k = 0; k < dim; ++k) {
+      const double t = X(k, a, j);
+      X(k, a, j) = X(k, b, j);
+      X(k, b, j) = t;
     }
+    unsigned *r = xq + (size_t)j * ldn;
+    const unsigned t = r[a];
+    r[a] = r[b];
+    r[b] = t;
   }
 };
 
@@ -293,33 +326,20 @@ __device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, 
 // ---------------------------------------------------------------------------
 // neighbour scans over one slice
 // ---------------------------------------------------------------------------
-// FP32 prefilter: min-image squared distance in FP32 plus a margin that
-// covers the FP32 rounding of positions within [-L, L] (|err| of each
-// coordinate difference <= 4 L 2^-24), so every pair within r of the exact
-// FP64 distance passes the filter.
+// neighbour prefilter on the mirror: every bead within R (exact FP64
+// minimum-image distance) of the centre passes; lim is the chain's bound for
+// R (q_lim_rc or q_lim_hard)
 struct Prefilter {
-  float L2f, ax, ay;
-  float lim;   // squared radius plus margin
-  int dim;
-  __device__ __forceinline__ void init(const ChainDesc &d, double px, double py, double r) {
-    dim = d.dim;
-    L2f = (float)(2.0 * d.L);
-    ax = (float)px;
-    ay = (float)py;
-    const double e = 4.0 * d.L * 5.9604644775390625e-8 + 1e-30;
-    lim = (float)((r + 2.0 * e) * (r + 2.0 * e) * (1.0 + 1e-6) + 1e-12);
+  unsigned c, lim;
+  __device__ __forceinline__ void init(const ChainDesc &d, double px, double py, unsigned lim_) {
+    c = qpos(d, px, py);
+    lim = lim_;
   }
-  __device__ __forceinline__ bool pass(const float *p) const {
-    float dx = fabsf(ax - p[0]);
-    dx = fminf(dx, L2f - dx);
-    float s = dx * dx;
-    if (dim > 1) {
-      float dy = fabsf(ay - p[1]);
-      dy = fminf(dy, L2f - dy);
-      s = fmaf(dy, dy, s);
-    }
-    return s <= lim;
+  __device__ __forceinline__ void init_q(unsigned centre, unsigned lim_) {
+    c = centre;
+    lim = lim_;
   }
+  __device__ __forceinline__ bool pass(unsigned p) const { return qdist2(c, p) <= lim; }
 };
 
 // ---------------------------------------------------------------------------
@@ -332,8 +352,9 @@ struct Prefilter {
 // one and evaluates it exactly in FP64.  The warp's divergent FP64 work is
 // then proportional to the neighbours found, not to the particles scanned.
 //
-// Seg provides: links(), slice(t), cur(side, t, &x, &y), nxt(side, t, &x, &y),
-// skip(side, t, b).  side 0 = old configuration, 1 = new.
+// Seg provides: slice(t), cur(side, t, &x, &y), nxt(side, t, &x, &y),
+// curq(side, t) (the bead's mirror word), skip(side, t, b).  side 0 = old
+// configuration, 1 = new.
 // ---------------------------------------------------------------------------
 constexpr int PQ_CAP = 96;  // queue entries per warp (64-bit)
 
@@ -384,17 +405,14 @@ __device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do
   for (int t = t0; t < t1; ++t) {
     const int j = s.slice(t);
     Prefilter fo, fn;
-    double ax, ay, px, py;
-    s.cur(0, t, ax, ay);
-    s.cur(1, t, px, py);
-    fo.init(d, ax, ay, d.rc);
-    fn.init(d, px, py, d.rc);
-    const float *row = c.xf + (size_t)j * c.ldn * dim;
+    fo.init_q(s.curq(0, t), d.q_lim_rc);
+    fn.init_q(s.curq(1, t), d.q_lim_rc);
+    const unsigned *row = c.xq + (size_t)j * c.ldn;
     for (int b0 = 0; b0 < N; b0 += 32) {
       const int b = b0 + lane;
       bool po = false, pn = false;
       if (b < N) {
-        const float *pb = row + (size_t)b * dim;
+        const unsigned pb = row[b];
         po = do_old && fo.pass(pb) && !s.skip(0, t, b);
         pn = do_new && fn.pass(pb) && !s.skip(1, t, b);
       }
@@ -417,7 +435,11 @@ struct WindowSeg {
   const CV *c;
   int n, nx, j0, M;
   const double *px, *py;
+  const unsigned *pq;   // mirror words of the new beads
   __device__ __forceinline__ int own(int t) const { return j0 + t < M ? n : nx; }
+  __device__ __forceinline__ unsigned curq(int side, int t) const {
+    return side ? pq[t] : c->Q(own(t), slice(t));
+  }
   __device__ __forceinline__ int slice(int t) const { return j0 + t < M ? j0 + t : j0 + t - M; }
   __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
     if (side) { x = px[t]; y = py[t]; }
@@ -437,11 +459,11 @@ __device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, 
   const int N = c.N, dim = c.dim;
   const double a2 = d.hard_a * d.hard_a;
   Prefilter f;
-  f.init(d, x, y, d.hard_a);
-  const float *row = c.xf + (size_t)j * c.ldn * dim;
+  f.init(d, x, y, d.q_lim_hard);
+  const unsigned *row = c.xq + (size_t)j * c.ldn;
   bool hit = false;
   for (int b = lane; b < N && !hit; b += lanes) {
-    if (b == e1 || b == e2 || !f.pass(row + (size_t)b * dim)) continue;
+    if (b == e1 || b == e2 || !f.pass(row[b])) continue;
     if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;
   }
   return hit;
@@ -543,6 +565,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   const bool hard = (d.flags & PF_HARD) != 0;
   double *sx_ = sb, *sy_ = sb + (WMAX + 1), *svb = sb + 2 * (WMAX + 1);
   double *sz = sb + 3 * (WMAX + 1);  // 2*(WMAX+1): normals
+  unsigned *sq = (unsigned *)(sb + 5 * (WMAX + 1) + 96);
   const int nx = c.next[n];
   const int jend = j0 + m;
   const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
@@ -610,6 +633,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     sx_[t] = qx;
     sy_[t] = qy;
     svb[t] = vext(d, qx, qy);
+    if (phys_pair) sq[t] = qpos(d, qx, qy);
   }
   __syncwarp();
   double wi = 0.0, wu = 0.0;
@@ -619,7 +643,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     wu += mhtau * (svb[t] + svb[t + 1]);
   }
   if (phys_pair) {
-    WindowSeg seg{&c, n, nx, j0, M, sx_, sy_};
+    WindowSeg seg{&c, n, nx, j0, M, sx_, sy_, sq};
     segment_pairs(c, seg, 0, m, true, true, (unsigned long long *)(sb + 5 * (WMAX + 1)), wi, wu,
                   lane);
   }

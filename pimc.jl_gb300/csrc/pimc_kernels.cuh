@@ -56,8 +56,10 @@ struct SwapScratch {
   double *r1x, *r1y, *r2x, *r2y, *vb1, *vb2;   // WMAX+1 each
   double *z;                                   // 4*WMAX normals
   unsigned long long *q;                       // PQ_CAP neighbour queue
+  unsigned *q1, *q2;                           // WMAX+1 mirror words each
   static __host__ __device__ size_t bytes(int N) {
-    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX + PQ_CAP);
+    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX + PQ_CAP) +
+           sizeof(unsigned) * 2 * (WMAX + 1);
   }
   __device__ void carve(void *base, int N) {
     double *p = (double *)base;
@@ -67,6 +69,30 @@ struct SwapScratch {
     vb1 = p; p += WMAX + 1; vb2 = p; p += WMAX + 1;
     z = p; p += 4 * WMAX;
     q = (unsigned long long *)p;
+    q1 = (unsigned *)(q + PQ_CAP);
+    q2 = q1 + (WMAX + 1);
+  }
+};
+
+// scratch of a centre-of-mass move: cycle members and their index, the
+// shifted single path (x, y, external potential, mirror words), and one
+// neighbour queue per warp
+struct ComScratch {
+  int *pol, *idx;
+  double *q;
+  unsigned *qq;
+  unsigned long long *qbuf;
+  static __host__ __device__ size_t bytes(int N, int M, int nwarps) {
+    return sizeof(int) * 2 * (size_t)N + sizeof(double) * 3 * (size_t)M +
+           sizeof(unsigned) * 2 * (size_t)((M + 1) / 2) +
+           sizeof(unsigned long long) * PQ_CAP * (size_t)nwarps;
+  }
+  __device__ void carve(void *base, int N, int M) {
+    pol = (int *)base;
+    idx = pol + N;
+    q = (double *)(pol + 2 * N);
+    qq = (unsigned *)(q + 3 * M);
+    qbuf = (unsigned long long *)(qq + 2 * ((M + 1) / 2));
   }
 };
 
@@ -77,8 +103,12 @@ struct SwapSeg {
   int j0, M, na, nxa, n1, nx1, n2, nx2;
   const double *px, *py;
   bool ref;
+  const unsigned *pq;   // mirror words of the new beads
   __device__ __forceinline__ int slice(int t) const { return j0 + t < M ? j0 + t : j0 + t - M; }
   __device__ __forceinline__ int own(int t) const { return j0 + t < M ? na : nxa; }
+  __device__ __forceinline__ unsigned curq(int side, int t) const {
+    return side ? pq[t] : c->Q(own(t), slice(t));
+  }
   __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
     if (side) { x = px[t]; y = py[t]; }
     else { x = c->X(0, own(t), slice(t)); y = c->Xd(1, own(t), slice(t)); }
@@ -103,7 +133,15 @@ struct ComSeg {
   int M;
   const double *q;   // single path: new x[M], y[M]; null for a cycle
   double shx, shy, L, inv2L;
+  const unsigned *qq;  // single path: the new beads' mirror words
+  unsigned qsh;        // the shift in mirror units (a cycle's new centres)
   __device__ __forceinline__ int slice(int t) const { return t % M; }
+  __device__ __forceinline__ unsigned curq(int side, int t) const {
+    const int i = pol[t / M], j = t % M;
+    if (!side) return c->Q(i, j);
+    if (q) return qq[j];
+    return __vadd2(c->Q(i, j), qsh);
+  }
   __device__ __forceinline__ void bead(int side, int i, int j, double &x, double &y) const {
     if (!side) { x = c->X(0, i, j); y = c->Xd(1, i, j); return; }
     if (q) { x = q[j]; y = q[M + j]; return; }
@@ -127,54 +165,44 @@ struct ComSeg {
 // proposal weights are then a deterministic FP32 function of the
 // configuration, and the physical ratio uses the same function, so detailed
 // balance is exact)
+// a bead for the heat bath: FP64 position and its mirror word
+struct HBead {
+  double x, y;
+  unsigned q;
+};
+
 template <bool FAST>
 struct HeatBath {
   const CV *c;
   double inv_den;
-  float inv_denf, L2f;
+  float inv_denf;   // 1 / (4 lambda m tau) times the squared mirror unit
   int se, j0;
   bool wrap;
   __device__ __forceinline__ int endp(int i) const { return wrap ? c->next[i] : i; }
-  __device__ __forceinline__ float d2f(float a, float b, float a2, float b2) const {
-    float dx = fabsf(a - b);
-    dx = fminf(dx, L2f - dx);
-    float s = dx * dx;
-    if (c->dim > 1) {
-      float dy = fabsf(a2 - b2);
-      dy = fminf(dy, L2f - dy);
-      s = fmaf(dy, dy, s);
-    }
-    return s;
+  __device__ __forceinline__ HBead bead(int n, int j) const {
+    return {c->X(0, n, j), c->Xd(1, n, j), c->Q(n, j)};
   }
-  // E = bead (endp(i), se) unless ex_given
-  __device__ __forceinline__ double expo(int i, double sx, double sy, double fx, double fy,
-                                         bool ex_given = false, double ex = 0.0,
-                                         double ey = 0.0) const {
+  // E = bead (endp(i), se) unless e is given
+  __device__ __forceinline__ double expo(int i, const HBead &s, const HBead &f,
+                                         const HBead *e = nullptr) const {
     const ChainDesc &d = *c->d;
     if (!FAST) {
-      if (!ex_given) {
+      double ex, ey;
+      if (!e) {
         const int ei = endp(i);
         ex = c->X(0, ei, se);
         ey = c->Xd(1, ei, se);
+      } else {
+        ex = e->x;
+        ey = e->y;
       }
-      const double t1 = mi2(d, sx, sy, ex, ey);
-      const double t2 = mi2(d, c->X(0, i, j0), c->Xd(1, i, j0), fx, fy);
+      const double t1 = mi2(d, s.x, s.y, ex, ey);
+      const double t2 = mi2(d, c->X(0, i, j0), c->Xd(1, i, j0), f.x, f.y);
       return -(t1 + t2) * inv_den;
     } else {
-      const int dim = c->dim;
-      float efx, efy = 0.f;
-      if (!ex_given) {
-        const float *pe = c->xf + ((size_t)se * c->ldn + endp(i)) * dim;
-        efx = pe[0];
-        if (dim > 1) efy = pe[1];
-      } else {
-        efx = (float)ex;
-        efy = (float)ey;
-      }
-      const float *pi = c->xf + ((size_t)j0 * c->ldn + i) * dim;
-      const float s = d2f((float)sx, efx, (float)sy, efy) +
-                      d2f(pi[0], (float)fx, dim > 1 ? pi[1] : 0.f, (float)fy);
-      return (double)(-s * inv_denf);
+      const unsigned eq = e ? e->q : c->Q(endp(i), se);
+      const float s2 = (float)qdist2(s.q, eq) + (float)qdist2(c->Q(i, j0), f.q);
+      return (double)(-s2 * inv_denf);
     }
   }
   __device__ __forceinline__ double ex_(double v) const {
@@ -199,24 +227,29 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
   hb.wrap = (j0 + m) >= M;
   hb.se = hb.wrap ? j0 + m - M : j0 + m;
   hb.inv_den = 1.0 / (4.0 * (m * d.tau) * d.lambda);
-  hb.inv_denf = (float)hb.inv_den;
-  hb.L2f = (float)(2.0 * L);
+  hb.inv_denf = (float)hb.inv_den * d.q_unit2;
   const int se = hb.se;
   const bool wrap = hb.wrap;
-  const double ax = c.X(0, n1, j0), ay = c.Xd(1, n1, j0);
+  const HBead A = hb.bead(n1, j0);
+  const double ax = A.x, ay = A.y;
   const int e1p = hb.endp(n1);
-  const double e1x = c.X(0, e1p, se), e1y = c.Xd(1, e1p, se);
+  const HBead E1 = hb.bead(e1p, se);
+  const double e1x = E1.x, e1y = E1.y;
   // weights exp(t_i + y_i) shifted by their maximum (the reference normalises
-  // them, helper.jl:260-263; the shift keeps them from underflowing)
+  // them, helper.jl:260-263; the shift keeps them from underflowing).  The
+  // exponents are formed lane-strided (coalesced reads of the slices); the
+  // sums and the cumulative search run over contiguous per-lane chunks so
+  // that the search order is the particle order
   const int chunk = (N + 31) / 32;
   const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
   double wmax = -INFINITY;
-  for (int i = i0; i < i1; ++i) {
-    const double v = hb.expo(i, ax, ay, e1x, e1y);
+  for (int i = lane; i < N; i += 32) {
+    const double v = hb.expo(i, A, E1);
     S.w[i] = v;
     wmax = fmax(wmax, v);
   }
   wmax = warp_max(wmax);
+  __syncwarp();
   double ls = 0.0;
   for (int i = i0; i < i1; ++i) {
     const double e = hb.ex_(S.w[i] - wmax);
@@ -249,26 +282,25 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
     // (1/S'_1 + 1/S'_2) / (1/S_1 + 1/S_2): S_a sums the heat-bath weights
     // with a chosen first; primes after the ends of n1 and n2 are exchanged
     const double l1 = wmax + log(ssum);
-    const double bx = c.X(0, n2, j0), by = c.Xd(1, n2, j0);
-    const int e2p = hb.endp(n2);
-    const double e2x = c.X(0, e2p, se), e2y = c.Xd(1, e2p, se);
+    const HBead B = hb.bead(n2, j0);
+    const HBead E2 = hb.bead(hb.endp(n2), se);
     // expo(i) with E(i) replaced by E'(i): the ends of n1 and n2 exchanged
-    auto expo_p = [&](int i, double sx_, double sy_, double fx, double fy) {
-      if (i != n1 && i != n2) return hb.expo(i, sx_, sy_, fx, fy);
-      return hb.expo(i, sx_, sy_, fx, fy, true, i == n1 ? e2x : e1x, i == n1 ? e2y : e1y);
+    auto expo_p = [&](int i, const HBead &s_, const HBead &f_) {
+      if (i != n1 && i != n2) return hb.expo(i, s_, f_);
+      return hb.expo(i, s_, f_, i == n1 ? &E2 : &E1);
     };
     double mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = i0; i < i1; ++i) {
-      mx[0] = fmax(mx[0], hb.expo(i, bx, by, e2x, e2y));
-      mx[1] = fmax(mx[1], expo_p(i, ax, ay, e2x, e2y));
-      mx[2] = fmax(mx[2], expo_p(i, bx, by, e1x, e1y));
+    for (int i = lane; i < N; i += 32) {
+      mx[0] = fmax(mx[0], hb.expo(i, B, E2));
+      mx[1] = fmax(mx[1], expo_p(i, A, E2));
+      mx[2] = fmax(mx[2], expo_p(i, B, E1));
     }
     for (int k = 0; k < 3; ++k) mx[k] = warp_max(mx[k]);
     double s3[3] = {0.0, 0.0, 0.0};
-    for (int i = i0; i < i1; ++i) {
-      s3[0] += hb.ex_(hb.expo(i, bx, by, e2x, e2y) - mx[0]);
-      s3[1] += hb.ex_(expo_p(i, ax, ay, e2x, e2y) - mx[1]);
-      s3[2] += hb.ex_(expo_p(i, bx, by, e1x, e1y) - mx[2]);
+    for (int i = lane; i < N; i += 32) {
+      s3[0] += hb.ex_(hb.expo(i, B, E2) - mx[0]);
+      s3[1] += hb.ex_(expo_p(i, A, E2) - mx[1]);
+      s3[2] += hb.ex_(expo_p(i, B, E1) - mx[2]);
     }
     for (int k = 0; k < 3; ++k) s3[k] = warp_sum(s3[k]);
     const double l2 = mx[0] + log(s3[0]);
@@ -364,6 +396,7 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
     (b == 0 ? S.r1x : S.r2x)[t] = qx;
     (b == 0 ? S.r1y : S.r2y)[t] = qy;
     (b == 0 ? S.vb1 : S.vb2)[t] = vext(d, qx, qy);
+    if (d.flags & PF_PAIR) (b == 0 ? S.q1 : S.q2)[t] = qpos(d, qx, qy);
   }
   __syncwarp();
   const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
@@ -377,7 +410,7 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
   if (any_pair) {
     for (int b = 0; b < 2; ++b) {
       SwapSeg seg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
-                  b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys};
+                  b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
       double wo = 0.0, wn = 0.0;
       segment_pairs(c, seg, 0, m, true, true, S.q, wo, wn, lane);
       // the reference adds the new paths' pair terms to w_initial and lets
@@ -435,9 +468,7 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
   }
   if (j0 + m < M - 1)
     for (int j = se + 1 + lane; j < M; j += 32) {
-      const double ax_ = c.X(0, n1, j), ay_ = c.Xd(1, n1, j);
-      c.set_pos(n1, j, c.X(0, n2, j), c.Xd(1, n2, j));
-      c.set_pos(n2, j, ax_, ay_);
+      c.exchange(n1, n2, j);
       const double v = c.Vl(n1, j);
       c.Vl(n1, j) = c.Vl(n2, j);
       c.Vl(n2, j) = v;
@@ -534,9 +565,11 @@ struct Group {
 };
 
 template <bool WARP, class D>
-__device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, int *pol, int *idx,
-                         double *q, unsigned long long *qbuf, double *red, double *shift,
-                         int *sflag, int *np_out) {
+__device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, const ComScratch &cs,
+                         double *red, double *shift, int *sflag, int *np_out) {
+  int *pol = cs.pol, *idx = cs.idx;
+  double *q = cs.q;
+  unsigned long long *qbuf = cs.qbuf;
   using G = Group<WARP>;
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M, dim = c.dim, tid = G::rank(), nt = G::size();
@@ -593,17 +626,18 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, i
     if (!G::any(hit)) break;
   }
   const double shx = shift[0], shy = shift[1];
-  auto qpos = [&](int i, int j, double &qx, double &qy) {
+  auto shifted = [&](int i, int j, double &qx, double &qy) {
     qx = teleport(c.X(0, i, j) + shx, L, inv2L);
     qy = dim > 1 ? teleport(c.X(1, i, j) + shy, L, inv2L) : 0.0;
   };
   if (!polymer) {
     for (int j = tid; j < M; j += nt) {
       double qx, qy;
-      qpos(n, j, qx, qy);
+      shifted(n, j, qx, qy);
       q[j] = qx;
       q[M + j] = qy;
       q[2 * M + j] = vext(d, qx, qy);
+      if (phys_pair) cs.qq[j] = qpos(d, qx, qy);
     }
     G::sync();
   }
@@ -616,15 +650,19 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, i
       ws[1] += mhtau * (q[2 * M + j] + q[2 * M + jn]);
     } else {
       double qx, qy, qnx, qny;
-      qpos(i, j, qx, qy);
-      qpos(in, jn, qnx, qny);
+      shifted(i, j, qx, qy);
+      shifted(in, jn, qnx, qny);
       ws[1] += mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
     }
   }
   if (phys_pair) {
     // warps split the links, lanes the particles of each slice; pairs inside
     // the cycle keep their relative positions under the rigid shift
-    ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L};
+    // a cycle's shifted centres: the mirror words plus the shift in mirror
+    // units (one more rounding, inside the prefilter bound)
+    const unsigned qsh = ((unsigned)__double2ll_rn(shx * d.q_scale) & 0xffffu) |
+                         (dim > 1 ? ((unsigned)__double2ll_rn(shy * d.q_scale) & 0xffffu) << 16 : 0u);
+    ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L, cs.qq, qsh};
     const int tot = np * M, per = (tot + nwarps - 1) / nwarps;
     const int t0 = min(tot, warp * per), t1 = min(tot, t0 + per);
     segment_pairs(c, seg, t0, t1, true, true, qbuf + (size_t)warp * PQ_CAP, ws[0], ws[1], lane);
@@ -646,8 +684,8 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, i
       c.Vl(i, j) = mhtau * (q[2 * M + j] + q[2 * M + jn]);
     } else {
       double qx, qy, qnx, qny;
-      qpos(i, j, qx, qy);
-      qpos(in, jn, qnx, qny);
+      shifted(i, j, qx, qy);
+      shifted(in, jn, qnx, qny);
       c.Vl(i, j) = mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
     }
   }
@@ -659,7 +697,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, i
       qx = q[j];
       qy = q[M + j];
     } else {
-      qpos(i, j, qx, qy);
+      shifted(i, j, qx, qy);
     }
     c.set_pos(i, j, qx, qy);
   }
@@ -751,11 +789,11 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
     for (int kk = k0; kk < k1; ++kk) {
       const int j = kk / N, i = kk % N;
       Prefilter f;
-      f.init(d, c.X(0, i, j), c.Xd(1, i, j), d.rc);
-      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      f.init_q(c.Q(i, j), d.q_lim_rc);
+      const unsigned *row = c.xq + (size_t)j * c.ldn;
       for (int b0 = i + 1; b0 < N; b0 += 32) {
         const int b = b0 + lane;
-        const bool p = b < N && f.pass(row + (size_t)b * dim);
+        const bool p = b < N && f.pass(row[b]);
         const unsigned mk = __ballot_sync(0xffffffffu, p);
         if (p) q[qn + __popc(mk & lt)] = ((unsigned long long)(unsigned)b << 32) | (unsigned)kk;
         qn += __popc(mk);

@@ -90,5 +90,9 @@ cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, 
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);
 cudaError_t upload_exp_table();
+// shared scratch of the device move routines (bytes; doubles for a window)
+size_t swap_scratch_bytes(int N);
+size_t com_scratch_bytes(int N, int M, int nwarps);
+int window_scratch_doubles();
 
 }  // namespace pimc

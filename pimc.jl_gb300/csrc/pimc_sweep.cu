@@ -25,7 +25,7 @@ __device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ip
   c.ldn = d->N;
   c.x = dpool + d->x_off;
   c.V = dpool + d->V_off;
-  c.xf = (float *)(dpool + d->xf_off);
+  c.xq = (unsigned *)(dpool + d->xq_off);
   c.next = ipool + d->next_off;
   c.tab = (const double2 *)(dpool + d->tab_off);
   c.hist = (d->dens_off >= 0 && upool) ? upool + d->dens_off : nullptr;
@@ -202,13 +202,12 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
       }
       G::sync();
     } else {
-      int *pol = (int *)scratch, *idx = pol + N;
-      double *q = (double *)(pol + 2 * N);
-      unsigned long long *qbuf = (unsigned long long *)(q + 3 * M);
+      ComScratch cs;
+      cs.carve(scratch, N, M);
       for (int n = 0; n < N; ++n) {
         if (c.next[n] != n) continue;
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_group<WARP>(c, n, false, step, dr, pol, idx, q, qbuf, red, sc.shift, &sc.iflag[2], nullptr);
+        const int r = com_group<WARP>(c, n, false, step, dr, cs, red, sc.shift, &sc.iflag[2], nullptr);
         if (tid == 0) {
           tal[2] += 1.0;
           tal[6] += r == RES_ACCEPT;
@@ -221,8 +220,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
 
   // ---- cycle centre of mass, one attempt per cycle (led by its lowest index)
   for (int ph = 0; ph < mix.polymer_com_phases; ++ph) {
-    int *pol = (int *)scratch, *idx = pol + N;
-    unsigned long long *qbuf = (unsigned long long *)((double *)(pol + 2 * N) + 3 * M);
+    ComScratch cs;
+    cs.carve(scratch, N, M);
     for (int n = 0; n < N; ++n) {
       if (tid == 0) {
         int lead = 1, i = c.next[n], guard = 0;
@@ -235,8 +234,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
       G::sync();
       if (!sc.iflag[1]) continue;
       GenDraws dr = gen_draws(make_stream(d, sweep, PH_PCOM, (unsigned)(ph * N + n)));
-      const int r = com_group<WARP>(c, n, true, sc.v.pcom_step, dr, pol, idx, nullptr, qbuf, red, sc.shift,
-                            &sc.iflag[2], &sc.iflag[3]);
+      const int r = com_group<WARP>(c, n, true, sc.v.pcom_step, dr, cs, red, sc.shift, &sc.iflag[2],
+                                    &sc.iflag[3]);
       const int np = sc.iflag[3];
       if (tid == 0) {
         tal[3] += 1.0;
@@ -356,15 +355,15 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
     if (staged) {
       double *sx = (double *)smem;
       double *sV = sx + nx;
-      float *sf = (float *)(sV + nv);
-      int *snx = (int *)(sf + nx);
+      unsigned *sq = (unsigned *)(sV + nv);
+      int *snx = (int *)(sq + nv);
       for (size_t e = tid; e < nx; e += nt) sx[e] = c.x[e];
       for (size_t e = tid; e < nv; e += nt) sV[e] = c.V[e];
-      for (size_t e = tid; e < nx; e += nt) sf[e] = c.xf[e];
+      for (size_t e = tid; e < nv; e += nt) sq[e] = c.xq[e];
       for (int e = tid; e < N; e += nt) snx[e] = c.next[e];
       c.x = sx;
       c.V = sV;
-      c.xf = sf;
+      c.xq = sq;
       c.next = snx;
       __syncthreads();
     }
@@ -372,11 +371,11 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
     for (int s = 0; s < a.sweeps; ++s) sweep_one<false>(sc, red, c, scratch, a.warp_scratch_d);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
-      float *gf = (float *)(a.dpool + d.xf_off);
+      unsigned *gq = (unsigned *)(a.dpool + d.xq_off);
       int *gn = a.ipool + d.next_off;
       for (size_t e = tid; e < nx; e += nt) gx[e] = c.x[e];
       for (size_t e = tid; e < nv; e += nt) gV[e] = c.V[e];
-      for (size_t e = tid; e < nx; e += nt) gf[e] = c.xf[e];
+      for (size_t e = tid; e < nv; e += nt) gq[e] = c.xq[e];
       for (int e = tid; e < N; e += nt) gn[e] = c.next[e];
     }
     if (tid == 0) a.var[sc.chain] = sc.v;
@@ -427,11 +426,10 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   } else if (a.kind == MV_COM && !serial && !a.force_warp) {
     if (tid == 0) res = com_thread(c, a.n, a.step, dr);
   } else {
-    int *pol = (int *)smem, *idx = pol + d.N;
-    double *q = (double *)(pol + 2 * d.N);
-    unsigned long long *qbuf = (unsigned long long *)(q + 3 * d.M);
-    res = com_group<false>(c, a.n, a.kind == MV_PCOM, a.step, dr, pol, idx, q, qbuf, red, sc.shift, &sc.iflag[2],
-                  &sc.iflag[3]);
+    ComScratch cs;
+    cs.carve(smem, d.N, d.M);
+    res = com_group<false>(c, a.n, a.kind == MV_PCOM, a.step, dr, cs, red, sc.shift, &sc.iflag[2],
+                           &sc.iflag[3]);
     extra = sc.iflag[3];
   }
   __syncthreads();
@@ -475,10 +473,10 @@ __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
       const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
       const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
       Prefilter f;
-      f.init(d, ax, ay, d.rc);
-      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      f.init_q(c.Q(i, j), d.q_lim_rc);
+      const unsigned *row = c.xq + (size_t)j * c.ldn;
       for (int b = i + 1 + lane; b < N; b += 32) {
-        if (!f.pass(row + (size_t)b * dim)) continue;
+        if (!f.pass(row[b])) continue;
         const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
         if (r2a > rc2) continue;
         const int bn = j == M - 1 ? c.next[b] : b;
@@ -513,13 +511,15 @@ __global__ void k_eval_weights(EvalArgs a) {
   }
   if ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) {
     __shared__ double wx[WMAX + 1], wy[WMAX + 1];
+    __shared__ unsigned wq[WMAX + 1];
     __shared__ unsigned long long q[PQ_CAP];
     for (int t = lane; t <= m; t += 32) {
       wx[t] = px(t);
       wy[t] = py(t);
+      wq[t] = qpos(d, wx[t], wy[t]);
     }
     __syncwarp();
-    WindowSeg seg{&c, n, nx, j0, M, wx, wy};
+    WindowSeg seg{&c, n, nx, j0, M, wx, wy, wq};
     segment_pairs(c, seg, 0, m, true, true, q, wi, wu, lane);
   }
   wi = warp_sum(wi);
@@ -604,9 +604,7 @@ __global__ void k_links(const ChainDesc *desc, double *dpool, int *ipool, int ch
     const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
     const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
     c.Vl(i, j) = -0.5 * d.tau * (vext(d, ax, ay) + vext(d, bx, by));
-    float *f = c.xf + ((size_t)j * c.ldn + i) * d.dim;
-    f[0] = (float)ax;
-    if (d.dim > 1) f[1] = (float)ay;
+    c.xq[(size_t)j * c.ldn + i] = qpos(d, ax, ay);
   }
 }
 
@@ -616,9 +614,7 @@ __global__ void k_mirror(const ChainDesc *desc, double *dpool, int chain0) {
   CV c = make_cv(&d, dpool, nullptr, nullptr);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < d.N * d.M; k += gridDim.x * blockDim.x) {
     const int j = k / d.N, i = k % d.N;
-    float *f = c.xf + ((size_t)j * c.ldn + i) * d.dim;
-    f[0] = (float)c.X(0, i, j);
-    if (d.dim > 1) f[1] = (float)c.X(1, i, j);
+    c.xq[(size_t)j * c.ldn + i] = qpos(d, c.X(0, i, j), c.Xd(1, i, j));
   }
 }
 
@@ -682,10 +678,10 @@ __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
     if (d.flags & PF_PAIR) {
       const double rc2 = d.rc * d.rc, cg = d.inv2s2, h = 0.5 * tau;
       Prefilter f;
-      f.init(d, ax, ay, d.rc);
-      const float *row = c.xf + (size_t)j * c.ldn * dim;
+      f.init_q(c.Q(i, j), d.q_lim_rc);
+      const unsigned *row = c.xq + (size_t)j * c.ldn;
       for (int b = 0; b < N; ++b) {
-        if (b == i || !f.pass(row + (size_t)b * dim)) continue;
+        if (b == i || !f.pass(row[b])) continue;
         const double bxv = c.X(0, b, j), byv = c.Xd(1, b, j);
         const double d1x = mi_signed(ax, bxv, d.L), d1y = dim > 1 ? mi_signed(ay, byv, d.L) : 0.0;
         const double r2a = mi2(d, ax, ay, bxv, byv);
@@ -760,6 +756,11 @@ __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
 // ---------------------------------------------------------------------------
 
 // the exp table of exp_neg for the current device
+// scratch sizes of the device move routines, for the host's shared-memory plans
+size_t swap_scratch_bytes(int N) { return SwapScratch::bytes(N); }
+size_t com_scratch_bytes(int N, int M, int nwarps) { return ComScratch::bytes(N, M, nwarps); }
+int window_scratch_doubles() { return WARP_SCRATCH_D; }
+
 cudaError_t upload_exp_table() {
   static double tab[EXPTAB_N + 1];
   for (int k = 0; k <= EXPTAB_N; ++k) tab[k] = std::exp(-k / 64.0);

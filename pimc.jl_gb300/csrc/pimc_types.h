@@ -31,9 +31,14 @@ struct ChainDesc {
   double hcoef, V0, lat_k;
   double g, inv2s2, rc, hard_a, mu;
   double dens_bw;
+  double q_scale;       // 65536 / (2L): box coordinate -> 16-bit mirror units
+  float q_unit2;        // (2L / 65536)^2: squared mirror unit
+  unsigned q_lim_rc;    // mirror prefilter bound (squared units) for rc
+  unsigned q_lim_hard;  // the same for the hard-core radius
+  int pad2_;
   long long x_off;      // doubles: x[d][j][n] (slice-major) at dpool + x_off
   long long V_off;      // doubles: V[j][n]
-  long long xf_off;     // doubles: FP32 position mirror [j][n][d] (floats)
+  long long xq_off;     // doubles: 16-bit fixed-point mirror [j][n] (x | y << 16, u32)
   long long host_off;   // doubles: offset of the chain in a host-layout batch buffer
   long long tab_off;    // double2: bridge table (alpha, sigma)[m*wtab + t]
   long long next_off;   // ints: next[n]

@@ -307,6 +307,12 @@ def test_failure_paths():
         e.attempt_com(0, 1.0, [0.5])  # too few uniforms
     with pytest.raises(PimcError, match="window"):
         e.attempt_staging(0, 0, 10, np.zeros(20), [0.5])
+    # windows longer than the device's 64-slice limit are refused on the host
+    big = engine(dim=2, N=3, M=80, L=4.0, T=1.0, lam=0.5, harmonic_omega=1.0, seed=13)
+    with pytest.raises(PimcError, match="window"):
+        big.staging_weights(0, 0, 70, np.zeros(71 * 2))
+    with pytest.raises(PimcError, match="window"):
+        big.attempt_staging(0, 0, 70, np.zeros(69 * 2), [0.5])
     # the hard-core retry cap ends a move as a rejection, not a hang
     # (3 cells per dimension: the stencil sees every bead, all closer than a)
     h = engine(dim=2, N=3, M=8, L=1.0, T=1.0, lam=0.5, hardcore_a=5.0, r_a=0.6, retry_cap=50,
