@@ -215,6 +215,23 @@ int pimc_reset_measurements(void *handle);
 /* dSdr [dim][N][M] (optional), dSdtheta[3] = d/dV0, d/domega, d/dg,
  * extra[4] = S_ext, S_pair, virial energy (external + pair), sum r.dS/dr */
 int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double *extra);
+/* The same adjoint, same arguments and results, with no device allocation:
+ * its scratch is a static 3.2 MB device array instead of a buffer that
+ * pimc_adjoint grows with cudaMalloc.  No reference counterpart (PIMC.jl
+ * has no adjoint).  For callers that must not allocate device memory while
+ * they run: an optimisation loop whose host framework owns the GPU's memory
+ * through its own pool (CUDA.jl, a caching allocator) that a cudaMalloc
+ * behind its back would fragment or push past its limit, or a process
+ * already at the edge of device memory where a late cudaMalloc can fail in
+ * the middle of a run.
+ * Limit: chains of at most 65536 beads (N*M) and 8192 particles; larger
+ * chains return PIMC_EARG and must use pimc_adjoint.  The handle's device
+ * must be the current device.  The first call on a device looks up the
+ * array's address (set-up) and should come before any stream capture.  The
+ * array is shared by all handles of the process: calls that overlap in time
+ * (from several threads, on any handles of one device) race on it. */
+int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta,
+                         double *extra);
 /* change (V0, omega, g) in place; cached links are recomputed */
 int pimc_set_potential(void *handle, int chain, double V0, double omega, double g);
 

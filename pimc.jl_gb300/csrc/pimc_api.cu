@@ -83,6 +83,7 @@ struct Handle {
   Plan bat;                    // batched launch shape (tuned or set)
   Plan one;                    // plain per-chain launches: one CTA each
   int num_sms = 0;
+  int device = 0;              // the device current at creation
   int max_dyn_smem = 0;         // opt-in shared bytes per CTA, less static use
   cudaGraphExec_t gexec = nullptr;
   int force_warp = 0;
@@ -356,6 +357,7 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   };
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cleanup(fail(PIMC_ECUDA, "no CUDA device"));
+  h->device = dev;
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&h->max_dyn_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   h->max_dyn_smem -= 4096;  // the CTA kernel's static control block and reduction buffer
@@ -1144,6 +1146,68 @@ int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double
   int rc = sync_check(h);
   if (rc) return rc;
   // totals: S_ext, dV0, domega, S_pair, dg, pair virial, r.g_ext
+  if (dSdtheta) {
+    dSdtheta[0] = tot[1];
+    dSdtheta[1] = tot[2];
+    dSdtheta[2] = tot[4];
+  }
+  if (extra) {
+    const double Mt = d.M * d.tau;
+    extra[0] = tot[0];
+    extra[1] = tot[3];
+    extra[2] = (tot[0] + 0.5 * tot[6]) / Mt + (tot[3] + 0.5 * tot[5]) / Mt;
+    extra[3] = tot[8];
+  }
+  return PIMC_OK;
+}
+
+// the adjoint with its scratch in static device memory instead of a buffer
+// grown by cudaMalloc: for callers that must not allocate device memory
+// while they run (see pimc.h)
+int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta, double *extra) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  const ChainDesc &d = h->desc[chain];
+  const size_t nbd = (size_t)d.N * d.M;
+  const int nblocks = (int)((nbd + 255) / 256);
+  const size_t need = 4 * nbd + (size_t)d.N + 8 * (size_t)nblocks + 16 + (size_t)d.dim * nbd;
+  if (nbd > (size_t)kNoAllocBeads || d.N > kNoAllocParticles || need > kNoAllocDoubles)
+    return fail(PIMC_EARG, "pimc_adjoint_noalloc serves chains of at most " +
+                               std::to_string(kNoAllocBeads) + " beads (N*M) and " +
+                               std::to_string(kNoAllocParticles) + " particles; chain " +
+                               std::to_string(chain) + " has N*M = " + std::to_string(nbd) +
+                               " (use pimc_adjoint)");
+  int cur = -1;
+  CK(cudaGetDevice(&cur));
+  if (cur != h->device)
+    return fail(PIMC_EARG, "pimc_adjoint_noalloc: the handle's device (" +
+                               std::to_string(h->device) + ") is not the current device (" +
+                               std::to_string(cur) + ")");
+  double *base = nullptr;
+  CK(adjoint_static_scratch(&base));
+  AdjArgs a;
+  a.desc = h->d_desc;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.chain = chain;
+  a.omega = h->params[chain].harmonic_omega;
+  a.gA = base;
+  a.gB = a.gA + 2 * nbd;
+  a.part = a.gB + 2 * nbd;
+  a.nblocks = nblocks;
+  a.totals = a.part + 8 * (size_t)nblocks;
+  a.sum_rg = a.totals + 8;
+  a.dSdr = a.sum_rg + 8;
+  a.inv = (int *)(a.dSdr + (size_t)d.dim * nbd);
+  // the only accumulator the kernels do not overwrite
+  CK(cudaMemsetAsync(a.sum_rg, 0, sizeof(double), h->stream));
+  CK(launch_adjoint(a, (int)nbd, h->stream));
+  double tot[9];
+  CK(cudaMemcpyAsync(tot, a.totals, 8 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(tot + 8, a.sum_rg, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (dSdr) CK(cudaMemcpyAsync(dSdr, a.dSdr, sizeof(double) * d.dim * nbd, cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
   if (dSdtheta) {
     dSdtheta[0] = tot[1];
     dSdtheta[1] = tot[2];

@@ -90,6 +90,15 @@ cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, 
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);
 cudaError_t upload_exp_table();
+// static adjoint scratch: kNoAllocDoubles doubles, enough for a chain of
+// kNoAllocBeads beads (N*M) and kNoAllocParticles particles
+constexpr int kNoAllocBeads = 65536;
+constexpr int kNoAllocParticles = 8192;
+constexpr size_t kNoAllocDoubles = 6 * (size_t)kNoAllocBeads +
+                                   8 * (size_t)((kNoAllocBeads + 255) / 256) + 16 +
+                                   (size_t)kNoAllocParticles;
+// its device address on the current device (looked up on the first call)
+cudaError_t adjoint_static_scratch(double **ptr);
 // shared scratch of the device move routines (bytes; doubles for a window)
 size_t swap_scratch_bytes(int N);
 size_t com_scratch_bytes(int N, int M, int nwarps);

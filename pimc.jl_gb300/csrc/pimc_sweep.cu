@@ -833,6 +833,32 @@ cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, 
   k_measure<<<nchains, 256, 0, s>>>(desc, var, dpool, ipool, upool, chain0);
   return cudaGetLastError();
 }
+// ---------------------------------------------------------------------------
+// adjoint scratch in static device memory (pimc_adjoint_noalloc): room for a
+// chain of up to kNoAllocBeads beads and kNoAllocParticles particles in the
+// layout of the allocating adjoint (gA, gB, partials, totals, dS/dr, inverse
+// permutation), 3.2 MB per device
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) double g_adj_static[kNoAllocDoubles];
+
+cudaError_t adjoint_static_scratch(double **ptr) {
+  constexpr int kMaxDevices = 64;
+  static double *addr[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  if (!addr[dev]) {
+    // set-up, once per device, with that device current
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_adj_static);
+    if (e != cudaSuccess) return e;
+    addr[dev] = static_cast<double *>(p);
+  }
+  *ptr = addr[dev];
+  return cudaSuccess;
+}
+
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s) {
   const int nb = (nbeads + 255) / 256;
   k_inverse_next<<<4, 256, 0, s>>>(a);

@@ -148,6 +148,7 @@ SIGNATURES = {
     "pimc_get_density": [_vp, C.c_int, _dp, _ull],
     "pimc_reset_measurements": [_vp],
     "pimc_adjoint": [_vp, C.c_int, _dp, _dp, _dp],
+    "pimc_adjoint_noalloc": [_vp, C.c_int, _dp, _dp, _dp],
     "pimc_set_potential": [_vp, C.c_int, C.c_double, C.c_double, C.c_double],
     "pimc_get_stats": [_vp, C.c_int, C.POINTER(Stats)],
     "pimc_get_total_stats": [_vp, C.POINTER(Stats)],
