@@ -269,7 +269,7 @@ Plan plan_smem(const Handle *h, int mode, int block, int spl, int state_cap) {
   p.state_cap = state_cap;
   p.warp_scratch_d = window_scratch_doubles();
   if (mode == 1) {
-    size_t w = std::max(swap_scratch_bytes(h->maxN), (size_t)window_scratch_doubles() * sizeof(double));
+    size_t w = std::max(swap_scratch_bytes(h->maxN, 1), (size_t)window_scratch_doubles() * sizeof(double));
     w = std::max(w, com_scratch_bytes(h->maxN, h->maxM, 1));
     w = (w + 15) & ~(size_t)15;
     p.state_bytes = 0;
@@ -279,7 +279,7 @@ Plan plan_smem(const Handle *h, int mode, int block, int spl, int state_cap) {
     return p;
   }
   const int nw = block / 32;
-  size_t scratch = std::max(swap_scratch_bytes(h->maxN),
+  size_t scratch = std::max(swap_scratch_bytes(h->maxN, nw),
                             (size_t)nw * p.warp_scratch_d * sizeof(double));
   scratch = std::max(scratch, com_scratch_bytes(h->maxN, h->maxM, nw));
   scratch = (scratch + 15) & ~(size_t)15;
@@ -657,7 +657,7 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   a.prop = proposal ? dprop : nullptr;
   a.out = h->d_iout;
   a.force_warp = h->force_warp;
-  size_t smem = std::max(swap_scratch_bytes(d.N), (size_t)window_scratch_doubles() * 8);
+  size_t smem = std::max(swap_scratch_bytes(d.N, 1), (size_t)window_scratch_doubles() * 8);
   smem = std::max(smem, com_scratch_bytes(d.N, d.M, 4));
   CK(launch_attempt(a, smem, h->stream));
   int out[5] = {0, 0, 0, 0, 0};

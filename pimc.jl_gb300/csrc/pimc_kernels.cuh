@@ -26,6 +26,21 @@ __device__ __forceinline__ void block_sum_k(double (&v)[K], double *red) {
   __syncthreads();
 }
 
+template <int K>
+__device__ __forceinline__ void block_max_k(double (&v)[K], double *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_max(v[k]);
+  __syncthreads();
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) red[k * 32 + w] = v[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = warp_max(lane < nw ? red[k * 32 + lane] : -INFINITY);
+  __syncthreads();
+}
+
 __device__ __forceinline__ double logaddexp(double a, double b) {
   const double mx = fmax(a, b);
   if (mx == -INFINITY) return -INFINITY;
@@ -55,13 +70,15 @@ struct SwapScratch {
   double *w;                                   // N heat-bath weights
   double *r1x, *r1y, *r2x, *r2y, *vb1, *vb2;   // WMAX+1 each
   double *z;                                   // 4*WMAX normals
-  unsigned long long *q;                       // PQ_CAP neighbour queue
+  unsigned long long *q;                       // PQ_CAP neighbour queue per warp
   unsigned *q1, *q2;                           // WMAX+1 mirror words each
-  static __host__ __device__ size_t bytes(int N) {
-    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX + PQ_CAP) +
-           sizeof(unsigned) * 2 * (WMAX + 1);
+  int *iv;                                     // 4 ints: group broadcasts
+  static __host__ __device__ size_t bytes(int N, int nwarps) {
+    return sizeof(double) * ((size_t)N + 6 * (WMAX + 1) + 4 * WMAX) +
+           sizeof(unsigned long long) * PQ_CAP * (size_t)nwarps +
+           sizeof(unsigned) * 2 * (WMAX + 1) + sizeof(int) * 4;
   }
-  __device__ void carve(void *base, int N) {
+  __device__ void carve(void *base, int N, int nwarps) {
     double *p = (double *)base;
     w = p; p += N;
     r1x = p; p += WMAX + 1; r1y = p; p += WMAX + 1;
@@ -69,8 +86,9 @@ struct SwapScratch {
     vb1 = p; p += WMAX + 1; vb2 = p; p += WMAX + 1;
     z = p; p += 4 * WMAX;
     q = (unsigned long long *)p;
-    q1 = (unsigned *)(q + PQ_CAP);
+    q1 = (unsigned *)(q + (size_t)PQ_CAP * nwarps);
     q2 = q1 + (WMAX + 1);
+    iv = (int *)(q2 + (WMAX + 1));
   }
 };
 
@@ -159,6 +177,37 @@ struct ComSeg {
   __device__ __forceinline__ bool skip(int, int, int b) const { return idx[b] >= 0; }
 };
 
+// a warp (WARP) or the whole CTA working on one chain
+template <bool WARP>
+struct Group {
+  __device__ __forceinline__ static int rank() { return WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
+  __device__ __forceinline__ static int size() { return WARP ? 32 : (int)blockDim.x; }
+  __device__ __forceinline__ static void sync() {
+    if (WARP) __syncwarp(); else __syncthreads();
+  }
+  __device__ __forceinline__ static int any(int p) {
+    return WARP ? __any_sync(0xffffffffu, p) : __syncthreads_or(p);
+  }
+  template <int K>
+  __device__ __forceinline__ static void max(double (&v)[K], double *red) {
+    if (WARP) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = warp_max(v[k]);
+    } else {
+      block_max_k<K>(v, red);
+    }
+  }
+  template <int K>
+  __device__ __forceinline__ static void sum(double (&v)[K], double *red) {
+    if (WARP) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
+    } else {
+      block_sum_k<K>(v, red);
+    }
+  }
+};
+
 // heat-bath exponent -(|s - E|^2 + |x_i(j0) - f|^2) / (4 lambda m tau) with
 // E the end bead of particle i's path (or an explicit end): FP64 as the
 // reference (attempt parity), or FP32 from the position mirror (sweeps: the
@@ -211,15 +260,23 @@ struct HeatBath {
 };
 
 // ---------------------------------------------------------------------------
-// permutation swap, one warp: (u::ReshapeSwapLinear)(s) with the heat-bath
-// partner choice sampleparticles (src/updates/reshape.jl:123-283,
-// src/updates/helper.jl:224-267).  Returns RES_*; n2_out receives n2.
+// permutation swap: (u::ReshapeSwapLinear)(s) with the heat-bath partner
+// choice sampleparticles (src/updates/reshape.jl:123-283,
+// src/updates/helper.jl:224-267), by a warp (WARP) or a whole CTA.  Every
+// thread of the group calls it.  The group forms the heat-bath exponents and
+// splits the pair scans of the two moving paths by links; the partner
+// search, the bridges and the decision are the first warp's (thread 0 draws
+// the Metropolis uniform).  Returns RES_*; n2_out receives n2.
 // ---------------------------------------------------------------------------
-template <bool FAST, class D>
-__device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &dr,
-                         SwapScratch &S, double *prop, int *n2_out) {
+template <bool WARP, bool FAST, class D>
+__device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &dr,
+                          SwapScratch &S, double *red, double *prop, int *n2_out) {
+  using G = Group<WARP>;
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M, dim = c.dim, lane = threadIdx.x & 31;
+  const int tid = G::rank(), nt = G::size();
+  const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
+  const bool lead = warp == 0;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
   HeatBath<FAST> hb;
   hb.c = &c;
@@ -237,51 +294,58 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
   const double e1x = E1.x, e1y = E1.y;
   // weights exp(t_i + y_i) shifted by their maximum (the reference normalises
   // them, helper.jl:260-263; the shift keeps them from underflowing).  The
-  // exponents are formed lane-strided (coalesced reads of the slices); the
-  // sums and the cumulative search run over contiguous per-lane chunks so
-  // that the search order is the particle order
+  // group forms the exponents (coalesced reads of the two slices); the first
+  // warp sums them and searches the cumulative weights over contiguous
+  // per-lane chunks, so that the search order is the particle order
   const int chunk = (N + 31) / 32;
   const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
-  double wmax = -INFINITY;
-  for (int i = lane; i < N; i += 32) {
+  double wm[1] = {-INFINITY};
+  for (int i = tid; i < N; i += nt) {
     const double v = hb.expo(i, A, E1);
     S.w[i] = v;
-    wmax = fmax(wmax, v);
+    wm[0] = fmax(wm[0], v);
   }
-  wmax = warp_max(wmax);
-  __syncwarp();
-  double ls = 0.0;
-  for (int i = i0; i < i1; ++i) {
-    const double e = hb.ex_(S.w[i] - wmax);
-    S.w[i] = e;
-    ls += e;
+  G::template max<1>(wm, red);
+  G::sync();
+  const double wmax = wm[0];
+  double ssum = 0.0;
+  if (lead) {
+    double ls = 0.0;
+    for (int i = i0; i < i1; ++i) {
+      const double e = hb.ex_(S.w[i] - wmax);
+      S.w[i] = e;
+      ls += e;
+    }
+    ssum = warp_sum(ls);
+    const double inv_s = 1.0 / ssum;
+    double lq = 0.0;
+    for (int i = i0; i < i1; ++i) {
+      const double q = S.w[i] * inv_s;
+      S.w[i] = q;
+      lq += q;
+    }
+    const double target = u_pick * warp_sum(lq);
+    // first i with cumulative weight >= target (StatsBase.sample)
+    double cw = warp_exclusive_scan(lq);
+    int cand = 0x7fffffff;
+    for (int i = i0; i < i1; ++i) {
+      cw += S.w[i];
+      if (cw >= target) { cand = i; break; }
+    }
+    int n2 = warp_min_int(cand);
+    if (n2 >= N) n2 = N - 1;
+    if (lane == 0) S.iv[0] = n2;
   }
-  const double ssum = warp_sum(ls);
-  const double inv_s = 1.0 / ssum;
-  double lq = 0.0;
-  for (int i = i0; i < i1; ++i) {
-    const double q = S.w[i] * inv_s;
-    S.w[i] = q;
-    lq += q;
-  }
-  const double target = u_pick * warp_sum(lq);
-  // first i with cumulative weight >= target (StatsBase.sample)
-  double cw = warp_exclusive_scan(lq);
-  int cand = 0x7fffffff;
-  for (int i = i0; i < i1; ++i) {
-    cw += S.w[i];
-    if (cw >= target) { cand = i; break; }
-  }
-  int n2 = warp_min_int(cand);
-  if (n2 >= N) n2 = N - 1;
-  if (n2_out && lane == 0) *n2_out = n2;
+  G::sync();
+  const int n2 = S.iv[0];
+  if (n2_out && tid == 0) *n2_out = n2;
+  G::sync();
   if (n2 == n1) return RES_SKIP;
 
   double log_ratio = 0.0;
   if (d.flags & PF_PHYS) {
     // (1/S'_1 + 1/S'_2) / (1/S_1 + 1/S_2): S_a sums the heat-bath weights
     // with a chosen first; primes after the ends of n1 and n2 are exchanged
-    const double l1 = wmax + log(ssum);
     const HBead B = hb.bead(n2, j0);
     const HBead E2 = hb.bead(hb.endp(n2), se);
     // expo(i) with E(i) replaced by E'(i): the ends of n1 and n2 exchanged
@@ -290,19 +354,22 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
       return hb.expo(i, s_, f_, i == n1 ? &E2 : &E1);
     };
     double mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int i = lane; i < N; i += 32) {
+    for (int i = tid; i < N; i += nt) {
       mx[0] = fmax(mx[0], hb.expo(i, B, E2));
       mx[1] = fmax(mx[1], expo_p(i, A, E2));
       mx[2] = fmax(mx[2], expo_p(i, B, E1));
     }
-    for (int k = 0; k < 3; ++k) mx[k] = warp_max(mx[k]);
-    double s3[3] = {0.0, 0.0, 0.0};
-    for (int i = lane; i < N; i += 32) {
+    G::template max<3>(mx, red);
+    double s3[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int i = tid; i < N; i += nt) {
       s3[0] += hb.ex_(hb.expo(i, B, E2) - mx[0]);
       s3[1] += hb.ex_(expo_p(i, A, E2) - mx[1]);
       s3[2] += hb.ex_(expo_p(i, B, E1) - mx[2]);
     }
-    for (int k = 0; k < 3; ++k) s3[k] = warp_sum(s3[k]);
+    // the first warp's S_1 rides along in the fourth slot
+    s3[3] = (lead && lane == 0) ? ssum : 0.0;
+    G::template sum<4>(s3, red);
+    const double l1 = wmax + log(s3[3]);
     const double l2 = mx[0] + log(s3[0]);
     const double l1p = mx[1] + log(s3[1]);
     const double l2p = mx[2] + log(s3[2]);
@@ -323,17 +390,16 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
   if (fabs(s2x - f2x) > L) f2x += sgn(s2x) * (2.0 * L);
   if (dim > 1 && fabs(s2y - f2y) > L) f2y += sgn(s2y) * (2.0 * L);
   const bool hard = (d.flags & PF_HARD) != 0;
-  int fail = 0;
   if (!hard) {
-    for (int k = lane; k < 2 * (m - 1); k += 32) {
+    for (int k = tid; k < 2 * (m - 1); k += nt) {
       double zz[2];
       dr.bead_normals(k, dim, zz);
       S.z[2 * k] = zz[0];
       S.z[2 * k + 1] = dim > 1 ? zz[1] : 0.0;
     }
     dr.consumed(2 * (m - 1) * dim);
-    __syncwarp();
-    if (lane < 2 * dim) {
+    G::sync();
+    if (lead && lane < 2 * dim) {
       const int b = lane / dim, k = lane % dim;
       double p = b == 0 ? (k == 0 ? s1x : s1y) : (k == 0 ? s2x : s2y);
       const double e = b == 0 ? (k == 0 ? f1x : f1y) : (k == 0 ? f2x : f2y);
@@ -344,7 +410,9 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
         dst[t] = p;
       }
     }
-  } else {
+    if (tid == 0) S.iv[1] = 0;
+  } else if (lead) {
+    int fail = 0;
     for (int b = 0; b < 2 && !fail; ++b) {
       double px = b == 0 ? s1x : s2x, py = b == 0 ? s1y : s2y;
       const double ex = b == 0 ? f1x : f2x, ey = b == 0 ? f1y : f2y;
@@ -378,10 +446,11 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
         }
       }
     }
+    if (lane == 0) S.iv[1] = fail;
   }
-  __syncwarp();
-  if (fail) return RES_HARDCORE;
-  for (int k = lane; k < 2 * (m + 1); k += 32) {
+  G::sync();
+  if (S.iv[1]) return RES_HARDCORE;
+  for (int k = tid; k < 2 * (m + 1); k += nt) {
     const int b = k / (m + 1), t = k % (m + 1);
     double qx, qy;
     if (b == 0) {
@@ -398,89 +467,102 @@ __device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &d
     (b == 0 ? S.vb1 : S.vb2)[t] = vext(d, qx, qy);
     if (d.flags & PF_PAIR) (b == 0 ? S.q1 : S.q2)[t] = qpos(d, qx, qy);
   }
-  __syncwarp();
+  G::sync();
   const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
-  double wi = 0.0, wu = 0.0;
-  for (int k = lane; k < 2 * m; k += 32) {
+  double w2[2] = {0.0, 0.0};  // w_initial, w_update
+  for (int k = tid; k < 2 * m; k += nt) {
     const int b = k / m, t = k % m;
     const int j = slc(t), o = b == 0 ? own1(t) : own2(t);
-    wi += c.Vl(o, j);
-    wu += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
+    w2[0] += c.Vl(o, j);
+    w2[1] += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
   }
   if (any_pair) {
+    // the 2m links of the two moving paths in contiguous ranges per warp
+    const int per = (2 * m + nwarps - 1) / nwarps;
+    const int a0 = min(2 * m, warp * per), a1 = min(2 * m, a0 + per);
     for (int b = 0; b < 2; ++b) {
+      const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
+      if (t0 >= t1) continue;
       SwapSeg seg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
                   b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
       double wo = 0.0, wn = 0.0;
-      segment_pairs(c, seg, 0, m, true, true, S.q, wo, wn, lane);
+      segment_pairs(c, seg, t0, t1, true, true, S.q + (size_t)warp * PQ_CAP, wo, wn, lane);
       // the reference adds the new paths' pair terms to w_initial and lets
       // the old ones see the other moving path (reshape.jl:166-240)
-      wi += wo;
-      if (phys) wu += wn; else wi += wn;
+      w2[0] += wo;
+      if (phys) w2[1] += wn; else w2[0] += wn;
     }
     if (phys)
-      for (int t = lane; t < m; t += 32) {
+      for (int t = tid; t < m; t += nt) {
         // the pair of the two moving paths, old and new
         const int j = slc(t), jn = slc(t + 1);
         const int o1 = own1(t), o1n = own1(t + 1), o2 = own2(t), o2n = own2(t + 1);
         const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
         const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
         if (r2o <= d.rc * d.rc)
-          wi += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
+          w2[0] += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
         const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
         if (r2n <= d.rc * d.rc)
-          wu += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+          w2[1] += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
       }
   }
-  wi = warp_sum(wi);
-  wu = warp_sum(wu);
+  G::template sum<2>(w2, red);
   if (prop)
-    for (int k = lane; k < 2 * (m + 1); k += 32) {
+    for (int k = tid; k < 2 * (m + 1); k += nt) {
       const int b = k / (m + 1), t = k % (m + 1);
       prop[k * dim] = (b == 0 ? S.r1x : S.r2x)[t];
       if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
     }
-  int acc = 0;
-  if (lane == 0) {
-    const double delta = exp(wu - wi + log_ratio);
-    acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  if (tid == 0) {
+    const double delta = exp(w2[1] - w2[0] + log_ratio);
+    S.iv[2] = (delta >= 1.0) || (delta > dr.uniform_accept());
   }
-  acc = __shfl_sync(0xffffffffu, acc, 0);
+  G::sync();
+  const int acc = S.iv[2];
+  G::sync();
   if (!acc) return RES_REJECT;
   // accept: exchange next, write the bridges along the new cycles, exchange
   // the tails (reshape.jl:247-279)
   const int nn1 = nx2, nn2 = nx1;
   auto nown1 = [&](int t) { return (j0 + t < M) ? n1 : nn1; };
   auto nown2 = [&](int t) { return (j0 + t < M) ? n2 : nn2; };
-  if (lane == 0) {
-    c.next[n1] = nn1;
-    c.next[n2] = nn2;
-  }
-  for (int t = 1 + lane; t <= m; t += 32) {
+  for (int t = 1 + tid; t <= m; t += nt) {
     const int j = slc(t);
     c.set_pos(nown1(t), j, S.r1x[t], S.r1y[t]);
     c.set_pos(nown2(t), j, S.r2x[t], S.r2y[t]);
   }
-  for (int t = lane; t < m; t += 32) {
+  for (int t = tid; t < m; t += nt) {
     const int j = slc(t);
     c.Vl(nown1(t), j) = mhtau * (S.vb1[t] + S.vb1[t + 1]);
     c.Vl(nown2(t), j) = mhtau * (S.vb2[t] + S.vb2[t + 1]);
   }
   if (j0 + m < M - 1)
-    for (int j = se + 1 + lane; j < M; j += 32) {
+    for (int j = se + 1 + tid; j < M; j += nt) {
       c.exchange(n1, n2, j);
       const double v = c.Vl(n1, j);
       c.Vl(n1, j) = c.Vl(n2, j);
       c.Vl(n2, j) = v;
     }
-  if (phys && !wrap && lane == 0) {
-    // the link leaving the end bead moves with the tail
-    const double v = c.Vl(n1, se);
-    c.Vl(n1, se) = c.Vl(n2, se);
-    c.Vl(n2, se) = v;
+  G::sync();
+  if (tid == 0) {
+    c.next[n1] = nn1;
+    c.next[n2] = nn2;
+    if (phys && !wrap) {
+      // the link leaving the end bead moves with the tail
+      const double v = c.Vl(n1, se);
+      c.Vl(n1, se) = c.Vl(n2, se);
+      c.Vl(n2, se) = v;
+    }
   }
-  __syncwarp();
+  G::sync();
   return RES_ACCEPT;
+}
+
+// the swap by one warp (injected-draw attempts)
+template <bool FAST, class D>
+__device__ int swap_warp(const CV &c, int j0, int m, int n1, double u_pick, D &dr,
+                         SwapScratch &S, double *prop, int *n2_out) {
+  return swap_group<true, FAST>(c, j0, m, n1, u_pick, dr, S, nullptr, prop, n2_out);
 }
 
 // ---------------------------------------------------------------------------
@@ -543,26 +625,6 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
 // PQ_CAP-entry neighbour queue per warp.
 // ---------------------------------------------------------------------------
 // the threads that run a move: a whole CTA, or one warp on its own
-template <bool WARP>
-struct Group {
-  __device__ __forceinline__ static int rank() { return WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x; }
-  __device__ __forceinline__ static int size() { return WARP ? 32 : (int)blockDim.x; }
-  __device__ __forceinline__ static void sync() {
-    if (WARP) __syncwarp(); else __syncthreads();
-  }
-  __device__ __forceinline__ static int any(int p) {
-    return WARP ? __any_sync(0xffffffffu, p) : __syncthreads_or(p);
-  }
-  template <int K>
-  __device__ __forceinline__ static void sum(double (&v)[K], double *red) {
-    if (WARP) {
-#pragma unroll
-      for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
-    } else {
-      block_sum_k<K>(v, red);
-    }
-  }
-};
 
 template <bool WARP, class D>
 __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, const ComScratch &cs,

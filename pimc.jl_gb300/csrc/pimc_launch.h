@@ -100,7 +100,7 @@ constexpr size_t kNoAllocDoubles = 6 * (size_t)kNoAllocBeads +
 // its device address on the current device (looked up on the first call)
 cudaError_t adjoint_static_scratch(double **ptr);
 // shared scratch of the device move routines (bytes; doubles for a window)
-size_t swap_scratch_bytes(int N);
+size_t swap_scratch_bytes(int N, int nwarps);
 size_t com_scratch_bytes(int N, int M, int nwarps);
 int window_scratch_doubles();
 

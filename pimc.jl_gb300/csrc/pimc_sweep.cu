@@ -158,30 +158,28 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
     G::sync();
   }
 
-  // ---- permutation swaps (ReshapeSwapLinear), one at a time by warp 0
+  // ---- permutation swaps (ReshapeSwapLinear), one at a time by the group
   if (N > 1 && mix.swaps_per_sweep > 0) {
-    if (warp == 0) {
-      SwapScratch S;
-      S.carve(scratch, N);
-      const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
-      for (int a = 0; a < mix.swaps_per_sweep; ++a) {
-        const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
-        const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
-        const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
-        const int sm = max(2, sc.v.swap_m);
-        const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
-        const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
-        const double upick = u53(r1.z, r1.w);
-        GenDraws dr = gen_draws(ss);
-        const int r = swap_warp<true>(c, j0, m, n1, upick, dr, S, nullptr, nullptr);
-        if (lane == 0) {
-          if (r == RES_SKIP) {
-            tal[8] += 1.0;
-          } else {
-            tal[1] += 1.0;
-            tal[5] += r == RES_ACCEPT;
-            if (r != RES_HARDCORE) tal[9] += 2.0 * (m - 1);
-          }
+    SwapScratch S;
+    S.carve(scratch, N, nwarps);
+    const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
+    for (int a = 0; a < mix.swaps_per_sweep; ++a) {
+      const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
+      const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
+      const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
+      const int sm = max(2, sc.v.swap_m);
+      const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
+      const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
+      const double upick = u53(r1.z, r1.w);
+      GenDraws dr = gen_draws(ss);
+      const int r = swap_group<WARP, true>(c, j0, m, n1, upick, dr, S, red, nullptr, nullptr);
+      if (tid == 0) {
+        if (r == RES_SKIP) {
+          tal[8] += 1.0;
+        } else {
+          tal[1] += 1.0;
+          tal[5] += r == RES_ACCEPT;
+          if (r != RES_HARDCORE) tal[9] += 2.0 * (m - 1);
         }
       }
     }
@@ -418,7 +416,7 @@ __global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
   } else if (a.kind == MV_SWAP) {
     if (tid < 32) {
       SwapScratch S;
-      S.carve(smem, d.N);
+      S.carve(smem, d.N, 1);
       res = swap_warp<false>(c, a.j0, a.m, a.n, a.u_pick, dr, S, a.prop, &sc.iflag[4]);
     }
     __syncthreads();
@@ -757,7 +755,7 @@ __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
 
 // the exp table of exp_neg for the current device
 // scratch sizes of the device move routines, for the host's shared-memory plans
-size_t swap_scratch_bytes(int N) { return SwapScratch::bytes(N); }
+size_t swap_scratch_bytes(int N, int nwarps) { return SwapScratch::bytes(N, nwarps); }
 size_t com_scratch_bytes(int N, int M, int nwarps) { return ComScratch::bytes(N, M, nwarps); }
 int window_scratch_doubles() { return WARP_SCRATCH_D; }
 
