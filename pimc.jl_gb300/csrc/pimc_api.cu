@@ -499,6 +499,7 @@ SweepArgs sweep_args(Handle *h, const Plan &p) {
   a.state_bytes = p.state_bytes;
   a.warp_scratch_d = p.warp_scratch_d;
   a.warp_bytes = p.warp_bytes;
+  a.teams = 0;
   return a;
 }
 
@@ -508,6 +509,7 @@ int run_plain(Handle *h, long long n) {
   CK(sweep_set_smem(p.mode, p.dyn_smem));
   SweepArgs a = sweep_args(h, p);
   a.nchains = 1;
+  a.teams = 1;  // a lone chain is latency-bound: idle warps join its slots
   CK(cudaEventRecord(h->ev0, h->stream));
   long long launches = 0;
   for (long long s = 0; s < n; ++s)
@@ -536,6 +538,15 @@ int grid_for(Handle *h, const Plan &p) {
   return std::max(1, std::min(need, per_sm * h->num_sms));
 }
 
+// teams of warps pay off only when every chain of the launch is resident at
+// once (the launch is latency-bound); with more chains than resident CTAs
+// the idle warps' issue slots are used by other chains anyway
+bool launch_teams(Handle *h, const Plan &p) {
+  int per_sm = 0;
+  if (p.mode != 0 || sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm) != cudaSuccess) return false;
+  return h->nchains <= per_sm * h->num_sms;
+}
+
 int build_graph(Handle *h) {
   if (h->gexec) return PIMC_OK;
   const Plan &p = h->bat;
@@ -543,6 +554,7 @@ int build_graph(Handle *h) {
   a.order = h->d_order;
   a.queue = h->d_queue;
   a.sweeps = p.spl;
+  a.teams = launch_teams(h, p);
   const int grid = grid_for(h, p);
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -573,6 +585,7 @@ int run_batched(Handle *h, long long n) {
     a.order = h->d_order;
     a.queue = h->d_queue;
     a.sweeps = (int)rem;
+    a.teams = launch_teams(h, p);
     CK(cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream));
     CK(launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream));
     ++launches;

@@ -32,9 +32,11 @@ namespace pimc {
 constexpr int WMAX = 64;     // largest staging / swap window m handled on the device
 constexpr int TWMAX = 32;    // thread-per-window variant handles m <= TWMAX
 // doubles of per-warp scratch of window_warp: new beads x, y, their external
-// potential, normals (2 per bead), the neighbour queue (96 entries), and the
-// new beads' mirror words
-constexpr int WARP_SCRATCH_D = 5 * (WMAX + 1) + 96 + (WMAX + 2) / 2;
+// potential, normals (2 per bead), the neighbour queue (96 entries), the
+// new beads' mirror words, and 4 doubles through which the warps of a
+// staging team exchange their partial sums
+constexpr int TEAM_SLOT_D = 5 * (WMAX + 1) + 96 + (WMAX + 2) / 2;
+constexpr int WARP_SCRATCH_D = TEAM_SLOT_D + 4;
 
 // move outcomes (PIMC_REJECT / ACCEPT / SKIP / HARDCORE of pimc.h)
 constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
@@ -669,6 +671,130 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     }
   }
   __syncwarp();
+  return acc;
+}
+
+// ---------------------------------------------------------------------------
+// a staging window by a team of warps (pair action, no hard core): the warps
+// of the team split the window's links for the pair scans, each with its own
+// neighbour queue; the first warp draws the bridge and decides.  Warp w of
+// the team has the scratch tb + w * tstride (the first warp's holds the
+// window).  Every thread of the team calls it; the team synchronises on
+// named barrier `bar`.
+// ---------------------------------------------------------------------------
+constexpr int kMaxTeams = 7;  // named barriers 1..7 (barrier 0 is the CTA's)
+struct Team {
+  int w, nw, bar;  // warp in the team, warps in the team, barrier 1..kMaxTeams
+  __device__ __forceinline__ void sync() const {
+    // immediate barrier ids, so that a CTA reserves kMaxTeams + 1 barriers
+    // (not all 16), which keeps CTAs per SM from being limited by barriers
+    const int cnt = nw * 32;
+    switch (bar) {
+      case 1: asm volatile("bar.sync 1, %0;" ::"r"(cnt) : "memory"); break;
+      case 2: asm volatile("bar.sync 2, %0;" ::"r"(cnt) : "memory"); break;
+      case 3: asm volatile("bar.sync 3, %0;" ::"r"(cnt) : "memory"); break;
+      case 4: asm volatile("bar.sync 4, %0;" ::"r"(cnt) : "memory"); break;
+      case 5: asm volatile("bar.sync 5, %0;" ::"r"(cnt) : "memory"); break;
+      case 6: asm volatile("bar.sync 6, %0;" ::"r"(cnt) : "memory"); break;
+      default: asm volatile("bar.sync 7, %0;" ::"r"(cnt) : "memory"); break;
+    }
+  }
+};
+
+template <class D>
+__device__ int window_team(const CV &c, const Team &tm, int n, int j0, int m, D &dr, double *tb,
+                           int tstride) {
+  auto sb = [&](int w) { return tb + (size_t)w * tstride; };
+  const ChainDesc &d = *c.d;
+  const int lane = threadIdx.x & 31, tid = tm.w * 32 + lane, nt = tm.nw * 32;
+  const int M = c.M, dim = c.dim;
+  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  double *b0 = sb(0);
+  double *sx_ = b0, *sy_ = b0 + (WMAX + 1), *svb = b0 + 2 * (WMAX + 1);
+  double *sz = b0 + 3 * (WMAX + 1);
+  unsigned *sq = (unsigned *)(b0 + 5 * (WMAX + 1) + 96);
+  const int nx = c.next[n];
+  const int jend = j0 + m;
+  const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
+  const double sx = c.X(0, n, j0), sy = c.Xd(1, n, j0);
+  double ex = c.X(0, oe, je), ey = c.Xd(1, oe, je);
+  if (fabs(sx - ex) > L) ex += sgn(sx) * (2.0 * L);
+  if (dim > 1 && fabs(sy - ey) > L) ey += sgn(sy) * (2.0 * L);
+  for (int t = 1 + tid; t < m; t += nt) {
+    double z[2];
+    dr.bead_normals(t - 1, dim, z);
+    sz[2 * t] = z[0];
+    sz[2 * t + 1] = dim > 1 ? z[1] : 0.0;
+  }
+  tm.sync();
+  if (tm.w == 0 && lane < dim) {
+    double p = lane == 0 ? sx : sy;
+    const double e = lane == 0 ? ex : ey;
+    double *dst = lane == 0 ? sx_ : sy_;
+    for (int t = 1; t < m; ++t) {
+      const double2 ab = bridge_coef(c, m, t);
+      p = ab.x * p + (1.0 - ab.x) * e + sz[2 * t + lane] * ab.y;
+      dst[t] = p;
+    }
+  }
+  tm.sync();
+  for (int t = tid; t <= m; t += nt) {
+    double qx = t == 0 ? sx : (t == m ? ex : sx_[t]);
+    double qy = t == 0 ? sy : (t == m ? ey : sy_[t]);
+    qx = teleport(qx, L, inv2L);
+    if (dim > 1) qy = teleport(qy, L, inv2L);
+    sx_[t] = qx;
+    sy_[t] = qy;
+    svb[t] = vext(d, qx, qy);
+    sq[t] = qpos(d, qx, qy);
+  }
+  tm.sync();
+  double wi = 0.0, wu = 0.0;
+  for (int t = tid; t < m; t += nt) {
+    const int a = j0 + t;
+    wi += c.Vl(a < M ? n : nx, a < M ? a : a - M);
+    wu += mhtau * (svb[t] + svb[t + 1]);
+  }
+  {
+    const int per = (m + tm.nw - 1) / tm.nw;
+    const int t0 = min(m, tm.w * per), t1 = min(m, t0 + per);
+    if (t0 < t1) {
+      WindowSeg seg{&c, n, nx, j0, M, sx_, sy_, sq};
+      segment_pairs(c, seg, t0, t1, true, true, (unsigned long long *)(sb(tm.w) + 5 * (WMAX + 1)),
+                    wi, wu, lane);
+    }
+  }
+  wi = warp_sum(wi);
+  wu = warp_sum(wu);
+  double *slot = sb(tm.w) + TEAM_SLOT_D;
+  if (lane == 0) {
+    slot[0] = wi;
+    slot[1] = wu;
+  }
+  tm.sync();
+  double *lead = b0 + TEAM_SLOT_D;
+  if (tid == 0) {
+    double si = 0.0, su = 0.0;
+    for (int w = 0; w < tm.nw; ++w) {
+      si += sb(w)[TEAM_SLOT_D];
+      su += sb(w)[TEAM_SLOT_D + 1];
+    }
+    const double delta = exp(su - si);
+    lead[2] = (delta >= 1.0) || (delta > dr.uniform_accept()) ? 1.0 : 0.0;
+  }
+  tm.sync();
+  const int acc = lead[2] != 0.0;
+  if (acc) {
+    for (int t = 1 + tid; t < m; t += nt) {
+      const int a = j0 + t;
+      c.set_pos(a < M ? n : nx, a < M ? a : a - M, sx_[t], sy_[t]);
+    }
+    for (int t = tid; t < m; t += nt) {
+      const int a = j0 + t;
+      c.Vl(a < M ? n : nx, a < M ? a : a - M) = mhtau * (svb[t] + svb[t + 1]);
+    }
+  }
+  tm.sync();
   return acc;
 }
 

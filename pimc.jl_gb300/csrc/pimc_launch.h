@@ -23,6 +23,8 @@ struct SweepArgs {
   int state_bytes;    // shared bytes reserved for staging a chain's state
   int warp_scratch_d; // doubles of scratch per warp
   int warp_bytes;     // warp-per-chain mode: scratch bytes of each warp
+  int teams;          // 1: staging slots walked by teams of warps (latency-bound
+                      // launches whose chains all fit on the GPU at once)
 };
 
 struct AttemptArgs {

@@ -81,7 +81,7 @@ struct SmemCtl {
 // one sweep of one chain by a group: the whole CTA, or one warp on its own
 template <bool WARP>
 __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *scratch,
-                          int warp_scratch_d) {
+                          int warp_scratch_d, bool teams) {
   using G = Group<WARP>;
   const ChainDesc &d = sc.d;
   const MixDev &mix = sc.mix;
@@ -134,6 +134,27 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
             tal[9] += m - 1;
           }
         }
+      }
+    } else if (!WARP && teams && !(d.flags & PF_HARD) && 2 * k <= nwarps && k <= kMaxTeams) {
+      // fewer slots than warps: a team of T warps walks each slot, the
+      // warps splitting every window's links (named barrier 1 + team)
+      const int T = min(nwarps / k, 8), team = warp / T;
+      if (team < k) {
+        const Team tm{warp - team * T, T, 1 + team};
+        double *tb = (double *)scratch + (size_t)(team * T) * warp_scratch_d;
+        const int len = team < k - 1 ? ell : M - (k - 1) * ell;
+        const int st = (o + team * ell) % M;
+        if (len >= 2)
+          for (int n = 0; n < N; ++n) {
+            GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + team * N + n)));
+            const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
+            const int r = window_team(c, tm, n, st, m, dr, tb, warp_scratch_d);
+            if (tm.w == 0 && lane == 0) {
+              tal[0] += 1.0;
+              tal[4] += r == RES_ACCEPT;
+              tal[9] += m - 1;
+            }
+          }
       }
     } else {
       // windows of one slot interact through the pair action or the hard
@@ -315,7 +336,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
     ++iter;
     if (ci >= a.nchains) break;
     CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<true>(sc, nullptr, c, scratch, a.warp_scratch_d);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<true>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
     if (lane == 0) a.var[sc.chain] = sc.v;
     __syncwarp();
   }
@@ -366,7 +387,7 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
       __syncthreads();
     }
     unsigned char *scratch = smem + a.state_bytes;
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<false>(sc, red, c, scratch, a.warp_scratch_d);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<false>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
       unsigned *gq = (unsigned *)(a.dpool + d.xq_off);
