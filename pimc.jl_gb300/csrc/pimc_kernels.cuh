@@ -1,6 +1,8 @@
 // pimc_kernels.cuh -- warp/CTA-level moves (permutation swap, centre-of-mass
 // shifts) and the estimators.
 #pragma once
+#include <type_traits>
+
 #include "pimc_device.cuh"
 
 namespace pimc {
@@ -8,8 +10,9 @@ namespace pimc {
 // ---------------------------------------------------------------------------
 // block reductions (red: >= 256 doubles of shared memory; K <= 8)
 // ---------------------------------------------------------------------------
-template <int K>
-__device__ __forceinline__ void block_sum_k(double (&v)[K], double *red) {
+template <int K, class T>
+__device__ __forceinline__ void block_sum_k(T (&v)[K], double *red_) {
+  T *red = reinterpret_cast<T *>(red_);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
@@ -20,14 +23,15 @@ __device__ __forceinline__ void block_sum_k(double (&v)[K], double *red) {
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    double s = lane < nw ? red[k * 32 + lane] : 0.0;
+    T s = lane < nw ? red[k * 32 + lane] : T(0);
     v[k] = warp_sum(s);
   }
   __syncthreads();
 }
 
-template <int K>
-__device__ __forceinline__ void block_max_k(double (&v)[K], double *red) {
+template <int K, class T>
+__device__ __forceinline__ void block_max_k(T (&v)[K], double *red_) {
+  T *red = reinterpret_cast<T *>(red_);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
   for (int k = 0; k < K; ++k) v[k] = warp_max(v[k]);
@@ -37,7 +41,7 @@ __device__ __forceinline__ void block_max_k(double (&v)[K], double *red) {
     for (int k = 0; k < K; ++k) red[k * 32 + w] = v[k];
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < K; ++k) v[k] = warp_max(lane < nw ? red[k * 32 + lane] : -INFINITY);
+  for (int k = 0; k < K; ++k) v[k] = warp_max(lane < nw ? red[k * 32 + lane] : T(-INFINITY));
   __syncthreads();
 }
 
@@ -47,13 +51,14 @@ __device__ __forceinline__ double logaddexp(double a, double b) {
   return mx + log(exp(a - mx) + exp(b - mx));
 }
 
-// exclusive prefix over the warp of one double per lane
-__device__ __forceinline__ double warp_exclusive_scan(double v) {
+// exclusive prefix over the warp of one value per lane
+template <class T>
+__device__ __forceinline__ T warp_exclusive_scan(T v) {
   const int lane = threadIdx.x & 31;
-  double incl = v;
+  T incl = v;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const double t = __shfl_up_sync(0xffffffffu, incl, o);
+    const T t = __shfl_up_sync(0xffffffffu, incl, o);
     if (lane >= o) incl += t;
   }
   return incl - v;
@@ -188,8 +193,8 @@ struct Group {
   __device__ __forceinline__ static int any(int p) {
     return WARP ? __any_sync(0xffffffffu, p) : __syncthreads_or(p);
   }
-  template <int K>
-  __device__ __forceinline__ static void max(double (&v)[K], double *red) {
+  template <int K, class T>
+  __device__ __forceinline__ static void max(T (&v)[K], double *red) {
     if (WARP) {
 #pragma unroll
       for (int k = 0; k < K; ++k) v[k] = warp_max(v[k]);
@@ -197,8 +202,8 @@ struct Group {
       block_max_k<K>(v, red);
     }
   }
-  template <int K>
-  __device__ __forceinline__ static void sum(double (&v)[K], double *red) {
+  template <int K, class T>
+  __device__ __forceinline__ static void sum(T (&v)[K], double *red) {
     if (WARP) {
 #pragma unroll
       for (int k = 0; k < K; ++k) v[k] = warp_sum(v[k]);
@@ -222,6 +227,7 @@ struct HBead {
 
 template <bool FAST>
 struct HeatBath {
+  using W = typename std::conditional<FAST, float, double>::type;  // weight arithmetic
   const CV *c;
   double inv_den;
   float inv_denf;   // 1 / (4 lambda m tau) times the squared mirror unit
@@ -232,8 +238,8 @@ struct HeatBath {
     return {c->X(0, n, j), c->Xd(1, n, j), c->Q(n, j)};
   }
   // E = bead (endp(i), se) unless e is given
-  __device__ __forceinline__ double expo(int i, const HBead &s, const HBead &f,
-                                         const HBead *e = nullptr) const {
+  __device__ __forceinline__ W expo(int i, const HBead &s, const HBead &f,
+                                    const HBead *e = nullptr) const {
     const ChainDesc &d = *c->d;
     if (!FAST) {
       double ex, ey;
@@ -251,11 +257,12 @@ struct HeatBath {
     } else {
       const unsigned eq = e ? e->q : c->Q(endp(i), se);
       const float s2 = (float)qdist2(s.q, eq) + (float)qdist2(c->Q(i, j0), f.q);
-      return (double)(-s2 * inv_denf);
+      return (W)(-s2 * inv_denf);
     }
   }
-  __device__ __forceinline__ double ex_(double v) const {
-    return FAST ? (double)__expf((float)v) : exp(v);
+  __device__ __forceinline__ W ex_(W v) const {
+    if (FAST) return (W)__expf((float)v);
+    return (W)exp((double)v);
   }
 };
 
@@ -297,39 +304,44 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   // group forms the exponents (coalesced reads of the two slices); the first
   // warp sums them and searches the cumulative weights over contiguous
   // per-lane chunks, so that the search order is the particle order
+  // sweeps (FAST) weigh in FP32 from the position mirror: a deterministic
+  // function of the configuration used for both directions of the move;
+  // injected-draw attempts weigh in FP64 as the reference
+  using W = typename HeatBath<FAST>::W;
+  W *Sw = reinterpret_cast<W *>(S.w);
   const int chunk = (N + 31) / 32;
   const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
-  double wm[1] = {-INFINITY};
+  W wm[1] = {W(-INFINITY)};
   for (int i = tid; i < N; i += nt) {
-    const double v = hb.expo(i, A, E1);
-    S.w[i] = v;
-    wm[0] = fmax(wm[0], v);
+    const W v = hb.expo(i, A, E1);
+    Sw[i] = v;
+    wm[0] = v > wm[0] ? v : wm[0];
   }
   G::template max<1>(wm, red);
   G::sync();
-  const double wmax = wm[0];
-  double ssum = 0.0;
+  const W wmax = wm[0];
+  W ssum = W(0);
   if (lead) {
-    double ls = 0.0;
+    W ls = W(0);
     for (int i = i0; i < i1; ++i) {
-      const double e = hb.ex_(S.w[i] - wmax);
-      S.w[i] = e;
+      const W e = hb.ex_(Sw[i] - wmax);
+      Sw[i] = e;
       ls += e;
     }
     ssum = warp_sum(ls);
-    const double inv_s = 1.0 / ssum;
-    double lq = 0.0;
+    const W inv_s = W(1) / ssum;
+    W lq = W(0);
     for (int i = i0; i < i1; ++i) {
-      const double q = S.w[i] * inv_s;
-      S.w[i] = q;
+      const W q = Sw[i] * inv_s;
+      Sw[i] = q;
       lq += q;
     }
-    const double target = u_pick * warp_sum(lq);
+    const W target = (W)u_pick * warp_sum(lq);
     // first i with cumulative weight >= target (StatsBase.sample)
-    double cw = warp_exclusive_scan(lq);
+    W cw = warp_exclusive_scan(lq);
     int cand = 0x7fffffff;
     for (int i = i0; i < i1; ++i) {
-      cw += S.w[i];
+      cw += Sw[i];
       if (cw >= target) { cand = i; break; }
     }
     int n2 = warp_min_int(cand);
@@ -353,26 +365,27 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       if (i != n1 && i != n2) return hb.expo(i, s_, f_);
       return hb.expo(i, s_, f_, i == n1 ? &E2 : &E1);
     };
-    double mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    W mx[3] = {W(-INFINITY), W(-INFINITY), W(-INFINITY)};
     for (int i = tid; i < N; i += nt) {
-      mx[0] = fmax(mx[0], hb.expo(i, B, E2));
-      mx[1] = fmax(mx[1], expo_p(i, A, E2));
-      mx[2] = fmax(mx[2], expo_p(i, B, E1));
+      const W a0 = hb.expo(i, B, E2), a1 = expo_p(i, A, E2), a2 = expo_p(i, B, E1);
+      mx[0] = a0 > mx[0] ? a0 : mx[0];
+      mx[1] = a1 > mx[1] ? a1 : mx[1];
+      mx[2] = a2 > mx[2] ? a2 : mx[2];
     }
     G::template max<3>(mx, red);
-    double s3[4] = {0.0, 0.0, 0.0, 0.0};
+    W s3[4] = {W(0), W(0), W(0), W(0)};
     for (int i = tid; i < N; i += nt) {
       s3[0] += hb.ex_(hb.expo(i, B, E2) - mx[0]);
       s3[1] += hb.ex_(expo_p(i, A, E2) - mx[1]);
       s3[2] += hb.ex_(expo_p(i, B, E1) - mx[2]);
     }
     // the first warp's S_1 rides along in the fourth slot
-    s3[3] = (lead && lane == 0) ? ssum : 0.0;
+    s3[3] = (lead && lane == 0) ? ssum : W(0);
     G::template sum<4>(s3, red);
-    const double l1 = wmax + log(s3[3]);
-    const double l2 = mx[0] + log(s3[0]);
-    const double l1p = mx[1] + log(s3[1]);
-    const double l2p = mx[2] + log(s3[2]);
+    const double l1 = (double)wmax + log((double)s3[3]);
+    const double l2 = (double)mx[0] + log((double)s3[0]);
+    const double l1p = (double)mx[1] + log((double)s3[1]);
+    const double l2p = (double)mx[2] + log((double)s3[2]);
     log_ratio = logaddexp(-l1p, -l2p) - logaddexp(-l1, -l2);
   }
 
