@@ -3,10 +3,11 @@
 // window written once and shared by the sweep kernels and the injected-draw
 // attempt kernels.
 //
-// Layout: positions are slice-major on the device, x[d][j][n] (all particles
-// of one imaginary-time slice contiguous), cached links V[j][n].  Thread-per-
-// window staging reads slices of consecutive particles (coalesced), and a
-// neighbour query at slice j is a contiguous row.  Every chain keeps a
+// Layout: positions are slice-major on the device, x[j][n][d] (all particles
+// of one imaginary-time slice contiguous, a bead's coordinates in one 16-byte
+// unit, so that gathering a neighbour touches one sector), cached links
+// V[j][n].  Thread-per-window staging reads slices of consecutive particles
+// (coalesced), and a neighbour query at slice j is a contiguous row.  Every chain keeps a
 // 16-bit fixed-point mirror xq[j][n] of the positions (one 32-bit word per
 // bead): a warp scans the row with integer arithmetic and a bound that
 // covers the rounding, and evaluates the few candidates exactly in FP64, so
@@ -188,7 +189,7 @@ __device__ __forceinline__ unsigned qdist2(unsigned a, unsigned b) {
 // ---------------------------------------------------------------------------
 struct CV {
   const ChainDesc *d;
-  double *x;          // x[(k*M + j)*ldn + n]
+  double *x;          // x[(j*ldn + n)*dim + k]: a bead's coordinates in one 16-byte unit
   double *V;          // V[j*ldn + n]
   int *next;
   unsigned *xq;       // fixed-point mirror [j*ldn + n]
@@ -197,7 +198,7 @@ struct CV {
   double *eser;
   int N, M, dim, ldn;
   __device__ __forceinline__ double &X(int k, int n, int j) const {
-    return x[((size_t)k * M + j) * ldn + n];
+    return x[((size_t)j * ldn + n) * dim + k];
   }
   __device__ __forceinline__ double &Vl(int n, int j) const { return V[(size_t)j * ldn + n]; }
   __device__ __forceinline__ double Xd(int k, int n, int j) const {

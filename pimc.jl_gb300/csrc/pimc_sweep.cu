@@ -553,7 +553,7 @@ __global__ void k_eval_weights(EvalArgs a) {
 // state maintenance: layout transposes, init_world, cached links + mirror,
 // measurements
 // ---------------------------------------------------------------------------
-// host layout x[d][n][j] (a batch buffer at d.host_off) -> device x[d][j][n]
+// host layout x[d][n][j] (a batch buffer at d.host_off) -> device x[j][n][d]
 __global__ void k_import(const ChainDesc *desc, double *dpool, const double *src, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
   const size_t tot = (size_t)d.dim * d.N * d.M;
@@ -561,8 +561,9 @@ __global__ void k_import(const ChainDesc *desc, double *dpool, const double *src
   const double *s = src + d.host_off;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot;
        e += (size_t)gridDim.x * blockDim.x) {
-    const size_t k = e / ((size_t)d.M * d.N), r = e % ((size_t)d.M * d.N);
-    const size_t j = r / d.N, n = r % d.N;
+    const size_t row = (size_t)d.N * d.dim;
+    const size_t j = e / row, r = e % row;
+    const size_t n = r / d.dim, k = r % d.dim;
     x[e] = s[(k * d.N + n) * d.M + j];
   }
 }
@@ -576,7 +577,7 @@ __global__ void k_export(const ChainDesc *desc, const double *dpool, double *dst
        e += (size_t)gridDim.x * blockDim.x) {
     const size_t k = e / ((size_t)d.M * d.N), r = e % ((size_t)d.M * d.N);
     const size_t n = r / d.M, j = r % d.M;
-    o[e] = x[(k * d.M + j) * d.N + n];
+    o[e] = x[(j * d.N + n) * d.dim + k];
   }
 }
 

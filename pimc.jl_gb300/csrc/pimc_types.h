@@ -36,7 +36,7 @@ struct ChainDesc {
   unsigned q_lim_rc;    // mirror prefilter bound (squared units) for rc
   unsigned q_lim_hard;  // the same for the hard-core radius
   int pad2_;
-  long long x_off;      // doubles: x[d][j][n] (slice-major) at dpool + x_off
+  long long x_off;      // doubles: x[j][n][d] (slice-major) at dpool + x_off
   long long V_off;      // doubles: V[j][n]
   long long xq_off;     // doubles: 16-bit fixed-point mirror [j][n] (x | y << 16, u32)
   long long host_off;   // doubles: offset of the chain in a host-layout batch buffer
