@@ -44,6 +44,14 @@ SEED = 20261203
 
 # --------------------------------------------------------------------- workloads
 PLAIN_STRIDE = 16
+# per bead update of k_sweep on the first 1216 C4 chains (block 128, ncu
+# --set full), by acceptance semantics: DRAM bytes (dram__bytes_read.sum +
+# dram__bytes_write.sum) and FP64 flops (dadd + dmul + 2 dfma thread
+# instructions) over the launch's bead updates
+C4_PER_BEAD = {
+    "physical": {"dram_bytes": 1327.0, "fp64_flops": 2100.0},   # 24.82 GB, 39.3 G / 18.70 M
+    "reference": {"dram_bytes": 438.0, "fp64_flops": 473.0},    # 7.83 GB, 8.45 G / 17.87 M
+}
 
 
 def c4_chain_list(n=4096):
@@ -266,10 +274,12 @@ def run_reference(args):
     rates = []
     cores = os.cpu_count() or 1
     sample = ""
+    # each step a bounded sample; the whole run stays within a few minutes
+    budget = max(1.0, min(args.ref_budget, 120.0 / max(args.steps, 1)))
     for _ in range(args.warmup):
-        cpu_oracle_rate(chains, mixes, 0, budget_s=2.0)
+        cpu_oracle_rate(chains, mixes, 0, budget_s=1.0)
     for _ in range(args.steps):
-        r, cores, sample = cpu_oracle_rate(chains, mixes, 0, budget_s=args.ref_budget)
+        r, cores, sample = cpu_oracle_rate(chains, mixes, 0, budget_s=budget)
         rates.append(r)
     v = float(np.median(rates))
     line = {
@@ -355,18 +365,36 @@ def run_ours(args):
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     achieved = beads_per_launch * bytes_per_bead / launch_s / 1e9
+    # DRAM bytes per launch: the ncu capture of the same kernel on a subset of
+    # the workload, scaled by the bead updates a full launch performs
+    tpb = args.traffic_per_bead
+    if tpb is None and args.workload == "c4":
+        tpb = C4_PER_BEAD[args.semantics]["dram_bytes"]
+    traffic = beads_per_launch * tpb if tpb else None
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                       "frac": achieved / hbm, "traffic": args.traffic,
-                       "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+                       "frac": achieved / hbm, "traffic": traffic,
+                       "peak_source": ("MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
+                                       else "fallback 6.8 TB/s (of fallback)"),
                        "bytes_per_bead_update": bytes_per_bead,
-                       "note": "the sweep is FP64-pipe and latency bound (chain state is "
-                               "shared-memory/L2 resident within a sweep); see fp64 below"}
-    fp64_peak = args.fp64_peak
-    flops = beads_per_launch * args.fp64_flops_per_bead / launch_s / 1e12
+                       "traffic_source": ("ncu dram__bytes_read+write of k_sweep on the first 1216 "
+                                          "C4 chains, per bead update, times this launch's "
+                                          "bead updates" if tpb else None),
+                       "note": "not the binding roof: the sweep is FP64-pipe and latency bound, "
+                               "see roofline_fp64"}
+    fp64_peak = args.fp64_peak if args.fp64_peak else eng.fp64_peak()
+    fpb = args.fp64_flops_per_bead
+    measured_fpb = args.workload == "c4" and C4_PER_BEAD[args.semantics]["fp64_flops"]
+    if fpb is None:
+        fpb = C4_PER_BEAD[args.semantics]["fp64_flops"] if measured_fpb else 25.0
+    flops = beads_per_launch * fpb / launch_s / 1e12
     out["roofline_fp64"] = {"bound": "fp64", "achieved": flops, "peak": fp64_peak,
-                            "unit": "TFLOP/s", "frac": flops / fp64_peak if fp64_peak else None,
-                            "flops_per_bead_update": args.fp64_flops_per_bead,
-                            "peak_source": "own DFMA probe (profiles/fp64_peak.md)"}
+                            "unit": "TFLOP/s", "frac": flops / fp64_peak,
+                            "flops_per_bead_update": fpb,
+                            "flops_source": ("ncu dadd+dmul+2*dfma thread instructions of k_sweep on "
+                                             "the first 1216 C4 chains, per bead update"
+                                             if measured_fpb and args.fp64_flops_per_bead is None
+                                             else "algorithmic estimate (no pair terms)"),
+                            "peak_source": "pimc_fp64_peak: DFMA throughput probe on this GPU (measured)"}
     out["clocks"] = clk.summary()
     # plain path: one launch per chain per sweep (no queue, no graph), timed
     # on every PLAIN_STRIDE-th chain of the workload so that it stays short
@@ -433,7 +461,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4", "c5"])
-    ap.add_argument("--semantics", default="physical", choices=["physical", "reference"])
+    # the library's default (the drop-in keeps the reference's acceptance
+    # rules); "physical" adds the pair action to every move
+    ap.add_argument("--semantics", default="reference", choices=["physical", "reference"])
     ap.add_argument("--tune", type=int, default=1)
     ap.add_argument("--chains", type=int, default=0,
                     help="keep only the first K chains of the workload (small profiling cases)")
@@ -446,10 +476,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=12.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
-    ap.add_argument("--traffic", type=float, default=None,
-                    help="DRAM bytes per sweep-kernel launch from an ncu capture")
-    ap.add_argument("--fp64-peak", type=float, default=None, help="TFLOP/s")
-    ap.add_argument("--fp64-flops-per-bead", type=float, default=25.0)
+    ap.add_argument("--traffic-per-bead", type=float, default=None,
+                    help="DRAM bytes per bead update of the sweep kernel (ncu)")
+    ap.add_argument("--fp64-peak", type=float, default=None, help="TFLOP/s (default: measured)")
+    ap.add_argument("--fp64-flops-per-bead", type=float, default=None)
     args = ap.parse_args()
     if args.steps < 1 or args.warmup < 0:
         raise SystemExit("steps >= 1 and warmup >= 0")

@@ -245,6 +245,11 @@ int pimc_get_total_stats(void *handle, pimc_stats *out);
 int pimc_state_size(void *handle, size_t *bytes);
 int pimc_get_state(void *handle, void *buf, size_t bytes);
 int pimc_set_state(void *handle, const void *buf, size_t bytes);
+/* measurement utility, no reference counterpart: FP64 fused multiply-add
+ * throughput of the handle's device in TFLOP/s (eight independent DFMA
+ * chains per thread over the whole GPU, best of three timed launches) --
+ * the denominator of the sweep's FP64 roofline */
+int pimc_fp64_peak(void *handle, double *tflops);
 /* device time of the last run call (CUDA events on the handle's stream) */
 int pimc_last_run_ms(void *handle, double *ms);
 /* kernel launches issued by the last run call */

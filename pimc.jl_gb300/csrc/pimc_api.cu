@@ -1236,6 +1236,13 @@ int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta
   return PIMC_OK;
 }
 
+int pimc_fp64_peak(void *handle, double *tflops) {
+  Handle *h = H(handle);
+  if (!h || !tflops) return fail(PIMC_EARG, "null argument");
+  CK(fp64_peak(h->num_sms, h->stream, tflops));
+  return PIMC_OK;
+}
+
 int pimc_set_potential(void *handle, int chain, double V0, double omega, double g) {
   Handle *h = H(handle);
   if (check_chain(h, chain)) return PIMC_EARG;

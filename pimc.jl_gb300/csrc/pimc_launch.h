@@ -101,6 +101,8 @@ constexpr size_t kNoAllocDoubles = 6 * (size_t)kNoAllocBeads +
                                    (size_t)kNoAllocParticles;
 // its device address on the current device (looked up on the first call)
 cudaError_t adjoint_static_scratch(double **ptr);
+// measured FP64 FMA throughput of the current device (TFLOP/s)
+cudaError_t fp64_peak(int num_sms, cudaStream_t st, double *tflops);
 // shared scratch of the device move routines (bytes; doubles for a window)
 size_t swap_scratch_bytes(int N, int nwarps);
 size_t com_scratch_bytes(int N, int M, int nwarps);

@@ -854,6 +854,53 @@ cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, 
   return cudaGetLastError();
 }
 // ---------------------------------------------------------------------------
+// FP64 pipe throughput probe: eight independent DFMA chains per thread
+// ---------------------------------------------------------------------------
+static __device__ double g_fp64_sink[256];
+
+__global__ void __launch_bounds__(256) k_fp64_peak(int iters, double b, double c) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * k + 1e-9 * threadIdx.x;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == -1.0) g_fp64_sink[threadIdx.x] = s;  // never true; keeps the chains live
+}
+
+cudaError_t fp64_peak(int num_sms, cudaStream_t st, double *tflops) {
+  const int iters = 1 << 14, blocks = num_sms * 8, threads = 256;
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e != cudaSuccess) return e;
+  e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return e;
+  }
+  float best = 1e30f;
+  for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, st);
+    k_fp64_peak<<<blocks, threads, 0, st>>>(iters, 0.9999999, 1e-7);
+    cudaEventRecord(e1, st);
+    e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess && rep > 0 && ms < best) best = ms;  // rep 0 warms up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return e;
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
 // adjoint scratch in static device memory (pimc_adjoint_noalloc): room for a
 // chain of up to kNoAllocBeads beads and kNoAllocParticles particles in the
 // layout of the allocating adjoint (gA, gB, partials, totals, dS/dr, inverse

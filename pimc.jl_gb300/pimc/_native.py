@@ -155,6 +155,7 @@ SIGNATURES = {
     "pimc_state_size": [_vp, C.POINTER(C.c_size_t)],
     "pimc_get_state": [_vp, C.c_void_p, C.c_size_t],
     "pimc_set_state": [_vp, C.c_void_p, C.c_size_t],
+    "pimc_fp64_peak": [_vp, _dp],
     "pimc_last_run_ms": [_vp, _dp],
     "pimc_last_run_launches": [_vp, C.POINTER(C.c_longlong)],
     "pimc_set_option": [_vp, C.c_int, C.c_longlong],

@@ -233,6 +233,12 @@ class Engine:
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes}
 
+    def fp64_peak(self) -> float:
+        """measured FP64 FMA throughput of the device, TFLOP/s"""
+        v = C.c_double()
+        check(self.L.pimc_fp64_peak(self.h, C.byref(v)))
+        return v.value
+
     def last_run_ms(self) -> float:
         v = C.c_double()
         check(self.L.pimc_last_run_ms(self.h, C.byref(v)))
