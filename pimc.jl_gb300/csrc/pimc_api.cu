@@ -130,6 +130,9 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   if (d.nbins < 1) d.nbins = 1;
   d.rc = 2.0 * p.L / d.nbins;
   d.ncell = p.dim == 2 ? d.nbins * d.nbins : d.nbins;
+  d.L2 = 2.0 * d.L;
+  d.rc2 = d.rc * d.rc;
+  d.mhtau_g = -0.5 * d.tau * d.g;
   // 16-bit fixed-point mirror of the positions on the periodic box: a pair
   // within R of each other has mirror coordinates within R/u + 1 (u the unit)
   // per axis; the bound adds 4 units so that a shifted mirror centre (one
@@ -1256,6 +1259,7 @@ int pimc_set_potential(void *handle, int chain, double V0, double omega, double 
   d.lat_k = V0 != 0.0 ? 1.0 / p.lattice_a : 0.0;
   d.hcoef = 0.5 * omega * omega;
   d.g = g;
+  d.mhtau_g = -0.5 * d.tau * d.g;
   d.flags &= ~(PF_LATT | PF_HARM);
   if (V0 != 0.0) d.flags |= PF_LATT;
   if (omega != 0.0) d.flags |= PF_HARM;

@@ -238,7 +238,10 @@ __device__ __forceinline__ double dist1(double a, double b, double L) {
 // The quotient is formed by a multiplication; when it lands within 1e-9 of an
 // integer the IEEE division of the reference is used instead, so the floor is
 // always the reference's.
+// Inside the box the floor is 0 and the result is (x + L) - L, the same bits
+// as the full expression; that path skips the floor and its guard.
 __device__ __forceinline__ double teleport(double x, double L, double inv2L) {
+  if (fabs(x) < 0.999999 * L) return (x + L) - L;
   const double q = x * inv2L + 0.5;
   double f = floor(q);
   const double fr = q - f;
@@ -315,13 +318,22 @@ __device__ __forceinline__ double2 bridge_coef(const CV &c, int m, int t) {
   return make_double2(a, sqrt(2.0 * c.d->lambda * a * c.d->tau));
 }
 
+// minimum-image difference a - b: the same magnitude as dist1 (|a-b| when it
+// is at most L, else 2L - |a-b|, both exactly rounded), with one subtraction
+// and a rarely taken wrap
+__device__ __forceinline__ double mi1(double a, double b, double L, double L2) {
+  double dx = a - b;
+  if (fabs(dx) > L) dx -= copysign(L2, dx);
+  return dx;
+}
+
 __device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, double bx,
                                       double by) {
-  const double dx = dist1(ax, bx, d.L);
+  const double dx = mi1(ax, bx, d.L, d.L2);
   double s = dx * dx;
   if (d.dim > 1) {
-    const double dy = dist1(ay, by, d.L);
-    s += dy * dy;
+    const double dy = mi1(ay, by, d.L, d.L2);
+    s = fma(dy, dy, s);
   }
   return s;
 }
@@ -361,9 +373,12 @@ struct Prefilter {
 // ---------------------------------------------------------------------------
 constexpr int PQ_CAP = 96;  // queue entries per warp (64-bit)
 
+// one queued entry: the link's two pair exponentials exp(-r^2/2s^2) at its
+// ends, added to the lane's old (so) or new (sn) sum; the caller applies the
+// link weight -tau g / 2 once per segment
 template <class Seg>
 __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long long e,
-                                        double &wo, double &wn) {
+                                        double &so, double &sn) {
   const ChainDesc &d = *c.d;
   const int M = c.M;
   const int b = (int)(e >> 32), t = (int)((e >> 1) & 0x7fffffffu), side = (int)(e & 1u);
@@ -371,11 +386,12 @@ __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long
   double ax, ay, anx, any;
   s.cur(side, t, ax, ay);
   const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
-  if (r2a > d.rc * d.rc) return;
+  if (r2a > d.rc2) return;
   s.nxt(side, t, anx, any);
   const int bn = j == M - 1 ? c.next[b] : b;
-  const double w = lnU2(d, r2a, mi2(d, anx, any, c.X(0, bn, jn), c.Xd(1, bn, jn)));
-  if (side) wn += w; else wo += w;
+  const double r2b = mi2(d, anx, any, c.X(0, bn, jn), c.Xd(1, bn, jn));
+  const double v = exp_neg(-r2a * d.inv2s2) + exp_neg(-r2b * d.inv2s2);
+  if (side) sn += v; else so += v;
 }
 
 // evaluate the first min(qn, 32) queued entries and move the rest up
@@ -398,9 +414,10 @@ __device__ __forceinline__ void pq_flush(const CV &c, const Seg &s, unsigned lon
   qn = nr;
 }
 
+// the lane's sums of the links' pair exponentials, old and new configuration
 template <class Seg>
-__device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
-                              unsigned long long *q, double &wo, double &wn, int lane) {
+__device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
+                             unsigned long long *q, double &wo, double &wn, int lane) {
   const ChainDesc &d = *c.d;
   const int N = c.N, dim = c.dim;
   const unsigned lt = (1u << lane) - 1u;
@@ -430,6 +447,17 @@ __device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do
     }
   }
   while (qn > 0) pq_flush(c, s, q, qn, wo, wn, lane);
+}
+
+// adds the links' pair terms -tau/2 (v(r_a) + v(r_b)) of the old (wo) and the
+// new (wn) configuration; every lane of the warp calls it
+template <class Seg>
+__device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
+                              unsigned long long *q, double &wo, double &wn, int lane) {
+  double so = 0.0, sn = 0.0;
+  segment_sums(c, s, t0, t1, do_old, do_new, q, so, sn, lane);
+  wo = fma(c.d->mhtau_g, so, wo);
+  wn = fma(c.d->mhtau_g, sn, wn);
 }
 
 // a staging window: bead t at absolute slice j0+t of particle n (next(n)

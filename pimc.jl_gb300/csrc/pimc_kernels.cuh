@@ -489,7 +489,19 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     w2[0] += c.Vl(o, j);
     w2[1] += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
   }
-  if (any_pair) {
+  // Under the reference's rules every pair term (-tau/2 g (..) <= 0 for
+  // g >= 0) enters w_initial, so it can only raise w_update - w_initial: when
+  // the pair-free part already accepts, the pair sums cannot change the
+  // decision and a sweep skips them (its Metropolis uniform is a pure function
+  // of the move's stream).  Injected-draw attempts always evaluate them.
+  bool pairs = any_pair;
+  if (FAST && any_pair && !phys && d.g >= 0.0) {
+    double c2[2] = {w2[0], w2[1]};
+    G::template sum<2>(c2, red);
+    const double delta = exp(c2[1] - c2[0] + log_ratio);
+    if (delta >= 1.0 || delta > dr.uniform_accept()) pairs = false;
+  }
+  if (pairs) {
     // the 2m links of the two moving paths in contiguous ranges per warp
     const int per = (2 * m + nwarps - 1) / nwarps;
     const int a0 = min(2 * m, warp * per), a1 = min(2 * m, a0 + per);

@@ -31,6 +31,9 @@ struct ChainDesc {
   double hcoef, V0, lat_k;
   double g, inv2s2, rc, hard_a, mu;
   double dens_bw;
+  double L2;            // 2L
+  double rc2;           // rc^2
+  double mhtau_g;       // -tau g / 2: weight of a link's pair exponentials
   double q_scale;       // 65536 / (2L): box coordinate -> 16-bit mirror units
   float q_unit2;        // (2L / 65536)^2: squared mirror unit
   unsigned q_lim_rc;    // mirror prefilter bound (squared units) for rc
