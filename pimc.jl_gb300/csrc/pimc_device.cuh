@@ -62,15 +62,22 @@ __device__ __forceinline__ double u53(unsigned a, unsigned b) {
   return (double)x * 0x1.0p-53;
 }
 
-// Box-Muller pair in FP64 (CUDA's log / sincospi / sqrt as library calls)
+// Box-Muller pair from two 53-bit uniforms.  The transcendental functions
+// run in FP32 (CUDA's logf / sincospif / sqrtf as library calls): the FP64
+// pipe of this part issues 2 lanes per SM clock, and a normal's relative
+// error of about 1e-7 distorts the sampled Gaussian far below any Monte Carlo
+// error.  u1 keeps its 53-bit range (as a float, exponent intact), so the
+// tails reach 8.6 sigma.  Injected-draw attempts take their normals as given.
 __device__ __forceinline__ void normal2(uint4 r, double &z0, double &z1) {
-  const double u1 = 1.0 - u53(r.x, r.y);  // (0, 1]
-  const double u2 = u53(r.z, r.w);
-  const double rad = sqrt(-2.0 * log(u1));
-  double s, c;
-  sincospi(2.0 * u2, &s, &c);
-  z0 = rad * c;
-  z1 = rad * s;
+  const unsigned long long x1 = ((((unsigned long long)r.x) << 32) | r.y) >> 11;
+  const unsigned long long x2 = ((((unsigned long long)r.z) << 32) | r.w) >> 11;
+  const float u1 = __ull2float_rn((1ull << 53) - x1) * 0x1.0p-53f;  // (0, 1]
+  const float u2 = __ull2float_rn(x2) * 0x1.0p-53f;                 // [0, 1]
+  const float rad = sqrtf(-2.f * logf(u1));
+  float s, c;
+  sincospif(2.f * u2, &s, &c);
+  z0 = (double)(rad * c);
+  z1 = (double)(rad * s);
 }
 
 struct Stream {
