@@ -147,6 +147,12 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
     };
     d.q_lim_rc = lim(d.rc);
     d.q_lim_hard = lim(p.hardcore_a);
+    // a mirror distance differs from the exact one by at most 3 units: two
+    // roundings per axis, plus one more for a shifted centre (cycle moves)
+    const double rq = d.rc / u, e = 3.0;
+    d.q_u2i = (float)(u * u * d.inv2s2);
+    d.q_lim_lo = rq > e ? (unsigned)std::floor((rq - e) * (rq - e)) : 0u;
+    d.q_lim_hi = (unsigned)std::min(std::ceil((rq + e) * (rq + e)), (double)d.q_lim_rc);
   }
   d.hard_a = p.hardcore_a;
   d.ctr = p.retry_cap > 0 ? p.retry_cap : 10000;

@@ -111,6 +111,7 @@ constexpr unsigned DRAW_ACCEPT = 0xC0000000u;  // Metropolis uniform
 // Generator-backed draws for one move.  bead_normals(k) is a pure function of
 // the bead index so lanes may evaluate beads in parallel.
 struct GenDraws {
+  static constexpr bool kSweep = true;  // counter-based: decisions may use bounded estimates
   Stream s;
   unsigned seq;
   int have;
@@ -146,6 +147,7 @@ __device__ __forceinline__ GenDraws gen_draws(const Stream &s) {
 // Injected draws (parity level b): normals bead-major, d per bead, in the
 // order the reference draws them; uniforms consumed sequentially.
 struct InjDraws {
+  static constexpr bool kSweep = false;  // injected draws: exact decisions only
   const double *nrm;
   int n_nrm, pn;
   const double *uni;
@@ -467,6 +469,111 @@ __device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do
   wn = fma(c.d->mhtau_g, sn, wn);
 }
 
+// ---------------------------------------------------------------------------
+// bounded estimate of a segment's pair sums, from the mirror alone.  For
+// every link it gives the lane's sum of exp(-r_a^2/2s^2) + exp(-r_b^2/2s^2)
+// over the neighbours within rc, old (so) and new (sn) configuration, and a
+// bound (bo, bn) on its distance from the exact FP64 sum: a mirror distance
+// is within kQErr units of the exact one, __expf is within (3 + 1.2 y) ulp
+// (CUDA's documented 2 + floor(1.16 |y|)), and a pair whose mirror distance
+// cannot settle the cut-off contributes the midpoint of [0, its value].
+// Only the decision of a move is taken from it, and only when the whole
+// interval lies on one side of the Metropolis threshold.
+// ---------------------------------------------------------------------------
+constexpr float kQErr = 3.f;
+
+struct PairEst {
+  float so, bo, sn, bn;  // sums and bounds, old and new configuration
+  int ko, kn;            // terms added (for the FP32 accumulation error)
+};
+
+// squared mirror distance, and whether an axis lies within 4 units of the
+// half box, where the exact minimum image may fold the other way
+__device__ __forceinline__ unsigned qdist2_w(unsigned a, unsigned b, bool &edge) {
+  const unsigned dd = __vsub2(a, b);
+  const int dx = ((int)(dd << 16)) >> 16, dy = ((int)dd) >> 16;
+  edge = abs(dx) > 32763 || abs(dy) > 32763;
+  return (unsigned)(dx * dx) + (unsigned)(dy * dy);
+}
+
+__device__ __forceinline__ void est_term(const ChainDesc &d, unsigned d2a, unsigned d2b, bool edge_b,
+                                         float &sum, float &bnd, int &k) {
+  const float ya = (float)d2a * d.q_u2i, yb = (float)d2b * d.q_u2i;
+  const float ea = __expf(-ya), eb = __expf(-yb);
+  // relative error of each exponential: argument error from the mirror plus
+  // the fast exponential's own
+  const float da = 1.01f * d.q_u2i * kQErr * (2.f * sqrtf((float)d2a) + kQErr) +
+                   (3.f + 1.2f * ya) * 1.2e-7f;
+  const float db = 1.01f * d.q_u2i * kQErr * (2.f * sqrtf((float)d2b) + kQErr) +
+                   (3.f + 1.2f * yb) * 1.2e-7f;
+  // an end next to the half box: anything in [0, 1]
+  const float vb = edge_b ? 0.5f : eb, eb_err = edge_b ? 0.5f : eb * db;
+  const float v = ea + vb, err = ea * da + eb_err + 2e-30f;
+  if (d2a < d.q_lim_lo) {
+    sum += v;
+    bnd += err;
+  } else {
+    // the exact cut-off may keep or drop the link: [0, v + err]
+    sum += 0.5f * v;
+    bnd += 0.5f * v + err;
+  }
+  ++k;
+}
+
+template <class Seg>
+__device__ void segment_estimate(const CV &c, const Seg &s, int t0, int t1, PairEst &e, int lane) {
+  const ChainDesc &d = *c.d;
+  const int N = c.N, M = c.M;
+  for (int t = t0; t < t1; ++t) {
+    const int j = s.slice(t), jn = j + 1 == M ? 0 : j + 1;
+    const bool wrap = j == M - 1;
+    const unsigned co = s.curq(0, t), cn = s.curq(1, t);
+    const unsigned no = s.nxtq(0, t), nn = s.nxtq(1, t);
+    const unsigned *row = c.xq + (size_t)j * c.ldn, *rown = c.xq + (size_t)jn * c.ldn;
+    for (int b = lane; b < N; b += 32) {
+      const unsigned pb = row[b];
+      const unsigned d2o = qdist2(co, pb), d2n = qdist2(cn, pb);
+      const bool io = d2o <= d.q_lim_hi && !s.skip(0, t, b);
+      const bool in = d2n <= d.q_lim_hi && !s.skip(1, t, b);
+      if (io || in) {
+        const unsigned pbn = rown[wrap ? c.next[b] : b];
+        bool edge;
+        if (io) {
+          const unsigned d2b = qdist2_w(no, pbn, edge);
+          est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
+        }
+        if (in) {
+          const unsigned d2b = qdist2_w(nn, pbn, edge);
+          est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
+        }
+      }
+    }
+  }
+}
+
+// a lane's estimates in FP64, with the error of its FP32 accumulation (two
+// ulp per addition of non-negative terms, on the sum and on the bound) added
+// to the bounds; the caller sums them over the group
+__device__ __forceinline__ void est_reduce_lanes(const PairEst &e, double (&v)[4]) {
+  const double ro = 2.4e-7 * (e.ko + 1), rn = 2.4e-7 * (e.kn + 1);
+  v[0] = (double)e.so;
+  v[1] = (double)e.bo * (1.0 + ro) + ro * (double)e.so + 1e-30;
+  v[2] = (double)e.sn;
+  v[3] = (double)e.bn * (1.0 + rn) + rn * (double)e.sn + 1e-30;
+}
+
+// the Metropolis decision from an interval [lo, hi] of the log acceptance
+// ratio, for a threshold log(u): 1 accept, 0 reject, -1 undecided.  The
+// margin covers the rounding of the exact path's own sum and exponential.
+__device__ __forceinline__ int decide_interval(double lo, double hi, double u) {
+  if (u <= 0.0) return lo > -INFINITY ? 1 : -1;
+  const double lu = log(u);
+  const double margin = 1e-9 * (1.0 + fabs(lu) + fabs(lo) + fabs(hi));
+  if (lo > lu + margin || lo > margin) return 1;
+  if (hi < lu - margin) return 0;
+  return -1;
+}
+
 // a staging window: bead t at absolute slice j0+t of particle n (next(n)
 // past slice M); new beads in shared arrays; the moving path is excluded
 struct WindowSeg {
@@ -478,6 +585,7 @@ struct WindowSeg {
   __device__ __forceinline__ unsigned curq(int side, int t) const {
     return side ? pq[t] : c->Q(own(t), slice(t));
   }
+  __device__ __forceinline__ unsigned nxtq(int side, int t) const { return curq(side, t + 1); }
   __device__ __forceinline__ int slice(int t) const { return j0 + t < M ? j0 + t : j0 + t - M; }
   __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
     if (side) { x = px[t]; y = py[t]; }
@@ -690,10 +798,25 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     wi += c.Vl(a < M ? n : nx, a < M ? a : a - M);
     wu += mhtau * (svb[t] + svb[t + 1]);
   }
+  int dec = -1;
   if (phys_pair) {
     WindowSeg seg{&c, n, nx, j0, M, sx_, sy_, sq};
-    segment_pairs(c, seg, 0, m, true, true, (unsigned long long *)(sb + 5 * (WMAX + 1)), wi, wu,
-                  lane);
+    if (D::kSweep) {
+      // bounded estimate from the mirror; the exact sums only when its
+      // interval straddles the Metropolis threshold
+      PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
+      segment_estimate(c, seg, 0, m, e, lane);
+      double v[4];
+      est_reduce_lanes(e, v);
+      for (int k = 0; k < 4; ++k) v[k] = warp_sum(v[k]);
+      const double h = d.mhtau_g;
+      const double centre = warp_sum(wu) - warp_sum(wi) + h * (v[2] - v[0]);
+      const double radius = fabs(h) * (v[1] + v[3]);
+      dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
+    }
+    if (dec == -1)
+      segment_pairs(c, seg, 0, m, true, true, (unsigned long long *)(sb + 5 * (WMAX + 1)), wi, wu,
+                    lane);
   }
   wi = warp_sum(wi);
   wu = warp_sum(wu);
@@ -702,12 +825,14 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
       prop[t * dim] = sx_[t];
       if (dim > 1) prop[t * dim + 1] = sy_[t];
     }
-  int acc = 0;
-  if (lane == 0) {
-    const double delta = exp(wu - wi);
-    acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  int acc = dec;
+  if (dec == -1) {
+    if (lane == 0) {
+      const double delta = exp(wu - wi);
+      acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+    }
+    acc = __shfl_sync(0xffffffffu, acc, 0);
   }
-  acc = __shfl_sync(0xffffffffu, acc, 0);
   if (acc) {
     for (int t = lane; t < m; t += 32) {
       const int a = j0 + t;

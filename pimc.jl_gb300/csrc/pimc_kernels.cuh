@@ -132,6 +132,7 @@ struct SwapSeg {
   __device__ __forceinline__ unsigned curq(int side, int t) const {
     return side ? pq[t] : c->Q(own(t), slice(t));
   }
+  __device__ __forceinline__ unsigned nxtq(int side, int t) const { return curq(side, t + 1); }
   __device__ __forceinline__ void cur(int side, int t, double &x, double &y) const {
     if (side) { x = px[t]; y = py[t]; }
     else { x = c->X(0, own(t), slice(t)); y = c->Xd(1, own(t), slice(t)); }
@@ -159,11 +160,17 @@ struct ComSeg {
   const unsigned *qq;  // single path: the new beads' mirror words
   unsigned qsh;        // the shift in mirror units (a cycle's new centres)
   __device__ __forceinline__ int slice(int t) const { return t % M; }
-  __device__ __forceinline__ unsigned curq(int side, int t) const {
-    const int i = pol[t / M], j = t % M;
+  __device__ __forceinline__ unsigned beadq(int side, int i, int j) const {
     if (!side) return c->Q(i, j);
     if (q) return qq[j];
     return __vadd2(c->Q(i, j), qsh);
+  }
+  __device__ __forceinline__ unsigned curq(int side, int t) const {
+    return beadq(side, pol[t / M], t % M);
+  }
+  __device__ __forceinline__ unsigned nxtq(int side, int t) const {
+    const int i = pol[t / M], j = t % M;
+    return j + 1 < M ? beadq(side, i, j + 1) : beadq(side, c->next[i], 0);
   }
   __device__ __forceinline__ void bead(int side, int i, int j, double &x, double &y) const {
     if (!side) { x = c->X(0, i, j); y = c->Xd(1, i, j); return; }
@@ -501,50 +508,79 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     const double delta = exp(c2[1] - c2[0] + log_ratio);
     if (delta >= 1.0 || delta > dr.uniform_accept()) pairs = false;
   }
-  if (pairs) {
-    // the 2m links of the two moving paths in contiguous ranges per warp
-    const int per = (2 * m + nwarps - 1) / nwarps;
-    const int a0 = min(2 * m, warp * per), a1 = min(2 * m, a0 + per);
+  // the pair of the two moving paths, old and new (physical rules), exact
+  if (pairs && phys)
+    for (int t = tid; t < m; t += nt) {
+      const int j = slc(t), jn = slc(t + 1);
+      const int o1 = own1(t), o1n = own1(t + 1), o2 = own2(t), o2n = own2(t + 1);
+      const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
+      const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
+      if (r2o <= d.rc2)
+        w2[0] += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
+      const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
+      if (r2n <= d.rc2)
+        w2[1] += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+    }
+  // the 2m links of the two moving paths in contiguous ranges per warp
+  const int per = (2 * m + nwarps - 1) / nwarps;
+  const int a0 = min(2 * m, warp * per), a1 = min(2 * m, a0 + per);
+  auto seg_of = [&](int b) {
+    return SwapSeg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
+                   b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
+  };
+  int dec = pairs ? -1 : 2;  // 2: decided by the exact sums at hand
+  if (FAST && pairs) {
+    // bounded estimate from the mirror: decides the move unless the log
+    // acceptance ratio's interval straddles the threshold
+    PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
+    for (int b = 0; b < 2; ++b) {
+      const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
+      if (t0 < t1) segment_estimate(c, seg_of(b), t0, t1, e, lane);
+    }
+    double v[6], l4[4];
+    est_reduce_lanes(e, l4);
+    for (int k = 0; k < 4; ++k) v[k] = l4[k];
+    v[4] = w2[0];
+    v[5] = w2[1];
+    G::template sum<6>(v, red);
+    // w_initial gets h*So and, under the reference's rules, h*Sn; the
+    // physical rules put h*Sn into w_update (h = -tau g / 2)
+    const double h = d.mhtau_g;
+    const double centre = v[5] - v[4] + log_ratio - h * v[0] + (phys ? h : -h) * v[2];
+    const double radius = fabs(h) * (v[1] + v[3]);
+    dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
+  }
+  if (dec == -1) {
     for (int b = 0; b < 2; ++b) {
       const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
       if (t0 >= t1) continue;
-      SwapSeg seg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
-                  b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
       double wo = 0.0, wn = 0.0;
-      segment_pairs(c, seg, t0, t1, true, true, S.q + (size_t)warp * PQ_CAP, wo, wn, lane);
+      segment_pairs(c, seg_of(b), t0, t1, true, true, S.q + (size_t)warp * PQ_CAP, wo, wn, lane);
       // the reference adds the new paths' pair terms to w_initial and lets
       // the old ones see the other moving path (reshape.jl:166-240)
       w2[0] += wo;
       if (phys) w2[1] += wn; else w2[0] += wn;
     }
-    if (phys)
-      for (int t = tid; t < m; t += nt) {
-        // the pair of the two moving paths, old and new
-        const int j = slc(t), jn = slc(t + 1);
-        const int o1 = own1(t), o1n = own1(t + 1), o2 = own2(t), o2n = own2(t + 1);
-        const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
-        const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
-        if (r2o <= d.rc * d.rc)
-          w2[0] += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
-        const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
-        if (r2n <= d.rc * d.rc)
-          w2[1] += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+  }
+  int acc;
+  if (dec == 0 || dec == 1) {
+    acc = dec;
+  } else {
+    G::template sum<2>(w2, red);
+    if (prop)
+      for (int k = tid; k < 2 * (m + 1); k += nt) {
+        const int b = k / (m + 1), t = k % (m + 1);
+        prop[k * dim] = (b == 0 ? S.r1x : S.r2x)[t];
+        if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
       }
-  }
-  G::template sum<2>(w2, red);
-  if (prop)
-    for (int k = tid; k < 2 * (m + 1); k += nt) {
-      const int b = k / (m + 1), t = k % (m + 1);
-      prop[k * dim] = (b == 0 ? S.r1x : S.r2x)[t];
-      if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
+    if (tid == 0) {
+      const double delta = exp(w2[1] - w2[0] + log_ratio);
+      S.iv[2] = (delta >= 1.0) || (delta > dr.uniform_accept());
     }
-  if (tid == 0) {
-    const double delta = exp(w2[1] - w2[0] + log_ratio);
-    S.iv[2] = (delta >= 1.0) || (delta > dr.uniform_accept());
+    G::sync();
+    acc = S.iv[2];
+    G::sync();
   }
-  G::sync();
-  const int acc = S.iv[2];
-  G::sync();
   if (!acc) return RES_REJECT;
   // accept: exchange next, write the bridges along the new cycles, exchange
   // the tails (reshape.jl:247-279)
@@ -742,6 +778,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
       ws[1] += mhtau * (vext(d, qx, qy) + vext(d, qnx, qny));
     }
   }
+  int dec = -1;
   if (phys_pair) {
     // warps split the links, lanes the particles of each slice; pairs inside
     // the cycle keep their relative positions under the rigid shift
@@ -752,16 +789,36 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
     ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L, cs.qq, qsh};
     const int tot = np * M, per = (tot + nwarps - 1) / nwarps;
     const int t0 = min(tot, warp * per), t1 = min(tot, t0 + per);
-    segment_pairs(c, seg, t0, t1, true, true, qbuf + (size_t)warp * PQ_CAP, ws[0], ws[1], lane);
+    if (D::kSweep) {
+      // bounded estimate from the mirror; the exact sums only when its
+      // interval straddles the Metropolis threshold
+      PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
+      if (t0 < t1) segment_estimate(c, seg, t0, t1, e, lane);
+      double v[6], l4[4];
+      est_reduce_lanes(e, l4);
+      for (int k = 0; k < 4; ++k) v[k] = l4[k];
+      v[4] = ws[0];
+      v[5] = ws[1];
+      G::template sum<6>(v, red);
+      const double h = d.mhtau_g;
+      const double centre = v[5] - v[4] + h * (v[2] - v[0]);
+      const double radius = fabs(h) * (v[1] + v[3]);
+      dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
+    }
+    if (dec == -1)
+      segment_pairs(c, seg, t0, t1, true, true, qbuf + (size_t)warp * PQ_CAP, ws[0], ws[1], lane);
   }
-  G::template sum<2>(ws, red);
-  if (tid == 0) {
-    const double delta = exp(ws[1] - ws[0]);
-    *sflag = (delta >= 1.0) || (delta > dr.uniform_accept());
+  int acc = dec;
+  if (dec == -1) {
+    G::template sum<2>(ws, red);
+    if (tid == 0) {
+      const double delta = exp(ws[1] - ws[0]);
+      *sflag = (delta >= 1.0) || (delta > dr.uniform_accept());
+    }
+    G::sync();
+    acc = *sflag;
+    G::sync();
   }
-  G::sync();
-  const int acc = *sflag;
-  G::sync();
   if (!acc) return RES_REJECT;
   // links first (they read the unshifted neighbours), then positions
   for (int k = tid; k < np * M; k += nt) {

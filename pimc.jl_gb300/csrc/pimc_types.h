@@ -38,6 +38,11 @@ struct ChainDesc {
   float q_unit2;        // (2L / 65536)^2: squared mirror unit
   unsigned q_lim_rc;    // mirror prefilter bound (squared units) for rc
   unsigned q_lim_hard;  // the same for the hard-core radius
+  // bounded pair estimates from the mirror: u^2 / (2 sigma^2), and the
+  // squared-unit bounds below which a pair is surely within rc and above
+  // which it is surely beyond (kQErr units of mirror error on a distance)
+  float q_u2i;
+  unsigned q_lim_lo, q_lim_hi;
   int pad2_;
   long long x_off;      // doubles: x[j][n][d] (slice-major) at dpool + x_off
   long long V_off;      // doubles: V[j][n]
