@@ -480,7 +480,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-budget", type=float, default=12.0)
+    ap.add_argument("--cpu-budget", type=float, default=6.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)
     ap.add_argument("--traffic-per-bead", type=float, default=None,
                     help="DRAM bytes per bead update of the sweep kernel (ncu)")

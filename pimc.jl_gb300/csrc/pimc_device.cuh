@@ -562,16 +562,45 @@ __device__ __forceinline__ void est_reduce_lanes(const PairEst &e, double (&v)[4
   v[3] = (double)e.bn * (1.0 + rn) + rn * (double)e.sn + 1e-30;
 }
 
+// log u in FP32 (logf within a few ulp, u a 53-bit uniform in (0, 1)) and
+// a margin that covers its error
+__device__ __forceinline__ double log_u_margin(double u, double &margin) {
+  const double lu = (double)logf((float)u);
+  margin = 1e-5 * (1.0 + fabs(lu));
+  return lu;
+}
+
 // the Metropolis decision from an interval [lo, hi] of the log acceptance
-// ratio, for a threshold log(u): 1 accept, 0 reject, -1 undecided.  The
-// margin covers the rounding of the exact path's own sum and exponential.
+// ratio: 1 accept, 0 reject, -1 undecided.  Decided only where exp(dS) > u
+// (accept) or exp(dS) < u < 1 (reject) holds for every dS in the interval,
+// so the outcome is the FP64 formula's for the exact dS.
 __device__ __forceinline__ int decide_interval(double lo, double hi, double u) {
-  if (u <= 0.0) return lo > -INFINITY ? 1 : -1;
-  const double lu = log(u);
-  const double margin = 1e-9 * (1.0 + fabs(lu) + fabs(lo) + fabs(hi));
-  if (lo > lu + margin || lo > margin) return 1;
+  if (u <= 0.0) return lo > -700.0 ? 1 : -1;
+  double margin;
+  const double lu = log_u_margin(u, margin);
+  margin += 1e-9 * (fabs(lo) + fabs(hi));
+  if (lo > lu + margin) return 1;
   if (hi < lu - margin) return 0;
   return -1;
+}
+
+// Metropolis acceptance of a log ratio dS (helper.jl:3-5: delta >= 1 ||
+// delta > rand()).  A sweep's uniform is a pure function of the move's
+// stream, so away from the threshold the comparison runs in FP32 log space
+// and the FP64 exponential settles only the rest; the outcome is the FP64
+// formula's.  Injected draws keep the reference's order: the uniform is read
+// only when delta < 1.
+template <class D>
+__device__ __forceinline__ bool metropolis(double dS, D &dr) {
+  if (D::kSweep) {
+    const double u = dr.uniform_accept();
+    const int k = decide_interval(dS, dS, u);
+    if (k >= 0) return k == 1;
+    const double delta = exp(dS);
+    return delta >= 1.0 || delta > u;
+  }
+  const double delta = exp(dS);
+  return (delta >= 1.0) || (delta > dr.uniform_accept());
 }
 
 // a staging window: bead t at absolute slice j0+t of particle n (next(n)
@@ -692,8 +721,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
       prop[t * dim] = bx[t];
       if (dim > 1) prop[t * dim + 1] = by[t];
     }
-  const double delta = exp(wu - wi);
-  const bool acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  const bool acc = metropolis(wu - wi, dr);
   if (acc) {
     for (int t = 0; t < m; ++t) {
       const int a = j0 + t;
@@ -827,10 +855,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     }
   int acc = dec;
   if (dec == -1) {
-    if (lane == 0) {
-      const double delta = exp(wu - wi);
-      acc = (delta >= 1.0) || (delta > dr.uniform_accept());
-    }
+    if (lane == 0) acc = metropolis(wu - wi, dr);
     acc = __shfl_sync(0xffffffffu, acc, 0);
   }
   if (acc) {
@@ -950,8 +975,7 @@ __device__ int window_team(const CV &c, const Team &tm, int n, int j0, int m, D 
       si += sb(w)[TEAM_SLOT_D];
       su += sb(w)[TEAM_SLOT_D + 1];
     }
-    const double delta = exp(su - si);
-    lead[2] = (delta >= 1.0) || (delta > dr.uniform_accept()) ? 1.0 : 0.0;
+    lead[2] = metropolis(su - si, dr) ? 1.0 : 0.0;
   }
   tm.sync();
   const int acc = lead[2] != 0.0;

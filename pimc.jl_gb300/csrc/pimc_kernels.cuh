@@ -505,8 +505,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   if (FAST && any_pair && !phys && d.g >= 0.0) {
     double c2[2] = {w2[0], w2[1]};
     G::template sum<2>(c2, red);
-    const double delta = exp(c2[1] - c2[0] + log_ratio);
-    if (delta >= 1.0 || delta > dr.uniform_accept()) pairs = false;
+    if (metropolis(c2[1] - c2[0] + log_ratio, dr)) pairs = false;
   }
   // the pair of the two moving paths, old and new (physical rules), exact
   if (pairs && phys)
@@ -574,8 +573,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
         if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
       }
     if (tid == 0) {
-      const double delta = exp(w2[1] - w2[0] + log_ratio);
-      S.iv[2] = (delta >= 1.0) || (delta > dr.uniform_accept());
+      S.iv[2] = metropolis(w2[1] - w2[0] + log_ratio, dr);
     }
     G::sync();
     acc = S.iv[2];
@@ -655,8 +653,7 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
     wu += mhtau * (vprev + vj);
     vprev = vj;
   }
-  const double delta = exp(wu - wi);
-  const bool acc = (delta >= 1.0) || (delta > dr.uniform_accept());
+  const bool acc = metropolis(wu - wi, dr);
   if (acc) {
     vprev = v0;
     double px = q0x, py = q0y;
@@ -812,8 +809,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
   if (dec == -1) {
     G::template sum<2>(ws, red);
     if (tid == 0) {
-      const double delta = exp(ws[1] - ws[0]);
-      *sflag = (delta >= 1.0) || (delta > dr.uniform_accept());
+      *sflag = metropolis(ws[1] - ws[0], dr);
     }
     G::sync();
     acc = *sflag;

@@ -33,23 +33,6 @@ __device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ip
   return c;
 }
 
-// hint L2 to fetch the mirror and position rows of slices j0..j0+m (a swap's
-// window) from HBM; chain state staged in shared memory needs none
-__device__ __forceinline__ void prefetch_rows(const CV &c, int j0, int m, int tid, int nt) {
-  if (!__isGlobal(c.xq)) return;
-  const int M = c.M;
-  const int qlines = (c.N * 4 + 127) / 128, xlines = (c.N * c.dim * 8 + 127) / 128;
-  const int per = qlines + xlines;
-  for (int k = tid; k < (m + 1) * per; k += nt) {
-    const int r = k / per, l = k % per;
-    int j = j0 + r;
-    if (j >= M) j -= M;
-    const char *p = l < qlines ? (const char *)(c.xq + (size_t)j * c.ldn) + (size_t)l * 128
-                               : (const char *)(c.x + (size_t)j * c.ldn * c.dim) + (size_t)(l - qlines) * 128;
-    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-  }
-}
-
 // moves whose acceptance depends on other paths at the same slice
 __device__ __forceinline__ bool chain_serial_local(const ChainDesc &d) {
   return ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) || (d.flags & PF_HARD);
@@ -196,34 +179,17 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
     G::sync();
   }
 
-  // ---- permutation swaps (ReshapeSwapLinear), one at a time by the group.
-  // A swap's slices come from its own counter-based stream, so the slice rows
-  // the next swap will scan are prefetched into L2 while this one runs.
+  // ---- permutation swaps (ReshapeSwapLinear), one at a time by the group
   if (N > 1 && mix.swaps_per_sweep > 0) {
     SwapScratch S;
     S.carve(scratch, N, nwarps);
     const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
     const int sm = max(2, sc.v.swap_m);
-    auto window_of = [&](int a, int &j0, int &m) {
-      const uint4 r0 = make_stream(d, sweep, PH_SWAP, (unsigned)a).at(DRAW_CHOICE);
-      j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
-      m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
-    };
-    if (d.flags & PF_PAIR) {
-      int j0, m;
-      window_of(0, j0, m);
-      prefetch_rows(c, j0, m, tid, nt);
-    }
     for (int a = 0; a < mix.swaps_per_sweep; ++a) {
       const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
       const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
       const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
       const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
-      if ((d.flags & PF_PAIR) && a + 1 < mix.swaps_per_sweep) {
-        int jn, mn;
-        window_of(a + 1, jn, mn);
-        prefetch_rows(c, jn, mn, tid, nt);
-      }
       const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
       const double upick = u53(r1.z, r1.w);
       GenDraws dr = gen_draws(ss);
