@@ -255,8 +255,13 @@ int pimc_last_run_ms(void *handle, double *ms);
 /* kernel launches issued by the last run call */
 int pimc_last_run_launches(void *handle, long long *launches);
 /* engine options: PIMC_OPT_FORCE_WARP_WINDOW routes pair-free staging
- * attempts through the warp-cooperative window as well (parity coverage) */
-enum { PIMC_OPT_FORCE_WARP_WINDOW = 1 };
+ * attempts through the warp-cooperative window as well (parity coverage);
+ * PIMC_OPT_EXACT_DECISIONS makes sweeps take every accept/reject decision
+ * from the exact FP64 sums, without the bounded shortcuts (pair-sum
+ * estimates from the position mirror, FP32 log-space Metropolis tests, the
+ * reference rules' pair-free early accept).  Both ways give the same chains
+ * bit for bit; the option exists to show it. */
+enum { PIMC_OPT_FORCE_WARP_WINDOW = 1, PIMC_OPT_EXACT_DECISIONS = 2 };
 int pimc_set_option(void *handle, int key, long long value);
 const char *pimc_last_error(void);
 int pimc_abi_version(void);

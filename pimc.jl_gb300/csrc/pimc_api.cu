@@ -1390,6 +1390,15 @@ int pimc_set_option(void *handle, int key, long long value) {
     h->force_warp = value != 0;
     return PIMC_OK;
   }
+  if (key == PIMC_OPT_EXACT_DECISIONS) {
+    for (auto &d : h->desc) d.flags = value ? (d.flags | PF_EXACT) : (d.flags & ~PF_EXACT);
+    if (upload_desc(h)) return PIMC_ECUDA;
+    if (h->gexec) {
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+    return sync_check(h);
+  }
   return fail(PIMC_EARG, "unknown option");
 }
 

@@ -591,8 +591,8 @@ __device__ __forceinline__ int decide_interval(double lo, double hi, double u) {
 // formula's.  Injected draws keep the reference's order: the uniform is read
 // only when delta < 1.
 template <class D>
-__device__ __forceinline__ bool metropolis(double dS, D &dr) {
-  if (D::kSweep) {
+__device__ __forceinline__ bool metropolis(const ChainDesc &d, double dS, D &dr) {
+  if (D::kSweep && !(d.flags & PF_EXACT)) {
     const double u = dr.uniform_accept();
     const int k = decide_interval(dS, dS, u);
     if (k >= 0) return k == 1;
@@ -721,7 +721,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
       prop[t * dim] = bx[t];
       if (dim > 1) prop[t * dim + 1] = by[t];
     }
-  const bool acc = metropolis(wu - wi, dr);
+  const bool acc = metropolis(d, wu - wi, dr);
   if (acc) {
     for (int t = 0; t < m; ++t) {
       const int a = j0 + t;
@@ -829,7 +829,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   int dec = -1;
   if (phys_pair) {
     WindowSeg seg{&c, n, nx, j0, M, sx_, sy_, sq};
-    if (D::kSweep) {
+    if (D::kSweep && !(d.flags & PF_EXACT)) {
       // bounded estimate from the mirror; the exact sums only when its
       // interval straddles the Metropolis threshold
       PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
@@ -855,7 +855,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     }
   int acc = dec;
   if (dec == -1) {
-    if (lane == 0) acc = metropolis(wu - wi, dr);
+    if (lane == 0) acc = metropolis(d, wu - wi, dr);
     acc = __shfl_sync(0xffffffffu, acc, 0);
   }
   if (acc) {
@@ -975,7 +975,7 @@ __device__ int window_team(const CV &c, const Team &tm, int n, int j0, int m, D 
       si += sb(w)[TEAM_SLOT_D];
       su += sb(w)[TEAM_SLOT_D + 1];
     }
-    lead[2] = metropolis(su - si, dr) ? 1.0 : 0.0;
+    lead[2] = metropolis(d, su - si, dr) ? 1.0 : 0.0;
   }
   tm.sync();
   const int acc = lead[2] != 0.0;

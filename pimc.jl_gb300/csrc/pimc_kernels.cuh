@@ -502,10 +502,11 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   // decision and a sweep skips them (its Metropolis uniform is a pure function
   // of the move's stream).  Injected-draw attempts always evaluate them.
   bool pairs = any_pair;
-  if (FAST && any_pair && !phys && d.g >= 0.0) {
+  const bool shortcuts = FAST && !(d.flags & PF_EXACT);
+  if (shortcuts && any_pair && !phys && d.g >= 0.0) {
     double c2[2] = {w2[0], w2[1]};
     G::template sum<2>(c2, red);
-    if (metropolis(c2[1] - c2[0] + log_ratio, dr)) pairs = false;
+    if (metropolis(d, c2[1] - c2[0] + log_ratio, dr)) pairs = false;
   }
   // the pair of the two moving paths, old and new (physical rules), exact
   if (pairs && phys)
@@ -528,7 +529,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
                    b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
   };
   int dec = pairs ? -1 : 2;  // 2: decided by the exact sums at hand
-  if (FAST && pairs) {
+  if (shortcuts && pairs) {
     // bounded estimate from the mirror: decides the move unless the log
     // acceptance ratio's interval straddles the threshold
     PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
@@ -573,7 +574,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
         if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
       }
     if (tid == 0) {
-      S.iv[2] = metropolis(w2[1] - w2[0] + log_ratio, dr);
+      S.iv[2] = metropolis(d, w2[1] - w2[0] + log_ratio, dr);
     }
     G::sync();
     acc = S.iv[2];
@@ -653,7 +654,7 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
     wu += mhtau * (vprev + vj);
     vprev = vj;
   }
-  const bool acc = metropolis(wu - wi, dr);
+  const bool acc = metropolis(d, wu - wi, dr);
   if (acc) {
     vprev = v0;
     double px = q0x, py = q0y;
@@ -786,7 +787,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
     ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L, cs.qq, qsh};
     const int tot = np * M, per = (tot + nwarps - 1) / nwarps;
     const int t0 = min(tot, warp * per), t1 = min(tot, t0 + per);
-    if (D::kSweep) {
+    if (D::kSweep && !(d.flags & PF_EXACT)) {
       // bounded estimate from the mirror; the exact sums only when its
       // interval straddles the Metropolis threshold
       PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
@@ -809,7 +810,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
   if (dec == -1) {
     G::template sum<2>(ws, red);
     if (tid == 0) {
-      *sflag = metropolis(ws[1] - ws[0], dr);
+      *sflag = metropolis(d, ws[1] - ws[0], dr);
     }
     G::sync();
     acc = *sflag;

@@ -11,6 +11,7 @@ enum : int {
   PF_HARD = 4,      // hard-core radius > 0
   PF_LATT = 8,      // square lattice term in V
   PF_HARM = 16,     // harmonic trap term in V
+  PF_EXACT = 32,    // sweeps decide every move from exact FP64 sums (no bounded shortcuts)
 };
 
 // move kinds for counters

@@ -17,6 +17,7 @@ SEM_REFERENCE = 0
 SEM_PHYSICAL = 1
 REJECT, ACCEPT, SKIP, HARDCORE = 0, 1, 2, 3
 OPT_FORCE_WARP_WINDOW = 1
+OPT_EXACT_DECISIONS = 2
 
 
 def _dp(a):
@@ -368,4 +369,5 @@ class Engine:
 
 
 __all__ = ["Engine", "ChainParams", "Mix", "EngineStats", "PimcError", "SEM_REFERENCE",
-           "SEM_PHYSICAL", "REJECT", "ACCEPT", "SKIP", "HARDCORE", "OPT_FORCE_WARP_WINDOW"]
+           "SEM_PHYSICAL", "REJECT", "ACCEPT", "SKIP", "HARDCORE", "OPT_FORCE_WARP_WINDOW",
+           "OPT_EXACT_DECISIONS"]

@@ -342,3 +342,38 @@ def test_api_mirror_end_to_end():
         pimc.apply(s, ups[1][1])
     w = s.world
     assert len(w) == 3 and w[0].r.shape == (10, 2)
+
+
+@pytest.mark.parametrize("semantics", [0, 1])
+def test_bounded_decisions_equal_exact_decisions(semantics):
+    """sweeps decide most moves from bounded estimates (pair sums from the
+    position mirror, FP32 log-space Metropolis tests, the reference rules'
+    pair-free early accept); with PIMC_OPT_EXACT_DECISIONS every decision
+    comes from the exact FP64 sums instead, and the chains stay identical bit
+    for bit through many sweeps of interacting, permuting chains"""
+    from pimc.engine import ChainParams, Engine, OPT_EXACT_DECISIONS
+    rng = np.random.default_rng(11 + semantics)
+    ps = []
+    for i in range(16):
+        N = int(rng.integers(8, 64))
+        M = int(rng.choice([16, 32]))
+        ps.append(ChainParams(dim=2, N=N, M=M, L=6.0, T=1.0 / rng.uniform(0.5, 3), lam=0.5,
+                              harmonic_omega=1.0, interactions=True, pair_g=float(rng.uniform(0.2, 2)),
+                              pair_sigma=0.5, r_a=1.5, semantics=semantics, seed=500 + i,
+                              energy_capacity=8))
+    fast, exact = Engine(ps), Engine(ps)
+    exact.set_option(OPT_EXACT_DECISIONS, 1)
+    for i, p in enumerate(ps):
+        m = mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=2, pcom=1)
+        fast.set_mix(m, chain=i)
+        exact.set_mix(m, chain=i)
+    fast.run_batched(12)
+    exact.run_batched(12)
+    for c in range(len(ps)):
+        np.testing.assert_array_equal(fast.get_beads(c), exact.get_beads(c))
+        np.testing.assert_array_equal(fast.get_next(c), exact.get_next(c))
+    sf, se = fast.total_stats(), exact.total_stats()
+    assert sf.accepts == se.accepts and sf.attempts == se.attempts
+    assert sum(sf.accepts) > 0 and min(sf.accepts[:3]) > 0  # staging, swaps, CoM all accept
+    fast.close()
+    exact.close()
