@@ -49,8 +49,8 @@ PLAIN_STRIDE = 16
 # dram__bytes_write.sum) and FP64 flops (dadd + dmul + 2 dfma thread
 # instructions) over the launch's bead updates
 C4_PER_BEAD = {
-    "physical": {"dram_bytes": 1327.0, "fp64_flops": 2100.0},   # 24.82 GB, 39.3 G / 18.70 M
-    "reference": {"dram_bytes": 438.0, "fp64_flops": 473.0},    # 7.83 GB, 8.45 G / 17.87 M
+    "physical": {"dram_bytes": 188.4, "fp64_flops": 1017.0},    # 3.52 GB, 19.0 G / 18.70 M
+    "reference": {"dram_bytes": 269.7, "fp64_flops": 204.0},    # 4.82 GB, 3.65 G / 17.87 M
 }
 
 
