@@ -245,6 +245,31 @@ int pimc_get_total_stats(void *handle, pimc_stats *out);
 int pimc_state_size(void *handle, size_t *bytes);
 int pimc_get_state(void *handle, void *buf, size_t bytes);
 int pimc_set_state(void *handle, const void *buf, size_t bytes);
+/* prop_rel_interpolate_terms (src/propagator.jl:36-73): the integral terms
+ * T[i1][i2] = -I1 - I2 + I3 of the contact-interaction propagator on the
+ * reference's grid r_i = 1e-20 + i (range - 1e-20)/(n - 1), n = 600 there,
+ * computed on the device (row-major, symmetric) */
+int pimc_contact_table(double g0, double tau, double range, int n, double *out);
+/* build_prop_int(range, g0, tau) attached as the pair propagator of a chain
+ * (chain < 0: every chain) that was created with interactions = 1:
+ *   lnU(r1, r2) = log(1 + T(|r1|, |r2|) / prop_rel0(r1, r2, tau)), or -mu
+ *   where the argument is negative (src/system.jl:26-28,
+ *   src/propagator.jl:74-89), T bilinear in the table above (n = 0 -> 600).
+ * tau is the chain's own; chains with equal (g0, tau, range, n) share one
+ * device table.  It replaces the Gaussian pair in every move and in
+ * pimc_eval_action; the pair energy columns of the estimators read 0 for it,
+ * and pimc_adjoint refuses it.  Radii outside [1e-20, range] are clamped to
+ * the grid, where the reference raises a BoundsError. */
+int pimc_set_contact_propagator(void *handle, int chain, double g0, double range, int n);
+/* the same with a caller-made table T[i1][i2] (row-major n*n, on the grid
+ * above), e.g. one stored by the reference's precompute_int_prop.jl */
+int pimc_set_contact_table(void *handle, int chain, const double *table, int n, double range);
+/* the chain's contact table: *n = 0 when it has none; out (optional) receives
+ * n*n values and must hold cap >= n*n */
+int pimc_get_contact_table(void *handle, int chain, double *out, size_t cap, int *n,
+                           double *range);
+/* back to the Gaussian pair of pimc_params (chain < 0: every chain) */
+int pimc_clear_contact(void *handle, int chain);
 /* measurement utility, no reference counterpart: FP64 fused multiply-add
  * throughput of the handle's device in TFLOP/s (eight independent DFMA
  * chains per thread over the whole GPU, best of three timed launches) --

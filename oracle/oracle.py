@@ -30,6 +30,7 @@ class Params(C.Structure):
         ("interactions", C.c_int), ("g", C.c_double), ("inv2s2", C.c_double),
         ("nbins", C.c_int), ("rc", C.c_double), ("hardcore_a", C.c_double),
         ("ctr", C.c_int), ("semantics", C.c_int),
+        ("ct_tab", C.POINTER(C.c_double)), ("ct_n", C.c_int), ("ct_range", C.c_double),
     ]
 
 
@@ -136,10 +137,13 @@ def _ip(a):
 
 def make_params(dim=2, N=2, M=100, L=4.0, T=1.0, lam=1.0, hcoef=0.0, V0=0.0, lat_a=1.0,
                 pair_g=0.0, pair_sigma=1.0, interactions=False, r_a=0.0, hardcore_a=0.0,
-                semantics=SEM_REFERENCE, ctr=10000, mu=0.0) -> Params:
+                semantics=SEM_REFERENCE, ctr=10000, mu=0.0, contact_table=None,
+                contact_range=0.0) -> Params:
     """Parameters with the System constructor's derived constants
     (src/system.jl:129-167): tau = beta/M, nbins = floor(2L/r_a), r_a = L/4
-    when unset without interactions."""
+    when unset without interactions.  contact_table (n x n, on the grid
+    1e-20 .. contact_range) switches lnU to the tabulated contact propagator
+    (src/propagator.jl:74-89); the Params object keeps the array alive."""
     p = Params()
     p.dim, p.N, p.M, p.L = dim, N, M, L
     p.beta = 1.0 / T
@@ -156,6 +160,16 @@ def make_params(dim=2, N=2, M=100, L=4.0, T=1.0, lam=1.0, hcoef=0.0, V0=0.0, lat
     p.hardcore_a = hardcore_a
     p.ctr = ctr
     p.semantics = semantics
+    if contact_table is not None:
+        tab = np.ascontiguousarray(contact_table, dtype=np.float64)
+        if tab.ndim != 2 or tab.shape[0] != tab.shape[1] or tab.shape[0] < 2:
+            raise ValueError("contact_table must be a square n x n array, n >= 2")
+        if not contact_range > 1e-20:
+            raise ValueError("contact_range must be positive")
+        p._ct_keep = tab
+        p.ct_tab = _dp(tab)
+        p.ct_n = tab.shape[0]
+        p.ct_range = contact_range
     return p
 
 

@@ -140,10 +140,59 @@ static double vpair_r2(const orc_params *p, double r2) { return p->g * exp(-r2 *
 /* src/system.jl:26-28 with the Gaussian pair propagator
  * propint(r1,r2,tau) = exp(-tau/2 (v(|r1|)+v(|r2|))), so log(propint) is the
  * primitive pair link action; d1, d2 are per-component min-image distances */
+static double contact_lnU(const orc_params *p, const double *d1, const double *d2);
 double orc_lnU(const orc_params *p, const double *d1, const double *d2) {
+  if (p->ct_tab) return contact_lnU(p, d1, d2);
   double a = 0.0, b = 0.0;
   for (int d = 0; d < p->dim; ++d) { a += d1[d] * d1[d]; b += d2[d] * d2[d]; }
   return -0.5 * p->tau * (vpair_r2(p, a) + vpair_r2(p, b));
+}
+
+/* Linear B-spline of the table scaled onto the grid (Interpolations.jl's
+ * scale(interpolate(A, BSpline(Linear())), r, r), src/propagator.jl:68-70):
+ * position (x - first)/step, the last cell for x at the end.  The reference
+ * raises a BoundsError outside [1e-20, range]; the engine clamps. */
+static int contact_cell(const orc_params *p, double r, double *w) {
+  const double r0 = 1e-20, h = (p->ct_range - r0) / (double)(p->ct_n - 1);
+  if (r < r0) r = r0;
+  if (r > p->ct_range) r = p->ct_range;
+  double pos = (r - r0) / h, f = floor(pos);
+  if (f > (double)(p->ct_n - 2)) f = (double)(p->ct_n - 2);
+  *w = pos - f;
+  return (int)f;
+}
+static double contact_T(const orc_params *p, double r1, double r2) {
+  double wx, wy;
+  int ix = contact_cell(p, r1, &wx), iy = contact_cell(p, r2, &wy), n = p->ct_n;
+  const double *a = p->ct_tab + (size_t)ix * n + iy, *b = a + n;
+  double c0 = (1.0 - wy) * a[0] + wy * a[1];
+  double c1 = (1.0 - wy) * b[0] + wy * b[1];
+  return (1.0 - wx) * c0 + wx * c1;
+}
+/* minimum-image wrap of a difference of two minimum-image vectors */
+static double wrap1(double x, double L) {
+  if (fabs(x) > L) x -= (x > 0 ? 2.0 * L : -2.0 * L);
+  return x;
+}
+/* lnU = log(prop_int) or -mu when prop_int < 0 (src/system.jl:26-28) with
+ * prop_int(r1, r2) = 1 + T(|r1|, |r2|) / prop_rel0(r1, r2, tau),
+ * prop_rel0 = exp(-|r1 - r2|^2 / (4 tau)) / (4 pi tau) (propagator.jl:74-89).
+ * d1, d2 are signed minimum-image differences; the reference passes their
+ * per-component absolute values (distance.()), the physical rules the signed
+ * vectors with their difference wrapped. */
+static double contact_lnU(const orc_params *p, const double *d1, const double *d2) {
+  double n1 = 0.0, n2 = 0.0, dd = 0.0;
+  for (int d = 0; d < p->dim; ++d) {
+    double a = fabs(d1[d]), b = fabs(d2[d]);
+    n1 += a * a;
+    n2 += b * b;
+    double e = p->semantics == ORC_SEM_PHYSICAL ? wrap1(d1[d] - d2[d], p->L) : a - b;
+    dd += e * e;
+  }
+  double T = contact_T(p, sqrt(n1), sqrt(n2));
+  double rel0 = exp(-dd / (4.0 * p->tau)) / (4.0 * 3.141592653589793 * p->tau);
+  double pi = 1.0 + T / rel0;
+  return pi < 0.0 ? -p->mu : log(pi);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -227,9 +276,18 @@ static int stencil(const orc_params *p, int c, int *out) {
   return k;
 }
 
+/* squared minimum-image distance; dv (optional) receives the signed
+ * minimum-image difference a - b, of magnitude distance(a, b) */
 static double mi_dist2(const orc_params *p, const double *a, const double *b, double *dv) {
   double s = 0.0;
-  for (int d = 0; d < p->dim; ++d) { double q = orc_distance(a[d], b[d], p->L); if (dv) dv[d] = q; s += q * q; }
+  for (int d = 0; d < p->dim; ++d) {
+    double q = orc_distance(a[d], b[d], p->L);
+    if (dv) {
+      double x = a[d] - b[d];
+      dv[d] = (fabs(x) > p->L) == (x > 0) ? -q : q;
+    }
+    s += q * q;
+  }
   return s;
 }
 
@@ -862,7 +920,8 @@ void orc_energy(const orc_state *st, double out[4]) {
   out[0] = (double)(dim * N) / (2.0 * tau) - 1.0 / (4.0 * p->lambda * (tau * tau) * M) * link + 1.0 / (2.0 * M) * pot;
   out[1] = 1.0 / (2.0 * M) * vkin + 1.0 / (2.0 * M) * vpot;
   out[2] = out[3] = 0.0;
-  if (p->interactions) pair_terms(st, &out[2], &out[3]);
+  /* the contact table has no tau derivative: no pair energy for it */
+  if (p->interactions && !p->ct_tab) pair_terms(st, &out[2], &out[3]);
 }
 
 /* Density (src/measurement.jl:45-55): bin floor((r+L)/bin), counted only for

@@ -53,6 +53,12 @@ typedef struct orc_params {
   double hardcore_a;
   int ctr;         /* hard-core retry cap (s.ctr) */
   int semantics;   /* ORC_SEM_REFERENCE or ORC_SEM_PHYSICAL */
+  /* tabulated contact propagator (build_prop_int, src/propagator.jl:74-89):
+   * when ct_tab is set and interactions is on, lnU comes from the table
+   * T[i1*ct_n + i2] on r_i = 1e-20 + i (ct_range - 1e-20)/(ct_n - 1) */
+  const double *ct_tab;
+  int ct_n;
+  double ct_range;
 } orc_params;
 
 typedef struct orc_rng {

@@ -87,6 +87,15 @@ struct Handle {
   int max_dyn_smem = 0;         // opt-in shared bytes per CTA, less static use
   cudaGraphExec_t gexec = nullptr;
   int force_warp = 0;
+  // contact-propagator tables on the device, shared by the chains whose
+  // (g0, tau, range, n) agree; tables given by the caller are never shared
+  struct ContactTab {
+    double g0, tau, range;
+    int n;
+    bool given;
+    double *d;
+  };
+  std::vector<ContactTab> ctabs;
 };
 
 int check_params(const pimc_params &p) {
@@ -733,6 +742,7 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_buf);
   cudaFree(h->d_adj);
   cudaFree(h->d_stage);
+  for (auto &t : h->ctabs) cudaFree(t.d);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1134,6 +1144,9 @@ int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double
   Handle *h = H(handle);
   if (check_chain(h, chain)) return PIMC_EARG;
   const ChainDesc &d = h->desc[chain];
+  if (d.flags & PF_CONTACT)
+    return fail(PIMC_EARG, "the adjoint covers the Gaussian pair; chain " + std::to_string(chain) +
+                               " uses the contact table, which has no parameter derivative");
   const size_t nbd = (size_t)d.N * d.M;
   const int nblocks = (int)((nbd + 255) / 256);
   const size_t need = 4 * nbd + (size_t)d.N + 8 * (size_t)nblocks + 16 + (size_t)d.dim * nbd;
@@ -1190,6 +1203,9 @@ int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta
   Handle *h = H(handle);
   if (check_chain(h, chain)) return PIMC_EARG;
   const ChainDesc &d = h->desc[chain];
+  if (d.flags & PF_CONTACT)
+    return fail(PIMC_EARG, "the adjoint covers the Gaussian pair; chain " + std::to_string(chain) +
+                               " uses the contact table, which has no parameter derivative");
   const size_t nbd = (size_t)d.N * d.M;
   const int nblocks = (int)((nbd + 255) / 256);
   const size_t need = 4 * nbd + (size_t)d.N + 8 * (size_t)nblocks + 16 + (size_t)d.dim * nbd;
@@ -1243,6 +1259,149 @@ int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta
     extra[3] = tot[8];
   }
   return PIMC_OK;
+}
+
+int pimc_contact_table(double g0, double tau, double range, int n, double *out) {
+  if (!(g0 != 0.0) || !std::isfinite(g0) || !(tau > 0.0) || !(range > 0.0) || n < 2 || n > 4096 ||
+      !out)
+    return fail(PIMC_EARG, "contact table needs g0 != 0, tau > 0, range > 0, 2 <= n <= 4096");
+  double *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * (size_t)n * n));
+  cudaError_t e = launch_contact_table(d, n, range, g0, tau, nullptr);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d, sizeof(double) * (size_t)n * n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(PIMC_ECUDA, std::string("contact table: ") + cudaGetErrorString(e));
+  return PIMC_OK;
+}
+
+namespace {
+// the reference's grid: range(1e-20, range, n) (src/propagator.jl:39-45)
+constexpr double kContactR0 = 1e-20;
+
+int contact_targets(Handle *h, int chain, int *c0, int *c1) {
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (chain < -1 || chain >= h->nchains) return fail(PIMC_EARG, "chain out of range");
+  *c0 = chain < 0 ? 0 : chain;
+  *c1 = chain < 0 ? h->nchains : chain + 1;
+  for (int c = *c0; c < *c1; ++c)
+    if (!(h->desc[c].flags & PF_PAIR))
+      return fail(PIMC_EARG, "chain " + std::to_string(c) +
+                                 " has no pair propagator (create it with interactions = 1)");
+  return PIMC_OK;
+}
+
+void attach_contact(ChainDesc &d, const double *tab, int n, double range) {
+  d.ct_tab = tab;
+  d.ct_n = n;
+  d.ct_r0 = kContactR0;
+  d.ct_rmax = range;
+  d.ct_h = (range - kContactR0) / (double)(n - 1);
+  d.flags |= PF_CONTACT;
+}
+
+// drop device tables no chain refers to any more
+void release_contact_tables(Handle *h) {
+  for (size_t i = 0; i < h->ctabs.size();) {
+    bool used = false;
+    for (const auto &d : h->desc) used = used || ((d.flags & PF_CONTACT) && d.ct_tab == h->ctabs[i].d);
+    if (used) { ++i; continue; }
+    cudaFree(h->ctabs[i].d);
+    h->ctabs.erase(h->ctabs.begin() + (long)i);
+  }
+}
+
+int contact_args(double range, int n) {
+  if (!(range > kContactR0) || !std::isfinite(range) || n < 2 || n > 4096)
+    return fail(PIMC_EARG, "contact table needs range > 0 and 2 <= n <= 4096");
+  return PIMC_OK;
+}
+}  // namespace
+
+int pimc_set_contact_propagator(void *handle, int chain, double g0, double range, int n) {
+  Handle *h = H(handle);
+  int c0, c1;
+  if (contact_targets(h, chain, &c0, &c1)) return PIMC_EARG;
+  if (n == 0) n = 600;
+  if (!(g0 != 0.0) || !std::isfinite(g0)) return fail(PIMC_EARG, "contact propagator needs g0 != 0");
+  if (contact_args(range, n)) return PIMC_EARG;
+  CK(cudaStreamSynchronize(h->stream));
+  for (int c = c0; c < c1; ++c) {
+    const double tau = h->desc[c].tau;
+    const double *tab = nullptr;
+    for (const auto &t : h->ctabs)
+      if (!t.given && t.g0 == g0 && t.tau == tau && t.range == range && t.n == n) tab = t.d;
+    if (!tab) {
+      double *d = nullptr;
+      CK(cudaMalloc(&d, sizeof(double) * (size_t)n * n));
+      h->ctabs.push_back({g0, tau, range, n, false, d});
+      CK(launch_contact_table(d, n, range, g0, tau, h->stream));
+      tab = d;
+    }
+    attach_contact(h->desc[c], tab, n, range);
+  }
+  if (upload_desc(h)) return PIMC_ECUDA;
+  int rc = sync_check(h);
+  release_contact_tables(h);
+  return rc;
+}
+
+int pimc_set_contact_table(void *handle, int chain, const double *tab, int n, double range) {
+  Handle *h = H(handle);
+  int c0, c1;
+  if (contact_targets(h, chain, &c0, &c1)) return PIMC_EARG;
+  if (!tab) return fail(PIMC_EARG, "null table");
+  if (contact_args(range, n)) return PIMC_EARG;
+  const size_t cnt = (size_t)n * n;
+  for (size_t i = 0; i < cnt; ++i)
+    if (std::isnan(tab[i])) return fail(PIMC_EARG, "contact table holds NaN");
+  CK(cudaStreamSynchronize(h->stream));
+  double *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(double) * cnt));
+  h->ctabs.push_back({0.0, 0.0, range, n, true, d});
+  CK(cudaMemcpy(d, tab, sizeof(double) * cnt, cudaMemcpyHostToDevice));
+  for (int c = c0; c < c1; ++c) attach_contact(h->desc[c], d, n, range);
+  if (upload_desc(h)) return PIMC_ECUDA;
+  int rc = sync_check(h);
+  release_contact_tables(h);
+  return rc;
+}
+
+int pimc_get_contact_table(void *handle, int chain, double *out, size_t cap, int *n, double *range) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  const ChainDesc &d = h->desc[chain];
+  if (!(d.flags & PF_CONTACT)) {
+    if (n) *n = 0;
+    if (range) *range = 0.0;
+    return PIMC_OK;
+  }
+  if (n) *n = d.ct_n;
+  if (range) *range = d.ct_rmax;
+  if (out) {
+    const size_t cnt = (size_t)d.ct_n * d.ct_n;
+    if (cap < cnt) return fail(PIMC_EARG, "output holds fewer than n*n values");
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaMemcpy(out, d.ct_tab, sizeof(double) * cnt, cudaMemcpyDeviceToHost));
+  }
+  return PIMC_OK;
+}
+
+int pimc_clear_contact(void *handle, int chain) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (chain < -1 || chain >= h->nchains) return fail(PIMC_EARG, "chain out of range");
+  const int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->nchains : chain + 1;
+  for (int c = c0; c < c1; ++c) {
+    ChainDesc &d = h->desc[c];
+    d.flags &= ~PF_CONTACT;
+    d.ct_tab = nullptr;
+    d.ct_n = 0;
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  if (upload_desc(h)) return PIMC_ECUDA;
+  int rc = sync_check(h);
+  release_contact_tables(h);
+  return rc;
 }
 
 int pimc_fp64_peak(void *handle, double *tflops) {

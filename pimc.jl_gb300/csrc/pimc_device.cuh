@@ -347,6 +347,65 @@ __device__ __forceinline__ double mi2(const ChainDesc &d, double ax, double ay, 
   return s;
 }
 
+// grid position of a radius in the contact table: cell i and weight of
+// cell i + 1 of the linear B-spline (Interpolations.jl's scaled linear
+// interpolation: (x - first)/step, the last cell for x at the end).  Radii
+// outside [r0, rmax] are clamped, where the reference raises a BoundsError.
+__device__ __forceinline__ int contact_cell(const ChainDesc &d, double r, double &w) {
+  r = fmin(fmax(r, d.ct_r0), d.ct_rmax);
+  const double p = (r - d.ct_r0) / d.ct_h;
+  double f = floor(p);
+  if (f > (double)(d.ct_n - 2)) f = (double)(d.ct_n - 2);
+  w = p - f;
+  return (int)f;
+}
+
+// the pair link action of the tabulated contact propagator between two
+// particles whose minimum-image differences are d1 (slice j) and d2 (slice
+// j+1): prop_int = 1 + T(|d1|, |d2|) / prop_rel0(d1, d2, tau) with
+// prop_rel0 = exp(-|d1 - d2|^2 / (4 tau)) / (4 pi tau), and lnU = log(prop_int),
+// or -mu where prop_int < 0 (src/propagator.jl:74-89, src/system.jl:26-28).
+// The reference passes per-component absolute differences (distance.(),
+// src/propagator.jl:6-9), so its |d1 - d2| is taken between the absolute
+// vectors; the physical rules use the signed differences, their own
+// difference wrapped to the minimum image.  Products and sums are rounded
+// separately as in the reference (no fused multiply-add).
+__device__ __forceinline__ double contact_lnU(const ChainDesc &d, double d1x, double d1y,
+                                              double d2x, double d2y) {
+  const double ax = fabs(d1x), ay = fabs(d1y), bx = fabs(d2x), by = fabs(d2y);
+  const double n1 = __dsqrt_rn(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay)));
+  const double n2 = __dsqrt_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)));
+  double ex, ey;
+  if (d.flags & PF_PHYS) {
+    ex = mi1(d1x, d2x, d.L, d.L2);
+    ey = mi1(d1y, d2y, d.L, d.L2);
+  } else {
+    ex = ax - bx;
+    ey = ay - by;
+  }
+  double wx, wy;
+  const int ix = contact_cell(d, n1, wx), iy = contact_cell(d, n2, wy);
+  const int n = d.ct_n;
+  const double *r0 = d.ct_tab + (size_t)ix * n + iy, *r1 = r0 + n;
+  const double c0 = __dadd_rn(__dmul_rn(1.0 - wy, __ldg(r0)), __dmul_rn(wy, __ldg(r0 + 1)));
+  const double c1 = __dadd_rn(__dmul_rn(1.0 - wy, __ldg(r1)), __dmul_rn(wy, __ldg(r1 + 1)));
+  const double T = __dadd_rn(__dmul_rn(1.0 - wx, c0), __dmul_rn(wx, c1));
+  const double dd = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey));
+  const double rel0 = exp(-dd / (4.0 * d.tau)) / (12.566370614359172 * d.tau);
+  const double p = 1.0 + T / rel0;
+  return p < 0.0 ? -d.mu : log(p);
+}
+
+// contact_lnU from the four beads of a link pair (a, b at slice j; an, bn at
+// slice j+1), kept out of line: the Gaussian pair path does not carry its code
+__device__ __noinline__ double contact_link(const ChainDesc &d, double ax, double ay, double bx,
+                                            double by, double anx, double any, double bnx,
+                                            double bny) {
+  const bool two = d.dim > 1;
+  return contact_lnU(d, mi1(ax, bx, d.L, d.L2), two ? mi1(ay, by, d.L, d.L2) : 0.0,
+                     mi1(anx, bnx, d.L, d.L2), two ? mi1(any, bny, d.L, d.L2) : 0.0);
+}
+
 // ---------------------------------------------------------------------------
 // neighbour scans over one slice
 // ---------------------------------------------------------------------------
@@ -384,7 +443,8 @@ constexpr int PQ_CAP = 96;  // queue entries per warp (64-bit)
 
 // one queued entry: the link's two pair exponentials exp(-r^2/2s^2) at its
 // ends, added to the lane's old (so) or new (sn) sum; the caller applies the
-// link weight -tau g / 2 once per segment
+// link weight -tau g / 2 once per segment.  With the contact table the entry
+// is the link's pair action itself (weight 1).
 template <class Seg>
 __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long long e,
                                         double &so, double &sn) {
@@ -394,12 +454,19 @@ __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long
   const int j = s.slice(t), jn = j + 1 == M ? 0 : j + 1;
   double ax, ay, anx, any;
   s.cur(side, t, ax, ay);
-  const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
+  const double bx = c.X(0, b, j), by = c.Xd(1, b, j);
+  const double r2a = mi2(d, ax, ay, bx, by);
   if (r2a > d.rc2) return;
   s.nxt(side, t, anx, any);
   const int bn = j == M - 1 ? c.next[b] : b;
-  const double r2b = mi2(d, anx, any, c.X(0, bn, jn), c.Xd(1, bn, jn));
-  const double v = exp_neg(-r2a * d.inv2s2) + exp_neg(-r2b * d.inv2s2);
+  const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
+  double v;
+  if (d.flags & PF_CONTACT) {
+    v = contact_link(d, ax, ay, bx, by, anx, any, bnx, bny);
+  } else {
+    const double r2b = mi2(d, anx, any, bnx, bny);
+    v = exp_neg(-r2a * d.inv2s2) + exp_neg(-r2b * d.inv2s2);
+  }
   if (side) sn += v; else so += v;
 }
 
@@ -465,8 +532,13 @@ __device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do
                               unsigned long long *q, double &wo, double &wn, int lane) {
   double so = 0.0, sn = 0.0;
   segment_sums(c, s, t0, t1, do_old, do_new, q, so, sn, lane);
-  wo = fma(c.d->mhtau_g, so, wo);
-  wn = fma(c.d->mhtau_g, sn, wn);
+  if (c.d->flags & PF_CONTACT) {
+    wo += so;
+    wn += sn;
+  } else {
+    wo = fma(c.d->mhtau_g, so, wo);
+    wn = fma(c.d->mhtau_g, sn, wn);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -829,7 +901,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   int dec = -1;
   if (phys_pair) {
     WindowSeg seg{&c, n, nx, j0, M, sx_, sy_, sq};
-    if (D::kSweep && !(d.flags & PF_EXACT)) {
+    if (D::kSweep && !(d.flags & (PF_EXACT | PF_CONTACT))) {
       // bounded estimate from the mirror; the exact sums only when its
       // interval straddles the Metropolis threshold
       PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};

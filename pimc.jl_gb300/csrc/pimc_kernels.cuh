@@ -502,7 +502,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   // decision and a sweep skips them (its Metropolis uniform is a pure function
   // of the move's stream).  Injected-draw attempts always evaluate them.
   bool pairs = any_pair;
-  const bool shortcuts = FAST && !(d.flags & PF_EXACT);
+  const bool shortcuts = FAST && !(d.flags & (PF_EXACT | PF_CONTACT));
   if (shortcuts && any_pair && !phys && d.g >= 0.0) {
     double c2[2] = {w2[0], w2[1]};
     G::template sum<2>(c2, red);
@@ -515,11 +515,21 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       const int o1 = own1(t), o1n = own1(t + 1), o2 = own2(t), o2n = own2(t + 1);
       const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
       const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
-      if (r2o <= d.rc2)
-        w2[0] += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
+      if (r2o <= d.rc2) {
+        if (d.flags & PF_CONTACT)
+          w2[0] += contact_link(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j), c.X(0, o1n, jn),
+                                c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn));
+        else
+          w2[0] += lnU2(d, r2o, mi2(d, c.X(0, o1n, jn), c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn)));
+      }
       const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
-      if (r2n <= d.rc2)
-        w2[1] += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+      if (r2n <= d.rc2) {
+        if (d.flags & PF_CONTACT)
+          w2[1] += contact_link(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t], S.r1x[t + 1],
+                                S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]);
+        else
+          w2[1] += lnU2(d, r2n, mi2(d, S.r1x[t + 1], S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]));
+      }
     }
   // the 2m links of the two moving paths in contiguous ranges per warp
   const int per = (2 * m + nwarps - 1) / nwarps;
@@ -787,7 +797,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
     ComSeg seg{&c, pol, idx, M, polymer ? nullptr : q, shx, shy, L, inv2L, cs.qq, qsh};
     const int tot = np * M, per = (tot + nwarps - 1) / nwarps;
     const int t0 = min(tot, warp * per), t1 = min(tot, t0 + per);
-    if (D::kSweep && !(d.flags & PF_EXACT)) {
+    if (D::kSweep && !(d.flags & (PF_EXACT | PF_CONTACT))) {
       // bounded estimate from the mirror; the exact sums only when its
       // interval straddles the Metropolis threshold
       PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
@@ -869,7 +879,8 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
   const int N = c.N, M = c.M, dim = c.dim, tid = G::rank(), nt = G::size();
   const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
   const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
-  const bool pair = (d.flags & PF_PAIR) != 0;
+  // the contact table carries no tau derivative: no pair energy for it
+  const bool pair = (d.flags & PF_PAIR) != 0 && !(d.flags & PF_CONTACT);
   const double rc2 = d.rc * d.rc, cg = d.inv2s2;
   double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // link, pot, vkin, pair, pair virial
   const double inv_bw = density ? 1.0 / d.dens_bw : 0.0;

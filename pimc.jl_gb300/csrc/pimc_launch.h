@@ -101,6 +101,9 @@ constexpr size_t kNoAllocDoubles = 6 * (size_t)kNoAllocBeads +
                                    (size_t)kNoAllocParticles;
 // its device address on the current device (looked up on the first call)
 cudaError_t adjoint_static_scratch(double **ptr);
+// the contact-interaction propagator table T[n][n] for (range, g0, tau)
+cudaError_t launch_contact_table(double *dtab, int n, double range, double g0, double tau,
+                                 cudaStream_t s);
 // measured FP64 FMA throughput of the current device (TFLOP/s)
 cudaError_t fp64_peak(int num_sms, cudaStream_t st, double *tflops);
 // shared scratch of the device move routines (bytes; doubles for a window)

@@ -499,7 +499,11 @@ __global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
         const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
         if (r2a > rc2) continue;
         const int bn = j == M - 1 ? c.next[b] : b;
-        s[2] += lnU2(d, r2a, mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn)));
+        if (d.flags & PF_CONTACT)
+          s[2] += contact_link(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j), bx, by, c.X(0, bn, jn),
+                               c.Xd(1, bn, jn));
+        else
+          s[2] += lnU2(d, r2a, mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn)));
       }
     }
   }
@@ -853,6 +857,94 @@ cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, 
   k_measure<<<nchains, 256, 0, s>>>(desc, var, dpool, ipool, upool, chain0);
   return cudaGetLastError();
 }
+// ---------------------------------------------------------------------------
+// contact-interaction propagator table (build_prop_int, src/propagator.jl:35-89):
+// T(r1, r2) = -I1 - I2 + I3 on the reference's 600 x 600 grid r = 1e-20 + i h,
+// with I = (1/2pi) int_0^inf k exp(-tau k^2) w(k) (Bessel products) dk
+// (Gautier et al., supplementary S28), t(k) = 1/((2/pi)(gamma + log(k/2)) - 4/g0):
+//   I1: w = t^2/(1+t^2), J0(k r1) J0(k r2)
+//   I2: w = t/(1+t^2),   J0(k r1) Y0(k r2) + J0(k r2) Y0(k r1)
+//   I3: w = t^2/(1+t^2), Y0(k r1) Y0(k r2)
+// Composite 8-point Gauss-Legendre in FP64: geometric panels from 1e-10 to 0.5
+// (the log behaviour at k -> 0), then uniform panels of a quarter of the
+// shortest oscillation period up to K with exp(-tau K^2) = 1e-18.  CUDA's j0 /
+// y0 are library calls.  One thread per entry of the upper triangle.
+// ---------------------------------------------------------------------------
+struct ContactQuad {
+  double tau, g0, K, k0, du;
+  int ngraded, nuniform;
+};
+
+// the integrand of the three Bessel integrals (Gautier et al., supplementary
+// S28; src/propagator.jl:50-64) combined, T = (-I1 - I2 + I3) / (2 pi).  With
+// t(k) = 1/s(k), s = (2/pi)(gamma + log(k/2)) - 4/g0, the weights
+// t^2/(1+t^2) = 1/(1+s^2) and t/(1+t^2) = s/(1+s^2) are taken in s, which
+// stays finite where t has its pole.
+__device__ __forceinline__ double contact_integrand(double k, double r1, double r2, const ContactQuad &q) {
+  const double sk = (2.0 / 3.141592653589793) * (0.5772156649015329 + log(0.5 * k)) - 4.0 / q.g0;
+  const double den = 1.0 / (1.0 + sk * sk), wa = den, wb = sk * den;
+  const double J1 = j0(k * r1), J2 = j0(k * r2), Y1 = y0(k * r1), Y2 = y0(k * r2);
+  return k * exp(-q.tau * k * k) * (-wa * J1 * J2 - wb * (J1 * Y2 + J2 * Y1) + wa * Y1 * Y2);
+}
+
+__device__ double contact_entry(double r1, double r2, const ContactQuad &q) {
+  const double xs[4] = {0.18343464249564978, 0.525532409916329, 0.7966664774136267, 0.9602898564975362};
+  const double ws[4] = {0.36268378337836166, 0.3137066458778869, 0.22238103445337443, 0.10122853629037706};
+  double sum = 0.0;
+  auto panel = [&](double a, double b) {
+    const double c = 0.5 * (a + b), hw = 0.5 * (b - a);
+    double ps = 0.0;
+    for (int i = 0; i < 4; ++i)
+      ps += ws[i] * (contact_integrand(c - hw * xs[i], r1, r2, q) + contact_integrand(c + hw * xs[i], r1, r2, q));
+    sum += hw * ps;
+  };
+  double a = 1e-10;
+  for (int p = 0; p < q.ngraded; ++p) {
+    const double b = p + 1 == q.ngraded ? q.k0 : 2.0 * a;
+    panel(a, b);
+    a = b;
+  }
+  for (int p = 0; p < q.nuniform; ++p) panel(q.k0 + p * q.du, q.k0 + (p + 1) * q.du);
+  return sum / (2.0 * 3.141592653589793);
+}
+
+__global__ void k_contact_table(double *tab, int n, double r0, double h, ContactQuad q) {
+  const long long ntri = (long long)n * (n + 1) / 2;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ntri;
+       e += (long long)gridDim.x * blockDim.x) {
+    // row i1 of the upper triangle holds n - i1 entries
+    int i1 = (int)((2.0 * n + 1.0 - sqrt((2.0 * n + 1.0) * (2.0 * n + 1.0) - 8.0 * (double)e)) / 2.0);
+    if (i1 < 0) i1 = 0;
+    while (i1 > 0 && (long long)i1 * (2 * n - i1 + 1) / 2 > e) --i1;
+    while ((long long)(i1 + 1) * (2 * n - i1) / 2 <= e) ++i1;
+    const int i2 = i1 + (int)(e - (long long)i1 * (2 * n - i1 + 1) / 2);
+    const double v = contact_entry(r0 + i1 * h, r0 + i2 * h, q);
+    tab[(size_t)i1 * n + i2] = v;
+    tab[(size_t)i2 * n + i1] = v;
+  }
+}
+
+cudaError_t launch_contact_table(double *dtab, int n, double range, double g0, double tau,
+                                 cudaStream_t s) {
+  ContactQuad q;
+  q.tau = tau;
+  q.g0 = g0;
+  q.K = sqrt(41.5 / tau);
+  q.k0 = 0.5;
+  q.ngraded = 33;  // 1e-10 * 2^32 > 0.5
+  // the Bessel products oscillate with period >= 2 pi / (2 range): quarter
+  // periods per panel
+  const double period = 2.0 * 3.141592653589793 / (2.0 * range);
+  q.nuniform = (int)ceil((q.K - q.k0) / (0.25 * period));
+  if (q.nuniform < 1) q.nuniform = 1;
+  q.du = (q.K - q.k0) / q.nuniform;
+  const double r0 = 1e-20, h = (range - r0) / (n - 1);
+  const long long ntri = (long long)n * (n + 1) / 2;
+  const int blocks = (int)std::min<long long>((ntri + 127) / 128, 65535);
+  k_contact_table<<<blocks, 128, 0, s>>>(dtab, n, r0, h, q);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // FP64 pipe throughput probe: eight independent DFMA chains per thread
 // ---------------------------------------------------------------------------

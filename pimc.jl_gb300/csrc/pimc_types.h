@@ -12,6 +12,7 @@ enum : int {
   PF_LATT = 8,      // square lattice term in V
   PF_HARM = 16,     // harmonic trap term in V
   PF_EXACT = 32,    // sweeps decide every move from exact FP64 sums (no bounded shortcuts)
+  PF_CONTACT = 64,  // pair link action from the tabulated contact propagator (with PF_PAIR)
 };
 
 // move kinds for counters
@@ -58,6 +59,12 @@ struct ChainDesc {
   unsigned key0, key1;  // Philox key
   unsigned chain_tag;   // chain id (low 24 bits of counter word 3)
   int pad_;
+  // tabulated contact propagator (PF_CONTACT): the Bessel-integral terms
+  // T(r1, r2) on the grid r_i = ct_r0 + i ct_h, i < ct_n, row-major
+  // ct_tab[i1 * ct_n + i2]
+  const double *ct_tab;
+  int ct_n, ct_pad_;
+  double ct_r0, ct_h, ct_rmax;
 };
 
 // move mix as seen by the device

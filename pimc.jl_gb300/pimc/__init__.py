@@ -6,16 +6,18 @@ handle wrapper over the C ABI in ``include/pimc.h``; ``pimc.build()``
 compiles the CUDA library for sm_103a.
 """
 from ._native import LIB_PATH, PimcError, build, load
-from .api import (Counter, Density, Energy, GaussianPair, Harmonic, NumbOfSlices, Particle,
-                  PolymerCenterOfMass, PotentialSum, ReshapeLinear, ReshapeSwapLinear,
-                  SingleCenterOfMass, SquareLattice, Step, System, Zero, acceptance, apply, run)
+from .api import (ContactPropagator, Counter, Density, Energy, GaussianPair, Harmonic,
+                  NumbOfSlices, Particle, PolymerCenterOfMass, PotentialSum, ReshapeLinear,
+                  ReshapeSwapLinear, SingleCenterOfMass, SquareLattice, Step, System, Zero,
+                  acceptance, apply, build_prop_int, determine_nnrange, run)
 from .engine import (ACCEPT, HARDCORE, REJECT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams,
-                     Engine, Mix)
+                     Engine, Mix, contact_table)
 
 __all__ = [
     "build", "load", "LIB_PATH", "PimcError", "Engine", "ChainParams", "Mix", "System", "Particle",
     "Harmonic", "SquareLattice", "PotentialSum", "Zero", "GaussianPair", "ReshapeLinear",
     "ReshapeSwapLinear", "SingleCenterOfMass", "PolymerCenterOfMass", "Counter", "Step",
     "NumbOfSlices", "acceptance", "run", "apply", "Density", "Energy", "SEM_REFERENCE",
-    "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE",
+    "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE", "ContactPropagator",
+    "build_prop_int", "determine_nnrange", "contact_table",
 ]

@@ -155,6 +155,11 @@ SIGNATURES = {
     "pimc_state_size": [_vp, C.POINTER(C.c_size_t)],
     "pimc_get_state": [_vp, C.c_void_p, C.c_size_t],
     "pimc_set_state": [_vp, C.c_void_p, C.c_size_t],
+    "pimc_contact_table": [C.c_double, C.c_double, C.c_double, C.c_int, _dp],
+    "pimc_set_contact_propagator": [_vp, C.c_int, C.c_double, C.c_double, C.c_int],
+    "pimc_set_contact_table": [_vp, C.c_int, _dp, C.c_int, C.c_double],
+    "pimc_get_contact_table": [_vp, C.c_int, _dp, C.c_size_t, _ip, _dp],
+    "pimc_clear_contact": [_vp, C.c_int],
     "pimc_fp64_peak": [_vp, _dp],
     "pimc_last_run_ms": [_vp, _dp],
     "pimc_last_run_launches": [_vp, C.POINTER(C.c_longlong)],

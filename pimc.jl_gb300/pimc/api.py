@@ -23,7 +23,7 @@ from collections import deque
 import numpy as np
 
 from .engine import (ACCEPT, HARDCORE, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams, Engine,
-                     Mix, PimcError)
+                     Mix, PimcError, contact_table)
 
 
 # --------------------------------------------------------------- potentials
@@ -96,6 +96,77 @@ class GaussianPair:
         return math.exp(-0.5 * tau * (self.v(float(np.linalg.norm(r1))) + self.v(float(np.linalg.norm(r2)))))
 
 
+class ContactPropagator:
+    """build_prop_int(L, g0, tau) (src/propagator.jl:35-89): the contact
+    interaction's propagator prop_int(r1, r2, tau) = 1 + T(|r1|, |r2|) /
+    prop_rel0(r1, r2, tau), T bilinear in a table over [1e-20, L]^2 whose n x n
+    Bessel integrals are computed on the device.  As the pair propagator of a
+    System it runs on the device; calling it evaluates the same formula on
+    the host (the reference's determine_nnrange calls it at set-up)."""
+
+    def __init__(self, L: float, g0: float, τ: float, n: int = 600, table=None):
+        self.range, self.g0, self.tau, self.n = float(L), float(g0), float(τ), int(n)
+        if table is None:
+            table = contact_table(self.g0, self.tau, self.range, self.n)
+        self.table = np.ascontiguousarray(table, dtype=np.float64)
+        if self.table.shape != (self.n, self.n):
+            raise PimcError("the contact table must be n x n")
+        self._h = (self.range - 1e-20) / (self.n - 1)
+
+    def terms(self, r1: float, r2: float) -> float:
+        """T(r1, r2) by the linear B-spline of the table (radii clamped)"""
+        def cell(r):
+            r = min(max(r, 1e-20), self.range)
+            p = (r - 1e-20) / self._h
+            f = min(math.floor(p), self.n - 2)
+            return f, p - f
+        i, wx = cell(float(r1))
+        j, wy = cell(float(r2))
+        t = self.table
+        c0 = (1.0 - wy) * t[i, j] + wy * t[i, j + 1]
+        c1 = (1.0 - wy) * t[i + 1, j] + wy * t[i + 1, j + 1]
+        return (1.0 - wx) * c0 + wx * c1
+
+    def __call__(self, r1_rel, r2_rel, τ):
+        r1 = np.asarray(r1_rel, dtype=np.float64)
+        r2 = np.asarray(r2_rel, dtype=np.float64)
+        d = r1 - r2
+        rel0 = math.exp(-float(np.dot(d, d)) / (4 * τ)) / (4 * math.pi * τ)
+        return 1.0 + self.terms(float(np.linalg.norm(r1)), float(np.linalg.norm(r2))) / rel0
+
+
+def build_prop_int(L: float, g0: float, τ: float, n: int = 600) -> ContactPropagator:
+    """build_prop_int (src/propagator.jl:79-89); L is the table's range"""
+    return ContactPropagator(L, g0, τ, n)
+
+
+def determine_nnrange(propint, τ: float, a: float, b: float) -> float:
+    """determine_nnrange (src/system.jl:10-15): the radius r > r_min where
+    propint([r], [r], tau) = 0.999, r_min the minimiser of that curve.  The
+    minimiser is taken on the table's grid (the reference runs Nelder-Mead
+    from a); the root is bisected to the last bit, as Roots.Bisection does."""
+    f = lambda r: propint([r], [r], τ) - 0.999
+    grid = np.linspace(a, b, 4097)
+    vals = np.array([f(r) for r in grid])
+    lo = float(grid[int(np.argmin(vals))])
+    hi = float(b)
+    flo, fhi = f(lo), f(hi)
+    if flo * fhi > 0:
+        raise PimcError("determine_nnrange: propint - 0.999 has no sign change on (r_min, b)")
+    while True:
+        mid = 0.5 * (lo + hi)
+        if mid <= lo or mid >= hi:
+            break
+        fm = f(mid)
+        if fm == 0.0:
+            return mid
+        if (fm < 0) == (flo < 0):
+            lo, flo = mid, fm
+        else:
+            hi = mid
+    return lo if abs(flo) <= abs(f(hi)) else hi
+
+
 def _potential_terms(potential):
     omega, V0, a = 0.0, 0.0, 1.0
     terms = potential.terms if isinstance(potential, PotentialSum) else (potential,)
@@ -137,12 +208,20 @@ class System:
                                    or dV in ("grad", np.asarray) or callable(dV)):
             raise PimcError("dV must be the potential's gradient")
         pair_g, pair_sigma = 0.0, 1.0
+        contact = None
         if interactions:
-            if not isinstance(propint, GaussianPair):
-                raise PimcError("interactions=True needs propint=GaussianPair(g, sigma)")
-            pair_g, pair_sigma = propint.g, propint.sigma
-            if ra == 0.0:
-                raise PimcError("pass ra (the neighbour range); determine_nnrange is not ported")
+            if isinstance(propint, GaussianPair):
+                pair_g, pair_sigma = propint.g, propint.sigma
+                if ra == 0.0:
+                    raise PimcError("pass ra (the neighbour range) with a GaussianPair")
+            elif isinstance(propint, ContactPropagator):
+                contact = propint
+                if ra == 0.0:
+                    # init_int (src/system.jl:17-34)
+                    ra = determine_nnrange(propint, 1.0 / (T * M), 1e-20, L)
+            else:
+                raise PimcError("interactions=True needs propint=GaussianPair(g, sigma) or "
+                                "build_prop_int(L, g0, tau)")
         self.dim, self.M, self.N, self.Ninit = dim, M, N, N
         self.μ, self.λ, self.L = μ, λ, L
         self.vol = (2 * L) ** dim
@@ -164,8 +243,14 @@ class System:
                                lattice_V0=V0, lattice_a=a, interactions=interactions,
                                pair_g=pair_g, pair_sigma=pair_sigma, r_a=ra,
                                hardcore_a=self.a, semantics=semantics, seed=seed)
+        self._contact = contact
         self.engine = Engine(self._cp)
+        self._attach_contact()
         self._eser_seen = 0
+
+    def _attach_contact(self):
+        if self._contact is not None:
+            self.engine.set_contact_table(self._contact.table, self._contact.range)
 
     # System() already ran init_world on the device
     @property
@@ -189,6 +274,7 @@ class System:
         cp.energy_capacity = max(cp.energy_capacity, energy_capacity)
         self.engine.close()
         self.engine = Engine(cp)
+        self._attach_contact()
         self.engine.set_raw(x, V, nx)
         self._eser_seen = 0
 

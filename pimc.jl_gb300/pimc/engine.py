@@ -24,6 +24,15 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+def contact_table(g0: float, tau: float, range_: float, n: int = 600) -> np.ndarray:
+    """The integral terms T[i1, i2] of the contact-interaction propagator on
+    the grid r_i = 1e-20 + i (range_ - 1e-20)/(n - 1), computed on the device
+    (prop_rel_interpolate_terms, src/propagator.jl:36-73)"""
+    out = np.empty((n, n))
+    check(load().pimc_contact_table(float(g0), float(tau), float(range_), int(n), _dp(out)))
+    return out
+
+
 def _ip(a):
     return a.ctypes.data_as(C.POINTER(C.c_int))
 
@@ -334,6 +343,33 @@ class Engine:
         th, ex = np.zeros(3), np.zeros(4)
         check(self.L.pimc_adjoint(self.h, chain, _dp(g) if want_beads else None, _dp(th), _dp(ex)))
         return g, th, ex
+
+    # ------------------------------------------------------------- contact propagator
+    def set_contact_propagator(self, g0: float, range_: float, n: int = 600, chain: int = -1):
+        """build_prop_int(range_, g0, tau) on the device as the pair propagator
+        of a chain (chain < 0: all), tau the chain's own"""
+        check(self.L.pimc_set_contact_propagator(self.h, chain, float(g0), float(range_), int(n)))
+
+    def set_contact_table(self, table, range_: float, chain: int = -1):
+        """a caller-made table T[i1, i2] on the grid 1e-20 .. range_"""
+        t = np.ascontiguousarray(table, dtype=np.float64)
+        if t.ndim != 2 or t.shape[0] != t.shape[1]:
+            raise PimcError("the contact table must be square")
+        check(self.L.pimc_set_contact_table(self.h, chain, _dp(t), t.shape[0], float(range_)))
+
+    def contact_table(self, chain: int = 0):
+        """(table, range) of the chain's contact propagator, or (None, 0.0)"""
+        n, rng = C.c_int(), C.c_double()
+        check(self.L.pimc_get_contact_table(self.h, chain, None, 0, C.byref(n), C.byref(rng)))
+        if n.value == 0:
+            return None, 0.0
+        out = np.empty((n.value, n.value))
+        check(self.L.pimc_get_contact_table(self.h, chain, _dp(out), out.size, C.byref(n),
+                                            C.byref(rng)))
+        return out, rng.value
+
+    def clear_contact(self, chain: int = -1):
+        check(self.L.pimc_clear_contact(self.h, chain))
 
     def set_potential(self, V0, omega, g, chain=0):
         check(self.L.pimc_set_potential(self.h, chain, V0, omega, g))

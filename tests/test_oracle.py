@@ -158,3 +158,83 @@ def test_physical_weights_are_action_differences(oracle_mod):
         a1 = o2.eval_action()
         dS = (a1[1] + a1[2]) - (a0[1] + a0[2])
         assert abs((wu - wi) - dS) < 1e-11 * max(1.0, abs(dS))
+
+
+def _contact_lnU_formula(tab, R, tau, mu, d1, d2, physical, L):
+    """build_prop_int's prop_int (src/propagator.jl:74-89) and lnU
+    (src/system.jl:26-28) restated with scipy's grid interpolator"""
+    from scipy.interpolate import RegularGridInterpolator
+    n = tab.shape[0]
+    grid = 1e-20 + np.arange(n) * ((R - 1e-20) / (n - 1))
+    itp = RegularGridInterpolator((grid, grid), tab, method="linear")
+    a, b = np.abs(d1), np.abs(d2)
+    r1 = min(max(float(np.sqrt(a @ a)), grid[0]), R)
+    r2 = min(max(float(np.sqrt(b @ b)), grid[0]), R)
+    if physical:
+        e = d1 - d2
+        e = np.where(np.abs(e) > L, e - np.sign(e) * 2 * L, e)
+    else:
+        e = a - b
+    rel0 = math.exp(-float(e @ e) / (4 * tau)) / (4 * math.pi * tau)
+    p = 1.0 + float(itp([[r1, r2]])[0]) / rel0
+    return -mu if p < 0 else math.log(p)
+
+
+def test_oracle_contact_lnU(oracle_mod):
+    """the oracle's tabulated contact lnU against an independent restatement:
+    linear interpolation on the reference's grid, per-component absolute
+    differences (reference rules) or wrapped signed ones (physical rules),
+    -mu where prop_int < 0, radii clamped to the table"""
+    O = oracle_mod
+    L = O.lib()
+    dp = lambda v: v.ctypes.data_as(O.C.POINTER(O.C.c_double))
+    rng = np.random.default_rng(3)
+    n, R, Lh, mu = 12, 2.0, 1.5, 0.7
+    tab = rng.normal(size=(n, n))
+    tab = tab + tab.T
+    for sem in (O.SEM_REFERENCE, O.SEM_PHYSICAL):
+        p = O.make_params(dim=2, N=2, M=8, L=Lh, T=2.0, interactions=True, r_a=0.5, semantics=sem,
+                          mu=mu, contact_table=tab, contact_range=R)
+        tau = p.tau
+        branches = set()
+        for _ in range(300):
+            d1 = rng.uniform(-Lh, Lh, 2)
+            d2 = rng.uniform(-Lh, Lh, 2) * rng.choice([0.05, 1.0])
+            got = L.orc_lnU(O.C.byref(p), dp(d1), dp(d2))
+            want = _contact_lnU_formula(tab, R, tau, mu, d1, d2, sem == O.SEM_PHYSICAL, Lh)
+            assert abs(got - want) <= 1e-12 * max(1.0, abs(want)), (sem, d1, d2, got, want)
+            branches.add(got == -mu)
+        assert branches == {True, False}
+    # radii beyond the table clamp to its last row and column
+    p = O.make_params(dim=2, N=2, M=8, L=4.0, T=2.0, interactions=True, r_a=0.5, mu=mu,
+                      contact_table=tab, contact_range=R)
+    d1, d2 = np.array([3.0, 1.0]), np.array([2.9, 1.1])
+    got = L.orc_lnU(O.C.byref(p), dp(d1), dp(d2))
+    assert abs(got - _contact_lnU_formula(tab, R, p.tau, mu, d1, d2, False, 4.0)) <= 1e-12
+
+
+def test_contact_propagator_host_and_nnrange(oracle_mod):
+    """pimc.build_prop_int's host evaluation is the oracle's prop_int, and
+    determine_nnrange finds the 0.999 crossing (src/system.jl:10-15)"""
+    import pimc
+    O = oracle_mod
+    L = O.lib()
+    dp = lambda v: v.ctypes.data_as(O.C.POINTER(O.C.c_double))
+    rng = np.random.default_rng(5)
+    n, R = 40, 3.0
+    tab = -np.abs(rng.normal(scale=0.05, size=(n, n)))
+    tab = tab + tab.T
+    p = O.make_params(dim=2, N=2, M=8, L=2.0, T=2.0, interactions=True, r_a=0.5, mu=0.0,
+                      contact_table=tab, contact_range=R)
+    prop = pimc.ContactPropagator(R, 1.0, p.tau, n=n, table=tab)
+    for _ in range(100):
+        d1, d2 = rng.uniform(0, 2.0, 2), rng.uniform(0, 2.0, 2)
+        v = prop(d1, d2, p.tau)
+        lnu = L.orc_lnU(O.C.byref(p), dp(d1), dp(d2))
+        if v > 0:
+            assert abs(math.log(v) - lnu) <= 1e-12 * max(1.0, abs(lnu))
+        else:
+            assert lnu == 0.0
+    f = lambda r1, r2, t: 1.0 - 0.5 * math.exp(-float(np.asarray(r1)[0]) ** 2)
+    r = pimc.determine_nnrange(f, 0.1, 1e-20, 4.0)
+    assert abs(r - math.sqrt(math.log(500.0))) < 1e-12
