@@ -44,6 +44,8 @@ SEED = 20261203
 
 # --------------------------------------------------------------------- workloads
 PLAIN_STRIDE = 16
+# the contact workload's propagator: build_prop_int(12, 1.16, tau)
+CONTACT_G0, CONTACT_RANGE = 1.16, 12.0
 # per bead update of k_sweep on the first 1216 C4 chains (block 128, ncu
 # --set full), by acceptance semantics: DRAM bytes (dram__bytes_read.sum +
 # dram__bytes_write.sum) and FP64 flops (dadd + dmul + 2 dfma thread
@@ -104,6 +106,17 @@ def workload(name, semantics):
                                   energy_capacity=0))
         mixes.append(mix_for(256, 64, 16, 8.0, 1))
         desc = "C3 plain: 2D trapped bosons, Gaussian pair g=1 sigma=0.5, N=256, beta=2, M=64"
+    elif name == "contact":
+        # the C4 list's particle numbers at one temperature and slice count, so
+        # that every chain shares one contact table (tau = 1/32)
+        for i, c in enumerate(c4_chain_list()[:1024]):
+            chains.append(ChainParams(dim=2, N=c["N"], M=64, L=8.0, T=0.5, lam=0.5,
+                                      harmonic_omega=1.0, interactions=True, r_a=1.5,
+                                      semantics=semantics, seed=SEED + i, energy_capacity=0))
+            mixes.append(mix_for(c["N"], 64, 16, 8.0, 10))
+        desc = ("contact: 1024 trapped-gas chains, N~U{8..512} (the C4 list), M=64, beta=2, "
+                "tabulated contact propagator g0=1.16 (600x600 table over [1e-20, 12], built on "
+                "the device), omega=1, L=8, cell 1.6, staging l=16, N swaps + 1 CoM phase")
     elif name == "c5":
         chains.append(ChainParams(dim=2, N=1024, M=64, L=16.0, T=0.25, lam=0.5, harmonic_omega=0.1,
                                   lattice_V0=4.0, lattice_a=1.0, interactions=True, pair_g=1.0,
@@ -221,9 +234,11 @@ def pinned_empty(n):
 
 
 # --------------------------------------------------------------------- CPU legs
-def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, threads=None):
+def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, threads=None,
+                    contact=None):
     """the CPU oracle (C restatement of the reference's sweep) on a bounded
-    sample of the workload's chains, one chain per host thread"""
+    sample of the workload's chains, one chain per host thread; contact =
+    (table, range) gives every chain the tabulated contact propagator"""
     import concurrent.futures as cf
     from oracle import oracle as O
     O.build()
@@ -237,7 +252,9 @@ def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, th
         p = O.make_params(dim=c.dim, N=c.N, M=c.M, L=c.L, T=c.T, lam=c.lam,
                           hcoef=0.5 * c.harmonic_omega ** 2, V0=c.lattice_V0, lat_a=c.lattice_a,
                           pair_g=c.pair_g, pair_sigma=c.pair_sigma, interactions=c.interactions,
-                          r_a=c.r_a, semantics=semantics)
+                          r_a=c.r_a, semantics=semantics, mu=c.mu,
+                          contact_table=None if contact is None else contact[0],
+                          contact_range=0.0 if contact is None else contact[1])
         return O.bench_chains(p, 1, 1, attempts, m.stage_slices, 1.0, SEED + int(i))
 
     # calibrate: one sweep's worth of attempts (N(k+2)) on each sampled chain
@@ -265,10 +282,38 @@ def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, th
     return beads / wall, threads, sample
 
 
+def cpu_contact_table_rate(g0, chain, range_, budget_s=4.0):
+    """entries per second of the contact table by adaptive quadrature of the
+    reference's integrals on one host core (oracle/contact_table.py), on a
+    bounded sample of entries spread over the table"""
+    from oracle import contact_table as CT
+    tau = 1.0 / (chain.T * chain.M)
+    r = CT.grid(range_, 600)
+    rng = np.random.default_rng(SEED)
+    t0 = time.perf_counter()
+    done = 0
+    while time.perf_counter() - t0 < budget_s and done < 400:
+        i1, i2 = (int(v) for v in rng.integers(0, 600, size=2))
+        CT.entry(float(r[i1]), float(r[i2]), g0, tau)
+        done += 1
+    wall = time.perf_counter() - t0
+    rate = done / wall
+    return {"entries_per_s": rate, "cores": 1, "kind": "port",
+            "full_table_s_estimate": 600 * 601 / 2 / rate,
+            "sample": f"{done} random entries in {wall:.1f} s, scipy QUADPACK on the "
+                      "reference's integrand (the reference uses QuadGK)"}
+
+
 # --------------------------------------------------------------------- arms
 def run_reference(args):
     ws, rank, local, pg = dist_setup()
     if rank != 0:
+        return 0
+    if args.workload == "contact":
+        print(json.dumps({"impl": "reference", "unavailable": (
+            "the contact workload's 600x600 table is built on the device (a CPU build by "
+            "adaptive quadrature takes hours); its CPU sweep rate is the cpu_baseline of "
+            "the engine's line")}))
         return 0
     chains, mixes, desc = workload(args.workload, 0)
     rates = []
@@ -312,6 +357,13 @@ def run_ours(args):
     eng = Engine(chains)
     for i, m in enumerate(mixes):
         eng.set_mix(m, chain=i)
+    table = None
+    if args.workload == "contact":
+        t0 = time.perf_counter()
+        eng.set_contact_propagator(CONTACT_G0, CONTACT_RANGE)
+        table = {"build_s": time.perf_counter() - t0, "entries": 600 * 600,
+                 "path": "pimc_set_contact_propagator: composite Gauss-Legendre in FP64 on the "
+                         "device, one thread per upper-triangle entry"}
     batched = len(chains) > 1
     run = eng.run_batched if batched else eng.run
     launch = None
@@ -450,8 +502,15 @@ def run_ours(args):
         c = chains[0]
         out["adjoint"] = {"beads": c.N * c.M, "ms_per_call": at * 1e3,
                           "bead_gradients_per_s": c.N * c.M / at}
+    contact = eng.contact_table(0) if args.workload == "contact" else None
+    if table is not None:
+        out["contact_table"] = table
+        if rank == 0 and not args.no_cpu:
+            out["contact_table"]["cpu"] = cpu_contact_table_rate(CONTACT_G0, chains[0],
+                                                                 CONTACT_RANGE)
     if rank == 0 and not args.no_cpu:
-        r, cores, sample = cpu_oracle_rate(chains, mixes, sem, budget_s=args.cpu_budget)
+        r, cores, sample = cpu_oracle_rate(chains, mixes, sem, budget_s=args.cpu_budget,
+                                           contact=contact)
         out["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": "C restatement of PIMC.jl's sweep (same semantics), "
                                          + sample}
@@ -466,7 +525,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4", "c5"])
+    ap.add_argument("--workload", default="c4", choices=["c1", "c2", "c3", "c4", "c5", "contact"])
     # the library's default (the drop-in keeps the reference's acceptance
     # rules); "physical" adds the pair action to every move
     ap.add_argument("--semantics", default="reference", choices=["physical", "reference"])

@@ -10,7 +10,8 @@ examples and tests): `System`, `ReshapeLinear`, `ReshapeSwapLinear`,
 `acceptance`, `Density`, `Energy`, `Counter`, `Step`, `NumbOfSlices`.
 Julia closures cannot cross the ABI: the potential must be built from
 `Harmonic`, `SquareLattice` (and their sum), the interaction propagator from
-`GaussianPair`; any other closure raises (there is no CPU fallback).
+`GaussianPair` or `build_prop_int` (the tabulated contact propagator, its table
+built on the device); any other closure raises (there is no CPU fallback).
 Slices and particles are 1-based on this side as in the reference.
 
 This file is written against the header and the Python mirror
@@ -20,10 +21,12 @@ toolchain exists on the build machines, so it is not executed there.
 module Pimc
 
 using ChainRulesCore
+using LinearAlgebra
 
 export System, run!, apply!, acceptance, ReshapeLinear, ReshapeSwapLinear,
        SingleCenterOfMass, PolymerCenterOfMass, Density, Energy, Counter, Step,
-       NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients
+       NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients,
+       build_prop_int, ContactPropagator, determine_nnrange
 
 const libpimc = get(ENV, "PIMC_GB300_LIB",
                     joinpath(@__DIR__, "..", "..", "..", "lib", "libpimc_gb300.so"))
@@ -80,6 +83,68 @@ struct GaussianPair; g::Float64; sigma::Float64; end
     exp(-tau / 2 * (gp.g * exp(-sum(abs2, r1) / (2gp.sigma^2)) +
                     gp.g * exp(-sum(abs2, r2) / (2gp.sigma^2))))
 
+"""
+    build_prop_int(L, g0, τ; n = 600)
+
+The contact-interaction propagator of the reference (src/propagator.jl:35-89):
+the n x n table of its Bessel integrals over the radii range(1e-20, L, n),
+computed on the device (`pimc_contact_table`), and a callable
+`prop_int(r1_rel, r2_rel, τ) = 1 + T(|r1|, |r2|) / prop_rel0(r1, r2, τ)` by
+linear interpolation of it.  As a System's `propint` it runs on the device.
+"""
+struct ContactPropagator
+    range::Float64; g0::Float64; tau::Float64; n::Int; table::Matrix{Float64}
+end
+function build_prop_int(L::Float64, g0::Float64, τ::Float64; n::Int = 600)
+    t = Matrix{Float64}(undef, n, n)
+    check(ccall((:pimc_contact_table, libpimc), Cint,
+                (Cdouble, Cdouble, Cdouble, Cint, Ptr{Cdouble}), g0, τ, L, n, t))
+    return ContactPropagator(L, g0, τ, n, t)   # symmetric: row- and column-major agree
+end
+function contact_terms(cp::ContactPropagator, r1::Float64, r2::Float64)
+    h = (cp.range - 1e-20) / (cp.n - 1)
+    function cell(r)
+        p = (clamp(r, 1e-20, cp.range) - 1e-20) / h
+        f = min(floor(p), cp.n - 2)
+        return Int(f) + 1, p - f
+    end
+    (i, wx), (j, wy) = cell(r1), cell(r2)
+    t = cp.table
+    c0 = (1 - wy) * t[i, j] + wy * t[i, j+1]
+    c1 = (1 - wy) * t[i+1, j] + wy * t[i+1, j+1]
+    return (1 - wx) * c0 + wx * c1
+end
+(cp::ContactPropagator)(r1_rel, r2_rel, τ) =
+    1 + contact_terms(cp, norm(r1_rel), norm(r2_rel)) /
+        (exp(-dot(r1_rel - r2_rel, r1_rel - r2_rel) / (4τ)) / (4π * τ))
+
+"""
+    determine_nnrange(propint, τ, a, b)
+
+The radius r where `propint([r], [r], τ) = 0.999` above the curve's minimum
+(src/system.jl:10-15): the minimiser on a 4097-point grid of [a, b], then
+bisection to the last bit.
+"""
+function determine_nnrange(propint, τ::Float64, a::Float64, b::Float64)
+    f(r) = propint([r], [r], τ) - 0.999
+    rs = range(a, b, length = 4097)
+    lo, hi = rs[argmin(f.(rs))], b
+    flo = f(lo)
+    flo * f(hi) > 0 && error("determine_nnrange: no sign change on (r_min, b)")
+    while true
+        mid = (lo + hi) / 2
+        (mid <= lo || mid >= hi) && break
+        fm = f(mid)
+        fm == 0 && return mid
+        if (fm < 0) == (flo < 0)
+            lo, flo = mid, fm
+        else
+            hi = mid
+        end
+    end
+    return abs(flo) <= abs(f(hi)) ? lo : hi
+end
+
 function potential_terms(V)
     omega, V0, a = 0.0, 0.0, 1.0
     for t in (V isa PotentialSum ? V.terms : [V])
@@ -116,9 +181,15 @@ function System(potential; dV = zero, dim::Int64 = 2, M::Int64 = 100, N::Int64 =
     omega, V0, a_lat = potential_terms(potential)
     pg, ps = 0.0, 1.0
     if interactions
-        propint isa GaussianPair || error("interactions=true needs propint = GaussianPair(g, σ)")
-        rₐ > 0 || error("pass rₐ (determine_nnrange is not ported)")
-        pg, ps = propint.g, propint.sigma
+        if propint isa GaussianPair
+            rₐ > 0 || error("pass rₐ with a GaussianPair")
+            pg, ps = propint.g, propint.sigma
+        elseif propint isa ContactPropagator
+            # init_int (src/system.jl:17-34)
+            rₐ == 0.0 && (rₐ = determine_nnrange(propint, 1 / (T * M), 1e-20, L))
+        else
+            error("interactions=true needs propint = GaussianPair(g, σ) or build_prop_int(L, g0, τ)")
+        end
     end
     a = interactions && g > 0 ? exp(-2π / g) : 0.0
     p = PimcParams(dim, N, M, L, T, λ, μ, omega, V0, a_lat, interactions, pg, ps, rₐ, a,
@@ -129,6 +200,12 @@ function System(potential; dV = zero, dim::Int64 = 2, M::Int64 = 100, N::Int64 =
                propint, a, 10_000, measure_scheme, Dict(N => 0), Dict(N => 0),
                length_measurement_cycle, p, 0)
     finalizer(s -> ccall((:pimc_destroy, libpimc), Cint, (Ptr{Cvoid},), s.handle), s)
+    if interactions && propint isa ContactPropagator
+        tab = Matrix(transpose(propint.table))   # the C side reads it row-major
+        check(ccall((:pimc_set_contact_table, libpimc), Cint,
+                    (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cdouble),
+                    s.handle, -1, tab, propint.n, propint.range))
+    end
     return s
 end
 

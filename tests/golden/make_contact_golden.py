@@ -11,11 +11,10 @@ r_i = 1e-20 + i (range - 1e-20)/(n - 1),
                  + t^2/(1+t^2) Y0(k r1) Y0(k r2) ] dk,
     t(k) = 1 / ((2/pi)(gamma + log(k/2)) - 4/g0)
 
-(Gautier et al., supplementary S28), with QuadGK at rtol 1e-11.  This script
-restates that formula, integrates it panel by panel (graded panels near
-k = 0, quarter-period panels of the Bessel products above) to
-sqrt(50/tau), where the Gaussian factor is below 2e-22, and records the
-values.  The reference's stored tables (JLD2 files under Store/) are not part
+(Gautier et al., supplementary S28), with QuadGK at rtol 1e-11.  The values
+come from oracle/contact_table.py, which integrates that formula adaptively
+with scipy's QUADPACK (the device uses a fixed composite Gauss-Legendre
+rule).  The reference's stored tables (JLD2 files under Store/) are not part
 of its repository, so these entries pin the engine's device table instead.
 
 The configurations are the reference's own: g0 = 1.16, tau = 0.01, range 6
@@ -26,14 +25,12 @@ tau = 1/(T M) = 1/(0.2 * 200), range ceil(sqrt(8^2 + 8^2)) = 12
 Run from the repository root: python tests/golden/make_contact_golden.py
 """
 import json
-import math
 import os
+import sys
 
-import numpy as np
-from scipy import integrate, special
-
-EULER_GAMMA = 0.57721566490153286
 HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+from oracle.contact_table import entry, grid  # noqa: E402
 
 CONFIGS = [
     dict(g0=1.16, tau=0.01, range=6.0, n=600),
@@ -50,39 +47,13 @@ INDEX_PAIRS = [
 ]
 
 
-def integrand(k, r1, r2, g0, tau):
-    t = 1.0 / ((2.0 / math.pi) * (EULER_GAMMA + math.log(k / 2.0)) - 4.0 / g0)
-    wa = t * t / (1.0 + t * t)
-    wb = t / (1.0 + t * t)
-    j1, j2 = special.j0(k * r1), special.j0(k * r2)
-    y1, y2 = special.y0(k * r1), special.y0(k * r2)
-    return k * math.exp(-tau * k * k) * (-wa * j1 * j2 - wb * (j1 * y2 + j2 * y1) + wa * y1 * y2)
-
-
-def entry(r1, r2, g0, tau):
-    kmax = math.sqrt(50.0 / tau)
-    edges = [0.0, 1e-14, 1e-12, 1e-10, 1e-8, 1e-6, 1e-4, 1e-3, 1e-2, 0.1, 0.5]
-    width = min(0.5, math.pi / (2.0 * (r1 + r2) + 1e-300))
-    k = 0.5
-    while k < kmax:
-        k = min(kmax, k + width)
-        edges.append(k)
-    total = 0.0
-    for a, b in zip(edges[:-1], edges[1:]):
-        v, _ = integrate.quad(integrand, a, b, args=(r1, r2, g0, tau), epsabs=1e-20,
-                              epsrel=1e-14, limit=200)
-        total += v
-    return total / (2.0 * math.pi)
-
-
 def main():
     out = {"generator": "tests/golden/make_contact_golden.py", "configs": []}
     for c in CONFIGS:
-        n, rng = c["n"], c["range"]
-        grid = 1e-20 + np.arange(n) * ((rng - 1e-20) / (n - 1))
+        r = grid(c["range"], c["n"])
         ents = []
         for i1, i2 in INDEX_PAIRS:
-            v = entry(float(grid[i1]), float(grid[i2]), c["g0"], c["tau"])
+            v = entry(float(r[i1]), float(r[i2]), c["g0"], c["tau"])
             ents.append([i1, i2, v])
             print(c["g0"], i1, i2, v, flush=True)
         out["configs"].append(dict(c, entries=ents))
