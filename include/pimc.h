@@ -27,7 +27,9 @@
 extern "C" {
 #endif
 
-#define PIMC_ABI_VERSION 1
+#define PIMC_ABI_VERSION 2
+/* columns of an observable row (pimc_get_observables) */
+#define PIMC_NOBS 8
 
 enum {
   PIMC_OK = 0,
@@ -209,6 +211,25 @@ int pimc_get_energy_sums(void *handle, int chain, double *sum, double *sumsq,
                          unsigned long long *count);
 /* Density (measurement.jl:45-55): nb^dim counts (column-major) and ndata */
 int pimc_get_density(void *handle, int chain, double *hist, unsigned long long *ndata);
+/* the estimators the reference leaves as TODOs (measurement.jl:125-127),
+ * measured with every Energy row: rows of PIMC_NOBS = E_th, E_v, pair
+ * energy, pair virial energy, W^2 (squared total minimum-image displacement
+ * of all links: the winding estimator, rho_s/rho = <W^2> / (2 dim lambda
+ * beta N) in a periodic box), A_z (1/2 sum over links of x dy - y dx: the
+ * area estimator about the origin, rho_s/rho = 2 <A_z^2> / (lambda beta
+ * <sum r^2 / M>) in a trap), sum r^2 / M, 0 */
+int pimc_get_observables(void *handle, int chain, double *out, int cap, int *count);
+/* running sums of the observables: sum[PIMC_NOBS], sumsq[PIMC_NOBS], count */
+int pimc_get_observable_sums(void *handle, int chain, double *sum, double *sumsq,
+                             unsigned long long *count);
+/* radial distribution: every measurement adds, for each slice, every
+ * unordered pair with minimum-image distance r to bin floor(r / dr),
+ * dr = rmax / nbins (rmax 0: L), bins past nbins dropped.  chain < 0: every
+ * chain; nbins 0 switches it off.  Setting it clears the histograms. */
+int pimc_set_radial(void *handle, int chain, int nbins, double rmax);
+/* the pair counts (nbins) and the number of measurements they hold; g(r) =
+ * hist[k] / (nmeas M N(N-1)/2 * shell(k) / (2L)^dim) */
+int pimc_get_radial(void *handle, int chain, double *hist, unsigned long long *nmeas);
 int pimc_reset_measurements(void *handle);
 
 /* ---------------- adjoint: per-bead dS_pot/dr and dS/d(V0, omega, g) */

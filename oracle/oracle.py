@@ -106,6 +106,8 @@ def lib():
         L.orc_polymer_com.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(Draws)]
         L.orc_energy.argtypes = [C.c_void_p, dp]
         L.orc_density.argtypes = [C.c_void_p, C.c_int, dp]
+        L.orc_superfluid.argtypes = [C.c_void_p, dp]
+        L.orc_radial.argtypes = [C.c_void_p, C.c_int, C.c_double, dp]
         L.orc_rng_init.argtypes = [C.POINTER(Rng), C.c_uint64, C.c_uint64]
         L.orc_rng_uniform.restype = C.c_double
         L.orc_rng_uniform.argtypes = [C.POINTER(Rng)]
@@ -271,6 +273,18 @@ class Oracle:
         out = np.zeros(4)
         self.L.orc_energy(self.h, _dp(out))
         return out
+
+    def superfluid(self):
+        """W^2, A_z, sum r^2 / M of the current configuration"""
+        out = np.zeros(3)
+        self.L.orc_superfluid(self.h, _dp(out))
+        return out
+
+    def radial(self, nb, dr, hist=None):
+        if hist is None:
+            hist = np.zeros(nb)
+        self.L.orc_radial(self.h, nb, dr, _dp(hist))
+        return hist
 
     def density(self, nb, hist=None):
         if hist is None:

@@ -896,6 +896,47 @@ static void pair_terms(const orc_state *st, double *epair, double *evir) {
   *evir = *epair + v / (2.0 * M * p->tau);
 }
 
+/* signed minimum-image difference b - a, of magnitude distance(a, b) */
+static double mi_signed1(double b, double a, double L) {
+  double q = orc_distance(a, b, L), x = b - a;
+  return (fabs(x) > L) == (x > 0) ? -q : q;
+}
+
+void orc_superfluid(const orc_state *st, double out[3]) {
+  const orc_params *p = &st->p;
+  int N = p->N, M = p->M, dim = p->dim;
+  double w[MAXDIM] = {0.0, 0.0}, area = 0.0, rsq = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < M; ++j) {
+      int inext = (j == M - 1) ? st->next[i] : i, jn = (j + 1) % M;
+      double a[MAXDIM] = {0.0, 0.0}, b[MAXDIM] = {0.0, 0.0}, dv[MAXDIM] = {0.0, 0.0};
+      bead_pos(st, i, j, a);
+      bead_pos(st, inext, jn, b);
+      for (int d = 0; d < dim; ++d) { dv[d] = mi_signed1(b[d], a[d], p->L); w[d] += dv[d]; }
+      area += 0.5 * (a[0] * dv[1] - a[1] * dv[0]);
+      rsq += a[0] * a[0] + a[1] * a[1];
+    }
+  out[0] = w[0] * w[0] + w[1] * w[1];
+  out[1] = area;
+  out[2] = rsq / M;
+}
+
+void orc_radial(const orc_state *st, int nb, double dr, double *hist) {
+  const orc_params *p = &st->p;
+  int N = p->N, M = p->M, dim = p->dim;
+  for (int j = 0; j < M; ++j)
+    for (int a = 0; a < N; ++a)
+      for (int b = a + 1; b < N; ++b) {
+        double ra[MAXDIM], rb[MAXDIM];
+        bead_pos(st, a, j, ra);
+        bead_pos(st, b, j, rb);
+        double s = 0.0;
+        for (int d = 0; d < dim; ++d) { double q = orc_distance(ra[d], rb[d], p->L); s += q * q; }
+        double k = floor(sqrt(s) / dr);
+        if (k < (double)nb) hist[(int)k] += 1.0;
+      }
+}
+
 void orc_energy(const orc_state *st, double out[4]) {
   const orc_params *p = &st->p;
   int N = p->N, M = p->M, dim = p->dim;

@@ -137,6 +137,14 @@ int orc_polymer_com(orc_state *st, int n, double maxd, orc_draws *dr);
 void orc_energy(const orc_state *st, double out[4]);
 /* Density: hist[nb*nb] (dim 2, column-major like dens[ix,iy]) += counts */
 void orc_density(const orc_state *st, int nb, double *hist);
+/* superfluid estimators (the TODO of src/measurement.jl:126): out[0] = W^2,
+ * |sum over links of the signed minimum-image displacement|^2; out[1] = A_z =
+ * 1/2 sum over links (x dy - y dx); out[2] = sum r^2 / M */
+void orc_superfluid(const orc_state *st, double out[3]);
+/* radial distribution (the TODO of src/measurement.jl:125): adds, for every
+ * slice, every unordered pair with minimum-image distance r to bin
+ * floor(r / dr) when that is below nb */
+void orc_radial(const orc_state *st, int nb, double dr, double *hist);
 
 /* ---- generator ---- */
 void orc_rng_init(orc_rng *r, uint64_t seed, uint64_t stream);

@@ -96,6 +96,8 @@ struct Handle {
     double *d;
   };
   std::vector<ContactTab> ctabs;
+  unsigned long long *d_rdf = nullptr;  // pair-distance histograms of every chain
+  size_t n_rdf = 0;
 };
 
 int check_params(const pimc_params &p) {
@@ -350,7 +352,7 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     h->n_stage += (size_t)p.dim * NM;
     d.tab_off = (long long)dp; dp += 2 * (size_t)d.wtab * d.wtab;
     d.eser_off = p.energy_capacity > 0 ? (long long)dp : -1;
-    dp += 4 * (size_t)p.energy_capacity;
+    dp += (size_t)NOBS * p.energy_capacity;
     d.next_off = (long long)ip; ip += p.N;
     if (p.density_nbins > 0) {
       d.dens_off = (long long)up;
@@ -743,6 +745,7 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_adj);
   cudaFree(h->d_stage);
   for (auto &t : h->ctabs) cudaFree(t.d);
+  cudaFree(h->d_rdf);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -1084,11 +1087,106 @@ int pimc_get_energies(void *handle, int chain, double *out, int cap, int *count)
   const int have = (int)std::min<unsigned long long>(v.eser_count, (unsigned long long)d.eser_cap);
   const int k = std::min(have, std::max(cap, 0));
   if (k > 0 && out) {
-    CK(cudaMemcpyAsync(out, h->d_dpool + d.eser_off, sizeof(double) * 4 * k, cudaMemcpyDeviceToHost, h->stream));
+    std::vector<double> rows((size_t)NOBS * k);
+    CK(cudaMemcpyAsync(rows.data(), h->d_dpool + d.eser_off, sizeof(double) * NOBS * k,
+                       cudaMemcpyDeviceToHost, h->stream));
+    rc = sync_check(h);
+    if (rc) return rc;
+    for (int r = 0; r < k; ++r)
+      for (int q = 0; q < 4; ++q) out[4 * r + q] = rows[(size_t)NOBS * r + q];
+  }
+  if (count) *count = have;
+  return PIMC_OK;
+}
+
+int pimc_get_observables(void *handle, int chain, double *out, int cap, int *count) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  ChainVar v;
+  int rc = read_var(h, chain, &v);
+  if (rc) return rc;
+  const ChainDesc &d = h->desc[chain];
+  const int have = (int)std::min<unsigned long long>(v.eser_count, (unsigned long long)d.eser_cap);
+  const int k = std::min(have, std::max(cap, 0));
+  if (k > 0 && out) {
+    CK(cudaMemcpyAsync(out, h->d_dpool + d.eser_off, sizeof(double) * NOBS * k,
+                       cudaMemcpyDeviceToHost, h->stream));
     rc = sync_check(h);
     if (rc) return rc;
   }
   if (count) *count = have;
+  return PIMC_OK;
+}
+
+int pimc_get_observable_sums(void *handle, int chain, double *sum, double *sumsq,
+                             unsigned long long *count) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  ChainVar v;
+  int rc = read_var(h, chain, &v);
+  if (rc) return rc;
+  for (int q = 0; q < NOBS; ++q) {
+    if (sum) sum[q] = v.esum[q];
+    if (sumsq) sumsq[q] = v.esum2[q];
+  }
+  if (count) *count = v.n_meas;
+  return PIMC_OK;
+}
+
+int pimc_set_radial(void *handle, int chain, int nbins, double rmax) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (chain < -1 || chain >= h->nchains) return fail(PIMC_EARG, "chain out of range");
+  if (nbins < 0 || nbins > (1 << 20)) return fail(PIMC_EARG, "nbins must be in [0, 2^20]");
+  if (nbins > 0 && !(rmax >= 0.0 && std::isfinite(rmax)))
+    return fail(PIMC_EARG, "rmax must be finite and >= 0 (0: the half-width L)");
+  const int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->nchains : chain + 1;
+  CK(cudaStreamSynchronize(h->stream));
+  for (int c = c0; c < c1; ++c) {
+    ChainDesc &d = h->desc[c];
+    d.rdf_nb = nbins;
+    d.rdf_dr = nbins > 0 ? (rmax > 0.0 ? rmax : d.L) / nbins : 0.0;
+  }
+  // one buffer for every chain's histogram, laid out afresh and zeroed
+  size_t tot = 0;
+  for (const auto &d : h->desc) tot += (size_t)std::max(d.rdf_nb, 0);
+  unsigned long long *buf = nullptr;
+  if (tot > 0) {
+    CK(cudaMalloc(&buf, sizeof(unsigned long long) * tot));
+    CK(cudaMemsetAsync(buf, 0, sizeof(unsigned long long) * tot, h->stream));
+  }
+  size_t off = 0;
+  for (auto &d : h->desc) {
+    d.rdf = d.rdf_nb > 0 ? buf + off : nullptr;
+    off += (size_t)std::max(d.rdf_nb, 0);
+  }
+  std::vector<ChainVar> v(h->nchains);
+  CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto &x : v) x.rdf_meas = 0;
+  CK(cudaMemcpyAsync(h->d_var, v.data(), sizeof(ChainVar) * h->nchains, cudaMemcpyHostToDevice, h->stream));
+  if (upload_desc(h)) return PIMC_ECUDA;
+  int rc = sync_check(h);
+  cudaFree(h->d_rdf);
+  h->d_rdf = buf;
+  h->n_rdf = tot;
+  return rc;
+}
+
+int pimc_get_radial(void *handle, int chain, double *hist, unsigned long long *nmeas) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain)) return PIMC_EARG;
+  const ChainDesc &d = h->desc[chain];
+  if (d.rdf_nb <= 0) return fail(PIMC_EARG, "no pair-distance histogram (pimc_set_radial)");
+  std::vector<unsigned long long> u((size_t)d.rdf_nb);
+  CK(cudaMemcpyAsync(u.data(), d.rdf, 8 * u.size(), cudaMemcpyDeviceToHost, h->stream));
+  ChainVar v;
+  CK(cudaMemcpyAsync(&v, h->d_var + chain, sizeof(ChainVar), cudaMemcpyDeviceToHost, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  if (hist)
+    for (size_t i = 0; i < u.size(); ++i) hist[i] = (double)u[i];
+  if (nmeas) *nmeas = v.rdf_meas;
   return PIMC_OK;
 }
 
@@ -1132,11 +1230,12 @@ int pimc_reset_measurements(void *handle) {
   CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
   if (sync_check(h)) return PIMC_ECUDA;
   for (auto &x : v) {
-    x.n_meas = x.ndata = x.eser_count = 0;
-    for (int q = 0; q < 4; ++q) x.esum[q] = x.esum2[q] = 0.0;
+    x.n_meas = x.ndata = x.eser_count = x.rdf_meas = 0;
+    for (int q = 0; q < NOBS; ++q) x.esum[q] = x.esum2[q] = 0.0;
   }
   CK(cudaMemcpyAsync(h->d_var, v.data(), sizeof(ChainVar) * h->nchains, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemsetAsync(h->d_upool, 0, sizeof(unsigned long long) * h->n_upool, h->stream));
+  if (h->d_rdf) CK(cudaMemsetAsync(h->d_rdf, 0, sizeof(unsigned long long) * h->n_rdf, h->stream));
   return sync_check(h);
 }
 
@@ -1472,7 +1571,7 @@ int pimc_get_total_stats(void *handle, pimc_stats *out) {
 
 // checkpoint layout: magic, version, nchains, then per chain ChainVar and the
 // raw device regions (positions, links and FP32 mirror, next, density,
-// energy series)
+// observable series); the pair-distance histograms are not part of it
 int pimc_state_size(void *handle, size_t *bytes) {
   Handle *h = H(handle);
   if (!h || !bytes) return fail(PIMC_EARG, "null argument");
@@ -1480,7 +1579,7 @@ int pimc_state_size(void *handle, size_t *bytes) {
   for (const auto &d : h->desc) {
     b += sizeof(ChainVar) + 8 * (size_t)(d.tab_off - d.x_off) + 4 * (size_t)d.N;
     if (d.dens_off >= 0) b += 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb);
-    if (d.eser_off >= 0) b += 8 * 4 * (size_t)d.eser_cap;
+    if (d.eser_off >= 0) b += 8 * (size_t)NOBS * d.eser_cap;
   }
   *bytes = b;
   return PIMC_OK;
@@ -1513,7 +1612,7 @@ static int state_io(Handle *h, char *buf, size_t bytes, bool save) {
     CK(io(h->d_dpool + d.x_off, 8 * (size_t)(d.tab_off - d.x_off)));
     CK(io(h->d_ipool + d.next_off, 4 * (size_t)d.N));
     if (d.dens_off >= 0) CK(io(h->d_upool + d.dens_off, 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb)));
-    if (d.eser_off >= 0) CK(io(h->d_dpool + d.eser_off, 8 * 4 * (size_t)d.eser_cap));
+    if (d.eser_off >= 0) CK(io(h->d_dpool + d.eser_off, 8 * (size_t)NOBS * d.eser_cap));
   }
   return sync_check(h);
 }

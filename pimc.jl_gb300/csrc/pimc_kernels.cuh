@@ -867,8 +867,12 @@ __device__ __forceinline__ long long bin_floor(double x, double L, double w, dou
 }
 
 // ---------------------------------------------------------------------------
-// estimators, whole CTA (src/measurement.jl:45-55, 92-122)
-// out[0] E_th, out[1] E_v, out[2] pair energy, out[3] pair virial energy;
+// estimators, whole CTA (src/measurement.jl:45-55, 92-122, and the radial
+// distribution and superfluid estimators its TODOs name, 125-127)
+// out[0] E_th, out[1] E_v, out[2] pair energy, out[3] pair virial energy,
+// out[4] W^2 = |sum over links of the minimum-image displacement|^2 (winding),
+// out[5] A_z = 1/2 sum over links (x dy - y dx) (signed area about the origin),
+// out[6] sum r^2 / M (classical moment of inertia / m), out[7] 0;
 // qbuf: one PQ_CAP-entry queue per warp (pair chains)
 // ---------------------------------------------------------------------------
 template <bool WARP>
@@ -883,6 +887,7 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
   const bool pair = (d.flags & PF_PAIR) != 0 && !(d.flags & PF_CONTACT);
   const double rc2 = d.rc * d.rc, cg = d.inv2s2;
   double s[5] = {0.0, 0.0, 0.0, 0.0, 0.0};  // link, pot, vkin, pair, pair virial
+  double sf[4] = {0.0, 0.0, 0.0, 0.0};       // winding x, y, area, sum r^2
   const double inv_bw = density ? 1.0 / d.dens_bw : 0.0;
   for (int k = tid; k < N * M; k += nt) {
     const int j = k / N, i = k % N;
@@ -892,6 +897,13 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
     s[0] += mi2(d, ax, ay, bx, by);
     s[1] += vext(d, ax, ay) + vext(d, bx, by);
     s[2] += ax * dvext(d, ax) + (dim > 1 ? ay * dvext(d, ay) : 0.0);
+    {
+      const double dx = mi1(bx, ax, d.L, d.L2), dy = dim > 1 ? mi1(by, ay, d.L, d.L2) : 0.0;
+      sf[0] += dx;
+      sf[1] += dy;
+      sf[2] += 0.5 * __dsub_rn(__dmul_rn(ax, dy), __dmul_rn(ay, dx));
+      sf[3] += __dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay));
+    }
     if (density) {
       const long long ib = bin_floor(ax, d.L, d.dens_bw, inv_bw);
       bool ok = ib >= 1 && ib <= d.dens_nb;
@@ -955,9 +967,41 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
     }
     while (qn > 0) flush();
   }
+  if (d.rdf_nb > 0) {
+    // pair-distance histogram: warps split the beads, lanes the partners of
+    // higher index; lanes with the same bin add once (match_any)
+    const int tot = N * M;
+    const int gw = WARP ? 0 : warp, ngw = WARP ? 1 : nwarps;
+    const int ib_max = d.rdf_nb;
+    for (int kk = gw; kk < tot; kk += ngw) {
+      const int j = kk / N, i = kk % N;
+      const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+      for (int b0 = i + 1; b0 < N; b0 += 32) {
+        const int b = b0 + lane;
+        int bin = -1;
+        if (b < N) {
+          const double dx = fabs(mi1(ax, c.X(0, b, j), d.L, d.L2));
+          const double dy = dim > 1 ? fabs(mi1(ay, c.Xd(1, b, j), d.L, d.L2)) : 0.0;
+          const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+          const double f = floor(r / d.rdf_dr);
+          if (f < (double)ib_max) bin = (int)f;
+        }
+        const unsigned act = __ballot_sync(0xffffffffu, bin >= 0);
+        if (bin >= 0) {
+          const unsigned peers = __match_any_sync(act, bin);
+          if (lane == __ffs(peers) - 1) atomicAdd(d.rdf + bin, (unsigned long long)__popc(peers));
+        }
+      }
+    }
+  }
   G::template sum<5>(s, red);
+  G::template sum<4>(sf, red);
   if (tid == 0) {
     const double tau = d.tau;
+    out[4] = sf[0] * sf[0] + sf[1] * sf[1];
+    out[5] = sf[2];
+    out[6] = sf[3] / M;
+    out[7] = 0.0;
     out[0] = (double)(dim * N) / (2.0 * tau) - 1.0 / (4.0 * d.lambda * (tau * tau) * M) * s[0] +
              1.0 / (2.0 * M) * s[1];
     out[1] = 1.0 / (2.0 * M) * s[2] + 1.0 / (2.0 * M) * s[1];

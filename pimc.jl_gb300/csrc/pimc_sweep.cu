@@ -41,14 +41,15 @@ __device__ __forceinline__ bool chain_serial_local(const ChainDesc &d) {
 __device__ void record_measurement(const ChainDesc &d, ChainVar &v, const CV &c, const double *e,
                                    bool density) {
   if (c.eser && v.eser_count < (unsigned long long)d.eser_cap) {
-    for (int q = 0; q < 4; ++q) c.eser[v.eser_count * 4 + q] = e[q];
+    for (int q = 0; q < NOBS; ++q) c.eser[v.eser_count * NOBS + q] = e[q];
     v.eser_count++;
   }
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < NOBS; ++q) {
     v.esum[q] += e[q];
     v.esum2[q] += e[q] * e[q];
   }
   v.n_meas++;
+  if (d.rdf_nb > 0) v.rdf_meas++;
   if (density) v.ndata += d.M;
 }
 
@@ -73,7 +74,7 @@ struct SmemCtl {
   ChainVar v;
   MixDev mix;
   double shift[2];
-  double e4[4];
+  double e4[NOBS];
   int iflag[8];
   int chain;
 };

@@ -15,6 +15,11 @@ enum : int {
   PF_CONTACT = 64,  // pair link action from the tabulated contact propagator (with PF_PAIR)
 };
 
+// observables of one measurement (a row of the series): E_th, E_v, pair
+// energy, pair virial energy, squared winding W^2, signed area A_z, sum r^2/M,
+// and one spare column
+constexpr int NOBS = 8;
+
 // move kinds for counters
 enum : int { MV_STAGE = 0, MV_SWAP = 1, MV_COM = 2, MV_PCOM = 3 };
 
@@ -53,7 +58,7 @@ struct ChainDesc {
   long long tab_off;    // double2: bridge table (alpha, sigma)[m*wtab + t]
   long long next_off;   // ints: next[n]
   long long dens_off;   // u64: hist[nb^dim]
-  long long eser_off;   // doubles: energy series [cap][4]
+  long long eser_off;   // doubles: observable series [cap][NOBS]
   int eser_cap;
   int smem_bytes;       // bytes to stage x, V, mirror, next in shared memory
   unsigned key0, key1;  // Philox key
@@ -65,6 +70,11 @@ struct ChainDesc {
   const double *ct_tab;
   int ct_n, ct_pad_;
   double ct_r0, ct_h, ct_rmax;
+  // pair-distance histogram (rdf_nb > 0): counts of unordered pairs per
+  // slice with floor(r / rdf_dr) = k, k < rdf_nb
+  unsigned long long *rdf;
+  int rdf_nb, rdf_pad_;
+  double rdf_dr;
 };
 
 // move mix as seen by the device
@@ -92,9 +102,10 @@ struct ChainVar {
   unsigned long long skips;
   double bead_updates;
   unsigned long long n_meas, ndata, eser_count;
-  double esum[4], esum2[4];
+  double esum[NOBS], esum2[NOBS];
   int err;
   int pad_;
+  unsigned long long rdf_meas;  // measurements in the pair-distance histogram
 };
 
 // device error codes (ChainVar::err, first error wins)

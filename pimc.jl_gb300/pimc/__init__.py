@@ -7,8 +7,9 @@ compiles the CUDA library for sm_103a.
 """
 from ._native import LIB_PATH, PimcError, build, load
 from .api import (ContactPropagator, Counter, Density, Energy, GaussianPair, Harmonic,
-                  NumbOfSlices, Particle, PolymerCenterOfMass, PotentialSum, ReshapeLinear,
-                  ReshapeSwapLinear, SingleCenterOfMass, SquareLattice, Step, System, Zero,
+                  NumbOfSlices, Particle, PolymerCenterOfMass, PotentialSum, RadialDistribution,
+                  ReshapeLinear, ReshapeSwapLinear, SingleCenterOfMass, SquareLattice, Step,
+                  Superfluid, System, Zero,
                   acceptance, apply, build_prop_int, determine_nnrange, run)
 from .engine import (ACCEPT, HARDCORE, REJECT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams,
                      Engine, Mix, contact_table)
@@ -19,5 +20,5 @@ __all__ = [
     "ReshapeSwapLinear", "SingleCenterOfMass", "PolymerCenterOfMass", "Counter", "Step",
     "NumbOfSlices", "acceptance", "run", "apply", "Density", "Energy", "SEM_REFERENCE",
     "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE", "ContactPropagator",
-    "build_prop_int", "determine_nnrange", "contact_table",
+    "build_prop_int", "determine_nnrange", "contact_table", "RadialDistribution", "Superfluid",
 ]

@@ -146,6 +146,10 @@ SIGNATURES = {
     "pimc_get_energies": [_vp, C.c_int, _dp, C.c_int, _ip],
     "pimc_get_energy_sums": [_vp, C.c_int, _dp, _dp, _ull],
     "pimc_get_density": [_vp, C.c_int, _dp, _ull],
+    "pimc_get_observables": [_vp, C.c_int, _dp, C.c_int, _ip],
+    "pimc_get_observable_sums": [_vp, C.c_int, _dp, _dp, _ull],
+    "pimc_set_radial": [_vp, C.c_int, C.c_int, C.c_double],
+    "pimc_get_radial": [_vp, C.c_int, _dp, _ull],
     "pimc_reset_measurements": [_vp],
     "pimc_adjoint": [_vp, C.c_int, _dp, _dp, _dp],
     "pimc_adjoint_noalloc": [_vp, C.c_int, _dp, _dp, _dp],

@@ -473,6 +473,66 @@ class Energy:
             raise PimcError("Energy storage is full (the reference errors here too)")
 
 
+class RadialDistribution:
+    """Pair radial distribution g(r) (the TODO of src/measurement.jl:125):
+    every measurement bins, at every slice, each unordered pair's
+    minimum-image distance into nbins bins over [0, rmax)."""
+
+    def __init__(self, s: System, nbins: int = 100, rmax: float | None = None):
+        self.nbins = int(nbins)
+        self.rmax = float(s.L if rmax is None else rmax)
+        self.bin = self.rmax / self.nbins
+        self.hist = np.zeros(self.nbins)
+        self.ndata = 0       # measurements
+        self._dim, self._L, self._M, self._N = s.dim, s.L, s.M, s.N
+
+    def _pull(self, s: System):
+        h, nm = s.engine.radial()
+        self.hist = self.hist + h
+        self.ndata += nm
+
+    def r(self):
+        return (np.arange(self.nbins) + 0.5) * self.bin
+
+    def g(self):
+        """counts over the ideal-gas expectation: pairs per slice
+        N(N-1)/2 times the shell's share of the box (2L)^dim"""
+        e = np.arange(self.nbins + 1) * self.bin
+        shell = np.pi * (e[1:] ** 2 - e[:-1] ** 2) if self._dim == 2 else 2.0 * (e[1:] - e[:-1])
+        pairs = self.ndata * self._M * self._N * (self._N - 1) / 2
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return self.hist / (pairs * shell / (2 * self._L) ** self._dim)
+
+
+class Superfluid:
+    """Superfluid-fraction estimators (the TODO of src/measurement.jl:126):
+    the winding estimator rho_s/rho = <W^2> / (2 dim lambda beta N) for a
+    periodic box, and the area estimator rho_s/rho = 2 <A_z^2> / (lambda beta
+    <sum r^2 / M>) about the trap centre (Sindzingre, Klein and Ceperley, PRL
+    63, 1601 (1989)), from per-measurement series keyed by N."""
+
+    def __init__(self, s: System, n: int = 20_000):
+        self.capacity = n
+        self.W2 = {0: []}
+        self.area = {0: []}
+        self.I = {0: []}
+        self._lam, self._beta, self._dim = s.λ, s.β, s.dim
+
+    def _add(self, s: System, rows):
+        self.W2.setdefault(s.N, []).extend(rows[:, 4].tolist())
+        self.area.setdefault(s.N, []).extend(rows[:, 5].tolist())
+        self.I.setdefault(s.N, []).extend(rows[:, 6].tolist())
+        if len(self.W2[s.N]) > self.capacity:
+            raise PimcError("Superfluid storage is full")
+
+    def winding_fraction(self, N: int) -> float:
+        return float(np.mean(self.W2[N])) / (2 * self._dim * self._lam * self._beta * N)
+
+    def area_fraction(self, N: int) -> float:
+        a = np.asarray(self.area[N])
+        return 2.0 * float(np.mean(a * a)) / (self._lam * self._beta * float(np.mean(self.I[N])))
+
+
 # --------------------------------------------------------------- driver
 def _mix_for(s: System, n: int, updates):
     """Map run!(s, n, updates) onto sweeps of the engine (one staging phase per
@@ -531,7 +591,8 @@ def run(s: System, n: int, updates, Zmeasurements=()):
     s.ctr = 10_000 if not Zmeasurements else 1_000
     mix, sweeps, per_sweep, objs = _mix_for(s, n, updates)
     dens = [z for z in Zmeasurements if isinstance(z, Density)]
-    ens = [z for z in Zmeasurements if isinstance(z, Energy)]
+    ens = [z for z in Zmeasurements if isinstance(z, (Energy, Superfluid))]
+    rdfs = [z for z in Zmeasurements if isinstance(z, RadialDistribution)]
     if Zmeasurements:
         mix.measure_every = max(1, round(s.Ncycle / per_sweep))
         nb = dens[0].nbins if dens else 0
@@ -539,6 +600,7 @@ def run(s: System, n: int, updates, Zmeasurements=()):
         s._ensure_engine(nb, cap)
         s.engine.reset_measurements()
         s._eser_seen = 0
+        s.engine.set_radial(rdfs[0].nbins if rdfs else 0, rdfs[0].rmax if rdfs else 0.0)
     before = s.engine.stats()
     s.engine.set_mix(mix)
     s.engine.run(sweeps)
@@ -566,12 +628,14 @@ def run(s: System, n: int, updates, Zmeasurements=()):
     if Zmeasurements:
         nmeas = after.measurements - before.measurements
         s.N_MC[s.N] = s.N_MC.get(s.N, 0) + nmeas
-        rows = s.engine.energies()
+        rows = s.engine.observables()
         for e in ens:
             e._add(s, rows[s._eser_seen:])
         s._eser_seen = len(rows)
         for d in dens:
             d._pull(s)
+        for r in rdfs:
+            r._pull(s)
     return None
 
 

@@ -15,6 +15,7 @@ from ._native import Launch, MoveMix, Params, PimcError, Stats, check, load
 
 SEM_REFERENCE = 0
 SEM_PHYSICAL = 1
+NOBS = 8  # columns of an observable row (PIMC_NOBS)
 REJECT, ACCEPT, SKIP, HARDCORE = 0, 1, 2, 3
 OPT_FORCE_WARP_WINDOW = 1
 OPT_EXACT_DECISIONS = 2
@@ -325,6 +326,36 @@ class Engine:
         cnt = C.c_ulonglong()
         check(self.L.pimc_get_energy_sums(self.h, chain, _dp(s), _dp(s2), C.byref(cnt)))
         return s, s2, cnt.value
+
+    def observables(self, chain=0):
+        """rows of NOBS: E_th, E_v, pair energy, pair virial energy, W^2, A_z,
+        sum r^2 / M, 0"""
+        cnt = C.c_int()
+        check(self.L.pimc_get_observables(self.h, chain, None, 0, C.byref(cnt)))
+        out = np.zeros((max(cnt.value, 1), NOBS))
+        check(self.L.pimc_get_observables(self.h, chain, _dp(out), cnt.value, C.byref(cnt)))
+        return out[: cnt.value]
+
+    def observable_sums(self, chain=0):
+        s, s2 = np.zeros(NOBS), np.zeros(NOBS)
+        cnt = C.c_ulonglong()
+        check(self.L.pimc_get_observable_sums(self.h, chain, _dp(s), _dp(s2), C.byref(cnt)))
+        return s, s2, cnt.value
+
+    def set_radial(self, nbins: int, rmax: float = 0.0, chain: int = -1):
+        """pair-distance histogram of nbins bins over [0, rmax) (rmax 0: L)"""
+        check(self.L.pimc_set_radial(self.h, chain, int(nbins), float(rmax)))
+        for i, p in enumerate(self.params):
+            if chain < 0 or i == chain:
+                p._rdf_nb = int(nbins)
+
+    def radial(self, chain=0):
+        """(pair counts per bin, measurements accumulated)"""
+        nb = getattr(self.params[chain], "_rdf_nb", 0)
+        hist = np.zeros(max(nb, 1))
+        nm = C.c_ulonglong()
+        check(self.L.pimc_get_radial(self.h, chain, _dp(hist), C.byref(nm)))
+        return hist[:nb], nm.value
 
     def density(self, chain=0):
         p = self.params[chain]

@@ -238,3 +238,32 @@ def test_contact_propagator_host_and_nnrange(oracle_mod):
     f = lambda r1, r2, t: 1.0 - 0.5 * math.exp(-float(np.asarray(r1)[0]) ** 2)
     r = pimc.determine_nnrange(f, 0.1, 1e-20, 4.0)
     assert abs(r - math.sqrt(math.log(500.0))) < 1e-12
+
+
+def test_oracle_superfluid_and_radial_on_known_paths(oracle_mod):
+    """a square path of side s enclosing the origin counter-clockwise has
+    A_z = s^2 and sum r^2 / M = s^2 / 2; a path that wraps the periodic box
+    once has W^2 = (2L)^2; pair distances land in their floor bins"""
+    O = oracle_mod
+    s = 0.8
+    o = O.Oracle(O.make_params(dim=2, N=1, M=4, L=3.0, T=1.0))
+    x = np.array([[[s / 2, -s / 2, -s / 2, s / 2]], [[s / 2, s / 2, -s / 2, -s / 2]]])
+    o.set_state(x)
+    w2, az, rsq = o.superfluid()
+    assert abs(w2) < 1e-24 and abs(az - s * s) < 1e-15 and abs(rsq - s * s / 2) < 1e-15
+    L, M = 2.0, 10
+    o = O.Oracle(O.make_params(dim=2, N=1, M=M, L=L, T=1.0))
+    xs = -L + 2 * L * (np.arange(M) + 0.5) / M
+    o.set_state(np.array([[xs], [np.zeros(M)]]))
+    w2, az, _ = o.superfluid()
+    assert abs(w2 - (2 * L) ** 2) < 1e-12 and abs(az) < 1e-15
+    o = O.Oracle(O.make_params(dim=2, N=3, M=1 + 3, L=2.0, T=1.0))
+    x = np.zeros((2, 3, 4))
+    x[0, 1, :] = 0.55     # particle 1 at distance 0.55 from particle 0
+    x[0, 2, :] = -1.9     # particle 2: 1.9 from 0 and, through the wall, 1.55 from 1
+    o.set_state(x)
+    hist = o.radial(20, 0.1)
+    want = np.zeros(20)
+    for r in (0.55, 1.9, 4.0 - 2.45):
+        want[int(np.floor(r / 0.1))] += 4
+    np.testing.assert_array_equal(hist, want)
