@@ -26,7 +26,8 @@ using LinearAlgebra
 export System, run!, apply!, acceptance, ReshapeLinear, ReshapeSwapLinear,
        SingleCenterOfMass, PolymerCenterOfMass, Density, Energy, Counter, Step,
        NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients,
-       build_prop_int, ContactPropagator, determine_nnrange
+       build_prop_int, ContactPropagator, determine_nnrange,
+       RadialDistribution, Superfluid, radial_g, winding_fraction, area_fraction
 
 const libpimc = get(ENV, "PIMC_GB300_LIB",
                     joinpath(@__DIR__, "..", "..", "..", "lib", "libpimc_gb300.so"))
@@ -305,6 +306,75 @@ mutable struct Energy
     Energy(s::System, n = 20_000) = new(Dict(0 => Float64[]), Dict(0 => Float64[]), n)
 end
 
+"""
+    RadialDistribution(s; nbins = 100, rmax = s.L)
+
+Pair radial distribution (the TODO of src/measurement.jl:125): every
+measurement bins, at every slice, each unordered pair's minimum-image distance.
+`radial_g(rd, s)` gives g(r) at the bin centres.
+"""
+mutable struct RadialDistribution
+    nbins::Int64; rmax::Float64; bin::Float64; hist::Vector{Float64}; ndata::Int64
+    RadialDistribution(s::System; nbins = 100, rmax = s.L) =
+        new(nbins, rmax, rmax / nbins, zeros(nbins), 0)
+end
+function radial_g(rd::RadialDistribution, s::System)
+    e = (0:rd.nbins) .* rd.bin
+    shell = s.dim == 2 ? π .* diff(e .^ 2) : 2 .* diff(e)
+    pairs = rd.ndata * s.M * s.N * (s.N - 1) / 2
+    return rd.hist ./ (pairs .* shell ./ (2s.L)^s.dim)
+end
+
+"""
+    Superfluid(s, n = 20_000)
+
+Superfluid-fraction estimators (the TODO of src/measurement.jl:126), series
+keyed by N: the squared winding `W2`, the signed area `area` about the origin
+and `I` = sum r^2 / M.  `winding_fraction(sf, s, N)` = <W^2>/(2 dim λ β N) in a
+periodic box; `area_fraction(sf, s, N)` = 2<A_z^2>/(λ β <I>) in a trap.
+"""
+mutable struct Superfluid
+    W2::Dict{Int64,Vector{Float64}}; area::Dict{Int64,Vector{Float64}}
+    I::Dict{Int64,Vector{Float64}}; n::Int
+    Superfluid(s::System, n = 20_000) =
+        new(Dict(0 => Float64[]), Dict(0 => Float64[]), Dict(0 => Float64[]), n)
+end
+mean_(v) = sum(v) / length(v)
+winding_fraction(sf::Superfluid, s::System, N::Int) = mean_(sf.W2[N]) / (2 * s.dim * s.λ * s.β * N)
+area_fraction(sf::Superfluid, s::System, N::Int) =
+    2 * mean_(sf.area[N] .^ 2) / (s.λ * s.β * mean_(sf.I[N]))
+
+# a handle with room for the requested histogram and series: the state moves
+# over verbatim (positions, cached links, permutation)
+function ensure_engine!(s::System, nb::Int, cap::Int)
+    p = s.params
+    (p.density_nbins == nb && p.energy_capacity >= cap) && return nothing
+    x = Vector{Float64}(undef, s.dim * s.N * s.M)
+    V = Vector{Float64}(undef, s.N * s.M)
+    nx = Vector{Cint}(undef, s.N)
+    check(ccall((:pimc_get_beads, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), s.handle, x))
+    check(ccall((:pimc_get_links, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}), s.handle, V))
+    check(ccall((:pimc_get_next, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cint}), s.handle, nx))
+    q = PimcParams(p.dim, p.N, p.M, p.L, p.T, p.lambda, p.mu, p.harmonic_omega, p.lattice_V0,
+                   p.lattice_a, p.interactions, p.pair_g, p.pair_sigma, p.r_a, p.hardcore_a,
+                   p.semantics, p.seed, nb, max(p.energy_capacity, cap), p.retry_cap)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pimc_create, libpimc), Cint, (Ref{PimcParams}, Ref{Ptr{Cvoid}}), q, h))
+    check(ccall((:pimc_set_raw, libpimc), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cint}),
+                h[], x, V, nx))
+    if s.propint isa ContactPropagator && p.interactions != 0
+        tab = Matrix(transpose(s.propint.table))
+        check(ccall((:pimc_set_contact_table, libpimc), Cint,
+                    (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cdouble),
+                    h[], -1, tab, s.propint.n, s.propint.range))
+    end
+    ccall((:pimc_destroy, libpimc), Cint, (Ptr{Cvoid},), s.handle)
+    s.handle = h[]
+    s.params = q
+    s.eser_seen = 0
+    return nothing
+end
+
 # ---------------------------------------------------------------- run!
 """
     run!(s, n, updates; Zmeasurements)
@@ -339,22 +409,55 @@ function run!(s::System, n::Int64, updates; Zmeasurements = Any[])
                       pc === nothing ? 0 : max(1, round(Int, frac(:PolymerCenterOfMass) / s.N)),
                       pc === nothing ? 1.0 : pc.var.size, 0.1, s.L / 2, 0.4, 0.6, 1,
                       isempty(Zmeasurements) ? 0 : max(1, round(Int, s.Ncycle / per)))
+    dens = [z for z in Zmeasurements if z isa Density]
+    series = [z for z in Zmeasurements if z isa Energy || z isa Superfluid]
+    rdfs = [z for z in Zmeasurements if z isa RadialDistribution]
+    if !isempty(Zmeasurements)
+        nmeas = cld(sweeps, mix.measure_every) + 1
+        ensure_engine!(s, isempty(dens) ? 0 : dens[1].nbins, isempty(series) ? 0 : nmeas)
+        check(ccall((:pimc_reset_measurements, libpimc), Cint, (Ptr{Cvoid},), s.handle))
+        s.eser_seen = 0
+        check(ccall((:pimc_set_radial, libpimc), Cint, (Ptr{Cvoid}, Cint, Cint, Cdouble), s.handle, -1,
+                    isempty(rdfs) ? 0 : rdfs[1].nbins, isempty(rdfs) ? 0.0 : rdfs[1].rmax))
+    end
     check(ccall((:pimc_set_move_mix, libpimc), Cint, (Ptr{Cvoid}, Cint, Ref{PimcMoveMix}), s.handle, -1, mix))
     check(ccall((:pimc_run, libpimc), Cint, (Ptr{Cvoid}, Clonglong), s.handle, sweeps))
-    for z in Zmeasurements
+    isempty(Zmeasurements) && return nothing
+    cnt = Ref{Cint}(0)
+    check(ccall((:pimc_get_observables, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+                s.handle, 0, C_NULL, 0, cnt))
+    rows = Vector{Float64}(undef, 8 * max(cnt[], 1))
+    check(ccall((:pimc_get_observables, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
+                s.handle, 0, rows, cnt[], cnt))
+    R = reshape(rows, 8, :)[:, s.eser_seen+1:cnt[]]
+    phys = s.params.semantics == 1
+    for z in series
         if z isa Energy
-            cnt = Ref{Cint}(0)
-            check(ccall((:pimc_get_energies, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
-                        s.handle, 0, C_NULL, 0, cnt))
-            rows = Vector{Float64}(undef, 4 * max(cnt[], 1))
-            check(ccall((:pimc_get_energies, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Ref{Cint}),
-                        s.handle, 0, rows, cnt[], cnt))
-            R = reshape(rows, 4, :)
-            append!(get!(z.energy, s.N, Float64[]), R[1, s.eser_seen+1:cnt[]])
-            append!(get!(z.energy_virial, s.N, Float64[]), R[2, s.eser_seen+1:cnt[]])
-            s.N_MC[s.N] = get(s.N_MC, s.N, 0) + cnt[] - s.eser_seen
-            s.eser_seen = cnt[]
+            append!(get!(z.energy, s.N, Float64[]), R[1, :] .+ (phys ? R[3, :] : 0.0))
+            append!(get!(z.energy_virial, s.N, Float64[]), R[2, :] .+ (phys ? R[4, :] : 0.0))
+        else
+            append!(get!(z.W2, s.N, Float64[]), R[5, :])
+            append!(get!(z.area, s.N, Float64[]), R[6, :])
+            append!(get!(z.I, s.N, Float64[]), R[7, :])
         end
+    end
+    s.N_MC[s.N] = get(s.N_MC, s.N, 0) + cnt[] - s.eser_seen
+    s.eser_seen = cnt[]
+    for d in dens
+        nd = Ref{Culonglong}(0)
+        h = Vector{Float64}(undef, d.nbins^s.dim)
+        check(ccall((:pimc_get_density, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ref{Culonglong}),
+                    s.handle, 0, h, nd))
+        d.dens .+= reshape(h, size(d.dens))
+        d.ndata += nd[]
+    end
+    for r in rdfs
+        nm = Ref{Culonglong}(0)
+        h = Vector{Float64}(undef, r.nbins)
+        check(ccall((:pimc_get_radial, libpimc), Cint, (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Ref{Culonglong}),
+                    s.handle, 0, h, nm))
+        r.hist .+= h
+        r.ndata += nm[]
     end
     return nothing
 end
