@@ -118,6 +118,8 @@ typedef struct pimc_stats {
 
 /* ---------------- lifecycle: System constructor (src/system.jl:129-167) */
 int pimc_create(const pimc_params *p, void **handle);
+/* the parameters a chain was created with */
+int pimc_get_params(void *handle, int chain, pimc_params *out);
 /* one handle with nchains independent chains (params[c], mix[c]) */
 int pimc_batch_create(const pimc_params *params, int nchains, void **handle);
 int pimc_destroy(void *handle);
@@ -266,6 +268,24 @@ int pimc_get_total_stats(void *handle, pimc_stats *out);
 int pimc_state_size(void *handle, size_t *bytes);
 int pimc_get_state(void *handle, void *buf, size_t bytes);
 int pimc_set_state(void *handle, const void *buf, size_t bytes);
+
+/* ---------------- files (examples/tools/savetools.jl) */
+/* save_paths (savetools.jl:4-35): a CSV with columns tau, "p<n> x"[, "p<n> y"]
+ * and M + 1 rows (tau = j beta/M; the last row closes each path with the
+ * first bead of the next particle of its cycle), numbers printed as Julia
+ * prints a Float64 */
+int pimc_write_paths_csv(void *handle, int chain, const char *path);
+/* save_density (savetools.jl:37-65): counts / ((2L/nbins) ndata) with a pos
+ * column range(-L, L, length = nbins); 2D: columns x1..x<nbins>, counts
+ * column-major (x index first) as pimc_get_density returns them */
+int pimc_write_density_csv(const char *path, int dim, int nbins, double L, const double *counts,
+                           unsigned long long ndata);
+/* the pimc_get_state snapshot in a file: "PIMCCKPT", ABI version, size,
+ * state, FNV-1a checksum; loading checks all four and the handle's shape */
+int pimc_save_checkpoint(void *handle, const char *path);
+int pimc_load_checkpoint(void *handle, const char *path);
+/* x printed as Julia prints a Float64 ("0.5", "1.0e-5", "1.234567e6") */
+int pimc_format_float(double x, char *out, size_t cap);
 /* prop_rel_interpolate_terms (src/propagator.jl:36-73): the integral terms
  * T[i1][i2] = -I1 - I2 + I3 of the contact-interaction propagator on the
  * reference's grid r_i = 1e-20 + i (range - 1e-20)/(n - 1), n = 600 there,

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/pimc.h"
+#include "pimc_internal.h"
 #include "pimc_launch.h"
 #include "pimc_types.h"
 
@@ -715,10 +716,13 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
 
 }  // namespace
 
+int pimc_fail(int code, const std::string &msg) { return fail(code, msg); }
+
 // ===================================================================== C ABI
 extern "C" {
 
 const char *pimc_last_error(void) { return g_err.c_str(); }
+
 int pimc_abi_version(void) { return PIMC_ABI_VERSION; }
 
 int pimc_create(const pimc_params *p, void **handle) { return create_impl(p, 1, handle); }
@@ -750,6 +754,13 @@ int pimc_destroy(void *handle) {
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+  return PIMC_OK;
+}
+
+int pimc_get_params(void *handle, int chain, pimc_params *out) {
+  Handle *h = H(handle);
+  if (check_chain(h, chain) || !out) return fail(PIMC_EARG, "bad argument");
+  *out = h->params[chain];
   return PIMC_OK;
 }
 

@@ -27,7 +27,8 @@ export System, run!, apply!, acceptance, ReshapeLinear, ReshapeSwapLinear,
        SingleCenterOfMass, PolymerCenterOfMass, Density, Energy, Counter, Step,
        NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients,
        build_prop_int, ContactPropagator, determine_nnrange,
-       RadialDistribution, Superfluid, radial_g, winding_fraction, area_fraction
+       RadialDistribution, Superfluid, radial_g, winding_fraction, area_fraction,
+       save_paths, save_density, save_checkpoint, load_checkpoint
 
 const libpimc = get(ENV, "PIMC_GB300_LIB",
                     joinpath(@__DIR__, "..", "..", "..", "lib", "libpimc_gb300.so"))
@@ -374,6 +375,29 @@ function ensure_engine!(s::System, nb::Int, cap::Int)
     s.eser_seen = 0
     return nothing
 end
+
+# ---------------------------------------------------------------- files
+"""`save_paths(s)` (examples/tools/savetools.jl:30-34): paths.csv from the device state."""
+save_paths(s::System; path::AbstractString = "paths.csv") =
+    check(ccall((:pimc_write_paths_csv, libpimc), Cint, (Ptr{Cvoid}, Cint, Cstring), s.handle, 0, path))
+
+"""`save_density(s, d, g, name, V)` (savetools.jl:52-65): the normalised density
+table under the reference's file name."""
+function save_density(s::System, d::Density, g, name, V)
+    path = "density$(name)M$(s.M)beta$(s.β)N$(s.N)g$(g)V$(V).csv"
+    counts = Vector{Float64}(vec(d.dens))
+    check(ccall((:pimc_write_density_csv, libpimc), Cint,
+                (Cstring, Cint, Cint, Cdouble, Ptr{Cdouble}, Culonglong),
+                path, s.dim, d.nbins, s.L, counts, d.ndata))
+    println("saved density")
+    return path
+end
+
+"""Every chain's state in a checksummed file; `load_checkpoint` resumes it bit for bit."""
+save_checkpoint(s::System, path::AbstractString) =
+    check(ccall((:pimc_save_checkpoint, libpimc), Cint, (Ptr{Cvoid}, Cstring), s.handle, path))
+load_checkpoint(s::System, path::AbstractString) =
+    check(ccall((:pimc_load_checkpoint, libpimc), Cint, (Ptr{Cvoid}, Cstring), s.handle, path))
 
 # ---------------------------------------------------------------- run!
 """

@@ -10,9 +10,10 @@ from .api import (ContactPropagator, Counter, Density, Energy, GaussianPair, Har
                   NumbOfSlices, Particle, PolymerCenterOfMass, PotentialSum, RadialDistribution,
                   ReshapeLinear, ReshapeSwapLinear, SingleCenterOfMass, SquareLattice, Step,
                   Superfluid, System, Zero,
-                  acceptance, apply, build_prop_int, determine_nnrange, run)
+                  acceptance, apply, build_prop_int, density_filename, determine_nnrange,
+                  load_checkpoint, run, save_checkpoint, save_density, save_paths)
 from .engine import (ACCEPT, HARDCORE, REJECT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams,
-                     Engine, Mix, contact_table)
+                     Engine, Mix, contact_table, julia_float, write_density_csv)
 
 __all__ = [
     "build", "load", "LIB_PATH", "PimcError", "Engine", "ChainParams", "Mix", "System", "Particle",
@@ -21,4 +22,6 @@ __all__ = [
     "NumbOfSlices", "acceptance", "run", "apply", "Density", "Energy", "SEM_REFERENCE",
     "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE", "ContactPropagator",
     "build_prop_int", "determine_nnrange", "contact_table", "RadialDistribution", "Superfluid",
+    "save_paths", "save_density", "density_filename", "save_checkpoint", "load_checkpoint",
+    "julia_float", "write_density_csv",
 ]

@@ -22,7 +22,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
-SOURCES = ["pimc_sweep.cu", "pimc_api.cu"]
+SOURCES = ["pimc_sweep.cu", "pimc_api.cu", "pimc_io.cpp"]
 
 
 class PimcError(RuntimeError):
@@ -42,7 +42,7 @@ def build(verbose: bool = False) -> str:
     objs = []
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -150,6 +150,12 @@ SIGNATURES = {
     "pimc_get_observable_sums": [_vp, C.c_int, _dp, _dp, _ull],
     "pimc_set_radial": [_vp, C.c_int, C.c_int, C.c_double],
     "pimc_get_radial": [_vp, C.c_int, _dp, _ull],
+    "pimc_get_params": [_vp, C.c_int, C.POINTER(Params)],
+    "pimc_write_paths_csv": [_vp, C.c_int, C.c_char_p],
+    "pimc_write_density_csv": [C.c_char_p, C.c_int, C.c_int, C.c_double, _dp, C.c_ulonglong],
+    "pimc_save_checkpoint": [_vp, C.c_char_p],
+    "pimc_load_checkpoint": [_vp, C.c_char_p],
+    "pimc_format_float": [C.c_double, C.c_char_p, C.c_size_t],
     "pimc_reset_measurements": [_vp],
     "pimc_adjoint": [_vp, C.c_int, _dp, _dp, _dp],
     "pimc_adjoint_noalloc": [_vp, C.c_int, _dp, _dp, _dp],

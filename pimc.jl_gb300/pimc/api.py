@@ -23,7 +23,7 @@ from collections import deque
 import numpy as np
 
 from .engine import (ACCEPT, HARDCORE, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams, Engine,
-                     Mix, PimcError, contact_table)
+                     Mix, PimcError, contact_table, julia_float, write_density_csv)
 
 
 # --------------------------------------------------------------- potentials
@@ -531,6 +531,39 @@ class Superfluid:
     def area_fraction(self, N: int) -> float:
         a = np.asarray(self.area[N])
         return 2.0 * float(np.mean(a * a)) / (self._lam * self._beta * float(np.mean(self.I[N])))
+
+
+# --------------------------------------------------------------- files
+def save_paths(s: System, path: str = "paths.csv"):
+    """save_paths (examples/tools/savetools.jl:30-34): the paths table
+    written from the device state"""
+    s.engine.write_paths_csv(path)
+
+
+def density_filename(s: System, g, name, V) -> str:
+    """the reference's save_density file name,
+    density<name>M<M>beta<beta>N<N>g<g>V<V>.csv (savetools.jl:55)"""
+    fmt = lambda v: julia_float(v) if isinstance(v, float) else str(v)
+    return f"density{name}M{s.M}beta{fmt(s.β)}N{s.N}g{fmt(g)}V{fmt(V)}.csv"
+
+
+def save_density(s: System, d: Density, g, name, V, directory: str = "."):
+    """save_density (savetools.jl:37-65): the normalised histogram with its
+    position column, under the reference's file name; returns the path"""
+    import os
+    path = os.path.join(directory, density_filename(s, g, name, V))
+    write_density_csv(path, s.dim, d.nbins, s.L, d.dens, d.ndata)
+    return path
+
+
+def save_checkpoint(s: System, path: str):
+    """every chain's state (beads, links, permutation, counters, adaptive
+    variables, generator position, series) in a checksummed file"""
+    s.engine.save_checkpoint(path)
+
+
+def load_checkpoint(s: System, path: str):
+    s.engine.load_checkpoint(path)
 
 
 # --------------------------------------------------------------- driver

@@ -7,6 +7,7 @@ Julia-shaped API (System, updates, run, Density, Energy) on top of it.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -32,6 +33,22 @@ def contact_table(g0: float, tau: float, range_: float, n: int = 600) -> np.ndar
     out = np.empty((n, n))
     check(load().pimc_contact_table(float(g0), float(tau), float(range_), int(n), _dp(out)))
     return out
+
+
+def julia_float(x: float) -> str:
+    """x printed as Julia prints a Float64 (the engine's CSV writers use it)"""
+    buf = C.create_string_buffer(64)
+    check(load().pimc_format_float(float(x), buf, 64))
+    return buf.value.decode()
+
+
+def write_density_csv(path: str, dim: int, nbins: int, L: float, counts, ndata: int):
+    """save_density's table (examples/tools/savetools.jl:37-65) from counts
+    (nbins^dim, column-major) and the number of bead samples ndata"""
+    c = np.ascontiguousarray(np.ravel(counts, order="F"), dtype=np.float64)
+    if c.size != nbins ** dim:
+        raise PimcError("counts must hold nbins^dim values")
+    check(load().pimc_write_density_csv(os.fsencode(path), dim, nbins, float(L), _dp(c), int(ndata)))
 
 
 def _ip(a):
@@ -374,6 +391,17 @@ class Engine:
         th, ex = np.zeros(3), np.zeros(4)
         check(self.L.pimc_adjoint(self.h, chain, _dp(g) if want_beads else None, _dp(th), _dp(ex)))
         return g, th, ex
+
+    # ------------------------------------------------------------- files
+    def write_paths_csv(self, path: str, chain: int = 0):
+        """save_paths (examples/tools/savetools.jl:4-35) from the device state"""
+        check(self.L.pimc_write_paths_csv(self.h, chain, os.fsencode(path)))
+
+    def save_checkpoint(self, path: str):
+        check(self.L.pimc_save_checkpoint(self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path: str):
+        check(self.L.pimc_load_checkpoint(self.h, os.fsencode(path)))
 
     # ------------------------------------------------------------- contact propagator
     def set_contact_propagator(self, g0: float, range_: float, n: int = 600, chain: int = -1):
