@@ -234,6 +234,16 @@ int pimc_set_radial(void *handle, int chain, int nbins, double rmax);
 int pimc_get_radial(void *handle, int chain, double *hist, unsigned long long *nmeas);
 int pimc_reset_measurements(void *handle);
 
+/* the optical-lattice potentials of the reference's examples
+ * (examples/tools/potentialtools.jl:1-39): adds depth * I(r) to V, with
+ * I = |(1/K) sum_k exp(i phi_k)|^2, phi_k = 2 pi scale (x sin a_k + y cos a_k),
+ * plus a_k when helical; K = nangles <= 16 beams (0 removes it); 2D chains
+ * only; chain < 0: every chain.  generate_V(scale, depth, sym; attractive)
+ * is depth -> -depth with the named angle sets.  The cached link actions are
+ * recomputed.  The adjoint's parameter derivatives do not cover depth. */
+int pimc_set_beams(void *handle, int chain, const double *angles, int nangles, double scale,
+                   double depth, int helical);
+
 /* ---------------- adjoint: per-bead dS_pot/dr and dS/d(V0, omega, g) */
 /* dSdr [dim][N][M] (optional), dSdtheta[3] = d/dV0, d/domega, d/dg,
  * extra[4] = S_ext, S_pair, virial energy (external + pair), sum r.dS/dr */

@@ -31,6 +31,8 @@ class Params(C.Structure):
         ("nbins", C.c_int), ("rc", C.c_double), ("hardcore_a", C.c_double),
         ("ctr", C.c_int), ("semantics", C.c_int),
         ("ct_tab", C.POINTER(C.c_double)), ("ct_n", C.c_int), ("ct_range", C.c_double),
+        ("nbeam", C.c_int), ("beam_helical", C.c_int), ("beam_depth", C.c_double),
+        ("beam_scale", C.c_double), ("beam_angle", C.c_double * 16),
     ]
 
 
@@ -140,7 +142,7 @@ def _ip(a):
 def make_params(dim=2, N=2, M=100, L=4.0, T=1.0, lam=1.0, hcoef=0.0, V0=0.0, lat_a=1.0,
                 pair_g=0.0, pair_sigma=1.0, interactions=False, r_a=0.0, hardcore_a=0.0,
                 semantics=SEM_REFERENCE, ctr=10000, mu=0.0, contact_table=None,
-                contact_range=0.0) -> Params:
+                contact_range=0.0, beams=None) -> Params:
     """Parameters with the System constructor's derived constants
     (src/system.jl:129-167): tau = beta/M, nbins = floor(2L/r_a), r_a = L/4
     when unset without interactions.  contact_table (n x n, on the grid
@@ -162,6 +164,15 @@ def make_params(dim=2, N=2, M=100, L=4.0, T=1.0, lam=1.0, hcoef=0.0, V0=0.0, lat
     p.hardcore_a = hardcore_a
     p.ctr = ctr
     p.semantics = semantics
+    if beams is not None:
+        # (angles, scale, depth, helical): the optical lattice of potentialtools.jl
+        angles, scale, depth, helical = beams
+        if not 0 < len(angles) <= 16:
+            raise ValueError("between 1 and 16 beam angles")
+        p.nbeam = len(angles)
+        for k, a in enumerate(angles):
+            p.beam_angle[k] = float(a)
+        p.beam_scale, p.beam_depth, p.beam_helical = float(scale), float(depth), int(bool(helical))
     if contact_table is not None:
         tab = np.ascontiguousarray(contact_table, dtype=np.float64)
         if tab.ndim != 2 or tab.shape[0] != tab.shape[1] or tab.shape[0] < 2:

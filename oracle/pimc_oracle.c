@@ -109,9 +109,37 @@ double orc_lnK(const orc_params *p, const double *r1, const double *r2, double t
   for (int d = 0; d < p->dim; ++d) { double q = orc_distance(r1[d], r2[d], p->L); s += q * q; }
   return -s / (4.0 * tau_eff * p->lambda);
 }
-/* engine-known potentials: Harmonic (hcoef = omega^2/2) + SquareLattice */
+/* normalized_intensity (examples/tools/potentialtools.jl:1-16): plane waves
+ * of every beam, r_k = x sin(a) + y cos(a), sin/cos of 2 pi r_k scale (+ a when
+ * helical), their means squared and added; optionally the gradient */
+static double beam_intensity(const orc_params *p, const double *r, double *grad) {
+  double s = 0.0, c = 0.0, sx = 0.0, sy = 0.0, cx = 0.0, cy = 0.0;
+  for (int k = 0; k < p->nbeam; ++k) {
+    double a = p->beam_angle[k], sa = sin(a), ca = cos(a);
+    double rk = r[0] * sa + r[1] * ca;
+    double ph = p->beam_helical ? 2.0 * 3.141592653589793 * rk * p->beam_scale + a
+                                : 2.0 * 3.141592653589793 * rk * p->beam_scale;
+    double sp = sin(ph), cp = cos(ph);
+    s += sp;
+    c += cp;
+    sx += cp * sa; sy += cp * ca;
+    cx -= sp * sa; cy -= sp * ca;
+  }
+  s /= p->nbeam;
+  c /= p->nbeam;
+  if (grad) {
+    double w = 2.0 * 3.141592653589793 * p->beam_scale / p->nbeam;
+    grad[0] = 2.0 * w * (s * sx + c * cx);
+    grad[1] = 2.0 * w * (s * sy + c * cy);
+  }
+  return s * s + c * c;
+}
+
+/* engine-known potentials: Harmonic (hcoef = omega^2/2) + SquareLattice +
+ * optical lattice */
 double orc_Vext(const orc_params *p, const double *r) {
   double v = 0.0;
+  if (p->nbeam > 0 && p->beam_depth != 0.0) v += p->beam_depth * beam_intensity(p, r, NULL);
   if (p->hcoef != 0.0) {
     double s = 0.0;
     for (int d = 0; d < p->dim; ++d) s += r[d] * r[d];
@@ -130,6 +158,12 @@ static void orc_dVext(const orc_params *p, const double *r, double *g) {
     if (p->hcoef != 0.0) q += 2.0 * p->hcoef * r[d];
     if (p->V0 != 0.0) q += p->V0 * p->lat_k * sin(2.0 * p->lat_k * r[d]);
     g[d] = q;
+  }
+  if (p->nbeam > 0 && p->beam_depth != 0.0) {
+    double bg[2];
+    beam_intensity(p, r, bg);
+    g[0] += p->beam_depth * bg[0];
+    g[1] += p->beam_depth * bg[1];
   }
 }
 /* src/propagator.jl:26-28 */

@@ -59,6 +59,11 @@ typedef struct orc_params {
   const double *ct_tab;
   int ct_n;
   double ct_range;
+  /* optical lattice (examples/tools/potentialtools.jl:1-39): V += beam_depth
+   * * normalized_intensity(r, beam_angle[0..nbeam), beam_scale; helical) */
+  int nbeam, beam_helical;
+  double beam_depth, beam_scale;
+  double beam_angle[16];
 } orc_params;
 
 typedef struct orc_rng {

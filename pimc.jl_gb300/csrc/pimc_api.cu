@@ -1543,6 +1543,40 @@ int pimc_set_potential(void *handle, int chain, double V0, double omega, double 
   return sync_check(h);
 }
 
+int pimc_set_beams(void *handle, int chain, const double *angles, int nangles, double scale,
+                   double depth, int helical) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  if (chain < -1 || chain >= h->nchains) return fail(PIMC_EARG, "chain out of range");
+  if (nangles < 0 || nangles > MAX_BEAMS || (nangles > 0 && !angles))
+    return fail(PIMC_EARG, "between 0 and " + std::to_string(MAX_BEAMS) + " beam angles");
+  if (nangles > 0 && !(std::isfinite(scale) && std::isfinite(depth)))
+    return fail(PIMC_EARG, "scale and depth must be finite");
+  for (int k = 0; k < nangles; ++k)
+    if (!std::isfinite(angles[k])) return fail(PIMC_EARG, "beam angles must be finite");
+  const int c0 = chain < 0 ? 0 : chain, c1 = chain < 0 ? h->nchains : chain + 1;
+  for (int c = c0; c < c1; ++c)
+    if (nangles > 0 && h->desc[c].dim != 2)
+      return fail(PIMC_EARG, "the optical lattice is two-dimensional (chain " + std::to_string(c) + ")");
+  CK(cudaStreamSynchronize(h->stream));
+  for (int c = c0; c < c1; ++c) {
+    ChainDesc &d = h->desc[c];
+    d.nbeam = nangles;
+    d.beam_helical = helical ? 1 : 0;
+    d.beam_scale = scale;
+    d.beam_depth = depth;
+    for (int k = 0; k < MAX_BEAMS; ++k) {
+      d.beam_sin[k] = k < nangles ? std::sin(angles[k]) : 0.0;
+      d.beam_cos[k] = k < nangles ? std::cos(angles[k]) : 0.0;
+    }
+    if (nangles > 0 && depth != 0.0) d.flags |= PF_BEAM;
+    else d.flags &= ~PF_BEAM;
+  }
+  if (upload_desc(h)) return PIMC_ECUDA;
+  CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, c0, c1 - c0, h->maxNM, h->stream));
+  return sync_check(h);
+}
+
 int pimc_get_stats(void *handle, int chain, pimc_stats *out) {
   Handle *h = H(handle);
   if (check_chain(h, chain) || !out) return fail(PIMC_EARG, "bad argument");

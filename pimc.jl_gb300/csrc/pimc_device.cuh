@@ -261,8 +261,44 @@ __device__ __forceinline__ double teleport(double x, double L, double inv2L) {
 __device__ __forceinline__ double sgn(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 0.0); }
 
 // engine-known external potential: hcoef |r|^2 + V0 sum sin^2(pi r_d / a)
+// the optical lattice's normalized intensity (examples/tools/potentialtools.jl:1-16):
+// with phi_k = 2 pi scale (x sin a_k + y cos a_k) (+ a_k when helical),
+// S = (1/K) sum sin phi_k, C = (1/K) sum cos phi_k, I = S^2 + C^2; optionally
+// the gradient of I
+__device__ __noinline__ double beam_intensity(const ChainDesc &d, double x, double y, double *gx,
+                                              double *gy) {
+  double S = 0.0, Cc = 0.0, sx = 0.0, sy = 0.0, cx = 0.0, cy = 0.0;
+  for (int k = 0; k < d.nbeam; ++k) {
+    const double sa = d.beam_sin[k], ca = d.beam_cos[k];
+    double s, c;
+    sincospi(2.0 * d.beam_scale * (x * sa + y * ca), &s, &c);
+    if (d.beam_helical) {  // rotate by the beam's own angle a_k
+      const double s2 = s * ca + c * sa, c2 = c * ca - s * sa;
+      s = s2;
+      c = c2;
+    }
+    S += s;
+    Cc += c;
+    // d(sin phi) = cos phi dphi, d(cos phi) = -sin phi dphi, dphi/dx = 2 pi scale sin a_k
+    sx += c * sa;
+    sy += c * ca;
+    cx -= s * sa;
+    cy -= s * ca;
+  }
+  const double inv = 1.0 / d.nbeam;
+  S *= inv;
+  Cc *= inv;
+  if (gx) {
+    const double w = 2.0 * 3.141592653589793 * d.beam_scale * inv;
+    *gx = 2.0 * w * (S * sx + Cc * cx);
+    *gy = 2.0 * w * (S * sy + Cc * cy);
+  }
+  return S * S + Cc * Cc;
+}
+
 __device__ __forceinline__ double vext(const ChainDesc &d, double x, double y) {
   double v = 0.0;
+  if (d.flags & PF_BEAM) v += d.beam_depth * beam_intensity(d, x, y, nullptr, nullptr);
   if (d.flags & PF_HARM) {
     double s = x * x;
     if (d.dim > 1) s += y * y;
@@ -280,12 +316,25 @@ __device__ __forceinline__ double vext(const ChainDesc &d, double x, double y) {
   return v;
 }
 
-// gradient of vext along one coordinate
+// gradient of vext along one coordinate, separable terms only
 __device__ __forceinline__ double dvext(const ChainDesc &d, double x) {
   double g = 0.0;
   if (d.flags & PF_HARM) g += 2.0 * d.hcoef * x;
   if (d.flags & PF_LATT) g += d.V0 * (d.lat_k * 3.141592653589793) * sinpi(2.0 * x * d.lat_k);
   return g;
+}
+
+// full gradient of vext (the optical lattice is not separable)
+__device__ __forceinline__ void grad_vext(const ChainDesc &d, double x, double y, double &gx,
+                                          double &gy) {
+  gx = dvext(d, x);
+  gy = d.dim > 1 ? dvext(d, y) : 0.0;
+  if (d.flags & PF_BEAM) {
+    double bx, by;
+    beam_intensity(d, x, y, &bx, &by);
+    gx += d.beam_depth * bx;
+    gy += d.beam_depth * by;
+  }
 }
 
 // exp(x) for x <= 0 by a table of exp(-k/64), k = 0..2560 (filled from the

@@ -896,7 +896,11 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
     const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
     s[0] += mi2(d, ax, ay, bx, by);
     s[1] += vext(d, ax, ay) + vext(d, bx, by);
-    s[2] += ax * dvext(d, ax) + (dim > 1 ? ay * dvext(d, ay) : 0.0);
+    {
+      double gx, gy;
+      grad_vext(d, ax, ay, gx, gy);
+      s[2] += ax * gx + (dim > 1 ? ay * gy : 0.0);
+    }
     {
       const double dx = mi1(bx, ax, d.L, d.L2), dy = dim > 1 ? mi1(by, ay, d.L, d.L2) : 0.0;
       sf[0] += dx;

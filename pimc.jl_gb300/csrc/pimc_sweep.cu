@@ -691,7 +691,10 @@ __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
     const double tau = d.tau;
     const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
     const double anx = c.X(0, in, jn), any = c.Xd(1, in, jn);
-    double ge[2] = {tau * dvext(d, ax), dim > 1 ? tau * dvext(d, ay) : 0.0};
+    double ge[2];
+    grad_vext(d, ax, ay, ge[0], ge[1]);
+    ge[0] *= tau;
+    ge[1] *= tau;
     v[0] = tau * vext(d, ax, ay);
     if (d.flags & PF_LATT) {
       const double sx = sinpi(ax * d.lat_k), sy = dim > 1 ? sinpi(ay * d.lat_k) : 0.0;

@@ -13,7 +13,10 @@ enum : int {
   PF_HARM = 16,     // harmonic trap term in V
   PF_EXACT = 32,    // sweeps decide every move from exact FP64 sums (no bounded shortcuts)
   PF_CONTACT = 64,  // pair link action from the tabulated contact propagator (with PF_PAIR)
+  PF_BEAM = 128,    // optical-lattice term depth * normalized_intensity in V (2D)
 };
+
+constexpr int MAX_BEAMS = 16;  // laser beams of an optical-lattice potential
 
 // observables of one measurement (a row of the series): E_th, E_v, pair
 // energy, pair virial energy, squared winding W^2, signed area A_z, sum r^2/M,
@@ -75,6 +78,12 @@ struct ChainDesc {
   unsigned long long *rdf;
   int rdf_nb, rdf_pad_;
   double rdf_dr;
+  // optical lattice (PF_BEAM): beam k has direction (sin a_k, cos a_k), phase
+  // a_k when helical; V = depth |(1/K) sum exp(i phi_k)|^2, phi_k =
+  // 2 pi scale (x sin a_k + y cos a_k) (+ a_k)
+  int nbeam, beam_helical;
+  double beam_depth, beam_scale;
+  double beam_sin[MAX_BEAMS], beam_cos[MAX_BEAMS];
 };
 
 // move mix as seen by the device

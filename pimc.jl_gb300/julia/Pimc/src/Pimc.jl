@@ -28,7 +28,8 @@ export System, run!, apply!, acceptance, ReshapeLinear, ReshapeSwapLinear,
        NumbOfSlices, Harmonic, SquareLattice, GaussianPair, action_gradients,
        build_prop_int, ContactPropagator, determine_nnrange,
        RadialDistribution, Superfluid, radial_g, winding_fraction, area_fraction,
-       save_paths, save_density, save_checkpoint, load_checkpoint
+       save_paths, save_density, save_checkpoint, load_checkpoint,
+       OpticalLattice, generate_V, lattice_angles
 
 const libpimc = get(ENV, "PIMC_GB300_LIB",
                     joinpath(@__DIR__, "..", "..", "..", "lib", "libpimc_gb300.so"))
@@ -77,9 +78,60 @@ struct Harmonic; omega::Float64; end
 (h::Harmonic)(r) = 0.5 * h.omega^2 * sum(abs2, r)
 struct SquareLattice; V0::Float64; a::Float64; end
 (s::SquareLattice)(r) = s.V0 * sum(x -> sin(pi * x / s.a)^2, r)
+"""
+    OpticalLattice(angles, scale, depth; helical = false)
+
+`depth * normalized_intensity(r, angles, scale)` of the reference's
+examples/tools/potentialtools.jl:1-16 (at most 16 beams, 2D), run on the device.
+"""
+struct OpticalLattice
+    angles::Vector{Float64}; scale::Float64; depth::Float64; helical::Bool
+end
+OpticalLattice(angles, scale, depth; helical::Bool = false) =
+    OpticalLattice(collect(Float64, angles), scale, depth, helical)
+function (o::OpticalLattice)(r)
+    s, c = 0.0, 0.0
+    for a in o.angles
+        rk = r[1] * sin(a) + r[2] * cos(a)
+        s += o.helical ? sin(2π * rk * o.scale + a) : sin(2π * rk * o.scale)
+        c += o.helical ? cos(2π * rk * o.scale + a) : cos(2π * rk * o.scale)
+    end
+    s /= length(o.angles); c /= length(o.angles)
+    return o.depth * (s * s + c * c)
+end
+
+"""
+    lattice_angles(sym)
+
+The beam sets of generate_V (potentialtools.jl:18-39): `:l25` / `:l65` point at
+the integer points of x^2 + y^2 = 25 / 65 (angle a with (sin a, cos a) = (x, y)/R),
+`:cubic` is 2πk/4.
+"""
+function lattice_angles(sym::Symbol)
+    sym === :cubic && return [2π * k / 4 for k in 0:3]
+    r2 = sym === :l25 ? 25 : sym === :l65 ? 65 : error("unknown lattice $sym")
+    return sort([atan(x, y) for x in -9:9 for y in -9:9 if x^2 + y^2 == r2])
+end
+
+"""
+    generate_V(scale, depth, sym; attractive = true)
+    generate_V(angles, scale, depth; helical = false)
+
+The reference's optical-lattice constructors (potentialtools.jl:18-39) as
+engine-known potentials; `:harmonic` gives `Harmonic(1.0)`.
+"""
+function generate_V(scale::Float64, depth::Float64, sym::Symbol; attractive::Bool = true)
+    sym === :harmonic && return Harmonic(1.0)
+    return OpticalLattice(lattice_angles(sym), scale, attractive ? -depth : depth, false)
+end
+generate_V(angles::Vector{Float64}, scale::Float64, depth::Float64; helical::Bool = false) =
+    OpticalLattice(angles, scale, depth, helical)
+
 struct PotentialSum; terms::Vector{Any}; end
 (p::PotentialSum)(r) = sum(t(r) for t in p.terms)
-Base.:+(a::Union{Harmonic,SquareLattice}, b::Union{Harmonic,SquareLattice}) = PotentialSum([a, b])
+const PotentialTerm = Union{Harmonic,SquareLattice,OpticalLattice}
+Base.:+(a::PotentialTerm, b::PotentialTerm) = PotentialSum([a, b])
+Base.:+(a::PotentialSum, b::PotentialTerm) = PotentialSum([a.terms; b])
 struct GaussianPair; g::Float64; sigma::Float64; end
 (gp::GaussianPair)(r1, r2, tau) =
     exp(-tau / 2 * (gp.g * exp(-sum(abs2, r1) / (2gp.sigma^2)) +
@@ -148,19 +200,29 @@ function determine_nnrange(propint, τ::Float64, a::Float64, b::Float64)
 end
 
 function potential_terms(V)
-    omega, V0, a = 0.0, 0.0, 1.0
+    omega, V0, a, beams = 0.0, 0.0, 1.0, nothing
     for t in (V isa PotentialSum ? V.terms : [V])
         if t isa Harmonic
             omega = t.omega
         elseif t isa SquareLattice
             V0, a = t.V0, t.a
+        elseif t isa OpticalLattice
+            beams === nothing || error("one optical lattice per potential")
+            beams = t
         elseif t === zero || t isa Function && t(zeros(2)) == 0 && t(ones(2)) == 0
             nothing
         else
-            error("potential must be Harmonic, SquareLattice or their sum")
+            error("potential must be Harmonic, SquareLattice, OpticalLattice or their sum")
         end
     end
-    return omega, V0, a
+    return omega, V0, a, beams
+end
+
+function attach_beams(h::Ptr{Cvoid}, b)
+    b === nothing && return nothing
+    check(ccall((:pimc_set_beams, libpimc), Cint,
+                (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cdouble, Cdouble, Cint),
+                h, -1, b.angles, length(b.angles), b.scale, b.depth, b.helical))
 end
 
 # ---------------------------------------------------------------- System
@@ -180,7 +242,7 @@ function System(potential; dV = zero, dim::Int64 = 2, M::Int64 = 100, N::Int64 =
                 interactions::Bool = false, propint = _ -> 0.0, g::Float64 = 0.0,
                 rₐ::Float64 = 0.0, length_measurement_cycle::Int64 = 10,
                 measure_scheme::Symbol = :c, semantics::Int = 0, seed::UInt64 = UInt64(20261203))
-    omega, V0, a_lat = potential_terms(potential)
+    omega, V0, a_lat, beams = potential_terms(potential)
     pg, ps = 0.0, 1.0
     if interactions
         if propint isa GaussianPair
@@ -202,6 +264,7 @@ function System(potential; dV = zero, dim::Int64 = 2, M::Int64 = 100, N::Int64 =
                propint, a, 10_000, measure_scheme, Dict(N => 0), Dict(N => 0),
                length_measurement_cycle, p, 0)
     finalizer(s -> ccall((:pimc_destroy, libpimc), Cint, (Ptr{Cvoid},), s.handle), s)
+    attach_beams(s.handle, beams)
     if interactions && propint isa ContactPropagator
         tab = Matrix(transpose(propint.table))   # the C side reads it row-major
         check(ccall((:pimc_set_contact_table, libpimc), Cint,
@@ -369,6 +432,7 @@ function ensure_engine!(s::System, nb::Int, cap::Int)
                     (Ptr{Cvoid}, Cint, Ptr{Cdouble}, Cint, Cdouble),
                     h[], -1, tab, s.propint.n, s.propint.range))
     end
+    attach_beams(h[], potential_terms(s.V)[4])
     ccall((:pimc_destroy, libpimc), Cint, (Ptr{Cvoid},), s.handle)
     s.handle = h[]
     s.params = q

@@ -10,8 +10,9 @@ from .api import (ContactPropagator, Counter, Density, Energy, GaussianPair, Har
                   NumbOfSlices, Particle, PolymerCenterOfMass, PotentialSum, RadialDistribution,
                   ReshapeLinear, ReshapeSwapLinear, SingleCenterOfMass, SquareLattice, Step,
                   Superfluid, System, Zero,
-                  acceptance, apply, build_prop_int, density_filename, determine_nnrange,
-                  load_checkpoint, run, save_checkpoint, save_density, save_paths)
+                  OpticalLattice, acceptance, apply, build_prop_int, density_filename,
+                  determine_nnrange, generate_V, lattice_angles, load_checkpoint, run,
+                  save_checkpoint, save_density, save_paths)
 from .engine import (ACCEPT, HARDCORE, REJECT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams,
                      Engine, Mix, contact_table, julia_float, write_density_csv)
 
@@ -23,5 +24,5 @@ __all__ = [
     "SEM_PHYSICAL", "ACCEPT", "REJECT", "SKIP", "HARDCORE", "ContactPropagator",
     "build_prop_int", "determine_nnrange", "contact_table", "RadialDistribution", "Superfluid",
     "save_paths", "save_density", "density_filename", "save_checkpoint", "load_checkpoint",
-    "julia_float", "write_density_csv",
+    "julia_float", "write_density_csv", "OpticalLattice", "generate_V", "lattice_angles",
 ]

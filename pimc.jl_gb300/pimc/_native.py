@@ -151,6 +151,7 @@ SIGNATURES = {
     "pimc_set_radial": [_vp, C.c_int, C.c_int, C.c_double],
     "pimc_get_radial": [_vp, C.c_int, _dp, _ull],
     "pimc_get_params": [_vp, C.c_int, C.POINTER(Params)],
+    "pimc_set_beams": [_vp, C.c_int, _dp, C.c_int, C.c_double, C.c_double, C.c_int],
     "pimc_write_paths_csv": [_vp, C.c_int, C.c_char_p],
     "pimc_write_density_csv": [C.c_char_p, C.c_int, C.c_int, C.c_double, _dp, C.c_ulonglong],
     "pimc_save_checkpoint": [_vp, C.c_char_p],

@@ -56,6 +56,65 @@ class SquareLattice:
         return self.V0 * (np.pi / self.a) * np.sin(2 * np.pi * r / self.a)
 
 
+class OpticalLattice:
+    """depth * normalized_intensity(r, angles, scale; helical) of
+    examples/tools/potentialtools.jl:1-16: K plane waves along (sin a, cos a),
+    phases 2 pi scale (r . (sin a, cos a)) (+ a when helical), the squared
+    modulus of their mean.  Two-dimensional, at most 16 beams."""
+
+    def __init__(self, angles, scale: float, depth: float, helical: bool = False):
+        self.angles = [float(a) for a in angles]
+        if not 0 < len(self.angles) <= 16:
+            raise PimcError("an optical lattice has between 1 and 16 beams")
+        self.scale, self.depth, self.helical = float(scale), float(depth), bool(helical)
+
+    def _phases(self, r):
+        a = np.asarray(self.angles)
+        ph = 2 * np.pi * (r[0] * np.sin(a) + r[1] * np.cos(a)) * self.scale
+        return a, ph + a if self.helical else ph
+
+    def __call__(self, r):
+        _, ph = self._phases(r)
+        return self.depth * (np.mean(np.sin(ph)) ** 2 + np.mean(np.cos(ph)) ** 2)
+
+    def grad(self, r):
+        a, ph = self._phases(r)
+        s, c = np.mean(np.sin(ph)), np.mean(np.cos(ph))
+        w = 2 * np.pi * self.scale
+        d = np.stack([np.sin(a), np.cos(a)])  # dphi/dr per beam, over w
+        return self.depth * 2 * w * (s * (d @ np.cos(ph)) - c * (d @ np.sin(ph))) / len(a)
+
+    def __add__(self, other):
+        return PotentialSum(self, other)
+
+
+def lattice_angles(sym: str):
+    """the beam sets of generate_V (potentialtools.jl:18-39): "l25" and "l65"
+    point the beams at the integer points of the circles x^2 + y^2 = 25 and 65
+    (12 and 16 beams), a = atan2(x, y) so that (sin a, cos a) = (x, y)/R;
+    "cubic" is 2 pi k / 4, k = 0..3"""
+    if sym == "cubic":
+        return [2 * math.pi * k / 4 for k in range(4)]
+    r2 = {"l25": 25, "l65": 65}.get(sym)
+    if r2 is None:
+        raise PimcError(f"unknown lattice {sym!r} (l25, l65, cubic, harmonic)")
+    return sorted(math.atan2(x, y) for x in range(-9, 10) for y in range(-9, 10)
+                  if x * x + y * y == r2)
+
+
+def generate_V(*args, attractive: bool = True, helical: bool = False):
+    """generate_V(scale, depth, sym; attractive) or generate_V(angles, scale,
+    depth; helical) (potentialtools.jl:18-39); sym "harmonic" gives the unit
+    trap 0.5 |r|^2"""
+    if len(args) == 3 and isinstance(args[2], str):
+        scale, depth, sym = args
+        if sym == "harmonic":
+            return Harmonic(1.0)
+        return OpticalLattice(lattice_angles(sym), scale, -depth if attractive else depth)
+    angles, scale, depth = args
+    return OpticalLattice(angles, scale, depth, helical)
+
+
 class PotentialSum:
     def __init__(self, *terms):
         self.terms = terms
@@ -168,19 +227,23 @@ def determine_nnrange(propint, τ: float, a: float, b: float) -> float:
 
 
 def _potential_terms(potential):
-    omega, V0, a = 0.0, 0.0, 1.0
+    omega, V0, a, beams = 0.0, 0.0, 1.0, None
     terms = potential.terms if isinstance(potential, PotentialSum) else (potential,)
     for t in terms:
         if isinstance(t, Harmonic):
             omega = t.omega
         elif isinstance(t, SquareLattice):
             V0, a = t.V0, t.a
+        elif isinstance(t, OpticalLattice):
+            if beams is not None:
+                raise PimcError("one optical lattice per potential")
+            beams = t
         elif isinstance(t, Zero) or t is None:
             pass
         else:
-            raise PimcError("potential must be Harmonic, SquareLattice, Zero or a sum of them; "
-                            "arbitrary closures cannot run on the device")
-    return omega, V0, a
+            raise PimcError("potential must be Harmonic, SquareLattice, OpticalLattice, Zero or a "
+                            "sum of them; arbitrary closures cannot run on the device")
+    return omega, V0, a, beams
 
 
 # --------------------------------------------------------------- world view
@@ -203,7 +266,9 @@ class System:
         if kw:
             raise TypeError(f"unknown keyword arguments {sorted(kw)}")
         potential = Zero() if potential is None else potential
-        omega, V0, a = _potential_terms(potential)
+        omega, V0, a, beams = _potential_terms(potential)
+        if beams is not None and dim != 2:
+            raise PimcError("the optical lattice is two-dimensional")
         if dV is not None and not (dV is potential or getattr(dV, "__self__", None) is potential
                                    or dV in ("grad", np.asarray) or callable(dV)):
             raise PimcError("dV must be the potential's gradient")
@@ -244,13 +309,18 @@ class System:
                                pair_g=pair_g, pair_sigma=pair_sigma, r_a=ra,
                                hardcore_a=self.a, semantics=semantics, seed=seed)
         self._contact = contact
+        self._beams = beams
         self.engine = Engine(self._cp)
-        self._attach_contact()
+        self._attach()
         self._eser_seen = 0
 
-    def _attach_contact(self):
+    def _attach(self):
+        """the parts of the potential that are set after creation"""
         if self._contact is not None:
             self.engine.set_contact_table(self._contact.table, self._contact.range)
+        if self._beams is not None:
+            b = self._beams
+            self.engine.set_beams(b.angles, b.scale, b.depth, b.helical)
 
     # System() already ran init_world on the device
     @property
@@ -274,7 +344,7 @@ class System:
         cp.energy_capacity = max(cp.energy_capacity, energy_capacity)
         self.engine.close()
         self.engine = Engine(cp)
-        self._attach_contact()
+        self._attach()
         self.engine.set_raw(x, V, nx)
         self._eser_seen = 0
 

@@ -430,6 +430,13 @@ class Engine:
     def clear_contact(self, chain: int = -1):
         check(self.L.pimc_clear_contact(self.h, chain))
 
+    def set_beams(self, angles, scale: float, depth: float, helical: bool = False,
+                  chain: int = -1):
+        """optical lattice depth * normalized_intensity (potentialtools.jl:1-16)"""
+        a = np.ascontiguousarray(angles, dtype=np.float64)
+        check(self.L.pimc_set_beams(self.h, chain, _dp(a) if a.size else None, a.size,
+                                    float(scale), float(depth), int(bool(helical))))
+
     def set_potential(self, V0, omega, g, chain=0):
         check(self.L.pimc_set_potential(self.h, chain, V0, omega, g))
         p = self.params[chain]

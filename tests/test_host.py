@@ -68,7 +68,7 @@ def test_potentials_are_callable_like_closures():
     V = Harmonic(1.0) + SquareLattice(4.0, 1.0)
     r = np.array([0.25, -0.5])
     assert math.isclose(V(r), 0.5 * 0.3125 + 4.0 * (0.5 + 1.0))
-    assert _potential_terms(V) == (1.0, 4.0, 1.0)
+    assert _potential_terms(V) == (1.0, 4.0, 1.0, None)
     gp = GaussianPair(1.0, 0.5)
     assert 0 < gp([0.1, 0.0], [0.2, 0.0], 0.05) < 1
     from pimc import PimcError

@@ -267,3 +267,38 @@ def test_oracle_superfluid_and_radial_on_known_paths(oracle_mod):
     for r in (0.55, 1.9, 4.0 - 2.45):
         want[int(np.floor(r / 0.1))] += 4
     np.testing.assert_array_equal(hist, want)
+
+
+def test_lattice_angle_sets_match_the_reference():
+    """l25 / l65 (examples/tools/potentialtools.jl) are the directions of the
+    integer points on x^2 + y^2 = 25 and 65; the engine builds them that way"""
+    import json
+    import os
+
+    import pimc
+    from common import HERE
+    gold = json.load(open(os.path.join(HERE, "golden", "lattice_angles.json")))
+    for name in ("l25", "l65"):
+        np.testing.assert_allclose(pimc.lattice_angles(name), sorted(gold[name]), rtol=0, atol=1e-15)
+    assert pimc.lattice_angles("cubic") == [0.0, math.pi / 2, math.pi, 3 * math.pi / 2]
+
+
+def test_oracle_optical_lattice_potential(oracle_mod):
+    """the oracle's V with beams equals normalized_intensity restated in
+    numpy (pimc.OpticalLattice), helical or not, summed with the trap"""
+    import pimc
+    O = oracle_mod
+    L = O.lib()
+    dp = lambda v: v.ctypes.data_as(O.C.POINTER(O.C.c_double))
+    rng = np.random.default_rng(8)
+    for helical in (False, True):
+        ang = pimc.lattice_angles("l25")
+        p = O.make_params(dim=2, N=1, M=4, L=5.0, T=1.0, hcoef=0.5,
+                          beams=(ang, 0.7, -4.0, helical))
+        host = pimc.OpticalLattice(ang, 0.7, -4.0, helical) + pimc.Harmonic(1.0)
+        for _ in range(50):
+            r = rng.uniform(-5, 5, 2)
+            assert abs(L.orc_Vext(O.C.byref(p), dp(r)) - host(r)) <= 1e-12 * max(1.0, abs(host(r)))
+            h = 1e-6
+            fd = [(host(r + h * e) - host(r - h * e)) / (2 * h) for e in np.eye(2)]
+            np.testing.assert_allclose(host.grad(r), fd, rtol=1e-6, atol=1e-6)
