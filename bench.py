@@ -371,7 +371,8 @@ def run_ours(args):
         f = args.launch.split(":")
         eng.set_launch(block=int(f[1]), sweeps_per_launch=int(f[2]),
                        state_smem_bytes=int(f[3]) if len(f) > 3 else 0,
-                       warp_per_chain=f[0] == "warp")
+                       warp_per_chain=f[0] == "warp",
+                       split_phases=int(f[4]) if len(f) > 4 else 0)
         launch = dict(eng.launch, tuned=False)
     elif batched and args.tune:
         launch = eng.tune(sweeps_per_trial=1)
@@ -533,8 +534,8 @@ def main():
     ap.add_argument("--chains", type=int, default=0,
                     help="keep only the first K chains of the workload (small profiling cases)")
     ap.add_argument("--launch", default=None,
-                    help="fixed batched launch shape instead of tuning: cta:BLOCK:SPL:STATE_BYTES "
-                         "or warp:BLOCK:SPL")
+                    help="fixed batched launch shape instead of tuning: "
+                         "cta:BLOCK:SPL:STATE_BYTES[:SPLIT] or warp:BLOCK:SPL")
     ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

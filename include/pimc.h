@@ -165,6 +165,10 @@ typedef struct {
   int block;
   int sweeps_per_launch;
   int state_smem_bytes;
+  /* 0: every phase of a sweep in one launch; 1 (one CTA per chain only):
+   * staging, swaps and the rest as three launches per sweep, each phase
+   * finished by every chain before the next starts */
+  int split_phases;
 } pimc_launch;
 /* time candidate launch shapes on the handle's own chains and keep the
  * fastest; the chains are restored afterwards.  chosen may be NULL. */

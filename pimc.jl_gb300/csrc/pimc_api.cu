@@ -50,6 +50,7 @@ struct Plan {
   int warp_scratch_d = window_scratch_doubles();
   int warp_bytes = 0;          // scratch bytes of one warp's chain (warp mode)
   size_t dyn_smem = 0;
+  int split = 0;               // CTA mode: 1 = staging, swaps, rest as three launches
 };
 
 struct Handle {
@@ -87,6 +88,7 @@ struct Handle {
   int device = 0;              // the device current at creation
   int max_dyn_smem = 0;         // opt-in shared bytes per CTA, less static use
   cudaGraphExec_t gexec = nullptr;
+  long long graph_launches = 0;  // kernel launches in one replay of gexec
   int force_warp = 0;
   // contact-propagator tables on the device, shared by the chains whose
   // (g0, tau, range, n) agree; tables given by the caller are never shared
@@ -551,9 +553,13 @@ int run_plain(Handle *h, long long n) {
 
 // persistent grid: every resident CTA (CTA mode) or resident warp (warp mode)
 // pulls chains from the work queue
-int grid_for(Handle *h, const Plan &p) {
+// resident CTAs (or warps) for a launch of the plan's kernel; phase >= 0
+// names a phase kernel of a split plan
+int grid_for(Handle *h, const Plan &p, int phase = -1) {
   int per_sm = 0;
-  if (sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm) != cudaSuccess || per_sm < 1) per_sm = 1;
+  const cudaError_t e = phase >= 0 ? sweep_phase_occupancy(phase, p.block, p.dyn_smem, &per_sm)
+                                   : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const int units_per_cta = p.mode == 1 ? p.block / 32 : 1;
   const int need = (h->nchains + units_per_cta - 1) / units_per_cta;
   return std::max(1, std::min(need, per_sm * h->num_sms));
@@ -564,8 +570,44 @@ int grid_for(Handle *h, const Plan &p) {
 // the idle warps' issue slots are used by other chains anyway
 bool launch_teams(Handle *h, const Plan &p) {
   int per_sm = 0;
-  if (p.mode != 0 || sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm) != cudaSuccess) return false;
+  if (p.mode != 0) return false;
+  const cudaError_t e = p.split ? sweep_phase_occupancy(0, p.block, p.dyn_smem, &per_sm)
+                                : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
+  if (e != cudaSuccess) return false;
   return h->nchains <= per_sm * h->num_sms;
+}
+
+// the dynamic shared-memory attribute of every kernel the plan launches
+cudaError_t plan_set_smem(const Plan &p) {
+  if (!p.split) return sweep_set_smem(p.mode, p.dyn_smem);
+  for (int ph = 0; ph < 3; ++ph) {
+    const cudaError_t e = sweep_phase_set_smem(ph, p.dyn_smem);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// n sweeps of every chain as launches on the stream: one launch of n sweeps,
+// or for a split plan n rounds of (staging, swaps, rest), each from a reset
+// work queue
+cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long *launches) {
+  if (!p.split) {
+    a.sweeps = n;
+    cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
+    if (e == cudaSuccess) e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);
+    if (launches) *launches += 1;
+    return e;
+  }
+  a.sweeps = 1;
+  for (int s = 0; s < n; ++s)
+    for (int ph = 0; ph < 3; ++ph) {
+      cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
+      if (e == cudaSuccess)
+        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), p.block, p.dyn_smem, h->stream);
+      if (e != cudaSuccess) return e;
+      if (launches) *launches += 1;
+    }
+  return cudaSuccess;
 }
 
 int build_graph(Handle *h) {
@@ -574,13 +616,12 @@ int build_graph(Handle *h) {
   SweepArgs a = sweep_args(h, p);
   a.order = h->d_order;
   a.queue = h->d_queue;
-  a.sweeps = p.spl;
   a.teams = launch_teams(h, p);
-  const int grid = grid_for(h, p);
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
-  launch_sweep(a, p.mode, grid, p.block, p.dyn_smem, h->stream);
+  long long nl = 0;
+  issue_sweeps(h, p, a, p.spl, &nl);
+  h->graph_launches = nl;
   CK(cudaStreamEndCapture(h->stream, &g));
   cudaError_t e = cudaGraphInstantiate(&h->gexec, g, 0);
   cudaGraphDestroy(g);
@@ -590,7 +631,7 @@ int build_graph(Handle *h) {
 
 int run_batched(Handle *h, long long n) {
   const Plan &p = h->bat;
-  CK(sweep_set_smem(p.mode, p.dyn_smem));
+  CK(plan_set_smem(p));
   const int spl = std::max(1, p.spl);
   int rc = build_graph(h);
   if (rc) return rc;
@@ -599,17 +640,14 @@ int run_batched(Handle *h, long long n) {
   const long long full = n / spl, rem = n % spl;
   for (long long i = 0; i < full; ++i) {
     CK(cudaGraphLaunch(h->gexec, h->stream));
-    ++launches;
+    launches += h->graph_launches;
   }
   if (rem) {
     SweepArgs a = sweep_args(h, p);
     a.order = h->d_order;
     a.queue = h->d_queue;
-    a.sweeps = (int)rem;
     a.teams = launch_teams(h, p);
-    CK(cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream));
-    CK(launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream));
-    ++launches;
+    CK(issue_sweeps(h, p, a, (int)rem, &launches));
   }
   CK(cudaEventRecord(h->ev1, h->stream));
   rc = sync_check(h);
@@ -929,7 +967,10 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
   if (l.sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
   if (l.state_smem_bytes < 0 || l.state_smem_bytes > 160 * 1024)
     return fail(PIMC_EARG, "state_smem_bytes must be in [0, 160 KiB]");
+  if (l.split_phases < 0 || l.split_phases > 1 || (l.split_phases && l.warp_per_chain))
+    return fail(PIMC_EARG, "split_phases must be 0, or 1 with one CTA per chain");
   Plan p = plan_smem(h, l.warp_per_chain, l.block, l.sweeps_per_launch, l.state_smem_bytes);
+  p.split = l.split_phases;
   if (h->max_dyn_smem > 0 && p.dyn_smem > (size_t)h->max_dyn_smem)
     return fail(PIMC_EARG, "launch shape needs " + std::to_string(p.dyn_smem) +
                                " shared bytes per CTA, more than the device offers");
@@ -958,6 +999,7 @@ int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
   launch->block = h->bat.block;
   launch->sweeps_per_launch = h->bat.spl;
   launch->state_smem_bytes = h->bat.state_cap;
+  launch->split_phases = h->bat.split;
   return PIMC_OK;
 }
 
@@ -986,6 +1028,9 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
     for (int b : {64, 128, 256})
       for (int m : {0, 32 * 1024, kStateBudget}) cand.push_back({0, b, s, m});
     for (int b : {64, 128, 256}) cand.push_back({1, b, s, 0});
+    // the phases as separate launches
+    for (int b : {64, 128, 256})
+      for (int m : {0, 32 * 1024}) cand.push_back({0, b, s, m, 1});
   }
   double best = 1e300;
   pimc_launch keep;

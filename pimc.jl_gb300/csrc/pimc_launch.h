@@ -73,6 +73,12 @@ struct AdjArgs {
 cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size_t smem,
                          cudaStream_t s);
 cudaError_t sweep_set_smem(int mode, size_t smem);
+// the sweep as three launches per sweep (phase 0 staging, 1 swaps, 2 the
+// rest), one CTA per chain; a.sweeps must be 1
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int grid, int block, size_t smem,
+                               cudaStream_t s);
+cudaError_t sweep_phase_set_smem(int phase, size_t smem);
+cudaError_t sweep_phase_occupancy(int phase, int block, size_t smem, int *blocks_per_sm);
 size_t sweep_ctl_bytes();
 cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm);
 cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s);

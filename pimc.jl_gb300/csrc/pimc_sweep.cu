@@ -80,7 +80,44 @@ struct SmemCtl {
 };
 
 // one sweep of one chain by a group: the whole CTA, or one warp on its own
+// the phases of a sweep; a kernel runs the ones its mask names, so that each
+// phase can run as its own launch with its own register budget
+enum : int { SW_STAGE = 1, SW_SWAP = 2, SW_REST = 4, SW_ALL = 7 };
+
+// closes one phase of move kind q: adds its tallies (attempts, accepts,
+// skips, bead updates) to the chain's counters and adapts the phase's own
+// variable (adjust!, src/updates/helper.jl:22-52) from this sweep's
+// acceptance.  Only the phase itself reads that variable, so adapting at its
+// end is the same as adapting at the end of the sweep.
 template <bool WARP>
+__device__ void close_phase(SmemCtl &sc, double *red, int q, double (&t)[4]) {
+  using G = Group<WARP>;
+  G::template sum<4>(t, red);
+  if (G::rank() == 0) {
+    ChainVar &v = sc.v;
+    const MixDev &mix = sc.mix;
+    v.att[q] += (unsigned long long)t[0];
+    v.acc[q] += (unsigned long long)t[1];
+    v.skips += (unsigned long long)t[2];
+    v.bead_updates += t[3];
+    // the reference divides by an empty queue (NaN) and leaves var alone
+    if (mix.adapt && t[0] > 0) {
+      const double r = t[1] / t[0];
+      if (q == MV_STAGE)
+        adapt_slices(v.stage_m, r, mix.stage_min, mix.stage_max, mix.stage_minacc, mix.stage_maxacc);
+      else if (q == MV_SWAP)
+        adapt_slices(v.swap_m, r, mix.swap_min, mix.swap_max, mix.swap_minacc, mix.swap_maxacc);
+      else if (q == MV_COM)
+        adapt_step(v.com_step, r, mix.com_minstep, mix.com_maxstep, mix.com_minacc, mix.com_maxacc);
+      else
+        adapt_step(v.pcom_step, r, mix.pcom_minstep, mix.pcom_maxstep, mix.pcom_minacc,
+                   mix.pcom_maxacc);
+    }
+  }
+  G::sync();
+}
+
+template <bool WARP, int PH>
 __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *scratch,
                           int warp_scratch_d, bool teams) {
   using G = Group<WARP>;
@@ -92,10 +129,11 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
   const bool serial_local = chain_serial_local(d);
   const unsigned long long sweep = sc.v.sweep;
   double *wsb = (double *)scratch + (size_t)warp * warp_scratch_d;
-  // per-thread tallies: attempts x4, accepts x4, skips, bead updates
-  double tal[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 
   // ---- staging phases (ReshapeLinear)
+  if (PH & SW_STAGE) {
+  // per-thread tallies: attempts, accepts, skips, bead updates
+  double tal[4] = {0, 0, 0, 0};
   for (int ph = 0; ph < mix.staging_phases; ++ph) {
     int ell = sc.v.stage_m;
     ell = max(2, min(ell, min(M - 1, WMAX)));
@@ -117,8 +155,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
           const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
           const int r = window_thread(c, n, st, m, dr, false, nullptr);
           tal[0] += 1.0;
-          tal[4] += r;
-          tal[9] += m - 1;
+          tal[1] += r;
+          tal[3] += m - 1;
         }
       } else {
         for (int it = warp; it < items; it += nwarps) {
@@ -131,8 +169,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
           const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
           if (lane == 0) {
             tal[0] += 1.0;
-            tal[4] += r == RES_ACCEPT;
-            tal[9] += m - 1;
+            tal[1] += r == RES_ACCEPT;
+            tal[3] += m - 1;
           }
         }
       }
@@ -152,8 +190,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
             const int r = window_team(c, tm, n, st, m, dr, tb, warp_scratch_d);
             if (tm.w == 0 && lane == 0) {
               tal[0] += 1.0;
-              tal[4] += r == RES_ACCEPT;
-              tal[9] += m - 1;
+              tal[1] += r == RES_ACCEPT;
+              tal[3] += m - 1;
             }
           }
       }
@@ -171,17 +209,20 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
           const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
           if (lane == 0) {
             tal[0] += 1.0;
-            tal[4] += r == RES_ACCEPT;
-            if (r != RES_HARDCORE) tal[9] += m - 1;
+            tal[1] += r == RES_ACCEPT;
+            if (r != RES_HARDCORE) tal[3] += m - 1;
           }
         }
       }
     }
     G::sync();
   }
+  if (mix.staging_phases > 0) close_phase<WARP>(sc, red, MV_STAGE, tal);
+  }
 
   // ---- permutation swaps (ReshapeSwapLinear), one at a time by the group
-  if (N > 1 && mix.swaps_per_sweep > 0) {
+  if ((PH & SW_SWAP) && N > 1 && mix.swaps_per_sweep > 0) {
+    double tal[4] = {0, 0, 0, 0};
     SwapScratch S;
     S.carve(scratch, N, nwarps);
     const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
@@ -197,18 +238,22 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
       const int r = swap_group<WARP, true>(c, j0, m, n1, upick, dr, S, red, nullptr, nullptr);
       if (tid == 0) {
         if (r == RES_SKIP) {
-          tal[8] += 1.0;
+          tal[2] += 1.0;
         } else {
-          tal[1] += 1.0;
-          tal[5] += r == RES_ACCEPT;
-          if (r != RES_HARDCORE) tal[9] += 2.0 * (m - 1);
+          tal[0] += 1.0;
+          tal[1] += r == RES_ACCEPT;
+          if (r != RES_HARDCORE) tal[3] += 2.0 * (m - 1);
         }
       }
     }
     G::sync();
+    close_phase<WARP>(sc, red, MV_SWAP, tal);
   }
 
+  if (!(PH & SW_REST)) return;
+
   // ---- single-path centre of mass
+  double tal[4] = {0, 0, 0, 0};
   for (int ph = 0; ph < mix.com_phases; ++ph) {
     const double step = sc.v.com_step;
     if (!serial_local) {
@@ -216,9 +261,9 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
         if (c.next[n] != n) continue;
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
         const int r = com_thread(c, n, step, dr);
-        tal[2] += 1.0;
-        tal[6] += r;
-        tal[9] += M;
+        tal[0] += 1.0;
+        tal[1] += r;
+        tal[3] += M;
       }
       G::sync();
     } else {
@@ -229,16 +274,19 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
         const int r = com_group<WARP>(c, n, false, step, dr, cs, red, sc.shift, &sc.iflag[2], nullptr);
         if (tid == 0) {
-          tal[2] += 1.0;
-          tal[6] += r == RES_ACCEPT;
-          if (r != RES_HARDCORE) tal[9] += M;
+          tal[0] += 1.0;
+          tal[1] += r == RES_ACCEPT;
+          if (r != RES_HARDCORE) tal[3] += M;
         }
         G::sync();
       }
     }
   }
 
+  if (mix.com_phases > 0) close_phase<WARP>(sc, red, MV_COM, tal);
+
   // ---- cycle centre of mass, one attempt per cycle (led by its lowest index)
+  double tlp[4] = {0, 0, 0, 0};
   for (int ph = 0; ph < mix.polymer_com_phases; ++ph) {
     ComScratch cs;
     cs.carve(scratch, N, M);
@@ -258,45 +306,14 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
                                     &sc.iflag[3]);
       const int np = sc.iflag[3];
       if (tid == 0) {
-        tal[3] += 1.0;
-        tal[7] += r == RES_ACCEPT;
-        if (r != RES_HARDCORE) tal[9] += (double)M * np;
+        tlp[0] += 1.0;
+        tlp[1] += r == RES_ACCEPT;
+        if (r != RES_HARDCORE) tlp[3] += (double)M * np;
       }
       G::sync();
     }
   }
-
-  // ---- tallies and adaptation (once per sweep)
-  {
-    double t8[8] = {tal[0], tal[1], tal[2], tal[3], tal[4], tal[5], tal[6], tal[7]};
-    double t2[2] = {tal[8], tal[9]};
-    G::template sum<8>(t8, red);
-    G::template sum<2>(t2, red);
-    if (tid == 0) {
-      ChainVar &v = sc.v;
-      for (int q = 0; q < 4; ++q) {
-        v.att[q] += (unsigned long long)t8[q];
-        v.acc[q] += (unsigned long long)t8[4 + q];
-      }
-      v.skips += (unsigned long long)t2[0];
-      v.bead_updates += t2[1];
-      if (mix.adapt) {
-        // the reference divides by an empty queue (NaN) and leaves var alone
-        if (t8[0] > 0)
-          adapt_slices(v.stage_m, t8[4] / t8[0], mix.stage_min, mix.stage_max, mix.stage_minacc,
-                       mix.stage_maxacc);
-        if (t8[1] > 0)
-          adapt_slices(v.swap_m, t8[5] / t8[1], mix.swap_min, mix.swap_max, mix.swap_minacc,
-                       mix.swap_maxacc);
-        if (t8[2] > 0)
-          adapt_step(v.com_step, t8[6] / t8[2], mix.com_minstep, mix.com_maxstep, mix.com_minacc,
-                     mix.com_maxacc);
-        if (t8[3] > 0)
-          adapt_step(v.pcom_step, t8[7] / t8[3], mix.pcom_minstep, mix.pcom_maxstep,
-                     mix.pcom_minacc, mix.pcom_maxacc);
-      }
-    }
-  }
+  if (mix.polymer_com_phases > 0) close_phase<WARP>(sc, red, MV_PCOM, tlp);
 
   // ---- measurement cadence (measurement_Z_sector)
   if (mix.measure_every > 0 && ((sweep + 1) % (unsigned long long)mix.measure_every) == 0) {
@@ -337,13 +354,14 @@ __global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
     ++iter;
     if (ci >= a.nchains) break;
     CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<true>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<true, SW_ALL>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
     if (lane == 0) a.var[sc.chain] = sc.v;
     __syncwarp();
   }
 }
 
-__global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
+template <int PH>
+__device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SmemCtl sc;
   __shared__ double red[256];
@@ -388,7 +406,7 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
       __syncthreads();
     }
     unsigned char *scratch = smem + a.state_bytes;
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<false>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
+    for (int s = 0; s < a.sweeps; ++s) sweep_one<false, PH>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
       unsigned *gq = (unsigned *)(a.dpool + d.xq_off);
@@ -402,6 +420,17 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) {
     __syncthreads();
   }
 }
+
+// one CTA per chain, every phase of the sweep in one launch
+__global__ void __launch_bounds__(512) k_sweep(SweepArgs a) { sweep_cta<SW_ALL>(a); }
+
+// the sweep's phases as separate launches (staging, swaps, the rest), each
+// compiled and scheduled on its own: every chain of the batch finishes one
+// phase before any starts the next, so the longest chain of each phase, not
+// the longest sum over phases, sets a sweep's time
+__global__ void __launch_bounds__(512) k_sweep_stage(SweepArgs a) { sweep_cta<SW_STAGE>(a); }
+__global__ void __launch_bounds__(512) k_sweep_swap(SweepArgs a) { sweep_cta<SW_SWAP>(a); }
+__global__ void __launch_bounds__(512) k_sweep_rest(SweepArgs a) { sweep_cta<SW_REST>(a); }
 
 // ---------------------------------------------------------------------------
 // single moves with injected draws (one CTA, state in global memory)
@@ -801,6 +830,29 @@ cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size
   else k_sweep<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
+// phase kernels: 0 staging, 1 swaps, 2 the rest
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int grid, int block, size_t smem,
+                               cudaStream_t s) {
+  if (phase == 0) k_sweep_stage<<<grid, block, smem, s>>>(a);
+  else if (phase == 1) k_sweep_swap<<<grid, block, smem, s>>>(a);
+  else k_sweep_rest<<<grid, block, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t sweep_phase_set_smem(int phase, size_t smem) {
+  const void *k = phase == 0 ? (const void *)k_sweep_stage
+                             : phase == 1 ? (const void *)k_sweep_swap : (const void *)k_sweep_rest;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t sweep_phase_occupancy(int phase, int block, size_t smem, int *blocks_per_sm) {
+  if (phase == 0)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_stage, block, smem);
+  if (phase == 1)
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_swap, block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_rest, block, smem);
+}
+
 cudaError_t sweep_set_smem(int mode, size_t smem) {
   if (mode == 1)
     return cudaFuncSetAttribute(k_sweep_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

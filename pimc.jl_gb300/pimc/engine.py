@@ -249,8 +249,10 @@ class Engine:
         return self.launch
 
     def set_launch(self, block: int, sweeps_per_launch: int = 1,
-                   state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False):
-        l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes)
+                   state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False,
+                   split_phases: int = 0):
+        l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes,
+                   int(split_phases))
         check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
 
     @property
@@ -259,7 +261,8 @@ class Engine:
         l = Launch()
         check(self.L.pimc_batch_get_launch(self.h, C.byref(l)))
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
-                "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes}
+                "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
+                "split_phases": l.split_phases}
 
     def fp64_peak(self) -> float:
         """measured FP64 FMA throughput of the device, TFLOP/s"""

@@ -174,7 +174,9 @@ def test_batched_equals_plain_and_tuner_is_transparent():
     shapes = [None, dict(block=64, sweeps_per_launch=2, warp_per_chain=True),
               dict(block=256, sweeps_per_launch=1, warp_per_chain=True),
               dict(block=128, sweeps_per_launch=3, state_smem_bytes=0),
-              dict(block=256, sweeps_per_launch=1, state_smem_bytes=100 * 1024)]
+              dict(block=256, sweeps_per_launch=1, state_smem_bytes=100 * 1024),
+              dict(block=64, sweeps_per_launch=2, state_smem_bytes=0, split_phases=1),
+              dict(block=128, sweeps_per_launch=1, state_smem_bytes=32 * 1024, split_phases=1)]
     b = Engine(ps)
     for i, p in enumerate(ps):
         b.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
