@@ -50,10 +50,15 @@ CONTACT_G0, CONTACT_RANGE = 1.16, 12.0
 # --set full), by acceptance semantics: DRAM bytes (dram__bytes_read.sum +
 # dram__bytes_write.sum) and FP64 flops (dadd + dmul + 2 dfma thread
 # instructions) over the launch's bead updates
-C4_PER_BEAD = {
-    "physical": {"dram_bytes": 188.4, "fp64_flops": 1017.0},    # 3.52 GB, 19.0 G / 18.70 M
-    "reference": {"dram_bytes": 269.7, "fp64_flops": 204.0},    # 4.82 GB, 3.65 G / 17.87 M
+PER_BEAD = {
+    # fused sweep kernel (one launch per sweep)
+    ("c4", "physical", "k_sweep"): {"dram_bytes": 188.4, "fp64_flops": 1017.0},   # 3.52 GB, 19.0 G / 18.70 M
+    ("c4", "reference", "k_sweep"): {"dram_bytes": 269.7, "fp64_flops": 204.0},   # 4.82 GB, 3.65 G / 17.87 M
+    # the swap launch of the split sweep (its bead updates are the swaps' 2(m-1)
+    # per attempt; every attempt also reads the N heat-bath candidates)
+    ("c4", "reference", "k_sweep_swap"): {"dram_bytes": 993.7, "fp64_flops": 547.2},  # 3.02 GB, 1.66 G / 3.037 M
 }
+ROOF_SWEEPS = 2  # sweeps of the per-phase timing pass
 
 
 def c4_chain_list(n=4096):
@@ -404,49 +409,69 @@ def run_ours(args):
     if batched and launch:
         cfg["launch"] = dict({"tuned": True}, **launch)
     out["config"] = cfg
-    # roofline of the sweep kernel: algorithmic bytes per bead-update (48 B
-    # pair-free, 64 B with the pair interaction) over its measured duration
+    # roofline of the dominant kernel.  A split launch shape runs each sweep as
+    # three kernels (staging, swaps, the rest): their device times come from
+    # a separate pass with CUDA events between the phases, and the kernel
+    # with the largest share is the one the roofline describes.  Algorithmic
+    # bytes per bead update: 48 B pair-free, 64 B with the pair interaction.
     bpb = np.array([64.0 if c.interactions else 48.0 for c in chains])
     w = np.array([c.N * c.M for c in chains], dtype=float)
     bytes_per_bead = float((bpb * w).sum() / w.sum())
-    launch_s = (ms / 1e3) / max(launches, 1)
-    beads_per_launch = beads / max(launches, 1)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     hbm = float(peaks.get("hbm_gbs", 6800.0))
+    split = bool(launch and launch.get("split_phases"))
+    if split:
+        p0 = eng.total_stats()
+        ph_ms = eng.phase_times(ROOF_SWEEPS)
+        p1 = eng.total_stats()
+        kb = [p1.bead_updates_kind[k] - p0.bead_updates_kind[k] for k in range(4)]
+        ph_beads = [kb[0], kb[1], kb[2] + kb[3]]
+        top = int(np.argmax(ph_ms))
+        kname = ["k_sweep_stage", "k_sweep_swap", "k_sweep_rest"][top]
+        launch_s = ph_ms[top] / 1e3 / ROOF_SWEEPS
+        beads_per_launch = ph_beads[top] / ROOF_SWEEPS
+        kernel_share = {n: float(t / ph_ms.sum()) for n, t in
+                        zip(["k_sweep_stage", "k_sweep_swap", "k_sweep_rest"], ph_ms)}
+    else:
+        kname = "k_sweep" if batched else "k_sweep (plain)"
+        launch_s = (ms / 1e3) / max(launches, 1)
+        beads_per_launch = beads / max(launches, 1)
+        kernel_share = {kname: 1.0}
     achieved = beads_per_launch * bytes_per_bead / launch_s / 1e9
-    # DRAM bytes per launch: the ncu capture of the same kernel on a subset of
-    # the workload, scaled by the bead updates a full launch performs
-    tpb = args.traffic_per_bead
-    if tpb is None and args.workload == "c4":
-        tpb = C4_PER_BEAD[args.semantics]["dram_bytes"]
+    # DRAM bytes and FP64 flops per bead update of that kernel: an ncu capture
+    # of the same kernel on the first 1216 chains, scaled by the bead updates
+    # a full launch performs
+    per_bead = PER_BEAD.get((args.workload, args.semantics, kname), {})
+    tpb = args.traffic_per_bead if args.traffic_per_bead is not None else per_bead.get("dram_bytes")
     traffic = beads_per_launch * tpb if tpb else None
-    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                       "frac": achieved / hbm, "traffic": traffic,
+    out["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": hbm,
+                       "unit": "GB/s", "frac": achieved / hbm, "traffic": traffic,
                        "peak_source": ("MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                                        else "fallback 6.8 TB/s (of fallback)"),
                        "bytes_per_bead_update": bytes_per_bead,
-                       "traffic_source": ("ncu dram__bytes_read+write of k_sweep on the first 1216 "
-                                          "C4 chains, per bead update, times this launch's "
-                                          "bead updates" if tpb else None),
+                       "launch_ms": launch_s * 1e3, "bead_updates_per_launch": beads_per_launch,
+                       "kernel_share_of_sweep": kernel_share,
+                       "traffic_source": (f"ncu dram__bytes_read+write of {kname} on the first 1216 "
+                                          "chains, per bead update, times this launch's bead "
+                                          "updates" if tpb else None),
                        "note": "not the binding roof: the sweep is FP64-pipe and latency bound, "
                                "see roofline_fp64"}
     fp64_peak = args.fp64_peak if args.fp64_peak else eng.fp64_peak()
     fpb = args.fp64_flops_per_bead
-    measured_fpb = args.workload == "c4" and C4_PER_BEAD[args.semantics]["fp64_flops"]
+    measured_fpb = fpb is None and "fp64_flops" in per_bead
     if fpb is None:
-        fpb = C4_PER_BEAD[args.semantics]["fp64_flops"] if measured_fpb else 25.0
+        fpb = per_bead.get("fp64_flops", 25.0)
     flops = beads_per_launch * fpb / launch_s / 1e12
-    out["roofline_fp64"] = {"bound": "fp64", "achieved": flops, "peak": fp64_peak,
+    out["roofline_fp64"] = {"bound": "fp64", "kernel": kname, "achieved": flops, "peak": fp64_peak,
                             "unit": "TFLOP/s", "frac": flops / fp64_peak,
                             "flops_per_bead_update": fpb,
-                            "flops_source": ("ncu dadd+dmul+2*dfma thread instructions of k_sweep on "
-                                             "the first 1216 C4 chains, per bead update"
-                                             if measured_fpb and args.fp64_flops_per_bead is None
-                                             else "algorithmic estimate (no pair terms)"),
+                            "flops_source": (f"ncu dadd+dmul+2*dfma thread instructions of {kname} "
+                                             "on the first 1216 chains, per bead update"
+                                             if measured_fpb else "algorithmic estimate (no pair terms)"),
                             "peak_source": "pimc_fp64_peak: DFMA throughput probe on this GPU (measured)"}
     out["clocks"] = clk.summary()
     # plain path: one launch per chain per sweep (no queue, no graph), timed

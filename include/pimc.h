@@ -114,6 +114,7 @@ typedef struct pimc_stats {
   unsigned long long measurements;
   int stage_slices, swap_slices;   /* current adaptive var.m */
   double com_step, pcom_step;      /* current adaptive step */
+  double bead_updates_kind[4];     /* bead_updates by move kind */
 } pimc_stats;
 
 /* ---------------- lifecycle: System constructor (src/system.jl:129-167) */
@@ -330,6 +331,11 @@ int pimc_clear_contact(void *handle, int chain);
  * chains per thread over the whole GPU, best of three timed launches) --
  * the denominator of the sweep's FP64 roofline */
 int pimc_fp64_peak(void *handle, double *tflops);
+/* measurement utility: n sweeps of every chain as separately issued phase
+ * launches (staging, swaps, rest; one launch when the launch shape is not
+ * split) with CUDA events around each phase; ms[3] receives the device time
+ * of each phase summed over the sweeps */
+int pimc_batch_phase_times(void *handle, long long n_sweeps, double ms[3]);
 /* device time of the last run call (CUDA events on the handle's stream) */
 int pimc_last_run_ms(void *handle, double *ms);
 /* kernel launches issued by the last run call */

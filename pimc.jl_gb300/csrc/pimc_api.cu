@@ -504,6 +504,7 @@ void fill_stats(const ChainVar &v, pimc_stats *o) {
   o->swap_slices = v.swap_m;
   o->com_step = v.com_step;
   o->pcom_step = v.pcom_step;
+  for (int q = 0; q < 4; ++q) o->bead_updates_kind[q] = v.beads_kind[q];
 }
 
 SweepArgs sweep_args(Handle *h, const Plan &p) {
@@ -976,6 +977,47 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
                                " shared bytes per CTA, more than the device offers");
   *out = p;
   return PIMC_OK;
+}
+
+int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
+  Handle *h = H(handle);
+  if (!h || !ms || n < 1) return fail(PIMC_EARG, "bad argument");
+  const Plan &p = h->bat;
+  CK(plan_set_smem(p));
+  SweepArgs a = sweep_args(h, p);
+  a.order = h->d_order;
+  a.queue = h->d_queue;
+  a.teams = launch_teams(h, p);
+  const int nph = p.split ? 3 : 1;
+  cudaEvent_t ev[4];
+  for (int k = 0; k <= nph; ++k) CK(cudaEventCreate(&ev[k]));
+  double acc[3] = {0.0, 0.0, 0.0};
+  cudaError_t e = cudaSuccess;
+  for (long long s = 0; s < n && e == cudaSuccess; ++s) {
+    cudaEventRecord(ev[0], h->stream);
+    for (int ph = 0; ph < nph && e == cudaSuccess; ++ph) {
+      e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
+      if (e != cudaSuccess) break;
+      if (p.split) {
+        a.sweeps = 1;
+        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), p.block, p.dyn_smem, h->stream);
+      } else {
+        a.sweeps = 1;
+        e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(ev[ph + 1], h->stream);
+    }
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[nph]);
+    for (int ph = 0; ph < nph && e == cudaSuccess; ++ph) {
+      float t = 0.f;
+      e = cudaEventElapsedTime(&t, ev[ph], ev[ph + 1]);
+      acc[ph] += t;
+    }
+  }
+  for (int k = 0; k <= nph; ++k) cudaEventDestroy(ev[k]);
+  if (e != cudaSuccess) return fail(PIMC_ECUDA, std::string("phase timing: ") + cudaGetErrorString(e));
+  for (int k = 0; k < 3; ++k) ms[k] = acc[k];
+  return sync_check(h);
 }
 
 int pimc_batch_set_launch(void *handle, const pimc_launch *launch) {
@@ -1647,6 +1689,7 @@ int pimc_get_total_stats(void *handle, pimc_stats *out) {
     }
     out->skips += x.skips;
     out->bead_updates += x.bead_updates;
+    for (int q = 0; q < 4; ++q) out->bead_updates_kind[q] += x.beads_kind[q];
     out->sweeps += x.sweep;
     out->measurements += x.n_meas;
   }

@@ -100,6 +100,7 @@ __device__ void close_phase(SmemCtl &sc, double *red, int q, double (&t)[4]) {
     v.acc[q] += (unsigned long long)t[1];
     v.skips += (unsigned long long)t[2];
     v.bead_updates += t[3];
+    v.beads_kind[q] += t[3];
     // the reference divides by an empty queue (NaN) and leaves var alone
     if (mix.adapt && t[0] > 0) {
       const double r = t[1] / t[0];

@@ -115,6 +115,7 @@ struct ChainVar {
   int err;
   int pad_;
   unsigned long long rdf_meas;  // measurements in the pair-distance histogram
+  double beads_kind[4];         // bead updates by move kind
 };
 
 // device error codes (ChainVar::err, first error wins)

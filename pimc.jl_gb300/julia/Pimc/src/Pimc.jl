@@ -65,6 +65,7 @@ struct PimcStats
     skips::Culonglong; bead_updates::Cdouble; sweeps::Culonglong
     measurements::Culonglong; stage_slices::Cint; swap_slices::Cint
     com_step::Cdouble; pcom_step::Cdouble
+    bead_updates_kind::NTuple{4,Cdouble}
 end
 
 function check(rc)

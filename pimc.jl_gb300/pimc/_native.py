@@ -99,6 +99,7 @@ class Stats(C.Structure):
         ("skips", C.c_ulonglong), ("bead_updates", C.c_double), ("sweeps", C.c_ulonglong),
         ("measurements", C.c_ulonglong), ("stage_slices", C.c_int), ("swap_slices", C.c_int),
         ("com_step", C.c_double), ("pcom_step", C.c_double),
+        ("bead_updates_kind", C.c_double * 4),
     ]
 
 
@@ -173,6 +174,7 @@ SIGNATURES = {
     "pimc_get_contact_table": [_vp, C.c_int, _dp, C.c_size_t, _ip, _dp],
     "pimc_clear_contact": [_vp, C.c_int],
     "pimc_fp64_peak": [_vp, _dp],
+    "pimc_batch_phase_times": [_vp, C.c_longlong, _dp],
     "pimc_last_run_ms": [_vp, _dp],
     "pimc_last_run_launches": [_vp, C.POINTER(C.c_longlong)],
     "pimc_set_option": [_vp, C.c_int, C.c_longlong],

@@ -138,6 +138,7 @@ class EngineStats:
     swap_slices: int = 0
     com_step: float = 0.0
     pcom_step: float = 0.0
+    bead_updates_kind: list = field(default_factory=list)
 
 
 class Engine:
@@ -263,6 +264,13 @@ class Engine:
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
                 "split_phases": l.split_phases}
+
+    def phase_times(self, n_sweeps: int = 2):
+        """device ms of the staging, swap and remaining phases over n sweeps,
+        issued as separate launches with events between them"""
+        ms = np.zeros(3)
+        check(self.L.pimc_batch_phase_times(self.h, int(n_sweeps), _dp(ms)))
+        return ms
 
     def fp64_peak(self) -> float:
         """measured FP64 FMA throughput of the device, TFLOP/s"""
@@ -449,7 +457,8 @@ class Engine:
     @staticmethod
     def _stats(s: Stats) -> EngineStats:
         return EngineStats(list(s.attempts), list(s.accepts), s.skips, s.bead_updates, s.sweeps,
-                           s.measurements, s.stage_slices, s.swap_slices, s.com_step, s.pcom_step)
+                           s.measurements, s.stage_slices, s.swap_slices, s.com_step, s.pcom_step,
+                           list(s.bead_updates_kind))
 
     def stats(self, chain=0) -> EngineStats:
         s = Stats()
