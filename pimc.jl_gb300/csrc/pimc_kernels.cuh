@@ -336,14 +336,21 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       ls += e;
     }
     ssum = warp_sum(ls);
-    const W inv_s = W(1) / ssum;
-    W lq = W(0);
-    for (int i = i0; i < i1; ++i) {
-      const W q = Sw[i] * inv_s;
-      Sw[i] = q;
-      lq += q;
+    W lq = ls, target;
+    if (FAST) {
+      // sweeps search the unnormalised weights against u times their sum
+      target = (W)u_pick * ssum;
+    } else {
+      // attempts normalise first, as StatsBase.sample does
+      const W inv_s = W(1) / ssum;
+      lq = W(0);
+      for (int i = i0; i < i1; ++i) {
+        const W q = Sw[i] * inv_s;
+        Sw[i] = q;
+        lq += q;
+      }
+      target = (W)u_pick * warp_sum(lq);
     }
-    const W target = (W)u_pick * warp_sum(lq);
     // first i with cumulative weight >= target (StatsBase.sample)
     W cw = warp_exclusive_scan(lq);
     int cand = 0x7fffffff;
@@ -939,9 +946,12 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
         if (r2a <= rc2) {
           const int bn = j == M - 1 ? c.next[b] : b;
           const double r2b = mi2(d, c.X(0, in, jn), c.Xd(1, in, jn), c.X(0, bn, jn), c.Xd(1, bn, jn));
-          const double v1 = vpair(d, r2a), v2 = vpair(d, r2b);
-          s[3] += 0.5 * d.tau * (v1 + v2);
-          s[4] += 0.5 * d.tau * (-2.0 * cg * r2a * v1 - 2.0 * cg * r2b * v2);
+          // the pair exponentials e = exp(x), x = -r^2/(2 s^2), and x e; the
+          // factors g tau/2 are applied once at the end
+          const double xa = -r2a * cg, xb = -r2b * cg;
+          const double ea = exp_neg(xa), eb = exp_neg(xb);
+          s[3] += ea + eb;
+          s[4] = fma(xa, ea, fma(xb, eb, s[4]));
         }
       }
       __syncwarp();
@@ -1009,8 +1019,10 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
     out[0] = (double)(dim * N) / (2.0 * tau) - 1.0 / (4.0 * d.lambda * (tau * tau) * M) * s[0] +
              1.0 / (2.0 * M) * s[1];
     out[1] = 1.0 / (2.0 * M) * s[2] + 1.0 / (2.0 * M) * s[1];
-    out[2] = pair ? s[3] / (M * tau) : 0.0;
-    out[3] = pair ? out[2] + s[4] / (2.0 * M * tau) : 0.0;
+    // pair energy sum (tau/2) g (e_a + e_b) / (M tau) and its virial part
+    // sum (tau/2) g (-2 r^2/(2 s^2)) (e_a, e_b) / (2 M tau)
+    out[2] = pair ? d.g * s[3] / (2.0 * M) : 0.0;
+    out[3] = pair ? out[2] + d.g * s[4] / (2.0 * M) : 0.0;
   }
 }
 
