@@ -377,7 +377,8 @@ def run_ours(args):
         eng.set_launch(block=int(f[1]), sweeps_per_launch=int(f[2]),
                        state_smem_bytes=int(f[3]) if len(f) > 3 else 0,
                        warp_per_chain=f[0] == "warp",
-                       split_phases=int(f[4]) if len(f) > 4 else 0)
+                       split_phases=int(f[4]) if len(f) > 4 else 0,
+                       phase_block=[int(b) for b in f[5].split(",")] if len(f) > 5 else (0, 0, 0))
         launch = dict(eng.launch, tuned=False)
     elif batched and args.tune:
         launch = eng.tune(sweeps_per_trial=1)
@@ -560,7 +561,7 @@ def main():
                     help="keep only the first K chains of the workload (small profiling cases)")
     ap.add_argument("--launch", default=None,
                     help="fixed batched launch shape instead of tuning: "
-                         "cta:BLOCK:SPL:STATE_BYTES[:SPLIT] or warp:BLOCK:SPL")
+                         "cta:BLOCK:SPL:STATE_BYTES[:SPLIT[:STAGE,SWAP,REST]] or warp:BLOCK:SPL")
     ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

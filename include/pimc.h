@@ -170,6 +170,9 @@ typedef struct {
    * staging, swaps and the rest as three launches per sweep, each phase
    * finished by every chain before the next starts */
   int split_phases;
+  /* with split_phases: CTA size of the staging, swap and remaining launches
+   * (0: block) */
+  int phase_block[3];
 } pimc_launch;
 /* time candidate launch shapes on the handle's own chains and keep the
  * fastest; the chains are restored afterwards.  chosen may be NULL. */

@@ -51,7 +51,13 @@ struct Plan {
   int warp_bytes = 0;          // scratch bytes of one warp's chain (warp mode)
   size_t dyn_smem = 0;
   int split = 0;               // CTA mode: 1 = staging, swaps, rest as three launches
+  int pblock[3] = {0, 0, 0};   // split: CTA size per phase (0: block)
+  size_t psmem[3] = {0, 0, 0}; // split: dynamic shared bytes per phase
 };
+
+// CTA size and dynamic shared bytes of phase ph of a plan
+int phase_block(const Plan &p, int ph) { return p.pblock[ph] > 0 ? p.pblock[ph] : p.block; }
+size_t phase_smem(const Plan &p, int ph) { return p.pblock[ph] > 0 ? p.psmem[ph] : p.dyn_smem; }
 
 struct Handle {
   int nchains = 0;
@@ -558,8 +564,9 @@ int run_plain(Handle *h, long long n) {
 // names a phase kernel of a split plan
 int grid_for(Handle *h, const Plan &p, int phase = -1) {
   int per_sm = 0;
-  const cudaError_t e = phase >= 0 ? sweep_phase_occupancy(phase, p.block, p.dyn_smem, &per_sm)
-                                   : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
+  const cudaError_t e = phase >= 0
+                            ? sweep_phase_occupancy(phase, phase_block(p, phase), phase_smem(p, phase), &per_sm)
+                            : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const int units_per_cta = p.mode == 1 ? p.block / 32 : 1;
   const int need = (h->nchains + units_per_cta - 1) / units_per_cta;
@@ -572,7 +579,7 @@ int grid_for(Handle *h, const Plan &p, int phase = -1) {
 bool launch_teams(Handle *h, const Plan &p) {
   int per_sm = 0;
   if (p.mode != 0) return false;
-  const cudaError_t e = p.split ? sweep_phase_occupancy(0, p.block, p.dyn_smem, &per_sm)
+  const cudaError_t e = p.split ? sweep_phase_occupancy(0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
                                 : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess) return false;
   return h->nchains <= per_sm * h->num_sms;
@@ -582,7 +589,7 @@ bool launch_teams(Handle *h, const Plan &p) {
 cudaError_t plan_set_smem(const Plan &p) {
   if (!p.split) return sweep_set_smem(p.mode, p.dyn_smem);
   for (int ph = 0; ph < 3; ++ph) {
-    const cudaError_t e = sweep_phase_set_smem(ph, p.dyn_smem);
+    const cudaError_t e = sweep_phase_set_smem(ph, phase_smem(p, ph));
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -604,7 +611,8 @@ cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long
     for (int ph = 0; ph < 3; ++ph) {
       cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
       if (e == cudaSuccess)
-        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), p.block, p.dyn_smem, h->stream);
+        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), phase_block(p, ph), phase_smem(p, ph),
+                               h->stream);
       if (e != cudaSuccess) return e;
       if (launches) *launches += 1;
     }
@@ -972,6 +980,17 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
     return fail(PIMC_EARG, "split_phases must be 0, or 1 with one CTA per chain");
   Plan p = plan_smem(h, l.warp_per_chain, l.block, l.sweeps_per_launch, l.state_smem_bytes);
   p.split = l.split_phases;
+  for (int ph = 0; ph < 3; ++ph) {
+    const int b = l.phase_block[ph];
+    if (b == 0) continue;
+    if (!l.split_phases || b < 64 || b > 512 || b % 32)
+      return fail(PIMC_EARG, "phase_block needs split_phases and a multiple of 32 in [64, 512]");
+    const Plan q = plan_smem(h, 0, b, 1, l.state_smem_bytes);
+    if (h->max_dyn_smem > 0 && q.dyn_smem > (size_t)h->max_dyn_smem)
+      return fail(PIMC_EARG, "phase launch needs more shared memory than the device offers");
+    p.pblock[ph] = b;
+    p.psmem[ph] = q.dyn_smem;
+  }
   if (h->max_dyn_smem > 0 && p.dyn_smem > (size_t)h->max_dyn_smem)
     return fail(PIMC_EARG, "launch shape needs " + std::to_string(p.dyn_smem) +
                                " shared bytes per CTA, more than the device offers");
@@ -1000,7 +1019,8 @@ int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
       if (e != cudaSuccess) break;
       if (p.split) {
         a.sweeps = 1;
-        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), p.block, p.dyn_smem, h->stream);
+        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), phase_block(p, ph), phase_smem(p, ph),
+                               h->stream);
       } else {
         a.sweeps = 1;
         e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);
@@ -1042,6 +1062,7 @@ int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
   launch->sweeps_per_launch = h->bat.spl;
   launch->state_smem_bytes = h->bat.state_cap;
   launch->split_phases = h->bat.split;
+  for (int ph = 0; ph < 3; ++ph) launch->phase_block[ph] = h->bat.pblock[ph];
   return PIMC_OK;
 }
 
@@ -1086,6 +1107,40 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
     if (h->last_ms < best) {
       best = h->last_ms;
       keep = l;
+    }
+  }
+  // a split shape: time each phase under every CTA size (events between
+  // the phases) and give each phase its fastest size, kept if the whole
+  // sweep gets faster
+  if (keep.split_phases) {
+    double pbest[3] = {1e300, 1e300, 1e300};
+    pimc_launch ref = keep;
+    for (int b : {64, 128, 256}) {
+      pimc_launch l = keep;
+      l.block = b;
+      for (int ph = 0; ph < 3; ++ph) l.phase_block[ph] = 0;
+      Plan p;
+      if (check_launch(h, l, &p)) continue;
+      if ((rc = pimc_batch_set_launch(h, &l))) return rc;
+      double ms[3];
+      if ((rc = pimc_batch_phase_times(h, 1, ms))) return rc;  // warm
+      if ((rc = pimc_batch_phase_times(h, sweeps_per_trial, ms))) return rc;
+      for (int ph = 0; ph < 3; ++ph)
+        if (ms[ph] < pbest[ph]) {
+          pbest[ph] = ms[ph];
+          ref.phase_block[ph] = b;
+        }
+    }
+    Plan p;
+    if (!check_launch(h, ref, &p)) {
+      if ((rc = pimc_batch_set_launch(h, &ref))) return rc;
+      if ((rc = run_batched(h, ref.sweeps_per_launch))) return rc;
+      if ((rc = run_batched(h, sweeps_per_trial))) return rc;
+      const double t_ref = h->last_ms;
+      if ((rc = pimc_batch_set_launch(h, &keep))) return rc;
+      if ((rc = run_batched(h, keep.sweeps_per_launch))) return rc;
+      if ((rc = run_batched(h, sweeps_per_trial))) return rc;
+      if (t_ref < h->last_ms) keep = ref;
     }
   }
   if ((rc = pimc_batch_set_launch(h, &keep))) return rc;

@@ -106,7 +106,7 @@ class Stats(C.Structure):
 class Launch(C.Structure):
     _fields_ = [("warp_per_chain", C.c_int), ("block", C.c_int),
                 ("sweeps_per_launch", C.c_int), ("state_smem_bytes", C.c_int),
-                ("split_phases", C.c_int)]
+                ("split_phases", C.c_int), ("phase_block", C.c_int * 3)]
 
 
 # every symbol include/pimc.h declares, with its argument types

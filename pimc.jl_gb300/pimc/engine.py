@@ -251,9 +251,9 @@ class Engine:
 
     def set_launch(self, block: int, sweeps_per_launch: int = 1,
                    state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False,
-                   split_phases: int = 0):
+                   split_phases: int = 0, phase_block=(0, 0, 0)):
         l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes,
-                   int(split_phases))
+                   int(split_phases), (C.c_int * 3)(*[int(b) for b in phase_block]))
         check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
 
     @property
@@ -263,7 +263,7 @@ class Engine:
         check(self.L.pimc_batch_get_launch(self.h, C.byref(l)))
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
-                "split_phases": l.split_phases}
+                "split_phases": l.split_phases, "phase_block": list(l.phase_block)}
 
     def phase_times(self, n_sweeps: int = 2):
         """device ms of the staging, swap and remaining phases over n sweeps,

@@ -176,7 +176,9 @@ def test_batched_equals_plain_and_tuner_is_transparent():
               dict(block=128, sweeps_per_launch=3, state_smem_bytes=0),
               dict(block=256, sweeps_per_launch=1, state_smem_bytes=100 * 1024),
               dict(block=64, sweeps_per_launch=2, state_smem_bytes=0, split_phases=1),
-              dict(block=128, sweeps_per_launch=1, state_smem_bytes=32 * 1024, split_phases=1)]
+              dict(block=128, sweeps_per_launch=1, state_smem_bytes=32 * 1024, split_phases=1),
+              dict(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
+                   phase_block=[256, 64, 128])]
     b = Engine(ps)
     for i, p in enumerate(ps):
         b.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
@@ -209,7 +211,10 @@ def test_launch_shape_rejects_bad_values():
     from pimc._native import PimcError
     e = Engine([ChainParams(dim=2, N=4, M=8, L=6.0, T=1.0, lam=0.5, harmonic_omega=1.0, seed=1)] * 2)
     for bad in [dict(block=48), dict(block=512, warp_per_chain=True), dict(block=16, warp_per_chain=True),
-                dict(block=128, sweeps_per_launch=0), dict(block=128, state_smem_bytes=-1)]:
+                dict(block=128, sweeps_per_launch=0), dict(block=128, state_smem_bytes=-1),
+                dict(block=64, split_phases=2), dict(block=64, warp_per_chain=True, split_phases=1),
+                dict(block=64, split_phases=0, phase_block=(128, 0, 0)),
+                dict(block=64, split_phases=1, phase_block=(96 + 1, 0, 0))]:
         with pytest.raises(PimcError):
             e.set_launch(**bad)
     e.close()
