@@ -641,8 +641,16 @@ __device__ __forceinline__ void est_term(const ChainDesc &d, unsigned d2a, unsig
   ++k;
 }
 
-template <class Seg>
-__device__ void segment_estimate(const CV &c, const Seg &s, int t0, int t1, PairEst &e, int lane) {
+// no early stop
+struct NoStop {
+  __device__ __forceinline__ bool operator()(const PairEst &) const { return false; }
+};
+
+// stop(e), called by the whole warp after every link, ends the scan early;
+// returns whether it did
+template <class Seg, class Stop = NoStop>
+__device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, PairEst &e, int lane,
+                                 const Stop &stop = Stop()) {
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M;
   for (int t = t0; t < t1; ++t) {
@@ -669,7 +677,9 @@ __device__ void segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
         }
       }
     }
+    if (stop(e)) return true;
   }
+  return false;
 }
 
 // a lane's estimates in FP64, with the error of its FP32 accumulation (two

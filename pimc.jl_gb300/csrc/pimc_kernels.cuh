@@ -510,10 +510,25 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   // of the move's stream).  Injected-draw attempts always evaluate them.
   bool pairs = any_pair;
   const bool shortcuts = FAST && !(d.flags & (PF_EXACT | PF_CONTACT));
+  int early = 0;  // 1: accepted on the pair-free sums, which are then the final sums
+  // reference rules, g >= 0: dS = dS_pf + (tau g / 2)(So + Sn) with So, Sn >= 0,
+  // so any lower bound of the pair sums that reaches `need` accepts the move
+  bool monotone = false;
+  double need = 0.0;
   if (shortcuts && any_pair && !phys && d.g >= 0.0) {
+    if (tid == 0) S.iv[3] = 0;
     double c2[2] = {w2[0], w2[1]};
     G::template sum<2>(c2, red);
-    if (metropolis(d, c2[1] - c2[0] + log_ratio, dr)) pairs = false;
+    const double dpf = c2[1] - c2[0] + log_ratio;
+    if (metropolis(d, dpf, dr)) {
+      pairs = false;
+      early = 1;
+    } else {
+      double margin;
+      const double lu = log_u_margin(dr.uniform_accept(), margin);
+      need = lu + margin + 1e-9 * (fabs(lu) + fabs(dpf)) - dpf;
+      monotone = d.g > 0.0;
+    }
   }
   // the pair of the two moving paths, old and new (physical rules), exact
   if (pairs && phys)
@@ -545,27 +560,52 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     return SwapSeg{&c, j0, M, b == 0 ? n1 : n2, b == 0 ? nx1 : nx2, n1, nx1, n2, nx2,
                    b == 0 ? S.r1x : S.r2x, b == 0 ? S.r1y : S.r2y, !phys, b == 0 ? S.q1 : S.q2};
   };
-  int dec = pairs ? -1 : 2;  // 2: decided by the exact sums at hand
+  int dec = early ? 1 : (pairs ? -1 : 2);  // 2: decided by the exact sums at hand
   if (shortcuts && pairs) {
     // bounded estimate from the mirror: decides the move unless the log
     // acceptance ratio's interval straddles the threshold
     PairEst e = {0.f, 0.f, 0.f, 0.f, 0, 0};
+    // under the monotone rules a warp whose own lower bound of the pair sums
+    // already accepts raises a flag in shared memory, and every warp stops at
+    // its next link (no group reduction inside the scan); a warp stops only
+    // once the flag is up, so without it every warp has scanned all its links
+    const double gh = 0.5 * d.tau * d.g;
+    volatile int *flag = S.iv + 3;
+    auto stop = [&](const PairEst &pe) -> bool {
+      if (!monotone) return false;
+      if (*flag) return true;
+      double l4[4];
+      est_reduce_lanes(pe, l4);
+      const double lb = warp_sum((l4[0] - l4[1]) + (l4[2] - l4[3]));
+      if (gh * lb > need) {
+        if (lane == 0) *flag = 1;
+        return true;
+      }
+      return false;
+    };
     for (int b = 0; b < 2; ++b) {
       const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
-      if (t0 < t1) segment_estimate(c, seg_of(b), t0, t1, e, lane);
+      if (t0 < t1 && segment_estimate(c, seg_of(b), t0, t1, e, lane, stop)) break;
     }
-    double v[6], l4[4];
-    est_reduce_lanes(e, l4);
-    for (int k = 0; k < 4; ++k) v[k] = l4[k];
-    v[4] = w2[0];
-    v[5] = w2[1];
-    G::template sum<6>(v, red);
-    // w_initial gets h*So and, under the reference's rules, h*Sn; the
-    // physical rules put h*Sn into w_update (h = -tau g / 2)
-    const double h = d.mhtau_g;
-    const double centre = v[5] - v[4] + log_ratio - h * v[0] + (phys ? h : -h) * v[2];
-    const double radius = fabs(h) * (v[1] + v[3]);
-    dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
+    if (monotone) {
+      G::sync();
+      if (*flag) dec = 1;
+      G::sync();
+    }
+    if (dec == -1) {
+      double v[6], l4[4];
+      est_reduce_lanes(e, l4);
+      for (int k = 0; k < 4; ++k) v[k] = l4[k];
+      v[4] = w2[0];
+      v[5] = w2[1];
+      G::template sum<6>(v, red);
+      // w_initial gets h*So and, under the reference's rules, h*Sn; the
+      // physical rules put h*Sn into w_update (h = -tau g / 2)
+      const double h = d.mhtau_g;
+      const double centre = v[5] - v[4] + log_ratio - h * v[0] + (phys ? h : -h) * v[2];
+      const double radius = fabs(h) * (v[1] + v[3]);
+      dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
+    }
   }
   if (dec == -1) {
     for (int b = 0; b < 2; ++b) {
@@ -590,12 +630,16 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
         prop[k * dim] = (b == 0 ? S.r1x : S.r2x)[t];
         if (dim > 1) prop[k * dim + 1] = (b == 0 ? S.r1y : S.r2y)[t];
       }
-    if (tid == 0) {
-      S.iv[2] = metropolis(d, w2[1] - w2[0] + log_ratio, dr);
+    if (D::kSweep) {
+      // every thread holds the same sums and the move's uniform is a pure
+      // function of its stream: each decides alone, no broadcast
+      acc = metropolis(d, w2[1] - w2[0] + log_ratio, dr);
+    } else {
+      if (tid == 0) S.iv[2] = metropolis(d, w2[1] - w2[0] + log_ratio, dr);
+      G::sync();
+      acc = S.iv[2];
+      G::sync();
     }
-    G::sync();
-    acc = S.iv[2];
-    G::sync();
   }
   if (!acc) return RES_REJECT;
   // accept: exchange next, write the bridges along the new cycles, exchange
