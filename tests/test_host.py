@@ -119,3 +119,50 @@ def test_multirank_reduction_gloo():
     out = mgr.dict()
     mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
     assert out[0] == (2.0, 30.0) and out[1] == (2.0, 30.0)
+
+
+def test_radial_and_superfluid_host_formulas():
+    """the host side of the new estimators: g(r) of the ideal-gas counts is 1,
+    and the superfluid fractions follow their published formulas"""
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    import pimc
+    s = SimpleNamespace(L=4.0, dim=2, M=8, N=10, λ=0.5, β=2.0)
+    rd = pimc.RadialDistribution(s, nbins=16)
+    e = np.arange(17) * (s.L / 16)
+    rd.ndata = 5
+    rd.hist = 5 * s.M * s.N * (s.N - 1) / 2 * np.pi * np.diff(e ** 2) / (2 * s.L) ** 2
+    np.testing.assert_allclose(rd.g(), 1.0, rtol=1e-12)
+    np.testing.assert_allclose(rd.r(), (np.arange(16) + 0.5) * s.L / 16)
+    sf = pimc.Superfluid(s)
+    rows = np.zeros((4, 8))
+    rows[:, 4] = [4.0, 0.0, 16.0, 4.0]      # W^2
+    rows[:, 5] = [0.1, -0.2, 0.3, 0.0]      # A_z
+    rows[:, 6] = [2.0, 2.5, 1.5, 2.0]       # sum r^2 / M
+    sf._add(SimpleNamespace(N=10), rows)
+    assert abs(sf.winding_fraction(10) - 6.0 / (2 * 2 * 0.5 * 2.0 * 10)) < 1e-15
+    a2 = np.mean(np.array([0.1, -0.2, 0.3, 0.0]) ** 2)
+    assert abs(sf.area_fraction(10) - 2 * a2 / (0.5 * 2.0 * 2.0)) < 1e-15
+
+
+def test_generate_V_forms():
+    """generate_V(scale, depth, sym; attractive) flips the depth's sign for an
+    attractive lattice and names the reference's beam sets; the angle-list
+    form keeps its depth; :harmonic is the unit trap"""
+    import math
+
+    import numpy as np
+
+    import pimc
+    V = pimc.generate_V(0.5, 3.0, "l25")
+    assert isinstance(V, pimc.OpticalLattice) and V.depth == -3.0 and len(V.angles) == 12
+    assert pimc.generate_V(0.5, 3.0, "l65", attractive=False).depth == 3.0
+    assert isinstance(pimc.generate_V(1.0, 1.0, "harmonic"), pimc.Harmonic)
+    W = pimc.generate_V([0.0, math.pi / 2], 1.0, 2.0, helical=True)
+    assert W.helical and W.depth == 2.0
+    # at the origin every plane wave has phase 0 (plus its own angle when helical)
+    assert abs(V(np.zeros(2)) - (-3.0)) < 1e-15
+    c = np.mean(np.cos([0.0, math.pi / 2])); s_ = np.mean(np.sin([0.0, math.pi / 2]))
+    assert abs(W(np.zeros(2)) - 2.0 * (c * c + s_ * s_)) < 1e-15
