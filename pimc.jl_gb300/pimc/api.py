@@ -22,7 +22,7 @@ from collections import deque
 
 import numpy as np
 
-from .engine import (ACCEPT, HARDCORE, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams, Engine,
+from .engine import (ACCEPT, SEM_PHYSICAL, SEM_REFERENCE, SKIP, ChainParams, Engine,
                      Mix, PimcError, contact_table, julia_float, write_density_csv)
 
 
