@@ -302,3 +302,43 @@ def test_oracle_optical_lattice_potential(oracle_mod):
             h = 1e-6
             fd = [(host(r + h * e) - host(r - h * e)) / (2 * h) for e in np.eye(2)]
             np.testing.assert_allclose(host.grad(r), fd, rtol=1e-6, atol=1e-6)
+
+
+@pytest.mark.parametrize("kind", ["contact", "lattice"])
+def test_physical_weights_are_action_differences_new_terms(oracle_mod, kind):
+    """the same identity with the tabulated contact propagator and with the
+    optical lattice: a staging window's w_upd - w_init is the change of the
+    whole configuration's potential + pair action"""
+    import pimc
+    O = oracle_mod
+    rng = np.random.default_rng(4)
+    extra = {}
+    if kind == "contact":
+        n = 40
+        tab = -np.abs(rng.normal(scale=0.02, size=(n, n)))
+        extra = dict(interactions=True, r_a=1.0, contact_table=tab + tab.T, contact_range=6.0)
+    else:
+        extra = dict(beams=(pimc.lattice_angles("l25"), 0.6, -2.0, False))
+    p = O.make_params(dim=2, N=10, M=16, L=4.0, T=0.5, lam=0.5, hcoef=0.5,
+                      semantics=O.SEM_PHYSICAL, **extra)
+    o = O.Oracle(p)
+    x = rng.normal(scale=0.8, size=(2, 10, 16))
+    nxt = rng.permutation(10).astype(np.int32)
+    o.set_state(x, nxt)
+    for _ in range(20):
+        nn, j0, m = int(rng.integers(10)), int(rng.integers(16)), int(rng.integers(2, 10))
+        x, _, nx = o.get_state()
+        own = [nn if j0 + t < 16 else nx[nn] for t in range(m + 1)]
+        sl = [(j0 + t) % 16 for t in range(m + 1)]
+        rp = np.array([[x[0, own[t], sl[t]], x[1, own[t], sl[t]]] for t in range(m + 1)])
+        rp[1:m] += rng.normal(scale=0.2, size=(m - 1, 2))
+        wi, wu = o.staging_weights(nn, j0, m, rp.ravel())
+        a0 = o.eval_action()
+        x2 = x.copy()
+        for t in range(1, m):
+            x2[:, own[t], sl[t]] = rp[t]
+        o2 = O.Oracle(p)
+        o2.set_state(x2, nx)
+        a1 = o2.eval_action()
+        dS = (a1[1] + a1[2]) - (a0[1] + a0[2])
+        assert abs((wu - wi) - dS) < 1e-11 * max(1.0, abs(dS)), (kind, wu - wi, dS)
