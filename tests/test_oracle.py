@@ -342,3 +342,17 @@ def test_physical_weights_are_action_differences_new_terms(oracle_mod, kind):
         a1 = o2.eval_action()
         dS = (a1[1] + a1[2]) - (a0[1] + a0[2])
         assert abs((wu - wi) - dS) < 1e-11 * max(1.0, abs(dS)), (kind, wu - wi, dS)
+
+
+def test_oracle_virial_matches_thermodynamic_with_the_lattice(oracle_mod):
+    """one particle in an optical lattice plus a trap: the virial estimator,
+    which uses the lattice's analytic gradient, and the thermodynamic one
+    sample the same energy"""
+    import pimc
+    O = oracle_mod
+    p = O.make_params(dim=2, N=1, M=16, L=6.0, T=1.0, lam=0.5, hcoef=0.5, semantics=O.SEM_PHYSICAL,
+                      beams=(pimc.lattice_angles("cubic"), 0.5, -1.5, False))
+    r = _run_energy(O, p, 30000, 8, 7)
+    eth, s1 = blocking(r["energies"][:, 0])
+    ev, s2 = blocking(r["energies"][:, 1])
+    assert abs(eth - ev) < 3 * math.hypot(s1, s2), (eth, s1, ev, s2)
