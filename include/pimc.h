@@ -56,7 +56,10 @@ enum { PIMC_REJECT = 0, PIMC_ACCEPT = 1, PIMC_SKIP = 2, PIMC_HARDCORE = 3 };
  * and the pair propagator are engine-known forms:
  *   V(r)  = 1/2 omega^2 |r|^2 + V0 sum_d sin^2(pi r_d / a)
  *   lnU   = -tau/2 (v(|r1|) + v(|r2|)),  v(r) = g exp(-r^2 / (2 sigma^2))
- * The hard-core radius is the reference's a = exp(-2 pi / g_contact) when
+ * The optical lattices of generate_V (pimc_set_beams) and the tabulated
+ * contact propagator of build_prop_int (pimc_set_contact_propagator,
+ * pimc_set_contact_table) are attached to a chain after creation.  The
+ * hard-core radius is the reference's a = exp(-2 pi / g_contact) when
  * interacting (src/system.jl:151), passed explicitly here. */
 typedef struct pimc_params {
   int dim;               /* 1 or 2 */
@@ -203,8 +206,8 @@ int pimc_attempt_polymer_com(void *handle, int n, double step, const double *uni
 
 /* ---------------- action evaluation (parity level a) */
 /* out[0] = sum lnK, out[1] = sum lnV (recomputed), out[2] = pair sum lnU
- * (each unordered pair once), out[3] = sum of cached V
- * (src/propagator.jl:16-28, src/system.jl:26-28) */
+ * (each unordered pair once; Gaussian pair or contact table), out[3] = sum
+ * of cached V (src/propagator.jl:16-28, src/system.jl:26-28) */
 int pimc_eval_action(void *handle, double out[4]);
 /* w_initial / w_updated of a staging move for a given proposed window
  * rp[(m+1)*dim] (reshape.jl:66-77) */
