@@ -242,48 +242,31 @@ def pinned_empty(n):
 def cpu_oracle_rate(chains, mixes, semantics, budget_s=15.0, max_chains=None, threads=None,
                     contact=None):
     """the CPU oracle (C restatement of the reference's sweep) on a bounded
-    sample of the workload's chains, one chain per host thread; contact =
-    (table, range) gives every chain the tabulated contact propagator"""
-    import concurrent.futures as cf
+    sample of the workload's chains: the sampled chains dealt longest-first to
+    the host threads, every thread sweeping its own chains in turn (run!
+    attempts, N(k+2) per sweep) until budget_s of wall time has passed, so no
+    core idles while another finishes; contact = (table, range) gives every
+    chain the tabulated contact propagator"""
     from oracle import oracle as O
     O.build()
     threads = threads or os.cpu_count() or 1
     n = len(chains)
-    take = max_chains or min(n, 4 * threads)
+    take = max_chains or min(n, 8 * threads)
     idx = np.linspace(0, n - 1, take).astype(int) if n > take else np.arange(n)
-
-    def one(i, attempts):
+    ps, ells = [], []
+    for i in idx:
         c, m = chains[i], mixes[i]
-        p = O.make_params(dim=c.dim, N=c.N, M=c.M, L=c.L, T=c.T, lam=c.lam,
-                          hcoef=0.5 * c.harmonic_omega ** 2, V0=c.lattice_V0, lat_a=c.lattice_a,
-                          pair_g=c.pair_g, pair_sigma=c.pair_sigma, interactions=c.interactions,
-                          r_a=c.r_a, semantics=semantics, mu=c.mu,
-                          contact_table=None if contact is None else contact[0],
-                          contact_range=0.0 if contact is None else contact[1])
-        return O.bench_chains(p, 1, 1, attempts, m.stage_slices, 1.0, SEED + int(i))
-
-    # calibrate: one sweep's worth of attempts (N(k+2)) on each sampled chain
-    def sweep_attempts(i):
-        c, m = chains[i], mixes[i]
-        k = -(-c.M // m.stage_slices)
-        return c.N * (k + 2)
-
-    t0 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        res = list(ex.map(lambda i: one(i, sweep_attempts(i)), idx))
-    t1 = time.perf_counter()
-    beads = sum(r[1] for r in res)
-    wall = t1 - t0
-    # scale the number of sweeps to fill about budget_s of wall time
-    reps = max(1, int(budget_s / max(wall, 1e-3)))
-    if reps > 1:
-        t0 = time.perf_counter()
-        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-            res = list(ex.map(lambda i: one(i, reps * sweep_attempts(i)), idx))
-        wall = time.perf_counter() - t0
-        beads = sum(r[1] for r in res)
-    sample = (f"{len(idx)} of {n} chains (evenly spaced), {reps} sweep(s) of run! attempts each "
-              f"(N(k+2) per sweep), {threads} host threads, {wall:.1f} s wall")
+        ps.append(O.make_params(dim=c.dim, N=c.N, M=c.M, L=c.L, T=c.T, lam=c.lam,
+                                hcoef=0.5 * c.harmonic_omega ** 2, V0=c.lattice_V0,
+                                lat_a=c.lattice_a, pair_g=c.pair_g, pair_sigma=c.pair_sigma,
+                                interactions=c.interactions, r_a=c.r_a, semantics=semantics,
+                                mu=c.mu, contact_table=None if contact is None else contact[0],
+                                contact_range=0.0 if contact is None else contact[1]))
+        ells.append(m.stage_slices)
+    wall, beads, sweeps = O.bench_budget(ps, ells, threads, budget_s, 1.0, SEED)
+    sample = (f"{len(idx)} of {n} chains (evenly spaced), dealt longest-first to {threads} host "
+              f"threads, each thread sweeping its own chains in turn for {wall:.1f} s of wall "
+              f"time ({sweeps:.0f} sweeps of N(k+2) run! attempts in all)")
     return beads / wall, threads, sample
 
 
@@ -327,7 +310,7 @@ def run_reference(args):
     # each step a bounded sample; the whole run stays within a few minutes
     budget = max(1.0, min(args.ref_budget, 120.0 / max(args.steps, 1)))
     for _ in range(args.warmup):
-        cpu_oracle_rate(chains, mixes, 0, budget_s=1.0)
+        cpu_oracle_rate(chains, mixes, 0, budget_s=0.5)
     for _ in range(args.steps):
         r, cores, sample = cpu_oracle_rate(chains, mixes, 0, budget_s=budget)
         rates.append(r)
@@ -349,6 +332,7 @@ def run_reference(args):
 def run_ours(args):
     import pimc
     from pimc.engine import Engine
+    from pimc.shard import shard_of
     ws, rank, local, pg = dist_setup()
     pimc.load()
     sem = 1 if args.semantics == "physical" else 0
@@ -356,7 +340,16 @@ def run_ours(args):
     if args.chains > 0:
         chains, mixes = chains[:args.chains], mixes[:args.chains]
         desc += f" (first {len(chains)} chains)"
-    if ws > 1:  # weak scaling: every rank runs the full workload with its own seeds
+    n_total = len(chains)
+    scaling = "weak"
+    if ws > 1 and len(chains) > 1:
+        # strong scaling: the batch's chains split across the ranks by LPT on
+        # the engine's chain cost; every rank runs its shard on its own GPU
+        mine = shard_of(chains, rank, ws)
+        chains, mixes = [chains[i] for i in mine], [mixes[i] for i in mine]
+        scaling = "strong"
+    elif ws > 1:
+        # a single chain does not shard: independent replicas, own seeds
         for c in chains:
             c.seed = c.seed + 1000003 * rank
     eng = Engine(chains)
@@ -374,16 +367,23 @@ def run_ours(args):
     launch = None
     if batched and args.launch:
         f = args.launch.split(":")
+        pb = f[5].split(",") if len(f) > 5 else ["0", "0", "0"]
         eng.set_launch(block=int(f[1]), sweeps_per_launch=int(f[2]),
                        state_smem_bytes=int(f[3]) if len(f) > 3 else 0,
                        warp_per_chain=f[0] == "warp",
                        split_phases=int(f[4]) if len(f) > 4 else 0,
-                       phase_block=[int(b) for b in f[5].split(",")] if len(f) > 5 else (0, 0, 0))
+                       phase_block=[int(b.lstrip("w")) for b in pb],
+                       phase_warp=[int(b.startswith("w")) for b in pb])
         launch = dict(eng.launch, tuned=False)
     elif batched and args.tune:
         launch = eng.tune(sweeps_per_trial=1)
     for _ in range(args.warmup):
         run(1)
+    prof = os.environ.get("PIMC_PROFILE", "0") == "1"
+    if prof:  # the profiling build: clear the swap counters before the timed sweeps
+        import ctypes as C
+        pbuf = (C.c_ulonglong * 32)()
+        eng.L.pimc_swap_profile(eng.h, pbuf, 1)
     s0 = eng.total_stats()
     barrier(pg)
     with ClockSampler(local) as clk:
@@ -393,17 +393,34 @@ def run_ours(args):
     ms = eng.last_run_ms()
     launches = eng.last_run_launches()
     s1 = eng.total_stats()
+    swap_profile = None
+    if prof:
+        eng.L.pimc_swap_profile(eng.h, pbuf, 1)
+        v = list(pbuf)
+        names = ["heat_bath", "partner_search", "physical_ratio", "bridges", "new_beads",
+                 "pair_free_decision", "pair_estimates", "exact_pair_sums", "decision",
+                 "accepted_writeback"]
+        tot = float(sum(v[:10])) or 1.0
+        swap_profile = {"cycle_share": {n: v[k] / tot for k, n in enumerate(names)},
+                        "cycles_per_attempt": tot / max(v[16], 1),
+                        "counts": dict(zip(["attempts", "n2_eq_n1", "early_accept",
+                                            "decided_by_estimate", "exact_sums", "accepted",
+                                            "rejected"], v[16:23])),
+                        "note": "PIMC_PROFILE build: clock64() cycles of thread 0 per CTA between "
+                                "section marks of the swap, summed over CTAs (timed sweeps only)"}
     beads = s1.bead_updates - s0.bead_updates
     tmax, beads_all = reduce_max_sum(pg, ms / 1e3, beads)
     value = beads_all / tmax
     ms_step = tmax * 1e3 / args.steps
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "scaling": scaling, "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "gpu_launches": int(launches)}
     state_bytes = sum(8 * (c.dim + 1) * c.N * c.M for c in chains)
-    cfg = {"workload": desc, "chains": len(chains), "semantics": args.semantics,
-           "parallelism": f"dp{ws} (independent chains per GPU)",
+    cfg = {"workload": desc, "chains": n_total, "semantics": args.semantics,
+           "parallelism": (f"dp{ws}: the chains split across GPUs by LPT on their cost "
+                           "(no device collective; host gather of the sums)" if scaling == "strong"
+                           else f"dp{ws} (independent replicas per GPU)"),
            "l2": (f"chain state {state_bytes / 1e9:.2f} GB > 129 MB L2"
                   if state_bytes > 129e6 else f"chain state {state_bytes / 1e6:.1f} MB (L2/shared resident)"),
            "bead_updates_per_step": beads / args.steps}
@@ -475,6 +492,8 @@ def run_ours(args):
                                              if measured_fpb else "algorithmic estimate (no pair terms)"),
                             "peak_source": "pimc_fp64_peak: DFMA throughput probe on this GPU (measured)"}
     out["clocks"] = clk.summary()
+    if swap_profile is not None:
+        out["swap_profile"] = swap_profile
     # plain path: one launch per chain per sweep (no queue, no graph), timed
     # on every PLAIN_STRIDE-th chain of the workload so that it stays short
     if batched and not args.no_plain:
@@ -520,6 +539,27 @@ def run_ours(args):
                       "d2h_bytes_per_step": nb + 8 * 9 * len(chains),
                       "path": "pimc_batch_set_beads_all (pinned host) -> pimc_run -> "
                               "pimc_batch_get_beads_all + pimc_batch_energy_sums_all"}
+    # the adjoint of every chain of the batch in one call (four launches),
+    # device time by CUDA events; a step of "batched + adjoint" is one sweep
+    # of every chain followed by the adjoint of every chain
+    if batched and not args.no_adjoint:
+        eng.batch_adjoint()  # makes the handle's adjoint pool
+        ams = []
+        for _ in range(3):
+            eng.batch_adjoint()
+            ams.append(eng.last_run_ms())
+        a_ms = float(np.median(ams))
+        tb = sum(c.N * c.M for c in chains)
+        amax, tb_all = reduce_max_sum(pg, a_ms / 1e3, tb)
+        out["batched_adjoint"] = {"chains": n_total, "beads": tb_all, "ms_per_call": amax * 1e3,
+                                  "bead_gradients_per_s": tb_all / amax, "launches": 4,
+                                  "path": "pimc_batch_adjoint: dS/dr of every bead, "
+                                          "dS/d(V0, omega, g) and the virial energy of every chain"}
+        step_s = ms_step / 1e3 + amax
+        out["batched_plus_adjoint"] = {"value": beads_all / args.steps / step_s, "unit": UNIT,
+                                       "ms_per_step": step_s * 1e3,
+                                       "step": "one sweep of every chain, then the adjoint of "
+                                               "every chain (device time)"}
     if args.workload == "c5" or args.adjoint:
         t0 = time.perf_counter()
         reps = 5
@@ -541,6 +581,20 @@ def run_ours(args):
         out["cpu_baseline"] = {"value": r, "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": "C restatement of PIMC.jl's sweep (same semantics), "
                                          + sample}
+    # the energies' side of the metric: a fixed sample of 24 C4 chains run to
+    # equilibrium on this GPU and compared per chain with the oracle's run!
+    # statistics committed in tests/golden/sweep_stats.json
+    if (rank == 0 and args.workload == "c4" and args.semantics == "reference"
+            and not args.no_energy_check):
+        eng.close()
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from sweep_parity import c4_energy_check
+        t0 = time.perf_counter()
+        summary, _ = c4_energy_check()
+        summary["wall_s"] = time.perf_counter() - t0
+        summary["reference"] = ("oracle run! (C restatement of the reference's sweep), "
+                                "tests/golden/sweep_stats.json")
+        out["energy_check"] = summary
     if rank == 0:
         print(json.dumps(out))
     return 0
@@ -561,8 +615,13 @@ def main():
                     help="keep only the first K chains of the workload (small profiling cases)")
     ap.add_argument("--launch", default=None,
                     help="fixed batched launch shape instead of tuning: "
-                         "cta:BLOCK:SPL:STATE_BYTES[:SPLIT[:STAGE,SWAP,REST]] or warp:BLOCK:SPL")
+                         "cta:BLOCK:SPL:STATE_BYTES[:SPLIT[:STAGE,SWAP,REST]] or warp:BLOCK:SPL; "
+                         "a phase size written wNNN runs that phase with one warp per chain")
     ap.add_argument("--adjoint", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="skip the batched adjoint timing")
+    ap.add_argument("--no-energy-check", action="store_true",
+                    help="skip the C4 sample's energies against the oracle's statistics")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -575,6 +634,11 @@ def main():
     args = ap.parse_args()
     if args.steps < 1 or args.warmup < 0:
         raise SystemExit("steps >= 1 and warmup >= 0")
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.gpus != ws:
+        raise SystemExit(f"--gpus {args.gpus} needs {args.gpus} ranks, one per GPU: launch with "
+                         f"python -m torch.distributed.run --nproc-per-node {args.gpus} bench.py "
+                         f"--gpus {args.gpus} (WORLD_SIZE is {ws})")
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PIMC_ABI_VERSION 2
+#define PIMC_ABI_VERSION 3
 /* columns of an observable row (pimc_get_observables) */
 #define PIMC_NOBS 8
 
@@ -138,13 +138,19 @@ int pimc_get_next(void *handle, int *next);
 /* positions, cached link actions V[n][j] and next verbatim */
 int pimc_set_raw(void *handle, const double *x, const double *V, const int *next);
 int pimc_get_links(void *handle, double *V);
-/* init_world (src/system.jl:36-78) on the device: uniform start + Levy loop */
+/* init_world (src/system.jl:36-78) on the device: uniform start + Levy loop;
+ * with a hard core (hardcore_a > 0) each particle is drawn again while a
+ * bead overlaps an earlier particle's bead at the same slice, at most 10000
+ * times (system.jl:44-64); a world that cannot be made returns PIMC_ESTATE.
+ * pimc_create and pimc_batch_create run it for every chain. */
 int pimc_init_world(void *handle);
 int pimc_batch_set_beads(void *handle, int chain, const double *x);
 int pimc_batch_get_beads(void *handle, int chain, double *x);
 int pimc_batch_get_next(void *handle, int chain, int *next);
 /* every chain at once: x_all is the concatenation of each chain's
- * x[d][n][j] in chain order (one host<->device copy per call) */
+ * x[d][n][j] in chain order.  A page-locked x_all (cudaHostAlloc,
+ * cudaHostRegister) is read or written by the GPU in place, the copy fused
+ * with the layout transpose; a pageable one takes one staged copy. */
 int pimc_batch_set_beads_all(void *handle, const double *x_all);
 int pimc_batch_get_beads_all(void *handle, double *x_all);
 /* running energy sums of every chain: sum[c][4], sumsq[c][4], count[c] */
@@ -176,6 +182,10 @@ typedef struct {
   /* with split_phases: CTA size of the staging, swap and remaining launches
    * (0: block) */
   int phase_block[3];
+  /* with split_phases: 1 runs that phase with one warp per chain (every warp
+   * of a phase_block-thread CTA its own chain, phase_block <= 256); the swap
+   * phase (index 1) only */
+  int phase_warp[3];
 } pimc_launch;
 /* time candidate launch shapes on the handle's own chains and keep the
  * fastest; the chains are restored afterwards.  chosen may be NULL. */
@@ -270,12 +280,23 @@ int pimc_adjoint(void *handle, int chain, double *dSdr, double *dSdtheta, double
  * the middle of a run.
  * Limit: chains of at most 65536 beads (N*M) and 8192 particles; larger
  * chains return PIMC_EARG and must use pimc_adjoint.  The handle's device
- * must be the current device.  The first call on a device looks up the
- * array's address (set-up) and should come before any stream capture.  The
- * array is shared by all handles of the process: calls that overlap in time
- * (from several threads, on any handles of one device) race on it. */
+ * must be the current device.  The array's address on a device is looked up
+ * when a handle is created on it (set-up, with that device current), so the
+ * calls themselves make no lookup; after a cudaDeviceReset, which destroys
+ * every handle made before it, the first handle created again repeats the
+ * set-up.  The array is shared by all handles of the process and keeps the
+ * last call's contents: calls that overlap in time (from several threads, on
+ * any handles of one device) race on it. */
 int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta,
                          double *extra);
+/* pimc_adjoint for every chain of the batch at once (four launches over all
+ * chains, scratch carved from a pool the handle allocates on the first call
+ * and keeps): dSdtheta[c][3], extra[c][4] as pimc_adjoint per chain c, and
+ * dSdr_all (optional) in the layout of pimc_batch_get_beads_all, each
+ * chain's [dim][N][M] in chain order.  pimc_last_run_ms then gives the
+ * device time of the four launches.  No reference counterpart (PIMC.jl has
+ * no adjoint); the examples' pmap over systems is what it batches. */
+int pimc_batch_adjoint(void *handle, double *dSdtheta, double *extra, double *dSdr_all);
 /* change (V0, omega, g) in place; cached links are recomputed */
 int pimc_set_potential(void *handle, int chain, double V0, double omega, double g);
 
@@ -284,8 +305,10 @@ int pimc_get_stats(void *handle, int chain, pimc_stats *out);
 /* aggregate over chains */
 int pimc_get_total_stats(void *handle, pimc_stats *out);
 /* opaque, versioned snapshot of every chain: beads, links, next, counters,
- * adaptive variables, generator position; restoring it reproduces the
- * following sweeps bit for bit */
+ * adaptive variables, generator position, density and pair-distance
+ * histograms; restoring it reproduces the following sweeps bit for bit.  A
+ * snapshot restores only into a handle of the same shape, including the
+ * pair-distance bins of pimc_set_radial (else PIMC_ESTATE, nothing written) */
 int pimc_state_size(void *handle, size_t *bytes);
 int pimc_get_state(void *handle, void *buf, size_t bytes);
 int pimc_set_state(void *handle, const void *buf, size_t bytes);
@@ -342,8 +365,19 @@ int pimc_fp64_peak(void *handle, double *tflops);
  * split) with CUDA events around each phase; ms[3] receives the device time
  * of each phase summed over the sweeps */
 int pimc_batch_phase_times(void *handle, long long n_sweeps, double ms[3]);
-/* device time of the last run call (CUDA events on the handle's stream) */
+/* device time of the last run call or pimc_batch_adjoint (CUDA events on
+ * the handle's stream) */
 int pimc_last_run_ms(void *handle, double *ms);
+/* diagnostics, no reference counterpart: in the profiling build (nvcc
+ * -DPIMC_PROFILE=1) the permutation swap adds the clock cycles of its
+ * sections (0 heat-bath exponents, 1 partner search, 2 physical ratio, 3
+ * bridges, 4 new beads, 5 pair-free sums and early accept, 6 bounded pair
+ * estimates, 7 exact pair sums, 8 decision, 9 accepted write-back) to
+ * out[0..15] and counts outcomes in out[16..31] (16 attempts, 17 n2 == n1,
+ * 18 early accepts, 19 decided by the estimates, 20 exact sums, 21
+ * accepted, 22 rejected), summed over every CTA; reset != 0 clears them
+ * after the read.  Other builds return PIMC_EARG. */
+int pimc_swap_profile(void *handle, unsigned long long *out, int reset);
 /* kernel launches issued by the last run call */
 int pimc_last_run_launches(void *handle, long long *launches);
 /* engine options: PIMC_OPT_FORCE_WARP_WINDOW routes pair-free staging

@@ -124,6 +124,9 @@ def lib():
         L.orc_run.argtypes = [C.c_void_p, C.c_long, C.POINTER(Update), C.c_int, C.POINTER(Rng),
                               C.c_int, dp, C.c_long, C.POINTER(C.c_long), C.c_int, dp,
                               C.POINTER(C.c_long), C.POINTER(RunStats)]
+        L.orc_bench_budget.restype = C.c_double
+        L.orc_bench_budget.argtypes = [C.POINTER(Params), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                       C.c_double, C.c_double, C.c_uint64, dp, dp]
         L.orc_bench_chains.restype = C.c_double
         L.orc_bench_chains.argtypes = [C.POINTER(Params), C.c_int, C.c_int, C.c_long, C.c_int,
                                        C.c_double, C.c_uint64, dp]
@@ -353,3 +356,17 @@ def bench_chains(params: Params, nchains, nthreads, attempts, ell, com_step=1.0,
     sec = lib().orc_bench_chains(C.byref(params), nchains, nthreads, attempts, ell, com_step,
                                  seed, _dp(b))
     return sec, float(b[0])
+
+
+def bench_budget(params_list, ells, nthreads, budget_s, com_step=1.0, seed=20261203):
+    """time-budgeted CPU rate of a list of chains (orc_bench_budget): the
+    chains dealt longest-first to nthreads threads, every thread sweeping its
+    own chains in turn until budget_s has passed.  Returns (wall seconds,
+    bead updates, sweeps)."""
+    n = len(params_list)
+    arr = (Params * max(n, 1))(*params_list)
+    el = (C.c_int * max(n, 1))(*[int(e) for e in ells])
+    b, sw = np.zeros(1), np.zeros(1)
+    wall = lib().orc_bench_budget(arr, el, n, int(nthreads), float(budget_s), float(com_step),
+                                  int(seed), _dp(b), _dp(sw))
+    return wall, float(b[0]), float(sw[0])

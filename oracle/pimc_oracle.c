@@ -471,20 +471,51 @@ static void levy_rows(orc_state *st, double *r, int rows, orc_draws *dr) {
   for (int i = 0; i < rows * dim; ++i) r[i] = orc_teleport(r[i], p->L);
 }
 
-/* init_world (src/system.jl:36-78), without the hard-core redraw */
+/* any bead of the new path r (M rows) closer than the hard-core radius to a
+ * bead of particles 0..n-1 at the same slice (system.jl:54-62: norm of the
+ * per-component minimum-image distances, strictly below a) */
+static int init_overlap(const orc_state *st, const double *r, int n) {
+  const orc_params *p = &st->p;
+  int M = p->M, dim = p->dim;
+  for (int j = 0; j < M; ++j)
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int d = 0; d < dim; ++d) {
+        double dd = orc_distance(st->x[XI(st, d, i, j)], r[(size_t)j * dim + d], p->L);
+        s += dd * dd;
+      }
+      if (sqrt(s) < p->hardcore_a) return 1;
+    }
+  return 0;
+}
+
+/* init_world (src/system.jl:36-78): per particle a uniform start, the last
+ * row equal to the first, a Levy loop through the rows between; with a hard
+ * core, particle n > 0 is drawn again (start and loop) while one of its beads
+ * overlaps a bead of an earlier particle at the same slice, at most 10000
+ * times, after which the world cannot be made (ORC_ESTATE; the reference
+ * logs an error and returns an empty world) */
 int orc_init_world(orc_state *st, orc_draws *dr) {
   const orc_params *p = &st->p;
   int N = p->N, M = p->M, dim = p->dim;
   double *r = (double *)malloc(sizeof(double) * (size_t)M * dim);
-  for (int n = 0; n < N; ++n) {
-    for (int d = 0; d < dim; ++d) r[d] = 2.0 * p->L * (draw_uniform(dr) - 0.5);
-    for (int d = 0; d < dim; ++d) r[(size_t)(M - 1) * dim + d] = r[d];
-    levy_rows(st, r, M, dr);
+  int rc = 0;
+  for (int n = 0; n < N && rc == 0; ++n) {
+    int tries = 0;
+    while (1) {
+      if (++tries > 10000) { rc = ORC_ESTATE; break; }
+      for (int d = 0; d < dim; ++d) r[d] = 2.0 * p->L * (draw_uniform(dr) - 0.5);
+      for (int d = 0; d < dim; ++d) r[(size_t)(M - 1) * dim + d] = r[d];
+      levy_rows(st, r, M, dr);
+      if (!(p->hardcore_a > 0.0) || n == 0 || !init_overlap(st, r, n)) break;
+    }
+    if (rc) break;
     for (int j = 0; j < M; ++j)
       for (int d = 0; d < dim; ++d) st->x[XI(st, d, n, j)] = r[(size_t)j * dim + d];
     st->next[n] = n;
   }
   free(r);
+  if (rc) return rc;
   recompute_V(st);
   cells_rebuild(st);
   return dr->exhausted ? ORC_EDRAWS : 0;
@@ -1214,4 +1245,113 @@ double orc_bench_chains(const orc_params *p, int nchains, int nthreads, long att
   free(th); free(jobs);
   if (bead_updates) *bead_updates = beads;
   return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
+
+/* ------------------------------------------------------------------------ */
+/* time-budgeted multi-chain timing                                          */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+  orc_state *st; orc_update ups[3]; orc_rng rng; long per; double cost;
+} budget_chain;
+
+typedef struct {
+  budget_chain **mine; int n; double budget; struct timespec t0;
+  double beads, sweeps, stop;
+  pthread_barrier_t *bar;
+} budget_job;
+
+static double secs_since(const struct timespec *t0) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)(t.tv_sec - t0->tv_sec) + 1e-9 * (double)(t.tv_nsec - t0->tv_nsec);
+}
+
+static void *budget_worker(void *arg) {
+  budget_job *jb = (budget_job *)arg;
+  pthread_barrier_wait(jb->bar);
+  int done = jb->n == 0;
+  while (!done) {
+    for (int c = 0; c < jb->n && !done; ++c) {
+      budget_chain *bc = jb->mine[c];
+      long left = bc->per;
+      while (left > 0) {
+        long chunk = left < 256 ? left : 256;
+        orc_run_stats s; memset(&s, 0, sizeof(s));
+        orc_run(bc->st, chunk, bc->ups, 3, &bc->rng, 0, NULL, 0, NULL, 0, NULL, NULL, &s);
+        jb->beads += s.bead_updates;
+        left -= chunk;
+        if (secs_since(&jb->t0) >= jb->budget) { done = 1; break; }
+      }
+      if (left == 0) jb->sweeps += 1.0;
+    }
+  }
+  jb->stop = secs_since(&jb->t0);
+  return NULL;
+}
+
+double orc_bench_budget(const orc_params *ps, const int *ells, int nchains, int nthreads,
+                        double budget_s, double com_step, uint64_t seed, double *bead_updates,
+                        double *sweeps) {
+  if (nthreads < 1) nthreads = 1;
+  budget_chain *bc = (budget_chain *)calloc(nchains > 0 ? nchains : 1, sizeof(budget_chain));
+  int *order = (int *)malloc(sizeof(int) * (nchains > 0 ? nchains : 1));
+  for (int c = 0; c < nchains; ++c) {
+    const orc_params *p = &ps[c];
+    bc[c].st = orc_create(p);
+    orc_rng_init(&bc[c].rng, seed, (uint64_t)c);
+    orc_draws dr; memset(&dr, 0, sizeof(dr)); dr.rng = &bc[c].rng;
+    orc_init_world(bc[c].st, &dr);
+    int ell = ells[c], maxs = p->M - 2;
+    int l = ell < maxs ? ell : maxs;
+    int k = (p->M + ell - 1) / ell;
+    orc_update_init(&bc[c].ups[0], 0, 1, l, 2, maxs, 0.0, 1.0, 10, 10000);
+    orc_update_init(&bc[c].ups[1], 1, k, l, 2, maxs, 0.0, 1.0, 10, 10000);
+    orc_update_init(&bc[c].ups[2], 2, k, com_step, 0.1, p->L / 2, 0.4, 0.6, 10, 10000);
+    bc[c].per = (long)p->N * (k + 2);
+    bc[c].cost = (double)p->N * p->M * (p->interactions ? 4.0 : 1.0) + 0.5 * (double)p->N * p->N;
+    order[c] = c;
+  }
+  /* longest first (insertion sort keeps it dependency-free), each chain to
+     the least-loaded thread */
+  for (int a = 1; a < nchains; ++a) {
+    int v = order[a], b = a - 1;
+    while (b >= 0 && bc[order[b]].cost < bc[v].cost) { order[b + 1] = order[b]; --b; }
+    order[b + 1] = v;
+  }
+  budget_job *jobs = (budget_job *)calloc(nthreads, sizeof(budget_job));
+  double *load = (double *)calloc(nthreads, sizeof(double));
+  for (int t = 0; t < nthreads; ++t) jobs[t].mine = (budget_chain **)malloc(sizeof(budget_chain *) * (nchains > 0 ? nchains : 1));
+  for (int a = 0; a < nchains; ++a) {
+    int best = 0;
+    for (int t = 1; t < nthreads; ++t) if (load[t] < load[best]) best = t;
+    jobs[best].mine[jobs[best].n++] = &bc[order[a]];
+    load[best] += bc[order[a]].cost;
+  }
+  pthread_barrier_t bar;
+  pthread_barrier_init(&bar, NULL, (unsigned)nthreads + 1);
+  pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+  for (int t = 0; t < nthreads; ++t) {
+    jobs[t].budget = budget_s; jobs[t].bar = &bar;
+    pthread_create(&th[t], NULL, budget_worker, &jobs[t]);
+  }
+  struct timespec t0;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
+  for (int t = 0; t < nthreads; ++t) jobs[t].t0 = t0;
+  pthread_barrier_wait(&bar);
+  double beads = 0.0, sw = 0.0, wall = 0.0;
+  for (int t = 0; t < nthreads; ++t) {
+    pthread_join(th[t], NULL);
+    beads += jobs[t].beads; sw += jobs[t].sweeps;
+    if (jobs[t].stop > wall) wall = jobs[t].stop;
+    free(jobs[t].mine);
+  }
+  pthread_barrier_destroy(&bar);
+  for (int c = 0; c < nchains; ++c) {
+    for (int q = 0; q < 3; ++q) orc_update_free(&bc[c].ups[q]);
+    orc_destroy(bc[c].st);
+  }
+  free(th); free(jobs); free(load); free(bc); free(order);
+  if (bead_updates) *bead_updates = beads;
+  if (sweeps) *sweeps = sw;
+  return wall;
 }

@@ -36,7 +36,8 @@ enum {
   ORC_SKIP = 2,      /* attempt returned before proposing (n1==n2, no singles, N<=1) */
   ORC_HARDCORE = 3,  /* hard-core retry cap reached: counts as a reject */
   ORC_EDRAWS = -1,   /* injected draw arrays ran out */
-  ORC_EARG = -2
+  ORC_EARG = -2,
+  ORC_ESTATE = -3    /* init_world could not place the hard spheres */
 };
 
 typedef struct orc_params {
@@ -194,6 +195,20 @@ void orc_update_free(orc_update *u);
 double orc_bench_chains(const orc_params *p, int nchains, int nthreads,
                         long attempts, int ell, double com_step, uint64_t seed,
                         double *bead_updates);
+
+/* time-budgeted timing of a list of chains (parameters ps[c], staging and
+ * swap window ells[c]) on nthreads host threads: the chains are dealt to the
+ * threads longest first (cost N M (4 with the pair interaction) + N^2 / 2,
+ * each to the least-loaded thread), every thread runs one sweep's worth of
+ * run! attempts (N (k + 2)) on each of its chains in turn, in chunks of 256
+ * attempts, until budget_s seconds have passed since the common start, so
+ * that no thread idles while another finishes.  Chains are created and
+ * initialised (init_world) before the start.  Returns the wall seconds of the
+ * timed region (the last thread's stop), bead updates through
+ * *bead_updates and completed sweeps through *sweeps. */
+double orc_bench_budget(const orc_params *ps, const int *ells, int nchains, int nthreads,
+                        double budget_s, double com_step, uint64_t seed, double *bead_updates,
+                        double *sweeps);
 
 #ifdef __cplusplus
 }

@@ -53,11 +53,15 @@ struct Plan {
   int split = 0;               // CTA mode: 1 = staging, swaps, rest as three launches
   int pblock[3] = {0, 0, 0};   // split: CTA size per phase (0: block)
   size_t psmem[3] = {0, 0, 0}; // split: dynamic shared bytes per phase
+  int pwarp[3] = {0, 0, 0};    // split: 1 = that phase with one warp per chain
+  int pwarp_bytes[3] = {0, 0, 0};  // ... and the scratch bytes of each warp
 };
 
 // CTA size and dynamic shared bytes of phase ph of a plan
 int phase_block(const Plan &p, int ph) { return p.pblock[ph] > 0 ? p.pblock[ph] : p.block; }
-size_t phase_smem(const Plan &p, int ph) { return p.pblock[ph] > 0 ? p.psmem[ph] : p.dyn_smem; }
+size_t phase_smem(const Plan &p, int ph) {
+  return (p.pblock[ph] > 0 || p.pwarp[ph]) ? p.psmem[ph] : p.dyn_smem;
+}
 
 struct Handle {
   int nchains = 0;
@@ -107,6 +111,14 @@ struct Handle {
   std::vector<ContactTab> ctabs;
   unsigned long long *d_rdf = nullptr;  // pair-distance histograms of every chain
   size_t n_rdf = 0;
+  // the batched adjoint's pool and block maps, made on its first call (the
+  // chains' shapes are fixed for the handle's lifetime)
+  double *d_badj = nullptr;
+  AdjBatchArgs badj{};
+  bool badj_ready = false;
+  // the batch's 32 x 32 (particle, slice) tiles: first tile of each chain
+  int *d_tile_off = nullptr;
+  int ntiles = 0;
 };
 
 int check_params(const pimc_params &p) {
@@ -333,6 +345,40 @@ int refresh_links(Handle *h, int chain0, int nch) {
   return PIMC_OK;
 }
 
+// init_world on the device for every chain: the uniform start and Levy loop
+// of each particle, the hard-core redraw for the chains that have one, then
+// the cached links.  A chain whose hard spheres cannot be placed fails the
+// call (the reference logs an error and returns an empty world,
+// src/system.jl:47-49).
+int init_world_impl(Handle *h) {
+  const int nc = h->nchains;
+  CK(launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, nc, h->maxN, h->stream));
+  bool any_hard = false;
+  for (const auto &d : h->desc) any_hard = any_hard || (d.flags & PF_HARD);
+  if (any_hard) {
+    CK(launch_init_world_hard(h->d_desc, h->d_var, h->d_dpool, h->d_ipool, 0, nc, h->stream));
+    std::vector<ChainVar> v(nc);
+    CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * nc, cudaMemcpyDeviceToHost, h->stream));
+    int rc = sync_check(h);
+    if (rc) return rc;
+    for (int c = 0; c < nc; ++c)
+      if (v[c].err == DERR_INIT) {
+        const ChainDesc &d = h->desc[c];
+        char vol[64];
+        snprintf(vol, sizeof vol, "%g", std::pow(2.0 * d.L, d.dim));
+        // the failed chain's flag is cleared so that a retry starts clean
+        v[c].err = 0;
+        cudaMemcpyAsync(h->d_var, v.data(), sizeof(ChainVar) * nc, cudaMemcpyHostToDevice, h->stream);
+        cudaStreamSynchronize(h->stream);
+        return fail(PIMC_ESTATE, "chain " + std::to_string(c) + ": creating world of " +
+                                     std::to_string(d.N) + " particles with hardspheres of length " +
+                                     std::to_string(d.hard_a) + " in the volume " + vol + " failed");
+      }
+  }
+  if (refresh_links(h, 0, nc)) return PIMC_ECUDA;
+  return PIMC_OK;
+}
+
 int create_impl(const pimc_params *params, int nchains, void **out) {
   if (!params || !out || nchains < 1) return fail(PIMC_EARG, "null argument or nchains < 1");
   if (nchains > (1 << 24)) return fail(PIMC_EARG, "too many chains");
@@ -443,10 +489,14 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   cudaMemcpyAsync(h->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, h->stream);
   if (upload_desc(h)) return cleanup(PIMC_ECUDA);
   if (upload_exp_table() != cudaSuccess) return cleanup(fail(PIMC_ECUDA, "exp table upload failed"));
+  // the address of pimc_adjoint_noalloc's static scratch on this device
+  if (adjoint_static_setup() != cudaSuccess)
+    return cleanup(fail(PIMC_ECUDA, "static adjoint scratch lookup failed"));
   // System(): init_world, cached links, neighbour grid
-  if (launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, nchains, h->maxN, h->stream) != cudaSuccess ||
-      refresh_links(h, 0, nchains))
-    return cleanup(fail(PIMC_ECUDA, "initialisation launch failed"));
+  {
+    const int rc = init_world_impl(h);
+    if (rc) return cleanup(rc);
+  }
   h->bat = plan_smem(h, 0, 256, 1, kStateBudget);
   h->one = h->bat;
   if (sync_check(h)) return cleanup(PIMC_ECUDA);
@@ -565,10 +615,12 @@ int run_plain(Handle *h, long long n) {
 int grid_for(Handle *h, const Plan &p, int phase = -1) {
   int per_sm = 0;
   const cudaError_t e = phase >= 0
-                            ? sweep_phase_occupancy(phase, phase_block(p, phase), phase_smem(p, phase), &per_sm)
+                            ? sweep_phase_occupancy(phase, p.pwarp[phase], phase_block(p, phase),
+                                                    phase_smem(p, phase), &per_sm)
                             : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-  const int units_per_cta = p.mode == 1 ? p.block / 32 : 1;
+  const bool warp = phase >= 0 ? p.pwarp[phase] != 0 : p.mode == 1;
+  const int units_per_cta = warp ? phase_block(p, phase >= 0 ? phase : 0) / 32 : 1;
   const int need = (h->nchains + units_per_cta - 1) / units_per_cta;
   return std::max(1, std::min(need, per_sm * h->num_sms));
 }
@@ -579,7 +631,7 @@ int grid_for(Handle *h, const Plan &p, int phase = -1) {
 bool launch_teams(Handle *h, const Plan &p) {
   int per_sm = 0;
   if (p.mode != 0) return false;
-  const cudaError_t e = p.split ? sweep_phase_occupancy(0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
+  const cudaError_t e = p.split ? sweep_phase_occupancy(0, 0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
                                 : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess) return false;
   return h->nchains <= per_sm * h->num_sms;
@@ -589,7 +641,7 @@ bool launch_teams(Handle *h, const Plan &p) {
 cudaError_t plan_set_smem(const Plan &p) {
   if (!p.split) return sweep_set_smem(p.mode, p.dyn_smem);
   for (int ph = 0; ph < 3; ++ph) {
-    const cudaError_t e = sweep_phase_set_smem(ph, phase_smem(p, ph));
+    const cudaError_t e = sweep_phase_set_smem(ph, p.pwarp[ph], phase_smem(p, ph));
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -609,10 +661,12 @@ cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long
   a.sweeps = 1;
   for (int s = 0; s < n; ++s)
     for (int ph = 0; ph < 3; ++ph) {
+      SweepArgs b = a;
+      if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
       cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
       if (e == cudaSuccess)
-        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), phase_block(p, ph), phase_smem(p, ph),
-                               h->stream);
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], grid_for(h, p, ph), phase_block(p, ph),
+                               phase_smem(p, ph), h->stream);
       if (e != cudaSuccess) return e;
       if (launches) *launches += 1;
     }
@@ -669,12 +723,22 @@ int run_batched(Handle *h, long long n) {
 }
 
 int check_device_errors(Handle *h) {
+  unsigned long long w = 0;
+  CK(check_word_take(h->stream, &w));
+  if (w)
+    return fail(PIMC_EDEVICE, "device bounds check failed: code " + std::to_string((int)(w >> 32)) +
+                                  " on chain " + std::to_string((int)(w & 0xFFFFFFu)) +
+                                  " (1 window, 3 scratch, 4 neighbour queue, 5 particle index)");
   std::vector<ChainVar> v(h->nchains);
   CK(cudaMemcpyAsync(v.data(), h->d_var, sizeof(ChainVar) * h->nchains, cudaMemcpyDeviceToHost, h->stream));
   int rc = sync_check(h);
   if (rc) return rc;
   for (int c = 0; c < h->nchains; ++c)
-    if (v[c].err) return fail(PIMC_EDEVICE, "device error " + std::to_string(v[c].err) + " on chain " + std::to_string(c));
+    if (v[c].err)
+      return fail(PIMC_EDEVICE, "device error " + std::to_string(v[c].err) +
+                                    (v[c].err == DERR_STATE ? " (next is not a permutation)" : "") +
+                                    " on chain " + std::to_string(c) +
+                                    "; the chain is skipped until its state is replaced");
   return PIMC_OK;
 }
 
@@ -749,6 +813,11 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
   }
   int rc = sync_check(h);
   if (rc) return rc;
+  unsigned long long w = 0;
+  CK(check_word_take(h->stream, &w));
+  if (w)
+    return fail(PIMC_EDEVICE, "device bounds check failed: code " + std::to_string((int)(w >> 32)) +
+                                  " in an injected-draw attempt");
   if (out[4]) {
     CK(cudaMemcpyAsync(h->d_dpool + d.x_off, sx.data(), nsnap * 8, cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_ipool + d.next_off, sn.data(), d.N * 4, cudaMemcpyHostToDevice, h->stream));
@@ -797,6 +866,8 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_stage);
   for (auto &t : h->ctabs) cudaFree(t.d);
   cudaFree(h->d_rdf);
+  cudaFree(h->d_badj);
+  cudaFree(h->d_tile_off);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -826,13 +897,59 @@ int pimc_batch_get_beads(void *handle, int chain, double *x) {
   return get_beads_impl(H(handle), chain, x);
 }
 
-// one host<->device copy of the whole batch (host layout, chain order) and
-// one transpose / link refresh launch for all chains
+// the tile list of the batch (once per handle)
+static int ensure_tiles(Handle *h) {
+  if (h->d_tile_off) return PIMC_OK;
+  std::vector<int> off(h->nchains + 1, 0);
+  long long t = 0;
+  for (int c = 0; c < h->nchains; ++c) {
+    off[c] = (int)t;
+    t += (long long)((h->desc[c].N + 31) / 32) * ((h->desc[c].M + 31) / 32);
+    if (t > 0x7fffffffLL) return fail(PIMC_EARG, "batch too large for the transpose tiles");
+  }
+  off[h->nchains] = (int)t;
+  int *d = nullptr;
+  CK(cudaMalloc(&d, sizeof(int) * off.size()));
+  cudaError_t e = cudaMemcpyAsync(d, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return fail(PIMC_ECUDA, std::string("tile list: ") + cudaGetErrorString(e));
+  }
+  h->d_tile_off = d;
+  h->ntiles = (int)t;
+  return PIMC_OK;
+}
+
+// the device address of a host buffer that the GPU can read and write in
+// place (page-locked memory: cudaHostAlloc, cudaHostRegister, a pinned torch
+// tensor), or null for pageable memory
+static double *device_view(const void *host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return static_cast<double *>(a.devicePointer);
+}
+
+// the whole batch (host layout, chain order) in one pass: from a pinned host
+// buffer the tiled transpose reads the caller's memory directly; a pageable
+// buffer goes through one copy into the staging buffer first.  Then one link
+// refresh launch for all chains.
 int pimc_batch_set_beads_all(void *handle, const double *x_all) {
   Handle *h = H(handle);
   if (!h || !x_all) return fail(PIMC_EARG, "null argument");
-  CK(cudaMemcpyAsync(h->d_stage, x_all, h->n_stage * 8, cudaMemcpyHostToDevice, h->stream));
-  CK(launch_import(h->d_desc, h->d_dpool, h->d_stage, 0, h->nchains, (size_t)2 * h->maxNM, h->stream));
+  int rc = ensure_tiles(h);
+  if (rc) return rc;
+  double *src = device_view(x_all);
+  if (!src) {
+    CK(cudaMemcpyAsync(h->d_stage, x_all, h->n_stage * 8, cudaMemcpyHostToDevice, h->stream));
+    src = h->d_stage;
+  }
+  CK(launch_transpose_tiles(true, h->d_desc, h->d_dpool, src, h->d_tile_off, h->nchains, h->ntiles,
+                            8 * h->num_sms, h->stream));
   if (refresh_links(h, 0, h->nchains)) return PIMC_ECUDA;
   return sync_check(h);
 }
@@ -840,8 +957,13 @@ int pimc_batch_set_beads_all(void *handle, const double *x_all) {
 int pimc_batch_get_beads_all(void *handle, double *x_all) {
   Handle *h = H(handle);
   if (!h || !x_all) return fail(PIMC_EARG, "null argument");
-  CK(launch_export(h->d_desc, h->d_dpool, h->d_stage, 0, h->nchains, (size_t)2 * h->maxNM, h->stream));
-  CK(cudaMemcpyAsync(x_all, h->d_stage, h->n_stage * 8, cudaMemcpyDeviceToHost, h->stream));
+  int rc = ensure_tiles(h);
+  if (rc) return rc;
+  double *dst = device_view(x_all);
+  CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, dst ? dst : h->d_stage, h->d_tile_off,
+                            h->nchains, h->ntiles, 8 * h->num_sms, h->stream));
+  if (!dst)
+    CK(cudaMemcpyAsync(x_all, h->d_stage, h->n_stage * 8, cudaMemcpyDeviceToHost, h->stream));
   return sync_check(h);
 }
 
@@ -914,8 +1036,8 @@ int pimc_get_links(void *handle, double *V) {
 int pimc_init_world(void *handle) {
   Handle *h = H(handle);
   if (!h) return fail(PIMC_EARG, "null handle");
-  CK(launch_init_world(h->d_desc, h->d_dpool, h->d_ipool, 0, h->nchains, h->maxN, h->stream));
-  if (refresh_links(h, 0, h->nchains)) return PIMC_ECUDA;
+  int rc = init_world_impl(h);
+  if (rc) return rc;
   return sync_check(h);
 }
 
@@ -982,6 +1104,23 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
   p.split = l.split_phases;
   for (int ph = 0; ph < 3; ++ph) {
     const int b = l.phase_block[ph];
+    const int w = l.phase_warp[ph];
+    if (w != 0 && w != 1) return fail(PIMC_EARG, "phase_warp must be 0 or 1");
+    if (w && (!l.split_phases || ph != 1))
+      return fail(PIMC_EARG, "phase_warp: one warp per chain is offered for the swap phase of a split sweep");
+    if (w) {
+      const int bw = b > 0 ? b : l.block;
+      if (bw < 32 || bw > 256 || bw % 32)
+        return fail(PIMC_EARG, "a warp-per-chain phase needs a CTA of 32 to 256 threads, a multiple of 32");
+      const Plan q = plan_smem(h, 1, bw, 1, 0);
+      if (h->max_dyn_smem > 0 && q.dyn_smem > (size_t)h->max_dyn_smem)
+        return fail(PIMC_EARG, "phase launch needs more shared memory than the device offers");
+      p.pblock[ph] = bw;
+      p.psmem[ph] = q.dyn_smem;
+      p.pwarp[ph] = 1;
+      p.pwarp_bytes[ph] = q.warp_bytes;
+      continue;
+    }
     if (b == 0) continue;
     if (!l.split_phases || b < 64 || b > 512 || b % 32)
       return fail(PIMC_EARG, "phase_block needs split_phases and a multiple of 32 in [64, 512]");
@@ -1018,9 +1157,11 @@ int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
       e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
       if (e != cudaSuccess) break;
       if (p.split) {
-        a.sweeps = 1;
-        e = launch_sweep_phase(a, ph, grid_for(h, p, ph), phase_block(p, ph), phase_smem(p, ph),
-                               h->stream);
+        SweepArgs b = a;
+        b.sweeps = 1;
+        if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], grid_for(h, p, ph), phase_block(p, ph),
+                               phase_smem(p, ph), h->stream);
       } else {
         a.sweeps = 1;
         e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);
@@ -1062,7 +1203,10 @@ int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
   launch->sweeps_per_launch = h->bat.spl;
   launch->state_smem_bytes = h->bat.state_cap;
   launch->split_phases = h->bat.split;
-  for (int ph = 0; ph < 3; ++ph) launch->phase_block[ph] = h->bat.pblock[ph];
+  for (int ph = 0; ph < 3; ++ph) {
+    launch->phase_block[ph] = h->bat.pblock[ph];
+    launch->phase_warp[ph] = h->bat.pwarp[ph];
+  }
   return PIMC_OK;
 }
 
@@ -1150,7 +1294,29 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
         if (ms[ph] < pbest[ph]) {
           pbest[ph] = ms[ph];
           ref.phase_block[ph] = b;
+          ref.phase_warp[ph] = 0;
         }
+    }
+    // the swap phase with one warp per chain, 2 to 8 chains per CTA
+    for (int b : {64, 128, 256}) {
+      pimc_launch l = keep;
+      for (int ph = 0; ph < 3; ++ph) {
+        l.phase_block[ph] = 0;
+        l.phase_warp[ph] = 0;
+      }
+      l.phase_block[1] = b;
+      l.phase_warp[1] = 1;
+      Plan p;
+      if (check_launch(h, l, &p)) continue;
+      if ((rc = pimc_batch_set_launch(h, &l))) return rc;
+      double ms[3];
+      if ((rc = pimc_batch_phase_times(h, 1, ms))) return rc;  // warm
+      if ((rc = pimc_batch_phase_times(h, sweeps_per_trial, ms))) return rc;
+      if (ms[1] < pbest[1]) {
+        pbest[1] = ms[1];
+        ref.phase_block[1] = b;
+        ref.phase_warp[1] = 1;
+      }
     }
     Plan p;
     if (!check_launch(h, ref, &p)) {
@@ -1248,7 +1414,9 @@ int pimc_measure(void *handle) {
   Handle *h = H(handle);
   if (!h) return fail(PIMC_EARG, "null handle");
   CK(launch_measure(h->d_desc, h->d_var, h->d_dpool, h->d_ipool, h->d_upool, 0, h->nchains, h->stream));
-  return sync_check(h);
+  int rc = sync_check(h);
+  if (rc) return rc;
+  return check_device_errors(h);
 }
 
 int pimc_get_energies(void *handle, int chain, double *out, int cap, int *count) {
@@ -1534,6 +1702,114 @@ int pimc_adjoint_noalloc(void *handle, int chain, double *dSdr, double *dSdtheta
   return PIMC_OK;
 }
 
+// the batched adjoint's pool: per bead gA, gB (2 doubles each), per block a
+// row of 9 partials, per chain 9 totals, dS/dr in the host layout of every
+// chain, per chain omega, then the int maps (block -> chain, first block,
+// inverse-permutation offsets, the inverse permutations) and the bead
+// offsets.  One cudaMalloc for the handle's lifetime.
+static int batch_adjoint_setup(Handle *h) {
+  if (h->badj_ready) return PIMC_OK;
+  const int nc = h->nchains;
+  std::vector<int> blk_chain, blk_first(nc), inv_off(nc);
+  std::vector<long long> bead_off(nc);
+  std::vector<double> omega(nc);
+  long long tb = 0;
+  int ninv = 0;
+  for (int c = 0; c < nc; ++c) {
+    const ChainDesc &d = h->desc[c];
+    const long long nm = (long long)d.N * d.M;
+    blk_first[c] = (int)blk_chain.size();
+    for (long long b = 0; b < (nm + 255) / 256; ++b) blk_chain.push_back(c);
+    bead_off[c] = tb;
+    tb += nm;
+    inv_off[c] = ninv;
+    ninv += d.N;
+    omega[c] = h->params[c].harmonic_omega;
+  }
+  const size_t nblocks = blk_chain.size();
+  if (nblocks > (size_t)0x7fffffff) return fail(PIMC_EARG, "batch too large for the adjoint");
+  const size_t nd = 4 * (size_t)tb + 9 * nblocks + 9 * (size_t)nc + h->n_stage + (size_t)nc;
+  const size_t ni = nblocks + 2 * (size_t)nc + (size_t)ninv;
+  const size_t bytes = 8 * nd + 4 * ((ni + 1) & ~(size_t)1) + 8 * (size_t)nc;
+  double *pool = nullptr;
+  if (cudaMalloc(&pool, bytes) != cudaSuccess)
+    return fail(PIMC_ENOMEM, "batched adjoint pool of " + std::to_string(bytes) + " bytes");
+  AdjBatchArgs &a = h->badj;
+  a.desc = h->d_desc;
+  a.dpool = h->d_dpool;
+  a.ipool = h->d_ipool;
+  a.gA = pool;
+  a.gB = a.gA + 2 * (size_t)tb;
+  a.part = a.gB + 2 * (size_t)tb;
+  a.totals = a.part + 9 * nblocks;
+  a.dSdr = a.totals + 9 * (size_t)nc;
+  double *om = a.dSdr + h->n_stage;
+  int *ip = (int *)(om + nc);
+  int *bc = ip, *bf = bc + nblocks, *io = bf + nc, *inv = io + nc;
+  long long *bo = (long long *)(ip + ((ni + 1) & ~(size_t)1));
+  a.omega = om;
+  a.blk_chain = bc;
+  a.blk_first = bf;
+  a.inv_off = io;
+  a.inv = inv;
+  a.bead_off = bo;
+  a.nblocks = (int)nblocks;
+  a.nchains = nc;
+  h->d_badj = pool;
+  CK(cudaMemcpyAsync(om, omega.data(), 8 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(bc, blk_chain.data(), 4 * nblocks, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(bf, blk_first.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(io, inv_off.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(bo, bead_off.data(), 8 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
+  int rc = sync_check(h);
+  if (rc) return rc;
+  h->badj_ready = true;
+  return PIMC_OK;
+}
+
+int pimc_batch_adjoint(void *handle, double *dSdtheta, double *extra, double *dSdr_all) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  for (int c = 0; c < h->nchains; ++c)
+    if (h->desc[c].flags & PF_CONTACT)
+      return fail(PIMC_EARG, "the adjoint covers the Gaussian pair; chain " + std::to_string(c) +
+                                 " uses the contact table, which has no parameter derivative");
+  int rc = batch_adjoint_setup(h);
+  if (rc) return rc;
+  AdjBatchArgs a = h->badj;
+  if (!dSdr_all) a.dSdr = nullptr;
+  CK(cudaEventRecord(h->ev0, h->stream));
+  CK(launch_adjoint_batch(a, h->maxN, h->stream));
+  CK(cudaEventRecord(h->ev1, h->stream));
+  std::vector<double> tot(9 * (size_t)h->nchains);
+  CK(cudaMemcpyAsync(tot.data(), a.totals, 8 * tot.size(), cudaMemcpyDeviceToHost, h->stream));
+  if (dSdr_all)
+    CK(cudaMemcpyAsync(dSdr_all, a.dSdr, 8 * h->n_stage, cudaMemcpyDeviceToHost, h->stream));
+  rc = sync_check(h);
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_launches = 4;
+  for (int c = 0; c < h->nchains; ++c) {
+    const double *t = tot.data() + 9 * (size_t)c;
+    const ChainDesc &d = h->desc[c];
+    if (dSdtheta) {
+      dSdtheta[3 * c] = t[1];
+      dSdtheta[3 * c + 1] = t[2];
+      dSdtheta[3 * c + 2] = t[4];
+    }
+    if (extra) {
+      const double Mt = d.M * d.tau;
+      extra[4 * c] = t[0];
+      extra[4 * c + 1] = t[3];
+      extra[4 * c + 2] = (t[0] + 0.5 * t[6]) / Mt + (t[3] + 0.5 * t[5]) / Mt;
+      extra[4 * c + 3] = t[8];
+    }
+  }
+  return PIMC_OK;
+}
+
 int pimc_contact_table(double g0, double tau, double range, int n, double *out) {
   if (!(g0 != 0.0) || !std::isfinite(g0) || !(tau > 0.0) || !(range > 0.0) || n < 2 || n > 4096 ||
       !out)
@@ -1778,9 +2054,12 @@ int pimc_get_total_stats(void *handle, pimc_stats *out) {
   return PIMC_OK;
 }
 
-// checkpoint layout: magic, version, nchains, then per chain ChainVar and the
-// raw device regions (positions, links and FP32 mirror, next, density,
-// observable series); the pair-distance histograms are not part of it
+// checkpoint layout: magic, version, nchains, then per chain ChainVar, the
+// raw device regions (positions, links and 16-bit mirror, next, density,
+// observable series), the number of pair-distance bins and those counts.
+// ChainVar::rdf_meas counts the measurements in the pair-distance histogram,
+// so both travel together: a restored chain's g(r) normalisation matches its
+// counts.
 int pimc_state_size(void *handle, size_t *bytes) {
   Handle *h = H(handle);
   if (!h || !bytes) return fail(PIMC_EARG, "null argument");
@@ -1789,6 +2068,7 @@ int pimc_state_size(void *handle, size_t *bytes) {
     b += sizeof(ChainVar) + 8 * (size_t)(d.tab_off - d.x_off) + 4 * (size_t)d.N;
     if (d.dens_off >= 0) b += 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb);
     if (d.eser_off >= 0) b += 8 * (size_t)NOBS * d.eser_cap;
+    b += sizeof(int) + 8 * (size_t)std::max(d.rdf_nb, 0);
   }
   *bytes = b;
   return PIMC_OK;
@@ -1815,6 +2095,35 @@ static int state_io(Handle *h, char *buf, size_t bytes, bool save) {
     p += n;
     return e;
   };
+  // every chain's next values (in range: a kernel indexes with them) and
+  // radial bin count are checked before anything is written to the device,
+  // so a refused snapshot leaves the handle untouched.  Whether next is a
+  // permutation is the device's check (ChainVar::err, PIMC_EDEVICE).
+  if (!save) {
+    const char *q = p;
+    for (int c = 0; c < h->nchains; ++c) {
+      const ChainDesc &d = h->desc[c];
+      q += sizeof(ChainVar) + 8 * (size_t)(d.tab_off - d.x_off);
+      for (int i = 0; i < d.N; ++i) {
+        int v = 0;
+        memcpy(&v, q + 4 * (size_t)i, sizeof(int));
+        if (v < 0 || v >= d.N)
+          return fail(PIMC_ESTATE, "state has next[" + std::to_string(i) + "] = " +
+                                       std::to_string(v) + " out of range on chain " +
+                                       std::to_string(c));
+      }
+      q += 4 * (size_t)d.N;
+      if (d.dens_off >= 0) q += 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb);
+      if (d.eser_off >= 0) q += 8 * (size_t)NOBS * d.eser_cap;
+      int nb = 0;
+      memcpy(&nb, q, sizeof(int));
+      if (nb != std::max(d.rdf_nb, 0))
+        return fail(PIMC_ESTATE, "state has " + std::to_string(nb) + " pair-distance bins on chain " +
+                                     std::to_string(c) + ", the handle " +
+                                     std::to_string(std::max(d.rdf_nb, 0)) + " (pimc_set_radial)");
+      q += sizeof(int) + 8 * (size_t)nb;
+    }
+  }
   for (int c = 0; c < h->nchains; ++c) {
     const ChainDesc &d = h->desc[c];
     CK(io(h->d_var + c, sizeof(ChainVar)));
@@ -1822,6 +2131,10 @@ static int state_io(Handle *h, char *buf, size_t bytes, bool save) {
     CK(io(h->d_ipool + d.next_off, 4 * (size_t)d.N));
     if (d.dens_off >= 0) CK(io(h->d_upool + d.dens_off, 8 * (d.dim == 2 ? (size_t)d.dens_nb * d.dens_nb : (size_t)d.dens_nb)));
     if (d.eser_off >= 0) CK(io(h->d_dpool + d.eser_off, 8 * (size_t)NOBS * d.eser_cap));
+    const int nb = std::max(d.rdf_nb, 0);
+    if (save) memcpy(p, &nb, sizeof(int));
+    p += sizeof(int);
+    if (nb > 0) CK(io(d.rdf, 8 * (size_t)nb));
   }
   return sync_check(h);
 }
@@ -1836,6 +2149,16 @@ int pimc_set_state(void *handle, const void *buf, size_t bytes) {
   Handle *h = H(handle);
   if (!h) return fail(PIMC_EARG, "null handle");
   return state_io(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+int pimc_swap_profile(void *handle, unsigned long long *out, int reset) {
+  Handle *h = H(handle);
+  if (!h || !out) return fail(PIMC_EARG, "null argument");
+  const cudaError_t e = profile_take(out, reset != 0, h->stream);
+  if (e == cudaErrorNotSupported)
+    return fail(PIMC_EARG, "pimc_swap_profile needs the profiling build (nvcc -DPIMC_PROFILE=1)");
+  if (e != cudaSuccess) return fail(PIMC_ECUDA, std::string("swap profile: ") + cudaGetErrorString(e));
+  return PIMC_OK;
 }
 
 int pimc_last_run_ms(void *handle, double *ms) {

@@ -43,6 +43,63 @@ constexpr int WARP_SCRATCH_D = TEAM_SLOT_D + 4;
 constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
 
 // ---------------------------------------------------------------------------
+// bounds checks of the PIMC_CHECK build (nvcc -DPIMC_CHECK=1).  A window or
+// slice index, a particle index, a shared-scratch carve or a neighbour-queue
+// push that falls outside its range records (code << 32 | chain) in
+// g_check_word, first error wins, and the access is skipped; the host reads
+// the word after every run and reports PIMC_EDEVICE.  Nothing traps.  In the
+// default build check_ok() is a constant true and compiles away.
+// ---------------------------------------------------------------------------
+#ifndef PIMC_CHECK
+#define PIMC_CHECK 0
+#endif
+// defined here: only the kernel translation unit includes this header
+__device__ unsigned long long g_check_word;
+
+__device__ __forceinline__ bool check_ok(bool cond, int code, const ChainDesc &d) {
+#if PIMC_CHECK
+  if (!cond) {
+    atomicCAS(&g_check_word, 0ull, ((unsigned long long)code << 32) | (d.chain_tag & 0xFFFFFFu));
+    return false;
+  }
+#endif
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// per-section clock counters of the permutation swap (nvcc -DPIMC_PROFILE=1):
+// thread 0 of the group adds the clock64() cycles between section marks to
+// g_prof[0..15] and counts outcomes in g_prof[16..31].  Compiled out in the
+// default build.
+// ---------------------------------------------------------------------------
+#ifndef PIMC_PROFILE
+#define PIMC_PROFILE 0
+#endif
+// defined here: only the kernel translation unit includes this header
+__device__ unsigned long long g_prof[32];
+#if PIMC_PROFILE
+#define PROF_DECL long long prof_t_ = clock64()
+#define PROF_MARK(slot)                                                              \
+  do {                                                                               \
+    const long long n_ = clock64();                                                  \
+    if (threadIdx.x == 0) atomicAdd(&g_prof[slot], (unsigned long long)(n_ - prof_t_)); \
+    prof_t_ = n_;                                                                    \
+  } while (0)
+#define PROF_COUNT(slot)                                          \
+  do {                                                            \
+    if (threadIdx.x == 0) atomicAdd(&g_prof[16 + (slot)], 1ull); \
+  } while (0)
+#else
+#define PROF_DECL
+#define PROF_MARK(slot) \
+  do {                  \
+  } while (0)
+#define PROF_COUNT(slot) \
+  do {                   \
+  } while (0)
+#endif
+
+// ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and draws derived from it
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint4 philox10(uint4 c, uint2 k) {
@@ -563,12 +620,24 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
       }
       const unsigned mo = __ballot_sync(0xffffffffu, po), mn = __ballot_sync(0xffffffffu, pn);
       const unsigned long long base = ((unsigned long long)(unsigned)b << 32) | ((unsigned)t << 1);
-      if (po) q[qn + __popc(mo & lt)] = base;
+      if (po) {
+        const int k = qn + __popc(mo & lt);
+        if (check_ok(k < PQ_CAP, DERR_QUEUE, d)) q[k] = base;
+      }
       qn += __popc(mo);
-      if (pn) q[qn + __popc(mn & lt)] = base | 1ull;
+      if (pn) {
+        const int k = qn + __popc(mn & lt);
+        if (check_ok(k < PQ_CAP, DERR_QUEUE, d)) q[k] = base | 1ull;
+      }
       qn += __popc(mn);
+#if PIMC_CHECK
+      if (qn > PQ_CAP) qn = PQ_CAP;
+#endif
       __syncwarp();
-      if (qn >= 32) pq_flush(c, s, q, qn, wo, wn, lane);
+      // a block of 32 particles queues up to 64 entries (old and new): drain
+      // to fewer than 32 before the next block, so that the queue holds at
+      // most 31 + 64 = 95 < PQ_CAP entries at any time
+      while (qn >= 32) pq_flush(c, s, q, qn, wo, wn, lane);
     }
   }
   while (qn > 0) pq_flush(c, s, q, qn, wo, wn, lane);
@@ -807,6 +876,9 @@ template <class D>
 __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
                              double *prop) {
   const ChainDesc &d = *c.d;
+  if (!check_ok(m >= 2 && m <= TWMAX && m < c.M && j0 >= 0 && j0 < c.M, DERR_WINDOW, d) ||
+      !check_ok(n >= 0 && n < c.N, DERR_INDEX, d))
+    return RES_REJECT;
   const int M = c.M, dim = c.dim;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
   const int nx = c.next[n];
@@ -873,6 +945,9 @@ template <class D>
 __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrite_start,
                            double *sb, double *prop) {
   const ChainDesc &d = *c.d;
+  if (!check_ok(m >= 2 && m <= WMAX && m < c.M && j0 >= 0 && j0 < c.M, DERR_WINDOW, d) ||
+      !check_ok(n >= 0 && n < c.N, DERR_INDEX, d))
+    return RES_REJECT;
   const int lane = threadIdx.x & 31;
   const int M = c.M, dim = c.dim;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;

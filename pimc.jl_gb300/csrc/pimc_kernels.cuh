@@ -292,6 +292,11 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
   const bool lead = warp == 0;
   const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  if (!check_ok(m >= 2 && m <= WMAX && m < M && j0 >= 0 && j0 < M, DERR_WINDOW, d) ||
+      !check_ok(n1 >= 0 && n1 < N, DERR_INDEX, d))
+    return RES_SKIP;
+  PROF_DECL;
+  PROF_COUNT(0);
   HeatBath<FAST> hb;
   hb.c = &c;
   hb.j0 = j0;
@@ -326,6 +331,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   }
   G::template max<1>(wm, red);
   G::sync();
+  PROF_MARK(0);
   const W wmax = wm[0];
   W ssum = W(0);
   if (lead) {
@@ -366,7 +372,11 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   const int n2 = S.iv[0];
   if (n2_out && tid == 0) *n2_out = n2;
   G::sync();
-  if (n2 == n1) return RES_SKIP;
+  PROF_MARK(1);
+  if (n2 == n1 || !check_ok(n2 >= 0 && n2 < N, DERR_INDEX, d)) {
+    PROF_COUNT(1);
+    return RES_SKIP;
+  }
 
   double log_ratio = 0.0;
   if (d.flags & PF_PHYS) {
@@ -403,6 +413,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     log_ratio = logaddexp(-l1p, -l2p) - logaddexp(-l1, -l2);
   }
 
+  PROF_MARK(2);
   // two bridges with exchanged ends
   const int nx1 = c.next[n1], nx2 = c.next[n2];
   auto own1 = [&](int t) { return (j0 + t < M) ? n1 : nx1; };
@@ -476,6 +487,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     if (lane == 0) S.iv[1] = fail;
   }
   G::sync();
+  PROF_MARK(3);
   if (S.iv[1]) return RES_HARDCORE;
   for (int k = tid; k < 2 * (m + 1); k += nt) {
     const int b = k / (m + 1), t = k % (m + 1);
@@ -495,6 +507,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     if (d.flags & PF_PAIR) (b == 0 ? S.q1 : S.q2)[t] = qpos(d, qx, qy);
   }
   G::sync();
+  PROF_MARK(4);
   const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
   double w2[2] = {0.0, 0.0};  // w_initial, w_update
   for (int k = tid; k < 2 * m; k += nt) {
@@ -530,6 +543,8 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       monotone = d.g > 0.0;
     }
   }
+  PROF_MARK(5);
+  if (early) PROF_COUNT(2);
   // the pair of the two moving paths, old and new (physical rules), exact
   if (pairs && phys)
     for (int t = tid; t < m; t += nt) {
@@ -606,7 +621,10 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       const double radius = fabs(h) * (v[1] + v[3]);
       dec = decide_interval(centre - radius, centre + radius, dr.uniform_accept());
     }
+    if (dec != -1) PROF_COUNT(3);
   }
+  PROF_MARK(6);
+  if (dec == -1) PROF_COUNT(4);
   if (dec == -1) {
     for (int b = 0; b < 2; ++b) {
       const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
@@ -619,6 +637,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       if (phys) w2[1] += wn; else w2[0] += wn;
     }
   }
+  PROF_MARK(7);
   int acc;
   if (dec == 0 || dec == 1) {
     acc = dec;
@@ -641,7 +660,12 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       G::sync();
     }
   }
-  if (!acc) return RES_REJECT;
+  PROF_MARK(8);
+  if (!acc) {
+    PROF_COUNT(6);
+    return RES_REJECT;
+  }
+  PROF_COUNT(5);
   // accept: exchange next, write the bridges along the new cycles, exchange
   // the tails (reshape.jl:247-279)
   const int nn1 = nx2, nn2 = nx1;
@@ -676,6 +700,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     }
   }
   G::sync();
+  PROF_MARK(9);
   return RES_ACCEPT;
 }
 
@@ -1017,8 +1042,15 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
         const int b = b0 + lane;
         const bool p = b < N && f.pass(row[b]);
         const unsigned mk = __ballot_sync(0xffffffffu, p);
-        if (p) q[qn + __popc(mk & lt)] = ((unsigned long long)(unsigned)b << 32) | (unsigned)kk;
+        if (p) {
+          const int k = qn + __popc(mk & lt);
+          if (check_ok(k < PQ_CAP, DERR_QUEUE, d))
+            q[k] = ((unsigned long long)(unsigned)b << 32) | (unsigned)kk;
+        }
         qn += __popc(mk);
+#if PIMC_CHECK
+        if (qn > PQ_CAP) qn = PQ_CAP;
+#endif
         __syncwarp();
         if (qn >= 32) flush();
       }

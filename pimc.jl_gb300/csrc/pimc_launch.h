@@ -69,16 +69,37 @@ struct AdjArgs {
   double *sum_rg;     // [1], zeroed before the launch
 };
 
+// the adjoint of every chain of a batch (pimc_batch_adjoint): beads in
+// blocks of 256, chain after chain
+struct AdjBatchArgs {
+  const ChainDesc *desc;
+  double *dpool;
+  int *ipool;
+  const double *omega;        // [nchains] trap frequency (d/domega)
+  const int *blk_chain;       // [nblocks] chain of each block
+  const int *blk_first;       // [nchains] first block of each chain
+  const long long *bead_off;  // [nchains] first bead of each chain in gA / gB
+  const int *inv_off;         // [nchains] offset of each chain's inverse permutation
+  double *gA, *gB;            // [total beads][2]
+  int *inv;                   // [sum of N]
+  double *part;               // [nblocks][9]
+  double *dSdr;               // host layout of every chain (desc.host_off), or null
+  double *totals;             // [nchains][9]: S_ext, dV0, domega, S_pair, dg, pair
+                              // virial, r.g_ext, 0, r.dS/dr
+  int nblocks, nchains;
+};
+
 // mode 0: one CTA per chain (k_sweep); mode 1: one warp per chain (k_sweep_warp)
 cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size_t smem,
                          cudaStream_t s);
 cudaError_t sweep_set_smem(int mode, size_t smem);
 // the sweep as three launches per sweep (phase 0 staging, 1 swaps, 2 the
-// rest), one CTA per chain; a.sweeps must be 1
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int grid, int block, size_t smem,
-                               cudaStream_t s);
-cudaError_t sweep_phase_set_smem(int phase, size_t smem);
-cudaError_t sweep_phase_occupancy(int phase, int block, size_t smem, int *blocks_per_sm);
+// rest), one CTA per chain, or for the swaps (warp = 1) one warp per chain;
+// a.sweeps must be 1
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int grid, int block,
+                               size_t smem, cudaStream_t s);
+cudaError_t sweep_phase_set_smem(int phase, int warp, size_t smem);
+cudaError_t sweep_phase_occupancy(int phase, int warp, int block, size_t smem, int *blocks_per_sm);
 size_t sweep_ctl_bytes();
 cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm);
 cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s);
@@ -86,6 +107,10 @@ cudaError_t launch_eval_action(const EvalArgs &a, cudaStream_t s);
 cudaError_t launch_eval_weights(const EvalArgs &a, cudaStream_t s);
 cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0,
                               int nchains, int maxN, cudaStream_t s);
+// the hard-core redraw of init_world for the chains with a hard core (one
+// warp per chain; others return at once); failures set ChainVar::err
+cudaError_t launch_init_world_hard(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
+                                   int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
                          int maxNM, cudaStream_t s);
 cudaError_t launch_import(const ChainDesc *desc, double *dpool, const double *src, int chain0,
@@ -94,10 +119,25 @@ cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *ds
                           int nchains, size_t maxn, cudaStream_t s);
 cudaError_t launch_mirror(const ChainDesc *desc, double *dpool, int chain0, int nchains, int maxNM,
                           cudaStream_t s);
+// every chain's positions between the host layout (at desc.host_off of
+// `host`, which may be pinned host memory the GPU reaches directly) and the
+// device layout, in 32 x 32 tiles; tile_off[nchains + 1] on the device
+cudaError_t launch_transpose_tiles(bool import, const ChainDesc *desc, double *dpool,
+                                   double *host, const int *tile_off, int nchains, int ntiles,
+                                   int grid, cudaStream_t s);
 cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);
+// four launches over every chain (inverse permutations, beads, gradients,
+// per-chain totals)
+cudaError_t launch_adjoint_batch(const AdjBatchArgs &a, int maxN, cudaStream_t s);
 cudaError_t upload_exp_table();
+// PIMC_CHECK builds: the device check word (code << 32 | chain of the first
+// failed bounds check, 0 if none), cleared by the read; always 0 otherwise
+cudaError_t check_word_take(cudaStream_t s, unsigned long long *w);
+// PIMC_PROFILE builds: the swap's section cycles [0..15] and outcome counts
+// [16..31]; cudaErrorNotSupported otherwise
+cudaError_t profile_take(unsigned long long *out, bool reset, cudaStream_t s);
 // static adjoint scratch: kNoAllocDoubles doubles, enough for a chain of
 // kNoAllocBeads beads (N*M) and kNoAllocParticles particles
 constexpr int kNoAllocBeads = 65536;
@@ -105,7 +145,10 @@ constexpr int kNoAllocParticles = 8192;
 constexpr size_t kNoAllocDoubles = 6 * (size_t)kNoAllocBeads +
                                    8 * (size_t)((kNoAllocBeads + 255) / 256) + 16 +
                                    (size_t)kNoAllocParticles;
-// its device address on the current device (looked up on the first call)
+// set-up: look up the array's address on the current device (every handle
+// creation calls it with its device current)
+cudaError_t adjoint_static_setup();
+// its address on the current device, as the last set-up on it found it
 cudaError_t adjoint_static_scratch(double **ptr);
 // the contact-interaction propagator table T[n][n] for (range, g0, tau)
 cudaError_t launch_contact_table(double *dtab, int n, double range, double g0, double tau,

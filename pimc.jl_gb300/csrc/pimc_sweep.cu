@@ -8,6 +8,7 @@
 // captured in a CUDA graph).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 
 #include "pimc_kernels.cuh"
@@ -36,6 +37,31 @@ __device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ip
 // moves whose acceptance depends on other paths at the same slice
 __device__ __forceinline__ bool chain_serial_local(const ChainDesc &d) {
   return ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) || (d.flags & PF_HARD);
+}
+
+// next[] of a chain must be a permutation of 0..N-1: every value in range
+// (the host refuses out-of-range values before they reach the device) and no
+// value twice.  The group marks each value in a bitmap of (N + 31) / 32 words
+// of shared memory; a chain that fails gets ChainVar::err = DERR_STATE and is
+// skipped by every kernel until its state is replaced.
+template <bool WARP>
+__device__ bool next_is_permutation(const int *next, int N, unsigned *bits) {
+  const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
+  const int nt = WARP ? 32 : (int)blockDim.x;
+  const int nw = (N + 31) >> 5;
+  for (int w = tid; w < nw; w += nt) bits[w] = 0u;
+  if (WARP) __syncwarp(); else __syncthreads();
+  int bad = 0;
+  for (int i = tid; i < N; i += nt) {
+    const int v = next[i];
+    if (v < 0 || v >= N) {
+      bad = 1;
+    } else {
+      const unsigned m = 1u << (v & 31);
+      if (atomicOr(&bits[v >> 5], m) & m) bad = 1;
+    }
+  }
+  return WARP ? !__any_sync(0xffffffffu, bad) : !__syncthreads_or(bad);
 }
 
 __device__ void record_measurement(const ChainDesc &d, ChainVar &v, const CV &c, const double *e,
@@ -77,7 +103,15 @@ struct SmemCtl {
   double e4[NOBS];
   int iflag[8];
   int chain;
+  int scratch_bytes;  // bytes of shared scratch the group's moves may carve
 };
+
+// bytes of dynamic shared memory of the running launch
+__device__ __forceinline__ unsigned dyn_smem_bytes() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
+  return r;
+}
 
 // one sweep of one chain by a group: the whole CTA, or one warp on its own
 // the phases of a sweep; a kernel runs the ones its mask names, so that each
@@ -130,6 +164,12 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
   const bool serial_local = chain_serial_local(d);
   const unsigned long long sweep = sc.v.sweep;
   double *wsb = (double *)scratch + (size_t)warp * warp_scratch_d;
+  // every carve below must fit the group's scratch (PIMC_CHECK builds)
+  if (!check_ok((size_t)nwarps * warp_scratch_d * sizeof(double) <= (size_t)sc.scratch_bytes &&
+                    SwapScratch::bytes(N, nwarps) <= (size_t)sc.scratch_bytes &&
+                    ComScratch::bytes(N, M, nwarps) <= (size_t)sc.scratch_bytes,
+                DERR_SCRATCH, d))
+    return;
 
   // ---- staging phases (ReshapeLinear)
   if (PH & SW_STAGE) {
@@ -327,8 +367,11 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
 
 // warp per chain: every warp of the grid pulls chains from the queue (or
 // takes chain0 + its global warp index once) and sweeps them alone; its
-// control block and scratch live in its own slice of dynamic shared memory
-__global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
+// control block and scratch live in its own slice of dynamic shared memory.
+// PH names the phases of the sweep it runs (all of them, or the swaps alone
+// as the swap launch of a split sweep).
+template <int PH>
+__device__ __forceinline__ void sweep_warp(const SweepArgs &a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const size_t ctl = (sizeof(SmemCtl) + 15) & ~(size_t)15;
@@ -348,6 +391,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
         sc.d = a.desc[ch];
         sc.v = a.var[ch];
         sc.mix = a.mix[ch];
+        sc.scratch_bytes = a.warp_bytes;
       }
     }
     ci = __shfl_sync(0xffffffffu, ci, 0);
@@ -355,11 +399,21 @@ __global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) {
     ++iter;
     if (ci >= a.nchains) break;
     CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<true, SW_ALL>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
+    // the warp's scratch (at least N doubles) holds the bitmap of the check
+    const bool ok = sc.v.err == 0 && next_is_permutation<true>(c.next, sc.d.N, (unsigned *)scratch);
+    if (!ok && lane == 0 && sc.v.err == 0) sc.v.err = DERR_STATE;
+    __syncwarp();
+    if (ok)
+      for (int s = 0; s < a.sweeps; ++s) sweep_one<true, PH>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
     if (lane == 0) a.var[sc.chain] = sc.v;
     __syncwarp();
   }
 }
+
+__global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) { sweep_warp<SW_ALL>(a); }
+// the swap phase of a split sweep with one warp per chain: twice the chains
+// in flight of a two-warp CTA per chain at the same registers per SM
+__global__ void __launch_bounds__(256, 2) k_sweep_swap_warp(SweepArgs a) { sweep_warp<SW_SWAP>(a); }
 
 template <int PH>
 __device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
@@ -379,6 +433,7 @@ __device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
         sc.d = a.desc[ch];
         sc.v = a.var[ch];
         sc.mix = a.mix[ch];
+        sc.scratch_bytes = (int)dyn_smem_bytes() - a.state_bytes;
       } else {
         sc.chain = -1;
       }
@@ -388,6 +443,18 @@ __device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
     if (sc.chain < 0) break;
     const ChainDesc &d = sc.d;
     CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
+    {
+      __shared__ unsigned bits[(kMaxParticles + 31) / 32];
+      const bool ok = sc.v.err == 0 && next_is_permutation<false>(c.next, d.N, bits);
+      if (!ok) {
+        if (tid == 0) {
+          if (sc.v.err == 0) sc.v.err = DERR_STATE;
+          a.var[sc.chain] = sc.v;
+        }
+        __syncthreads();
+        continue;
+      }
+    }
     const int N = d.N, M = d.M, dim = d.dim;
     const bool staged = d.smem_bytes > 0 && d.smem_bytes <= a.state_bytes;
     const size_t nx = (size_t)dim * M * N, nv = (size_t)M * N;
@@ -616,6 +683,71 @@ __global__ void k_export(const ChainDesc *desc, const double *dpool, double *dst
   }
 }
 
+// The same transposes through 32 x 32 tiles of (particle, slice), over a
+// flat list of every chain's tiles (tile_off[c] = first tile of chain c), so
+// that both sides are read and written in whole rows: the host layout
+// x[d][n][j] in runs of 32 slices, the device layout x[j][n][d] in runs of
+// 32 particles.  The host-layout side may be the caller's pinned host buffer,
+// which the GPU reads and writes directly over the coherent CPU-GPU link
+// (Grace-Blackwell NVLink-C2C): the copy and the transpose are one pass.
+// Persistent grid; each block walks tiles t = blockIdx.x, += gridDim.x.
+__device__ __forceinline__ int tile_chain(const int *tile_off, int nchains, int t) {
+  int lo = 0, hi = nchains;  // tile_off[lo] <= t < tile_off[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (tile_off[mid] <= t) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <bool IMPORT>
+__global__ void __launch_bounds__(256) k_transpose_tiles(const ChainDesc *desc, double *dpool,
+                                                          double *host, const int *tile_off,
+                                                          int nchains) {
+  __shared__ double tile[2][32][33];
+  const int ntiles = tile_off[nchains];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int c = tile_chain(tile_off, nchains, t);
+    const ChainDesc &d = desc[c];
+    const int N = d.N, M = d.M, dim = d.dim;
+    const int tj = (M + 31) >> 5, lt = t - tile_off[c];
+    const int n0 = (lt / tj) * 32, j0 = (lt % tj) * 32;
+    const int nn = min(32, N - n0), nj = min(32, M - j0);
+    double *x = dpool + d.x_off;
+    double *hx = host + d.host_off;
+    if (IMPORT) {
+      // host rows (k, n): 32 consecutive slices per warp-wide read
+      for (int r = w; r < dim * nn; r += 8) {
+        const int k = r / nn, n = r % nn;
+        if (lane < nj) tile[k][n][lane] = hx[((size_t)k * N + n0 + n) * M + j0 + lane];
+      }
+      __syncthreads();
+      // device rows j: 32 particles x dim consecutive doubles each
+      const int row = nn * dim;
+      for (int q = threadIdx.x; q < nj * row; q += blockDim.x) {
+        const int jj = q / row, e = q % row;
+        const int n = e / dim, k = e % dim;
+        x[((size_t)(j0 + jj) * N + n0) * dim + e] = tile[k][n][jj];
+      }
+      __syncthreads();
+    } else {
+      const int row = nn * dim;
+      for (int q = threadIdx.x; q < nj * row; q += blockDim.x) {
+        const int jj = q / row, e = q % row;
+        const int n = e / dim, k = e % dim;
+        tile[k][n][jj] = x[((size_t)(j0 + jj) * N + n0) * dim + e];
+      }
+      __syncthreads();
+      for (int r = w; r < dim * nn; r += 8) {
+        const int k = r / nn, n = r % nn;
+        if (lane < nj) hx[((size_t)k * N + n0 + n) * M + j0 + lane] = tile[k][n][lane];
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // init_world (src/system.jl:36-78): uniform start, closed Levy loop through
 // M rows whose first and last rows coincide, teleport
 __global__ void k_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0) {
@@ -647,6 +779,71 @@ __global__ void k_init_world(const ChainDesc *desc, double *dpool, int *ipool, i
   for (int k = 0; k < dim; ++k)
     for (int j = 0; j < M; ++j) c.X(k, n, j) = teleport(c.X(k, n, j), L, inv2L);
   c.next[n] = n;
+}
+
+// init_world with a hard core (src/system.jl:44-64): one warp per chain, the
+// particles in order.  Lane 0 draws a particle's start and Levy loop from the
+// particle's own stream in k_init_world's order (so a particle that fits at
+// once gets k_init_world's path); the warp then checks every bead against the
+// beads of the earlier particles at its slice (norm of the per-component
+// minimum-image distances below a).  A particle that overlaps is drawn again
+// from its continuing stream, at most 10000 times, after which the chain gets
+// ChainVar::err = DERR_INIT and the world is not made.
+__global__ void k_init_world_hard(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
+                                  int chain0) {
+  const int ch = chain0 + blockIdx.x;
+  const ChainDesc &d = desc[ch];
+  if (!(d.flags & PF_HARD)) return;
+  const int lane = threadIdx.x & 31;
+  CV c = make_cv(&d, dpool, ipool, nullptr);
+  const int N = d.N, M = d.M, dim = d.dim;
+  const double L = d.L, inv2L = 1.0 / (2.0 * L);
+  for (int n = 0; n < N; ++n) {
+    GenDraws dr = gen_draws(make_stream(d, 0, PH_INIT, (unsigned)n));
+    bool placed = false;
+    for (int tries = 0; tries < 10000 && !placed; ++tries) {
+      if (lane == 0) {
+        double st[2] = {0.0, 0.0};
+        for (int k = 0; k < dim; ++k) {
+          st[k] = 2.0 * L * (dr.uniform() - 0.5);
+          c.X(k, n, 0) = st[k];
+          c.X(k, n, M - 1) = st[k];
+        }
+        const int mm = M - 2;
+        double pp[2] = {st[0], st[1]};
+        for (int j = 1; j <= mm; ++j) {
+          const double al = (double)(mm + 1 - j) / (double)(mm + 2 - j);
+          const double sg = sqrt(2.0 * d.lambda * al * d.tau);
+          double z[2];
+          for (int k = 0; k < dim; ++k) z[k] = dr.normal();
+          for (int k = 0; k < dim; ++k) {
+            pp[k] = al * pp[k] + (1.0 - al) * st[k] + z[k] * sg;
+            c.X(k, n, j) = pp[k];
+          }
+        }
+        for (int k = 0; k < dim; ++k)
+          for (int j = 0; j < M; ++j) c.X(k, n, j) = teleport(c.X(k, n, j), L, inv2L);
+      }
+      __syncwarp();
+      int hit = 0;
+      for (int q = lane; q < M * n && !hit; q += 32) {
+        const int j = q / n, i = q % n;
+        double s2 = 0.0;
+        for (int k = 0; k < dim; ++k) {
+          const double dd = dist1(c.X(k, i, j), c.X(k, n, j), L);
+          s2 = __dadd_rn(s2, __dmul_rn(dd, dd));
+        }
+        if (__dsqrt_rn(s2) < d.hard_a) hit = 1;
+      }
+      placed = !__any_sync(0xffffffffu, hit);
+    }
+    if (!placed) {
+      if (lane == 0) var[ch].err = DERR_INIT;
+      return;
+    }
+    if (lane == 0) c.next[n] = n;
+    __syncwarp();
+  }
 }
 
 // cached link actions V[j][n] = lnV(bead, next bead) and the FP32 mirror
@@ -685,6 +882,14 @@ __global__ void __launch_bounds__(256) k_measure(const ChainDesc *desc, ChainVar
   __syncthreads();
   CV c = make_cv(&sc.d, dpool, ipool, upool);
   __shared__ unsigned long long qbuf[8 * PQ_CAP];
+  __shared__ unsigned bits[(kMaxParticles + 31) / 32];
+  if (sc.v.err != 0 || !next_is_permutation<false>(c.next, sc.d.N, bits)) {
+    if (threadIdx.x == 0) {
+      if (sc.v.err == 0) sc.v.err = DERR_STATE;
+      var[ch] = sc.v;
+    }
+    return;
+  }
   measure_group<false>(c, red, sc.e4, c.hist != nullptr, qbuf);
   if (threadIdx.x == 0) {
     record_measurement(sc.d, sc.v, c, sc.e4, c.hist != nullptr);
@@ -706,65 +911,81 @@ __device__ __forceinline__ double mi_signed(double a, double b, double L) {
   return s;
 }
 
+// adjoint terms of bead k (slice-major k = j N + i) of one chain: v[8] the
+// block partials above, ga the bead's gradient from the external potential
+// and from the pair terms of the link it starts, gb the gradient of the next
+// bead of its path (in_, jn) from the pair terms of that link
+__device__ __forceinline__ void adjoint_bead(const ChainDesc &d, const CV &c, int k, double omega,
+                                             double (&v)[8], double (&ga)[2], double (&gb)[2]) {
+  const int N = c.N, M = c.M, dim = c.dim;
+  const int j = k / N, i = k % N;
+  const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
+  const double tau = d.tau;
+  const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+  const double anx = c.X(0, in, jn), any = c.Xd(1, in, jn);
+  double ge[2];
+  grad_vext(d, ax, ay, ge[0], ge[1]);
+  ge[0] *= tau;
+  ge[1] *= tau;
+  v[0] = tau * vext(d, ax, ay);
+  if (d.flags & PF_LATT) {
+    const double sx = sinpi(ax * d.lat_k), sy = dim > 1 ? sinpi(ay * d.lat_k) : 0.0;
+    v[1] = tau * (sx * sx + sy * sy);
+  }
+  if (d.flags & PF_HARM) v[2] = tau * omega * (ax * ax + ay * ay);
+  v[6] = ax * ge[0] + ay * ge[1];
+  double go[2] = {0.0, 0.0}, gn[2] = {0.0, 0.0};
+  if (d.flags & PF_PAIR) {
+    const double rc2 = d.rc * d.rc, cg = d.inv2s2, h = 0.5 * tau;
+    Prefilter f;
+    f.init_q(c.Q(i, j), d.q_lim_rc);
+    const unsigned *row = c.xq + (size_t)j * c.ldn;
+    for (int b = 0; b < N; ++b) {
+      if (b == i || !f.pass(row[b])) continue;
+      const double bxv = c.X(0, b, j), byv = c.Xd(1, b, j);
+      const double d1x = mi_signed(ax, bxv, d.L), d1y = dim > 1 ? mi_signed(ay, byv, d.L) : 0.0;
+      const double r2a = mi2(d, ax, ay, bxv, byv);
+      if (r2a > rc2) continue;
+      const int bn = j == M - 1 ? c.next[b] : b;
+      const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
+      const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
+      const double r2b = mi2(d, anx, any, bnx, bny);
+      const double e1 = exp_neg(-r2a * cg), e2 = exp_neg(-r2b * cg);
+      const double v1 = d.g * e1, v2 = d.g * e2;
+      go[0] += h * (-2.0 * cg * v1) * d1x;
+      go[1] += h * (-2.0 * cg * v1) * d1y;
+      gn[0] += h * (-2.0 * cg * v2) * d2x;
+      gn[1] += h * (-2.0 * cg * v2) * d2y;
+      // each unordered pair is visited from both sides
+      v[3] += 0.5 * h * (v1 + v2);
+      v[4] += 0.5 * h * (e1 + e2);
+      v[5] += 0.5 * h * (-2.0 * cg) * (r2a * v1 + r2b * v2);
+    }
+  }
+  ga[0] = ge[0] + go[0];
+  ga[1] = ge[1] + go[1];
+  gb[0] = gn[0];
+  gb[1] = gn[1];
+}
+
 __global__ void __launch_bounds__(256) k_adjoint_beads(AdjArgs a) {
   __shared__ double red[256];
   __shared__ ChainDesc d;
   if (threadIdx.x == 0) d = a.desc[a.chain];
   __syncthreads();
   CV c = make_cv(&d, a.dpool, a.ipool, nullptr);
-  const int N = c.N, M = c.M, dim = c.dim;
+  const int N = c.N, M = c.M;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (k < N * M) {
-    const int j = k / N, i = k % N;
-    const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-    const double tau = d.tau;
-    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
-    const double anx = c.X(0, in, jn), any = c.Xd(1, in, jn);
-    double ge[2];
-    grad_vext(d, ax, ay, ge[0], ge[1]);
-    ge[0] *= tau;
-    ge[1] *= tau;
-    v[0] = tau * vext(d, ax, ay);
-    if (d.flags & PF_LATT) {
-      const double sx = sinpi(ax * d.lat_k), sy = dim > 1 ? sinpi(ay * d.lat_k) : 0.0;
-      v[1] = tau * (sx * sx + sy * sy);
-    }
-    if (d.flags & PF_HARM) v[2] = tau * a.omega * (ax * ax + ay * ay);
-    v[6] = ax * ge[0] + ay * ge[1];
-    double go[2] = {0.0, 0.0}, gn[2] = {0.0, 0.0};
-    if (d.flags & PF_PAIR) {
-      const double rc2 = d.rc * d.rc, cg = d.inv2s2, h = 0.5 * tau;
-      Prefilter f;
-      f.init_q(c.Q(i, j), d.q_lim_rc);
-      const unsigned *row = c.xq + (size_t)j * c.ldn;
-      for (int b = 0; b < N; ++b) {
-        if (b == i || !f.pass(row[b])) continue;
-        const double bxv = c.X(0, b, j), byv = c.Xd(1, b, j);
-        const double d1x = mi_signed(ax, bxv, d.L), d1y = dim > 1 ? mi_signed(ay, byv, d.L) : 0.0;
-        const double r2a = mi2(d, ax, ay, bxv, byv);
-        if (r2a > rc2) continue;
-        const int bn = j == M - 1 ? c.next[b] : b;
-        const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
-        const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
-        const double r2b = mi2(d, anx, any, bnx, bny);
-        const double e1 = exp_neg(-r2a * cg), e2 = exp_neg(-r2b * cg);
-        const double v1 = d.g * e1, v2 = d.g * e2;
-        go[0] += h * (-2.0 * cg * v1) * d1x;
-        go[1] += h * (-2.0 * cg * v1) * d1y;
-        gn[0] += h * (-2.0 * cg * v2) * d2x;
-        gn[1] += h * (-2.0 * cg * v2) * d2y;
-        // each unordered pair is visited from both sides
-        v[3] += 0.5 * h * (v1 + v2);
-        v[4] += 0.5 * h * (e1 + e2);
-        v[5] += 0.5 * h * (-2.0 * cg) * (r2a * v1 + r2b * v2);
-      }
-    }
+    double ga[2], gb[2];
+    adjoint_bead(d, c, k, a.omega, v, ga, gb);
     // per-bead buffers in the chain's [i][j] order (k2 = i*M + j)
+    const int j = k / N, i = k % N;
     const size_t k2 = (size_t)i * M + j;
     for (int q = 0; q < 2; ++q) {
-      a.gA[k2 * 2 + q] = ge[q] + go[q];
-      a.gB[k2 * 2 + q] = gn[q];
+      a.gA[k2 * 2 + q] = ga[q];
+      a.gB[k2 * 2 + q] = gb[q];
     }
   }
   block_sum_k<8>(v, red);
@@ -810,6 +1031,99 @@ __global__ void __launch_bounds__(256) k_adjoint_finish(AdjArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// batched adjoint: every chain of a batch in one launch per stage.  Blocks of
+// 256 beads are laid out chain after chain (blk_first[c] is chain c's first
+// block, blk_chain[b] the chain of block b), so one grid covers chains of any
+// size; each block works on one chain only and writes its partial sums to
+// its own row of part, which k_adjoint_totals_b reduces per chain.
+// ---------------------------------------------------------------------------
+__global__ void k_adjoint_inv_b(AdjBatchArgs a) {
+  const int ch = blockIdx.y;
+  const ChainDesc &d = a.desc[ch];
+  const int *next = a.ipool + d.next_off;
+  int *inv = a.inv + a.inv_off[ch];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < d.N; i += gridDim.x * blockDim.x)
+    inv[next[i]] = i;
+}
+
+__global__ void __launch_bounds__(256) k_adjoint_beads_b(AdjBatchArgs a) {
+  __shared__ double red[256];
+  __shared__ ChainDesc d;
+  __shared__ int ch, lb;
+  if (threadIdx.x == 0) {
+    ch = a.blk_chain[blockIdx.x];
+    lb = blockIdx.x - a.blk_first[ch];
+    d = a.desc[ch];
+  }
+  __syncthreads();
+  CV c = make_cv(&d, a.dpool, a.ipool, nullptr);
+  const int N = c.N, M = c.M;
+  const int k = lb * blockDim.x + threadIdx.x;
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (k < N * M) {
+    double ga[2], gb[2];
+    adjoint_bead(d, c, k, a.omega[ch], v, ga, gb);
+    const int j = k / N, i = k % N;
+    const size_t k2 = (size_t)a.bead_off[ch] + (size_t)i * M + j;
+    for (int q = 0; q < 2; ++q) {
+      a.gA[k2 * 2 + q] = ga[q];
+      a.gB[k2 * 2 + q] = gb[q];
+    }
+  }
+  block_sum_k<8>(v, red);
+  if (threadIdx.x == 0)
+    for (int q = 0; q < 8; ++q) a.part[(size_t)blockIdx.x * 9 + q] = v[q];
+}
+
+// per bead the full gradient gA[k] + gB[prev(k)]: dS/dr (host layout
+// x[d][n][j] of the chain at desc.host_off, when requested) and r . dS/dr
+__global__ void __launch_bounds__(256) k_adjoint_finish_b(AdjBatchArgs a) {
+  __shared__ double red[256];
+  __shared__ int ch, lb;
+  if (threadIdx.x == 0) {
+    ch = a.blk_chain[blockIdx.x];
+    lb = blockIdx.x - a.blk_first[ch];
+  }
+  __syncthreads();
+  const ChainDesc &d = a.desc[ch];
+  const int N = d.N, M = d.M, dim = d.dim;
+  const double *x = a.dpool + d.x_off;
+  const int k = lb * blockDim.x + threadIdx.x;  // k = i*M + j
+  double rg[1] = {0.0};
+  if (k < N * M) {
+    const int i = k / M, j = k % M;
+    const size_t base = (size_t)a.bead_off[ch];
+    const int kp = j > 0 ? k - 1 : a.inv[a.inv_off[ch] + i] * M + (M - 1);
+    for (int q = 0; q < dim; ++q) {
+      const double g = a.gA[(base + k) * 2 + q] + a.gB[(base + kp) * 2 + q];
+      if (a.dSdr) a.dSdr[(size_t)d.host_off + (size_t)q * N * M + k] = g;
+      rg[0] += x[((size_t)j * N + i) * dim + q] * g;
+    }
+  }
+  block_sum_k<1>(rg, red);
+  if (threadIdx.x == 0) a.part[(size_t)blockIdx.x * 9 + 8] = rg[0];
+}
+
+// totals[c][9]: the partial rows of chain c's blocks summed
+__global__ void __launch_bounds__(256) k_adjoint_totals_b(AdjBatchArgs a) {
+  __shared__ double red[256];
+  const int ch = blockIdx.x;
+  const int b0 = a.blk_first[ch];
+  const int b1 = ch + 1 < a.nchains ? a.blk_first[ch + 1] : a.nblocks;
+  double t[8] = {0, 0, 0, 0, 0, 0, 0, 0}, r[1] = {0.0};
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    for (int q = 0; q < 8; ++q) t[q] += a.part[(size_t)b * 9 + q];
+    r[0] += a.part[(size_t)b * 9 + 8];
+  }
+  block_sum_k<8>(t, red);
+  block_sum_k<1>(r, red);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 8; ++q) a.totals[(size_t)ch * 9 + q] = t[q];
+    a.totals[(size_t)ch * 9 + 8] = r[0];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
 
@@ -831,27 +1145,29 @@ cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size
   else k_sweep<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
-// phase kernels: 0 staging, 1 swaps, 2 the rest
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int grid, int block, size_t smem,
-                               cudaStream_t s) {
+// phase kernels: 0 staging, 1 swaps, 2 the rest; warp = 1 (swaps only): one
+// warp per chain
+static const void *phase_kernel(int phase, int warp) {
+  if (phase == 1) return warp ? (const void *)k_sweep_swap_warp : (const void *)k_sweep_swap;
+  return phase == 0 ? (const void *)k_sweep_stage : (const void *)k_sweep_rest;
+}
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int grid, int block,
+                               size_t smem, cudaStream_t s) {
   if (phase == 0) k_sweep_stage<<<grid, block, smem, s>>>(a);
+  else if (phase == 1 && warp) k_sweep_swap_warp<<<grid, block, smem, s>>>(a);
   else if (phase == 1) k_sweep_swap<<<grid, block, smem, s>>>(a);
   else k_sweep_rest<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t sweep_phase_set_smem(int phase, size_t smem) {
-  const void *k = phase == 0 ? (const void *)k_sweep_stage
-                             : phase == 1 ? (const void *)k_sweep_swap : (const void *)k_sweep_rest;
-  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t sweep_phase_set_smem(int phase, int warp, size_t smem) {
+  return cudaFuncSetAttribute(phase_kernel(phase, warp), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
 }
 
-cudaError_t sweep_phase_occupancy(int phase, int block, size_t smem, int *blocks_per_sm) {
-  if (phase == 0)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_stage, block, smem);
-  if (phase == 1)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_swap, block, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_rest, block, smem);
+cudaError_t sweep_phase_occupancy(int phase, int warp, int block, size_t smem, int *blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, phase_kernel(phase, warp),
+                                                       block, smem);
 }
 
 cudaError_t sweep_set_smem(int mode, size_t smem) {
@@ -891,10 +1207,23 @@ cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *ds
   k_export<<<g, 256, 0, s>>>(desc, dpool, dst, chain0);
   return cudaGetLastError();
 }
+cudaError_t launch_transpose_tiles(bool import, const ChainDesc *desc, double *dpool,
+                                   double *host, const int *tile_off, int nchains, int ntiles,
+                                   int grid, cudaStream_t s) {
+  const int g = std::max(1, std::min(grid, ntiles));
+  if (import) k_transpose_tiles<true><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, nchains);
+  else k_transpose_tiles<false><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, nchains);
+  return cudaGetLastError();
+}
 cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0,
                               int nchains, int maxN, cudaStream_t s) {
   dim3 g((maxN + 127) / 128, nchains);
   k_init_world<<<g, 128, 0, s>>>(desc, dpool, ipool, chain0);
+  return cudaGetLastError();
+}
+cudaError_t launch_init_world_hard(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
+                                   int chain0, int nchains, cudaStream_t s) {
+  k_init_world_hard<<<nchains, 32, 0, s>>>(desc, var, dpool, ipool, chain0);
   return cudaGetLastError();
 }
 cudaError_t launch_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0, int nchains,
@@ -1057,22 +1386,91 @@ cudaError_t fp64_peak(int num_sms, cudaStream_t st, double *tflops) {
 // ---------------------------------------------------------------------------
 static __device__ __align__(256) double g_adj_static[kNoAllocDoubles];
 
-cudaError_t adjoint_static_scratch(double **ptr) {
-  constexpr int kMaxDevices = 64;
-  static double *addr[kMaxDevices] = {};
+// The array's device address, per device, in an atomic slot.  Handle
+// creation takes it (with the handle's device current: the set-up) and every
+// later creation on that device takes it again, so the slot always holds the
+// address in the device's current context: a cudaDeviceReset destroys the
+// handles made before it, and the first handle made after it refreshes the
+// slot before any call can use it.  Concurrent set-ups store the same value;
+// readers never see a half-written entry.
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<double *> g_adj_addr[kMaxDevices];
+}  // namespace
+
+cudaError_t adjoint_static_setup() {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  if (!addr[dev]) {
-    // set-up, once per device, with that device current
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_adj_static);
-    if (e != cudaSuccess) return e;
-    addr[dev] = static_cast<double *>(p);
-  }
-  *ptr = addr[dev];
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_adj_static);
+  if (e != cudaSuccess) return e;
+  g_adj_addr[dev].store(static_cast<double *>(p), std::memory_order_release);
   return cudaSuccess;
+}
+
+cudaError_t adjoint_static_scratch(double **ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  double *a = g_adj_addr[dev].load(std::memory_order_acquire);
+  if (!a) {
+    e = adjoint_static_setup();
+    if (e != cudaSuccess) return e;
+    a = g_adj_addr[dev].load(std::memory_order_acquire);
+  }
+  *ptr = a;
+  return cudaSuccess;
+}
+
+// the PIMC_PROFILE build's swap counters (g_prof): read, then cleared on
+// request; cudaErrorNotSupported in other builds
+cudaError_t profile_take(unsigned long long *out, bool reset, cudaStream_t s) {
+#if PIMC_PROFILE
+  cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_prof, sizeof(g_prof), 0, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && reset) {
+    static const unsigned long long z[32] = {};
+    e = cudaMemcpyToSymbolAsync(g_prof, z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return e;
+#else
+  (void)out;
+  (void)reset;
+  (void)s;
+  return cudaErrorNotSupported;
+#endif
+}
+
+// the PIMC_CHECK build's device check word: read and cleared (0 in the
+// default build, which has no bounds checks)
+cudaError_t check_word_take(cudaStream_t s, unsigned long long *w) {
+  *w = 0;
+#if PIMC_CHECK
+  cudaError_t e = cudaMemcpyFromSymbolAsync(w, g_check_word, sizeof(*w), 0, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && *w) {
+    const unsigned long long z = 0;
+    e = cudaMemcpyToSymbolAsync(g_check_word, &z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return e;
+#else
+  (void)s;
+  return cudaSuccess;
+#endif
+}
+
+cudaError_t launch_adjoint_batch(const AdjBatchArgs &a, int maxN, cudaStream_t s) {
+  dim3 gi((unsigned)std::max(1, (maxN + 255) / 256), (unsigned)a.nchains);
+  k_adjoint_inv_b<<<gi, 256, 0, s>>>(a);
+  k_adjoint_beads_b<<<a.nblocks, 256, 0, s>>>(a);
+  k_adjoint_finish_b<<<a.nblocks, 256, 0, s>>>(a);
+  k_adjoint_totals_b<<<a.nchains, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s) {

@@ -17,6 +17,7 @@ enum : int {
 };
 
 constexpr int MAX_BEAMS = 16;  // laser beams of an optical-lattice potential
+constexpr int kMaxParticles = 8192;  // particles per chain (pimc_params.N)
 
 // observables of one measurement (a row of the series): E_th, E_v, pair
 // energy, pair virial energy, squared winding W^2, signed area A_z, sum r^2/M,
@@ -118,7 +119,16 @@ struct ChainVar {
   double beads_kind[4];         // bead updates by move kind
 };
 
-// device error codes (ChainVar::err, first error wins)
-enum : int { DERR_NONE = 0, DERR_WINDOW = 1, DERR_STATE = 2, DERR_SCRATCH = 3 };
+// device error codes (ChainVar::err and, in PIMC_CHECK builds, the device
+// check word; first error wins).  DERR_STATE: next is not a permutation.  The
+// others are raised only by the bounds checks of a PIMC_CHECK build:
+// DERR_WINDOW a window or slice index out of range, DERR_SCRATCH a shared
+// scratch carve past the launch's dynamic shared memory, DERR_QUEUE a
+// neighbour-queue push past its capacity, DERR_INDEX a particle index out of
+// range.  DERR_INIT: init_world could not place the hard spheres.
+enum : int {
+  DERR_NONE = 0, DERR_WINDOW = 1, DERR_STATE = 2, DERR_SCRATCH = 3, DERR_QUEUE = 4, DERR_INDEX = 5,
+  DERR_INIT = 6
+};
 
 }  // namespace pimc

@@ -18,6 +18,14 @@ CSRC = os.path.join(DIST_DIR, "csrc")
 BUILD_DIR = os.path.join(DIST_DIR, "_build")
 LIB_DIR = os.path.join(DIST_DIR, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libpimc_gb300.so")
+# the bounds-checking build (nvcc -DPIMC_CHECK=1): every window/slice and
+# particle index, shared-scratch carve and neighbour-queue push is checked on
+# the device, and a miss is reported as PIMC_EDEVICE instead of being
+# performed.  load() picks it when the environment sets PIMC_CHECK=1.
+LIB_CHECK_PATH = os.path.join(LIB_DIR, "libpimc_gb300_check.so")
+# the profiling build (nvcc -DPIMC_PROFILE=1): per-section clock counters of
+# the permutation swap (pimc_swap_profile); picked when PIMC_PROFILE=1
+LIB_PROF_PATH = os.path.join(LIB_DIR, "libpimc_gb300_prof.so")
 INCLUDE = os.path.join(REPO_DIR, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -34,16 +42,22 @@ def _nvcc():
     return cand if os.path.exists(cand) else "nvcc"
 
 
-def build(verbose: bool = False) -> str:
-    """Compile csrc/*.cu for sm_103a into lib/libpimc_gb300.so (parallel TUs)."""
-    os.makedirs(BUILD_DIR, exist_ok=True)
+def build(verbose: bool = False, check: bool = False, profile: bool = False) -> str:
+    """Compile csrc/*.cu for sm_103a into lib/libpimc_gb300.so (parallel TUs);
+    check=True builds the bounds-checking variant lib/libpimc_gb300_check.so,
+    profile=True the swap-profiling variant lib/libpimc_gb300_prof.so."""
+    tag = "_check" if check else ("_prof" if profile else "")
+    bdir = BUILD_DIR + tag
+    out = LIB_CHECK_PATH if check else (LIB_PROF_PATH if profile else LIB_PATH)
+    os.makedirs(bdir, exist_ok=True)
     os.makedirs(LIB_DIR, exist_ok=True)
     nvcc = _nvcc()
     objs = []
+    extra = ["-DPIMC_CHECK=1"] if check else (["-DPIMC_PROFILE=1"] if profile else [])
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        obj = os.path.join(bdir, os.path.splitext(src)[0] + ".o")
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise PimcError(f"nvcc failed on {src}:\n{r.stderr}")
@@ -53,13 +67,18 @@ def build(verbose: bool = False) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    tmp = LIB_PATH + ".tmp"
+    tmp = out + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise PimcError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, out)
+    return out
+
+
+def check_build_requested() -> bool:
+    """PIMC_CHECK=1 in the environment selects the bounds-checking build"""
+    return os.environ.get("PIMC_CHECK", "0") == "1"
 
 
 # ------------------------------------------------------------------ structs
@@ -106,7 +125,8 @@ class Stats(C.Structure):
 class Launch(C.Structure):
     _fields_ = [("warp_per_chain", C.c_int), ("block", C.c_int),
                 ("sweeps_per_launch", C.c_int), ("state_smem_bytes", C.c_int),
-                ("split_phases", C.c_int), ("phase_block", C.c_int * 3)]
+                ("split_phases", C.c_int), ("phase_block", C.c_int * 3),
+                ("phase_warp", C.c_int * 3)]
 
 
 # every symbol include/pimc.h declares, with its argument types
@@ -162,6 +182,7 @@ SIGNATURES = {
     "pimc_reset_measurements": [_vp],
     "pimc_adjoint": [_vp, C.c_int, _dp, _dp, _dp],
     "pimc_adjoint_noalloc": [_vp, C.c_int, _dp, _dp, _dp],
+    "pimc_batch_adjoint": [_vp, _dp, _dp, _dp],
     "pimc_set_potential": [_vp, C.c_int, C.c_double, C.c_double, C.c_double],
     "pimc_get_stats": [_vp, C.c_int, C.POINTER(Stats)],
     "pimc_get_total_stats": [_vp, C.POINTER(Stats)],
@@ -175,6 +196,7 @@ SIGNATURES = {
     "pimc_clear_contact": [_vp, C.c_int],
     "pimc_fp64_peak": [_vp, _dp],
     "pimc_batch_phase_times": [_vp, C.c_longlong, _dp],
+    "pimc_swap_profile": [_vp, _ull, C.c_int],
     "pimc_last_run_ms": [_vp, _dp],
     "pimc_last_run_launches": [_vp, C.POINTER(C.c_longlong)],
     "pimc_set_option": [_vp, C.c_int, C.c_longlong],
@@ -185,11 +207,17 @@ SIGNATURES = {
 _lib = None
 
 
-def load(path: str = LIB_PATH):
-    """Load the built library (no fallback: a missing library raises)."""
+def load(path: str = None):
+    """Load the built library (no fallback: a missing library raises).  The
+    default is lib/libpimc_gb300.so, or the bounds-checking build when the
+    environment sets PIMC_CHECK=1."""
     global _lib
     if _lib is not None:
         return _lib
+    if path is None:
+        path = LIB_CHECK_PATH if check_build_requested() else LIB_PATH
+        if os.environ.get("PIMC_PROFILE", "0") == "1":
+            path = LIB_PROF_PATH
     if not os.path.exists(path):
         raise PimcError(f"engine library {path} is missing; run __graft_entry__.build()")
     L = C.CDLL(path)

@@ -251,9 +251,10 @@ class Engine:
 
     def set_launch(self, block: int, sweeps_per_launch: int = 1,
                    state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False,
-                   split_phases: int = 0, phase_block=(0, 0, 0)):
+                   split_phases: int = 0, phase_block=(0, 0, 0), phase_warp=(0, 0, 0)):
         l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes,
-                   int(split_phases), (C.c_int * 3)(*[int(b) for b in phase_block]))
+                   int(split_phases), (C.c_int * 3)(*[int(b) for b in phase_block]),
+                   (C.c_int * 3)(*[int(w) for w in phase_warp]))
         check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
 
     @property
@@ -263,7 +264,8 @@ class Engine:
         check(self.L.pimc_batch_get_launch(self.h, C.byref(l)))
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
-                "split_phases": l.split_phases, "phase_block": list(l.phase_block)}
+                "split_phases": l.split_phases, "phase_block": list(l.phase_block),
+                "phase_warp": list(l.phase_warp)}
 
     def phase_times(self, n_sweeps: int = 2):
         """device ms of the staging, swap and remaining phases over n sweeps,
@@ -402,6 +404,23 @@ class Engine:
         th, ex = np.zeros(3), np.zeros(4)
         check(self.L.pimc_adjoint(self.h, chain, _dp(g) if want_beads else None, _dp(th), _dp(ex)))
         return g, th, ex
+
+    def batch_adjoint(self, want_beads=False):
+        """the adjoint of every chain in one call (pimc_batch_adjoint):
+        dS/dtheta [chains][3], extra [chains][4] and, with want_beads, dS/dr
+        as a list of per-chain [dim][N][M] arrays"""
+        n = len(self.params)
+        th, ex = np.zeros((n, 3)), np.zeros((n, 4))
+        g = np.zeros(self.beads_all_size()) if want_beads else None
+        check(self.L.pimc_batch_adjoint(self.h, _dp(th), _dp(ex), _dp(g) if want_beads else None))
+        if not want_beads:
+            return None, th, ex
+        out, o = [], 0
+        for p in self.params:
+            k = p.dim * p.N * p.M
+            out.append(g[o:o + k].reshape(p.dim, p.N, p.M))
+            o += k
+        return out, th, ex
 
     # ------------------------------------------------------------- files
     def write_paths_csv(self, path: str, chain: int = 0):

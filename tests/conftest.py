@@ -27,8 +27,11 @@ def engine_lib():
     import pimc
     srcs = glob.glob(os.path.join(ROOT, "pimc.jl_gb300", "csrc", "*")) + \
         [os.path.join(ROOT, "include", "pimc.h")]
-    stale = not os.path.exists(pimc.LIB_PATH) or \
-        max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(pimc.LIB_PATH)
+    from pimc._native import LIB_CHECK_PATH, check_build_requested
+    check = check_build_requested()
+    path = LIB_CHECK_PATH if check else pimc.LIB_PATH
+    stale = not os.path.exists(path) or \
+        max(os.path.getmtime(s) for s in srcs) > os.path.getmtime(path)
     if stale:
-        pimc.build()
+        pimc.build(check=check)
     return pimc.load()

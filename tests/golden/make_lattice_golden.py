@@ -4,19 +4,24 @@ examples/tools/potentialtools.jl in oameye/PIMC.jl), read from that file, so
 that the engine's construction of them (directions of the integer points on
 the circles x^2 + y^2 = 25 and 65) is checked against the reference's numbers.
 
-Run from the repository root with the reference checked out at
-/root/reference: python tests/golden/make_lattice_golden.py
+Run with the path of a checkout of the reference project:
+
+    python tests/golden/make_lattice_golden.py <reference checkout>
 """
+import argparse
 import json
 import os
 import re
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = "/root/reference/examples/tools/potentialtools.jl"
+REL = os.path.join("examples", "tools", "potentialtools.jl")
 
 
 def main():
-    text = open(SRC).read()
+    ap = argparse.ArgumentParser()
+    ap.add_argument("reference", help="root of a checkout of oameye/PIMC.jl")
+    args = ap.parse_args()
+    text = open(os.path.join(args.reference, REL)).read()
     out = {"generator": "tests/golden/make_lattice_golden.py",
            "source": "examples/tools/potentialtools.jl (top-level l25 and l65)"}
     for name in ("l25", "l65"):

@@ -356,3 +356,22 @@ def test_oracle_virial_matches_thermodynamic_with_the_lattice(oracle_mod):
     eth, s1 = blocking(r["energies"][:, 0])
     ev, s2 = blocking(r["energies"][:, 1])
     assert abs(eth - ev) < 3 * math.hypot(s1, s2), (eth, s1, ev, s2)
+
+
+def test_oracle_init_world_hard_core(oracle_mod):
+    """init_world's hard-core redraw (src/system.jl:44-64) in the oracle: no
+    two beads of a slice closer than a, and ORC_ESTATE when the spheres do
+    not fit"""
+    O = oracle_mod
+    o = O.Oracle(O.make_params(dim=2, N=20, M=8, L=3.0, T=1.0, lam=0.5, hardcore_a=0.5,
+                               interactions=True, r_a=1.0))
+    assert o.init_world(seed=3) == 0
+    x, _, nxt = o.get_state()
+    d = np.abs(x[:, :, None, :] - x[:, None, :, :])
+    d = np.minimum(d, 6.0 - d)
+    r = np.sqrt((d ** 2).sum(axis=0))
+    r[np.arange(20), np.arange(20), :] = np.inf
+    assert r.min() >= 0.5 and (nxt == np.arange(20)).all()
+    o2 = O.Oracle(O.make_params(dim=2, N=40, M=8, L=1.0, T=1.0, lam=0.5, hardcore_a=0.5,
+                                interactions=True, r_a=0.6))
+    assert o2.init_world(seed=3) == -3
