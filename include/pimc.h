@@ -368,6 +368,9 @@ int pimc_batch_phase_times(void *handle, long long n_sweeps, double ms[3]);
 /* device time of the last run call or pimc_batch_adjoint (CUDA events on
  * the handle's stream) */
 int pimc_last_run_ms(void *handle, double *ms);
+/* the handle's device: its name (NUL-terminated, at most cap bytes) and SM
+ * count; no reference counterpart (keys the tuner's cache of launch shapes) */
+int pimc_device_info(void *handle, char *name, size_t cap, int *num_sms);
 /* diagnostics, no reference counterpart: in the profiling build (nvcc
  * -DPIMC_PROFILE=1) the permutation swap adds the clock cycles of its
  * sections (0 heat-bath exponents, 1 partner search, 2 physical ratio, 3

@@ -124,6 +124,10 @@ def lib():
         L.orc_run.argtypes = [C.c_void_p, C.c_long, C.POINTER(Update), C.c_int, C.POINTER(Rng),
                               C.c_int, dp, C.c_long, C.POINTER(C.c_long), C.c_int, dp,
                               C.POINTER(C.c_long), C.POINTER(RunStats)]
+        L.orc_run_sweeps.argtypes = [C.c_void_p, C.c_long, C.c_int, C.c_int, dp, C.c_double,
+                                     C.c_double, C.c_double, C.c_double, C.POINTER(Rng), C.c_int,
+                                     dp, C.c_long, C.POINTER(C.c_long), C.c_int, dp,
+                                     C.POINTER(C.c_long), C.POINTER(RunStats)]
         L.orc_bench_budget.restype = C.c_double
         L.orc_bench_budget.argtypes = [C.POINTER(Params), C.POINTER(C.c_int), C.c_int, C.c_int,
                                        C.c_double, C.c_double, C.c_uint64, dp, dp]
@@ -333,6 +337,27 @@ class Oracle:
         for i in range(len(updates)):
             self.L.orc_update_free(C.byref(ups[i]))
         return out
+
+
+def run_sweeps(o: Oracle, nsweeps, ell, swaps, com, seed=7, stream=0, measure_every=0, e_cap=0,
+               dens_nb=0):
+    """nsweeps sweeps in the engine's schedule (orc_run_sweeps); com =
+    [step, min, max, minacc, maxacc], its step updated in place"""
+    r = Rng()
+    o.L.orc_rng_init(C.byref(r), seed, stream)
+    step = np.array([float(com[0])])
+    e = np.zeros(max(e_cap, 1) * 4)
+    ec = C.c_long(0)
+    hist = np.zeros(dens_nb ** o.p.dim) if dens_nb else None
+    nd = C.c_long(0)
+    st = RunStats()
+    rc = o.L.orc_run_sweeps(o.h, nsweeps, ell, swaps, _dp(step), com[1], com[2], com[3], com[4],
+                            C.byref(r), measure_every, _dp(e), e_cap, C.byref(ec), dens_nb,
+                            None if hist is None else _dp(hist), C.byref(nd), C.byref(st))
+    com[0] = float(step[0])
+    return {"rc": rc, "energies": e[: ec.value * 4].reshape(-1, 4), "hist": hist,
+            "ndata": nd.value, "attempts": list(st.attempts), "accepts": list(st.accepts),
+            "bead_updates": st.bead_updates}
 
 
 def distance(a, b, L):

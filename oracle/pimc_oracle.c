@@ -1355,3 +1355,83 @@ double orc_bench_budget(const orc_params *ps, const int *ells, int nchains, int 
   if (sweeps) *sweeps = sw;
   return wall;
 }
+
+/* ------------------------------------------------------------------------ */
+/* the engine's sweep schedule with the reference's moves                     */
+/* ------------------------------------------------------------------------ */
+int orc_run_sweeps(orc_state *st, long nsweeps, int ell, int swaps, double *com_step,
+                   double com_min, double com_max, double com_minacc, double com_maxacc,
+                   orc_rng *rng, int measure_every, double *e_out, long e_cap, long *e_count,
+                   int dens_nb, double *hist, long *ndata, orc_run_stats *stats) {
+  const orc_params *p = &st->p;
+  const int N = p->N, M = p->M;
+  orc_draws dr; memset(&dr, 0, sizeof(dr)); dr.rng = rng;
+  int l = ell;
+  if (l > M - 1) l = M - 1;
+  if (l > 64) l = 64;
+  if (l < 2) l = 2;
+  const int k = (M + l - 1) / l;
+  for (long sw = 0; sw < nsweeps; ++sw) {
+    /* staging phase */
+    const int o = (int)fmin((double)(M - 1), floor(orc_rng_uniform(rng) * M));
+    for (int s = 0; s < k; ++s) {
+      const int len = s < k - 1 ? l : M - (k - 1) * l;
+      if (len < 2) continue;
+      const int j0 = (o + s * l) % M;
+      for (int n = 0; n < N; ++n) {
+        int m = 2 + (int)floor(orc_rng_uniform(rng) * (l - 1));
+        if (m > len) m = len;
+        const int rc = orc_staging(st, n, j0, m, &dr, NULL);
+        if (rc < 0) return rc;
+        if (stats) {
+          stats->attempts[0]++; stats->accepts[0] += rc == ORC_ACCEPT;
+          if (rc != ORC_HARDCORE) stats->bead_updates += m - 1;
+        }
+      }
+    }
+    /* swaps */
+    if (N > 1)
+      for (int a = 0; a < swaps; ++a) {
+        const int j0 = (int)fmin((double)(M - 1), floor(orc_rng_uniform(rng) * M));
+        int m = 2 + (int)floor(orc_rng_uniform(rng) * (l - 1));
+        if (m > l) m = l;
+        const int n1 = (int)fmin((double)(N - 1), floor(orc_rng_uniform(rng) * N));
+        const double up = orc_rng_uniform(rng);
+        const int rc = orc_swap(st, j0, m, n1, up, &dr, NULL, NULL);
+        if (rc < 0) return rc;
+        if (stats && rc != ORC_SKIP) {
+          stats->attempts[1]++; stats->accepts[1] += rc == ORC_ACCEPT;
+          if (rc != ORC_HARDCORE) stats->bead_updates += 2.0 * (m - 1);
+        }
+      }
+    /* centre of mass: one attempt per single path */
+    long catt = 0, cacc = 0;
+    for (int n = 0; n < N; ++n) {
+      if (st->next[n] != n) continue;
+      const int rc = orc_com(st, n, *com_step, &dr);
+      if (rc < 0) return rc;
+      ++catt; cacc += rc == ORC_ACCEPT;
+      if (stats) {
+        stats->attempts[2]++; stats->accepts[2] += rc == ORC_ACCEPT;
+        if (rc != ORC_HARDCORE) stats->bead_updates += M;
+      }
+    }
+    if (catt > 0) {
+      const double r = (double)cacc / (double)catt;
+      if (r < com_minacc) *com_step *= 0.9;
+      else if (r > com_maxacc) *com_step *= 1.1;
+      if (*com_step < com_min) *com_step = com_min;
+      if (*com_step > com_max) *com_step = com_max;
+    }
+    if (measure_every > 0 && (sw + 1) % measure_every == 0) {
+      if (e_out && e_count && *e_count < e_cap) {
+        double e[4]; orc_energy(st, e);
+        for (int q = 0; q < 4; ++q) e_out[*e_count * 4 + q] = e[q];
+        (*e_count)++;
+      }
+      if (hist) { orc_density(st, dens_nb, hist); if (ndata) *ndata += M; }
+      if (stats) stats->measurements++;
+    }
+  }
+  return dr.exhausted ? ORC_EDRAWS : 0;
+}

@@ -196,6 +196,26 @@ double orc_bench_chains(const orc_params *p, int nchains, int nthreads,
                         long attempts, int ell, double com_step, uint64_t seed,
                         double *bead_updates);
 
+/* sweeps in the engine's schedule (pimc_run / pimc_batch_run), with the
+ * reference's moves: per sweep one staging phase -- a random offset o, the
+ * imaginary-time circle cut into k = ceil(M/ell) slots starting at o + s ell,
+ * one window per (slot, particle) of m = min(slot length, 2 + floor(u (ell -
+ * 1))) slices from the slot's start (ReshapeLinear) -- then `swaps` swap
+ * attempts (ReshapeSwapLinear: j0, m, n1 and the partner uniform drawn per
+ * attempt), then one SingleCenterOfMass attempt per particle with next == n
+ * in particle order; the centre-of-mass step adapts once per sweep on that
+ * sweep's acceptance (x0.9 below com_minacc, x1.1 above com_maxacc, clamped
+ * to [com_min, com_max]).  Measurements (Energy, and Density when dens_nb >
+ * 0) at the end of every measure_every-th sweep.  The reference's run!
+ * interleaves the same moves at random instead; under the reference's
+ * acceptance rules, which are not reversible, the two schedules sample
+ * different distributions, so the engine's implementation of those rules is
+ * checked against this schedule.  Returns 0 or a negative ORC_* code. */
+int orc_run_sweeps(orc_state *st, long nsweeps, int ell, int swaps, double *com_step,
+                   double com_min, double com_max, double com_minacc, double com_maxacc,
+                   orc_rng *rng, int measure_every, double *e_out, long e_cap, long *e_count,
+                   int dens_nb, double *hist, long *ndata, orc_run_stats *stats);
+
 /* time-budgeted timing of a list of chains (parameters ps[c], staging and
  * swap window ells[c]) on nthreads host threads: the chains are dealt to the
  * threads longest first (cost N M (4 with the pair interaction) + N^2 / 2,

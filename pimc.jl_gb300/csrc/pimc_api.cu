@@ -1728,8 +1728,19 @@ static int batch_adjoint_setup(Handle *h) {
   }
   const size_t nblocks = blk_chain.size();
   if (nblocks > (size_t)0x7fffffff) return fail(PIMC_EARG, "batch too large for the adjoint");
-  const size_t nd = 4 * (size_t)tb + 9 * nblocks + 9 * (size_t)nc + h->n_stage + (size_t)nc;
-  const size_t ni = nblocks + 2 * (size_t)nc + (size_t)ninv;
+  // one CTA per chain slice when every chain's accumulators (32 N bytes, and
+  // 12 KB for the kernel's static reduction buffer, queues and descriptor)
+  // fit the device's shared memory
+  std::vector<int> slice_first(nc);
+  long long ns = 0;
+  for (int c = 0; c < nc; ++c) {
+    slice_first[c] = (int)ns;
+    ns += h->desc[c].M;
+  }
+  const bool slices = 32LL * h->maxN + 12288 <= (long long)h->max_dyn_smem && ns < 0x7fffffffLL;
+  const size_t nd = 4 * (size_t)tb + 9 * nblocks + 9 * (size_t)nc + h->n_stage + (size_t)nc +
+                    8 * (size_t)ns;
+  const size_t ni = nblocks + 3 * (size_t)nc + (size_t)ninv;
   const size_t bytes = 8 * nd + 4 * ((ni + 1) & ~(size_t)1) + 8 * (size_t)nc;
   double *pool = nullptr;
   if (cudaMalloc(&pool, bytes) != cudaSuccess)
@@ -1744,8 +1755,9 @@ static int batch_adjoint_setup(Handle *h) {
   a.totals = a.part + 9 * nblocks;
   a.dSdr = a.totals + 9 * (size_t)nc;
   double *om = a.dSdr + h->n_stage;
-  int *ip = (int *)(om + nc);
-  int *bc = ip, *bf = bc + nblocks, *io = bf + nc, *inv = io + nc;
+  a.part_s = om + nc;
+  int *ip = (int *)(a.part_s + 8 * (size_t)ns);
+  int *bc = ip, *bf = bc + nblocks, *io = bf + nc, *sf = io + nc, *inv = sf + nc;
   long long *bo = (long long *)(ip + ((ni + 1) & ~(size_t)1));
   a.omega = om;
   a.blk_chain = bc;
@@ -1755,11 +1767,15 @@ static int batch_adjoint_setup(Handle *h) {
   a.bead_off = bo;
   a.nblocks = (int)nblocks;
   a.nchains = nc;
+  a.use_slices = slices ? 1 : 0;
+  a.nslices = (int)ns;
+  a.slice_first = sf;
   h->d_badj = pool;
   CK(cudaMemcpyAsync(om, omega.data(), 8 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(bc, blk_chain.data(), 4 * nblocks, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(bf, blk_first.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(io, inv_off.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(sf, slice_first.data(), 4 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(bo, bead_off.data(), 8 * (size_t)nc, cudaMemcpyHostToDevice, h->stream));
   int rc = sync_check(h);
   if (rc) return rc;
@@ -2149,6 +2165,19 @@ int pimc_set_state(void *handle, const void *buf, size_t bytes) {
   Handle *h = H(handle);
   if (!h) return fail(PIMC_EARG, "null handle");
   return state_io(h, (char *)const_cast<void *>(buf), bytes, false);
+}
+
+int pimc_device_info(void *handle, char *name, size_t cap, int *num_sms) {
+  Handle *h = H(handle);
+  if (!h) return fail(PIMC_EARG, "null handle");
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, h->device));
+  if (name && cap > 0) {
+    strncpy(name, prop.name, cap - 1);
+    name[cap - 1] = '\0';
+  }
+  if (num_sms) *num_sms = h->num_sms;
+  return PIMC_OK;
 }
 
 int pimc_swap_profile(void *handle, unsigned long long *out, int reset) {

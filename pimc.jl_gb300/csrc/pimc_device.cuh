@@ -728,22 +728,41 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
     const unsigned co = s.curq(0, t), cn = s.curq(1, t);
     const unsigned no = s.nxtq(0, t), nn = s.nxtq(1, t);
     const unsigned *row = c.xq + (size_t)j * c.ldn, *rown = c.xq + (size_t)jn * c.ldn;
-    for (int b = lane; b < N; b += 32) {
-      const unsigned pb = row[b];
+    // one candidate b: its mirror words at slices j (pb) and j+1 (pbn)
+    auto cand = [&](int b, unsigned pb, unsigned pbn) {
       const unsigned d2o = qdist2(co, pb), d2n = qdist2(cn, pb);
       const bool io = d2o <= d.q_lim_hi && !s.skip(0, t, b);
       const bool in = d2n <= d.q_lim_hi && !s.skip(1, t, b);
-      if (io || in) {
-        const unsigned pbn = rown[wrap ? c.next[b] : b];
-        bool edge;
-        if (io) {
-          const unsigned d2b = qdist2_w(no, pbn, edge);
-          est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
-        }
-        if (in) {
-          const unsigned d2b = qdist2_w(nn, pbn, edge);
-          est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
-        }
+      bool edge;
+      if (io) {
+        const unsigned d2b = qdist2_w(no, pbn, edge);
+        est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
+      }
+      if (in) {
+        const unsigned d2b = qdist2_w(nn, pbn, edge);
+        est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
+      }
+    };
+    if (!wrap) {
+      // the words at both slices are read together, two blocks of 32
+      // candidates at a time, so that one round trip to memory serves four
+      // loads (the latency, not the bytes, bounds this scan); the lane's
+      // candidates are visited in the same order as one block at a time
+      for (int b0 = lane; b0 < N; b0 += 64) {
+        const int b1 = b0 + 32;
+        const unsigned pa0 = row[b0], pn0 = rown[b0];
+        const unsigned pa1 = b1 < N ? row[b1] : 0u, pn1 = b1 < N ? rown[b1] : 0u;
+        cand(b0, pa0, pn0);
+        if (b1 < N) cand(b1, pa1, pn1);
+      }
+    } else {
+      // past slice M the partner's next bead belongs to next[b]
+      for (int b = lane; b < N; b += 32) {
+        const unsigned pb = row[b];
+        const unsigned d2o = qdist2(co, pb), d2n = qdist2(cn, pb);
+        const bool io = d2o <= d.q_lim_hi && !s.skip(0, t, b);
+        const bool in = d2n <= d.q_lim_hi && !s.skip(1, t, b);
+        if (io || in) cand(b, pb, rown[c.next[b]]);
       }
     }
     if (stop(e)) return true;
@@ -842,6 +861,14 @@ __device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, 
     if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;
   }
   return hit;
+}
+
+// ---------------------------------------------------------------------------
+// an L1 prefetch of a chain word in global memory (a no-op for chains staged
+// in shared memory)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  if (__isGlobal(p)) asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
 // ---------------------------------------------------------------------------

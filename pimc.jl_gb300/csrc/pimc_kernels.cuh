@@ -324,10 +324,42 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   const int chunk = (N + 31) / 32;
   const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
   W wm[1] = {W(-INFINITY)};
-  for (int i = tid; i < N; i += nt) {
-    const W v = hb.expo(i, A, E1);
-    Sw[i] = v;
-    wm[0] = v > wm[0] ? v : wm[0];
+  if (FAST) {
+    // four candidates per thread at a time: their next[] and mirror words are
+    // loaded before any is used, one round trip for four (the same
+    // arithmetic as HeatBath::expo, in the same order)
+    constexpr int U = 4;
+    for (int i0 = tid; i0 < N; i0 += U * nt) {
+      int ie[U];
+      unsigned qa[U], qe[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * nt;
+        ie[u] = i < N ? (wrap ? c.next[i] : i) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * nt;
+        qa[u] = i < N ? c.Q(i, j0) : 0u;
+        qe[u] = i < N ? c.Q(ie[u], se) : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * nt;
+        if (i < N) {
+          const float s2 = (float)qdist2(A.q, qe[u]) + (float)qdist2(qa[u], E1.q);
+          const W v = (W)(-s2 * hb.inv_denf);
+          Sw[i] = v;
+          wm[0] = v > wm[0] ? v : wm[0];
+        }
+      }
+    }
+  } else {
+    for (int i = tid; i < N; i += nt) {
+      const W v = hb.expo(i, A, E1);
+      Sw[i] = v;
+      wm[0] = v > wm[0] ? v : wm[0];
+    }
   }
   G::template max<1>(wm, red);
   G::sync();
@@ -377,6 +409,30 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     PROF_COUNT(1);
     return RES_SKIP;
   }
+  // the partner is known: start the reads the rest of the attempt waits on
+  const int nx1 = c.next[n1], nx2 = c.next[n2];
+  auto own1 = [&](int t) { return (j0 + t < M) ? n1 : nx1; };
+  auto own2 = [&](int t) { return (j0 + t < M) ? n2 : nx2; };
+  auto slc = [&](int t) { return (j0 + t < M) ? j0 + t : j0 + t - M; };
+  if (FAST && j0 + m < M - 1) {
+    // an accepted swap exchanges the tails past slice se (most decided
+    // swaps under the reference's rules accept): bring those rows into L1
+    // while the bridges are built
+    for (int j = se + 1 + tid; j < M; j += nt) {
+      prefetch_l1(&c.X(0, n1, j));
+      prefetch_l1(&c.X(0, n2, j));
+      prefetch_l1(&c.V[(size_t)j * c.ldn + n1]);
+      prefetch_l1(&c.V[(size_t)j * c.ldn + n2]);
+      prefetch_l1(&c.xq[(size_t)j * c.ldn + n1]);
+      prefetch_l1(&c.xq[(size_t)j * c.ldn + n2]);
+    }
+  }
+  // the old paths' cached links (w_initial below), read now
+  double vold = 0.0;
+  for (int k = tid; k < 2 * m; k += nt) {
+    const int b = k / m, t = k % m;
+    vold += c.Vl(b == 0 ? own1(t) : own2(t), slc(t));
+  }
 
   double log_ratio = 0.0;
   if (d.flags & PF_PHYS) {
@@ -415,10 +471,6 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
 
   PROF_MARK(2);
   // two bridges with exchanged ends
-  const int nx1 = c.next[n1], nx2 = c.next[n2];
-  auto own1 = [&](int t) { return (j0 + t < M) ? n1 : nx1; };
-  auto own2 = [&](int t) { return (j0 + t < M) ? n2 : nx2; };
-  auto slc = [&](int t) { return (j0 + t < M) ? j0 + t : j0 + t - M; };
   const double s1x = ax, s1y = ay, s2x = c.X(0, n2, j0), s2y = c.Xd(1, n2, j0);
   const int e2p = hb.endp(n2);
   double f1x = c.X(0, e2p, se), f1y = c.Xd(1, e2p, se);  // r1 ends at E(n2)
@@ -509,11 +561,9 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   G::sync();
   PROF_MARK(4);
   const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
-  double w2[2] = {0.0, 0.0};  // w_initial, w_update
+  double w2[2] = {vold, 0.0};  // w_initial, w_update
   for (int k = tid; k < 2 * m; k += nt) {
     const int b = k / m, t = k % m;
-    const int j = slc(t), o = b == 0 ? own1(t) : own2(t);
-    w2[0] += c.Vl(o, j);
     w2[1] += mhtau * ((b == 0 ? S.vb1 : S.vb2)[t] + (b == 0 ? S.vb1 : S.vb2)[t + 1]);
   }
   // Under the reference's rules every pair term (-tau/2 g (..) <= 0 for

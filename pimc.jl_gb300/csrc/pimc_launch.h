@@ -87,6 +87,11 @@ struct AdjBatchArgs {
   double *totals;             // [nchains][9]: S_ext, dV0, domega, S_pair, dg, pair
                               // virial, r.g_ext, 0, r.dS/dr
   int nblocks, nchains;
+  // the slice kernel (one CTA per chain slice, 32 maxN bytes of shared
+  // memory): used when use_slices != 0
+  int use_slices, nslices;
+  const int *slice_first;     // [nchains] first slice CTA of each chain
+  double *part_s;             // [nslices][8]
 };
 
 // mode 0: one CTA per chain (k_sweep); mode 1: one warp per chain (k_sweep_warp)

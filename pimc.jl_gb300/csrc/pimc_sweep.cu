@@ -1075,6 +1075,134 @@ __global__ void __launch_bounds__(256) k_adjoint_beads_b(AdjBatchArgs a) {
     for (int q = 0; q < 8; ++q) a.part[(size_t)blockIdx.x * 9 + q] = v[q];
 }
 
+// the pair terms and the external potential of one slice of one chain per
+// CTA (blocks slice_first[c] .. slice_first[c] + M - 1 are chain c's slices):
+// warps take particles i, lanes scan the higher-numbered partners b of the
+// slice through the mirror prefilter and queue the survivors, and every
+// queued pair is evaluated once in FP64, 32 at a time on full warps; its
+// force goes to both particles through accumulators in shared memory
+// (4 doubles per particle: the bead's gradient from the link it starts, and
+// the gradient of its next bead from the same link).  Needs 32 N bytes of
+// dynamic shared memory.  The accumulators add the pair forces in the order
+// the atomics land, so results repeat to rounding, not bit for bit.  Partial
+// sums to part_s[cta][8] as k_adjoint_beads.
+__global__ void __launch_bounds__(256) k_adjoint_slice_b(AdjBatchArgs a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ double red[256];
+  __shared__ ChainDesc d;
+  __shared__ int ch, j;
+  __shared__ unsigned long long qbuf[8 * PQ_CAP];
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = a.nchains;  // slice_first[lo] <= blockIdx.x < slice_first[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (a.slice_first[mid] <= (int)blockIdx.x) lo = mid; else hi = mid;
+    }
+    ch = lo;
+    j = blockIdx.x - a.slice_first[lo];
+    d = a.desc[lo];
+  }
+  __syncthreads();
+  CV c = make_cv(&d, a.dpool, a.ipool, nullptr);
+  const int N = c.N, M = c.M, dim = c.dim, jn = j + 1 == M ? 0 : j + 1;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = nt >> 5;
+  double *acc = reinterpret_cast<double *>(dsm);  // [4][N]: ga.x, ga.y, gb.x, gb.y
+  for (int e = tid; e < 4 * N; e += nt) acc[e] = 0.0;
+  __syncthreads();
+  const double tau = d.tau;
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (d.flags & PF_PAIR) {
+    const double cg = d.inv2s2, h = 0.5 * tau, rc2 = d.rc * d.rc;
+    unsigned long long *q = qbuf + (size_t)warp * PQ_CAP;
+    const unsigned lt = (1u << lane) - 1u;
+    const unsigned *row = c.xq + (size_t)j * c.ldn;
+    int qn = 0;
+    auto flush = [&]() {
+      const int k = qn < 32 ? qn : 32;
+      if (lane < k) {
+        const unsigned long long e = q[lane];
+        const int i = (int)(e >> 32), b = (int)(e & 0xffffffffu);
+        const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+        const double bx = c.X(0, b, j), by = c.Xd(1, b, j);
+        const double r2a = mi2(d, ax, ay, bx, by);
+        if (r2a <= rc2) {
+          const int in = j == M - 1 ? c.next[i] : i, bn = j == M - 1 ? c.next[b] : b;
+          const double anx = c.X(0, in, jn), any = c.Xd(1, in, jn);
+          const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
+          const double d1x = mi_signed(ax, bx, d.L), d1y = dim > 1 ? mi_signed(ay, by, d.L) : 0.0;
+          const double d2x = mi_signed(anx, bnx, d.L), d2y = dim > 1 ? mi_signed(any, bny, d.L) : 0.0;
+          const double r2b = mi2(d, anx, any, bnx, bny);
+          const double e1 = exp_neg(-r2a * cg), e2 = exp_neg(-r2b * cg);
+          const double v1 = d.g * e1, v2 = d.g * e2;
+          const double f1 = h * (-2.0 * cg * v1), f2 = h * (-2.0 * cg * v2);
+          atomicAdd(&acc[i], f1 * d1x);
+          atomicAdd(&acc[b], -f1 * d1x);
+          atomicAdd(&acc[2 * N + i], f2 * d2x);
+          atomicAdd(&acc[2 * N + b], -f2 * d2x);
+          if (dim > 1) {
+            atomicAdd(&acc[N + i], f1 * d1y);
+            atomicAdd(&acc[N + b], -f1 * d1y);
+            atomicAdd(&acc[3 * N + i], f2 * d2y);
+            atomicAdd(&acc[3 * N + b], -f2 * d2y);
+          }
+          v[3] += h * (v1 + v2);
+          v[4] += h * (e1 + e2);
+          v[5] += h * (-2.0 * cg) * (r2a * v1 + r2b * v2);
+        }
+      }
+      __syncwarp();
+      unsigned long long rest[2];
+      const int nr = qn - k;
+      for (int r = 0; r < 2; ++r) rest[r] = (lane + 32 * r < nr) ? q[32 + lane + 32 * r] : 0ull;
+      __syncwarp();
+      for (int r = 0; r < 2; ++r)
+        if (lane + 32 * r < nr) q[lane + 32 * r] = rest[r];
+      __syncwarp();
+      qn = nr;
+    };
+    for (int i = warp; i < N; i += nwarps) {
+      Prefilter f;
+      f.init_q(row[i], d.q_lim_rc);
+      for (int b0 = i + 1; b0 < N; b0 += 32) {
+        const int b = b0 + lane;
+        const bool p = b < N && f.pass(row[b]);
+        const unsigned mk = __ballot_sync(0xffffffffu, p);
+        if (p) q[qn + __popc(mk & lt)] = ((unsigned long long)(unsigned)i << 32) | (unsigned)b;
+        qn += __popc(mk);
+        __syncwarp();
+        if (qn >= 32) flush();
+      }
+    }
+    while (qn > 0) flush();
+  }
+  __syncthreads();
+  // the external potential per bead, and the per-bead buffers in the
+  // chain's [i][j] order (k2 = i M + j)
+  for (int i = tid; i < N; i += nt) {
+    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
+    double ge[2];
+    grad_vext(d, ax, ay, ge[0], ge[1]);
+    ge[0] *= tau;
+    ge[1] *= tau;
+    v[0] += tau * vext(d, ax, ay);
+    if (d.flags & PF_LATT) {
+      const double sx = sinpi(ax * d.lat_k), sy = dim > 1 ? sinpi(ay * d.lat_k) : 0.0;
+      v[1] += tau * (sx * sx + sy * sy);
+    }
+    if (d.flags & PF_HARM) v[2] += tau * a.omega[ch] * (ax * ax + ay * ay);
+    v[6] += ax * ge[0] + ay * ge[1];
+    const size_t k2 = (size_t)a.bead_off[ch] + (size_t)i * M + j;
+    a.gA[k2 * 2] = ge[0] + acc[i];
+    a.gA[k2 * 2 + 1] = ge[1] + acc[N + i];
+    a.gB[k2 * 2] = acc[2 * N + i];
+    a.gB[k2 * 2 + 1] = acc[3 * N + i];
+  }
+  block_sum_k<8>(v, red);
+  if (tid == 0)
+    for (int q = 0; q < 8; ++q) a.part_s[(size_t)blockIdx.x * 8 + q] = v[q];
+}
+
 // per bead the full gradient gA[k] + gB[prev(k)]: dS/dr (host layout
 // x[d][n][j] of the chain at desc.host_off, when requested) and r . dS/dr
 __global__ void __launch_bounds__(256) k_adjoint_finish_b(AdjBatchArgs a) {
@@ -1104,7 +1232,8 @@ __global__ void __launch_bounds__(256) k_adjoint_finish_b(AdjBatchArgs a) {
   if (threadIdx.x == 0) a.part[(size_t)blockIdx.x * 9 + 8] = rg[0];
 }
 
-// totals[c][9]: the partial rows of chain c's blocks summed
+// totals[c][9]: the partial rows of chain c's blocks summed (its slice CTAs'
+// rows when the slice kernel ran)
 __global__ void __launch_bounds__(256) k_adjoint_totals_b(AdjBatchArgs a) {
   __shared__ double red[256];
   const int ch = blockIdx.x;
@@ -1112,8 +1241,14 @@ __global__ void __launch_bounds__(256) k_adjoint_totals_b(AdjBatchArgs a) {
   const int b1 = ch + 1 < a.nchains ? a.blk_first[ch + 1] : a.nblocks;
   double t[8] = {0, 0, 0, 0, 0, 0, 0, 0}, r[1] = {0.0};
   for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
-    for (int q = 0; q < 8; ++q) t[q] += a.part[(size_t)b * 9 + q];
+    if (!a.use_slices)
+      for (int q = 0; q < 8; ++q) t[q] += a.part[(size_t)b * 9 + q];
     r[0] += a.part[(size_t)b * 9 + 8];
+  }
+  if (a.use_slices) {
+    const int s0 = a.slice_first[ch], s1 = s0 + a.desc[ch].M;
+    for (int b = s0 + threadIdx.x; b < s1; b += blockDim.x)
+      for (int q = 0; q < 8; ++q) t[q] += a.part_s[(size_t)b * 8 + q];
   }
   block_sum_k<8>(t, red);
   block_sum_k<1>(r, red);
@@ -1467,7 +1602,14 @@ cudaError_t check_word_take(cudaStream_t s, unsigned long long *w) {
 cudaError_t launch_adjoint_batch(const AdjBatchArgs &a, int maxN, cudaStream_t s) {
   dim3 gi((unsigned)std::max(1, (maxN + 255) / 256), (unsigned)a.nchains);
   k_adjoint_inv_b<<<gi, 256, 0, s>>>(a);
-  k_adjoint_beads_b<<<a.nblocks, 256, 0, s>>>(a);
+  if (a.use_slices) {
+    const size_t sm = 32 * (size_t)maxN;
+    cudaError_t e = cudaFuncSetAttribute(k_adjoint_slice_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    k_adjoint_slice_b<<<a.nslices, 256, sm, s>>>(a);
+  } else {
+    k_adjoint_beads_b<<<a.nblocks, 256, 0, s>>>(a);
+  }
   k_adjoint_finish_b<<<a.nblocks, 256, 0, s>>>(a);
   k_adjoint_totals_b<<<a.nchains, 256, 0, s>>>(a);
   return cudaGetLastError();

@@ -197,6 +197,7 @@ SIGNATURES = {
     "pimc_fp64_peak": [_vp, _dp],
     "pimc_batch_phase_times": [_vp, C.c_longlong, _dp],
     "pimc_swap_profile": [_vp, _ull, C.c_int],
+    "pimc_device_info": [_vp, C.c_char_p, C.c_size_t, _ip],
     "pimc_last_run_ms": [_vp, _dp],
     "pimc_last_run_launches": [_vp, C.POINTER(C.c_longlong)],
     "pimc_set_option": [_vp, C.c_int, C.c_longlong],

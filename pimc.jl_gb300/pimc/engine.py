@@ -243,10 +243,33 @@ class Engine:
     def run_plain(self, n_sweeps: int):
         check(self.L.pimc_batch_run_plain(self.h, int(n_sweeps)))
 
-    def tune(self, sweeps_per_trial: int = 2) -> dict:
-        """time the candidate launch shapes and keep the fastest (chains restored)"""
+    def device_name(self) -> str:
+        buf = C.create_string_buffer(256)
+        sms = C.c_int()
+        check(self.L.pimc_device_info(self.h, buf, 256, C.byref(sms)))
+        return buf.value.decode()
+
+    def tune(self, sweeps_per_trial: int = 2, cache: str | None = None) -> dict:
+        """time the candidate launch shapes and keep the fastest (chains
+        restored).  With cache (a JSON file path), a shape kept there for a
+        batch of the same mix of chain shapes on the same GPU is used without
+        timing, and a newly timed shape is stored (pimc/tuning.py)."""
+        sig = tc = None
+        if cache:
+            from .tuning import TuneCache, batch_signature
+            sig = batch_signature(self.params, self.device_name(), self.L.pimc_abi_version())
+            tc = TuneCache(cache)
+            hit = tc.get(sig)
+            if hit is not None:
+                try:
+                    self.set_launch(**hit)
+                    return dict(self.launch, cached=True)
+                except PimcError:
+                    pass  # a shape this build no longer accepts: time afresh
         l = Launch()
         check(self.L.pimc_batch_tune(self.h, sweeps_per_trial, C.byref(l)))
+        if tc is not None:
+            tc.put(sig, self.launch)
         return self.launch
 
     def set_launch(self, block: int, sweeps_per_launch: int = 1,

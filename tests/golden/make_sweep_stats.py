@@ -1,22 +1,37 @@
 """Oracle statistics of the benchmarked configurations.
 
-Runs the oracle's run! (oracle/pimc_oracle.c, the C restatement of the
-reference's src/simulation.jl:29-42 with its update callables) on
-independent chains of C1 (2D trapped ideal bosons, N=10, beta=1, M=20), C2
-(2D free bosons in the periodic box [-10, 10)^2, N=64, beta=2, M=32), C3
-(2D trapped bosons with the Gaussian pair g=1, sigma=0.5, N=256, beta=2,
-M=64) and a sample of 24 chains of the batched C4 list, with the survey's
-mapping of a sweep onto run! attempts (N k staging, N swaps, N centre of
-mass; window lengths frozen).  Each chain starts from the oracle's
-init_world, is thermalised, then measured once per sweep.  Per chain the mean
-of every estimator column is kept; the configuration's value is the mean over
-chains and its standard error the spread of the chain means / sqrt(chains),
-which needs no autocorrelation model because the chains are independent.
-Densities are kept per bin the same way (counts / ndata per chain).
+Runs the oracle (oracle/pimc_oracle.c, the C restatement of the reference's
+moves) on independent chains of C1 (2D trapped ideal bosons, N=10, beta=1,
+M=20), C2 (2D free bosons in the periodic box [-10, 10)^2, N=64, beta=2,
+M=32), C3 (2D trapped bosons with the Gaussian pair g=1, sigma=0.5, N=256,
+beta=2, M=64) and a sample of 24 chains of the batched C4 list, in one of two
+schedules of the same moves:
 
-Writes tests/golden/sweep_stats.json and tests/golden/density_<name>.npz.
-The GPU tests (tests/test_gpu_sweep_parity.py) and bench.py's energy check
-compare the engine's sweeps against these numbers.
+* "run": the reference's run! (src/simulation.jl:29-42), attempts chosen at
+  random with weights 1/every, with the survey's mapping of a sweep onto
+  N(k+2) attempts (N k staging, N swaps, N centre of mass);
+* "sweep": the engine's sweep (orc_run_sweeps): a staging phase of one window
+  per (slot, particle), N swaps, one centre-of-mass attempt per single path,
+  a measurement at the end of the sweep.
+
+Under the physical rules both schedules sample the same distribution and the
+engine is held to run!.  The reference's own rules are not reversible (the
+swap leaves out its partner-choice ratio and puts the new paths' pair terms
+into w_initial), so what they sample depends on the schedule: the engine is
+held to the "sweep" schedule under those rules, and the "run" numbers are
+kept as the record of the difference.
+
+Each chain starts from the oracle's init_world, is thermalised, then measured
+once per sweep.  Per chain the mean of every estimator column is kept; the
+configuration's value is the mean over chains and its standard error the
+spread of the chain means / sqrt(chains), which needs no autocorrelation model
+because the chains are independent.  Densities are kept per bin the same way
+(counts / ndata per chain).
+
+Writes tests/golden/sweep_stats.json and tests/golden/density_<name>.npz; an
+entry already in the file is kept unless --only names it.  The GPU tests
+(tests/test_gpu_sweep_parity.py) and bench.py's energy check compare the
+engine's sweeps against these numbers.
 
     python tests/golden/make_sweep_stats.py [--only c1_ref,c4_sample] [--threads 8]
 """
@@ -39,26 +54,39 @@ sys.path.insert(0, os.path.dirname(HERE))
 from common import c4_sample, oracle_updates, sweep_configs  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-# chains, thermalisation sweeps, measured sweeps
+# name: (configuration, schedule, chains, thermalisation sweeps, measured sweeps)
 PLAN = {
-    "c1_ref": (64, 2000, 20000),
-    "c1_phys": (64, 2000, 20000),
-    "c2_ref": (64, 1000, 10000),
-    "c2_phys": (64, 1000, 10000),
-    "c3_ref": (32, 300, 1200),
+    "c1_ref": ("c1_ref", "sweep", 64, 2000, 20000),
+    "c1_ref_run": ("c1_ref", "run", 64, 2000, 20000),
+    "c1_phys": ("c1_phys", "run", 64, 2000, 20000),
+    "c2_ref": ("c2_ref", "sweep", 64, 1000, 10000),
+    "c2_ref_run": ("c2_ref", "run", 64, 1000, 10000),
+    "c2_phys": ("c2_phys", "run", 64, 1000, 10000),
+    "c3_ref": ("c3_ref", "sweep", 32, 300, 1200),
+    "c3_ref_run": ("c3_ref", "run", 32, 300, 1200),
 }
+# C4 sample: name -> (schedule, semantics); replicas, thermalisation, measured
+C4_PLAN = {"c4_sample": ("sweep", 0), "c4_sample_run": ("run", 0), "c4_sample_phys": ("run", 1)}
 C4_REPLICAS, C4_THERM, C4_SWEEPS = 16, 1000, 4000
 
 
-def run_chain(orc_kw, ell, dens_nb, therm, sweeps, seed):
+def run_chain(orc_kw, ell, dens_nb, therm, sweeps, seed, schedule="run"):
     """one oracle chain: init_world, therm sweeps, then sweeps measured sweeps"""
     p = O.make_params(**orc_kw)
     o = O.Oracle(p)
     o.init_world(seed=seed, stream=1)
-    ups, per = oracle_updates(orc_kw["N"], orc_kw["M"], ell, orc_kw["L"])
-    o.run(therm * per, ups, seed=seed, stream=2)
-    r = o.run(sweeps * per, ups, seed=seed, stream=3, ncycle=per, e_cap=sweeps + 1,
-              dens_nb=dens_nb)
+    N, M, L = orc_kw["N"], orc_kw["M"], orc_kw["L"]
+    if schedule == "run":
+        ups, per = oracle_updates(N, M, ell, L)
+        o.run(therm * per, ups, seed=seed, stream=2)
+        r = o.run(sweeps * per, ups, seed=seed, stream=3, ncycle=per, e_cap=sweeps + 1,
+                  dens_nb=dens_nb)
+    else:
+        com = [1.0, 0.1, L / 2, 0.4, 0.6]
+        O.run_sweeps(o, therm, ell, N, com, seed=seed, stream=2)
+        r = O.run_sweeps(o, sweeps, ell, N, com, seed=seed, stream=3, measure_every=1,
+                         e_cap=sweeps, dens_nb=dens_nb)
+    assert r["rc"] == 0, r["rc"]
     E = r["energies"]
     assert len(E) == sweeps, (len(E), sweeps)
     out = {"mean": E.mean(axis=0)}
@@ -83,25 +111,29 @@ def main():
     O.build()
     path = os.path.join(HERE, "sweep_stats.json")
     stats = json.load(open(path)) if os.path.exists(path) else {}
-    stats["_about"] = ("oracle run! statistics (mean over independent chains, standard error "
-                       "from the spread of chain means); made by tests/golden/make_sweep_stats.py")
-    jobs = []  # (cost, key, callable)
+    stats["_about"] = ("oracle statistics in the run! schedule or the engine's sweep schedule "
+                       "(mean over independent chains, standard error from the spread of chain "
+                       "means); made by tests/golden/make_sweep_stats.py")
+    jobs = []  # (cost, key, arguments)
     cfgs = sweep_configs()
-    for name, (nch, therm, sweeps) in PLAN.items():
+    for name, (cfg, sched, nch, therm, sweeps) in PLAN.items():
         if only and name not in only:
             continue
-        c = cfgs[name]
+        c = cfgs[cfg]
         cost = c["orc"]["N"] ** 2 * c["orc"]["M"] * (therm + sweeps) * (8 if c["orc"]["interactions"] else 1)
         for k in range(nch):
             jobs.append((cost, (name, k), (c["orc"], c["ell"], c["dens_nb"], therm, sweeps,
-                                           100000 * (1 + list(PLAN).index(name)) + k)))
+                                           100000 * (1 + list(PLAN).index(name)) + k, sched)))
     sample = c4_sample()
-    if not only or "c4_sample" in only:
+    for name, (sched, sem) in C4_PLAN.items():
+        if only and name not in only:
+            continue
         for idx, _, orc, ell in sample:
+            orc = dict(orc, semantics=sem)
             cost = orc["N"] ** 2 * orc["M"] * (C4_THERM + C4_SWEEPS) * 8
             for r in range(C4_REPLICAS):
-                jobs.append((cost, ("c4", idx, r), (orc, ell, 0, C4_THERM, C4_SWEEPS,
-                                                    7000000 + 100 * idx + r)))
+                jobs.append((cost, (name, idx, r), (orc, ell, 0, C4_THERM, C4_SWEEPS,
+                                                    7000000 + 100 * idx + r, sched)))
     jobs.sort(key=lambda j: -j[0])
     t0 = time.time()
     res = {}
@@ -110,12 +142,13 @@ def main():
         for f in cf.as_completed(futs):
             res[futs[f]] = f.result()
     print(f"{len(jobs)} chains in {time.time() - t0:.0f} s", flush=True)
-    for name, (nch, therm, sweeps) in PLAN.items():
+    for name, (cfg, sched, nch, therm, sweeps) in PLAN.items():
         if only and name not in only:
             continue
         chains = [res[(name, k)] for k in range(nch)]
-        c = cfgs[name]
-        entry = {"orc": c["orc"], "ell": c["ell"], "chains": nch, "therm": therm, "sweeps": sweeps}
+        c = cfgs[cfg]
+        entry = {"orc": c["orc"], "ell": c["ell"], "chains": nch, "therm": therm,
+                 "sweeps": sweeps, "schedule": sched}
         entry.update(summarise(chains))
         if c["dens_nb"]:
             d = np.array([ch["dens"] for ch in chains])
@@ -125,14 +158,16 @@ def main():
             entry["density"] = fn
             entry["dens_nb"] = c["dens_nb"]
         stats[name] = entry
-    if not only or "c4_sample" in only:
+    for name, (sched, sem) in C4_PLAN.items():
+        if only and name not in only:
+            continue
         per = []
         for idx, _, orc, ell in sample:
-            s = summarise([res[("c4", idx, r)] for r in range(C4_REPLICAS)])
+            s = summarise([res[(name, idx, r)] for r in range(C4_REPLICAS)])
             per.append({"index": idx, "N": orc["N"], "M": orc["M"], "beta": 1.0 / orc["T"],
                         "g": orc["pair_g"], **s})
-        stats["c4_sample"] = {"replicas": C4_REPLICAS, "therm": C4_THERM, "sweeps": C4_SWEEPS,
-                              "chains": per}
+        stats[name] = {"replicas": C4_REPLICAS, "therm": C4_THERM, "sweeps": C4_SWEEPS,
+                       "schedule": sched, "semantics": sem, "chains": per}
     with open(path, "w") as f:
         json.dump(stats, f, indent=1, sort_keys=True)
     print("wrote", path)

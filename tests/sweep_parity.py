@@ -1,5 +1,5 @@
 """Engine-side statistics of the benchmarked configurations, compared with
-the oracle's committed run! statistics (tests/golden/sweep_stats.json).
+the oracle's committed statistics (tests/golden/sweep_stats.json).
 
 Both sides use independent chains: every estimator's value is the mean over
 chains of each chain's mean over its measured sweeps, and its standard error
@@ -91,18 +91,23 @@ def density_compare(gpu_dens, orc_mean, orc_se, min_mean=None):
             "total_rel_diff": float(abs(g_mean.sum() - orc_mean.sum()) / orc_mean.sum())}
 
 
-def c4_energy_check(replicas=32, therm=1000, sweeps=4000, seed0=9100000):
+def c4_energy_check(replicas=32, therm=1000, sweeps=4000, seed0=9100000, semantics=0):
     """the 24 sampled C4 chains (tests/common.py c4_sample), replicas each, in
     one batch of the engine against the oracle's committed per-chain
-    statistics: per chain z of E_th + E_pair, and the summary"""
+    statistics: under the reference's rules those of the engine's sweep
+    schedule (the rules are not reversible, so the schedule matters), under the
+    physical rules those of run!.  Per chain z of E_th + E_pair, and the
+    summary."""
     from pimc.engine import ChainParams, Engine
-    stats = load_stats()["c4_sample"]
+    key = "c4_sample" if semantics == 0 else "c4_sample_phys"
+    stats = load_stats()[key]
     by_index = {c["index"]: c for c in stats["chains"]}
     sample = c4_sample()
     ps, which = [], []
     for k, (idx, eng, _, ell) in enumerate(sample):
         for r in range(replicas):
-            ps.append(ChainParams(**eng, seed=seed0 + 1000 * k + r, energy_capacity=0))
+            ps.append(ChainParams(**dict(eng, semantics=semantics), seed=seed0 + 1000 * k + r,
+                                  energy_capacity=0))
             which.append(k)
     e = Engine(ps)
     for c, k in enumerate(which):
@@ -127,6 +132,8 @@ def c4_energy_check(replicas=32, therm=1000, sweeps=4000, seed0=9100000):
     zz = np.array([r["z"] for r in rows])
     summary = {"chains": len(rows), "replicas": replicas, "oracle_replicas": stats["replicas"],
                "therm": therm, "sweeps": sweeps, "quantity": "E_th + E_pair per chain",
+               "semantics": "reference" if semantics == 0 else "physical",
+               "oracle_schedule": "the engine's sweep" if stats["schedule"] == "sweep" else "run!",
                "within_2sigma": int(np.sum(np.abs(zz) < 2.0)), "max_abs_z": float(np.abs(zz).max()),
                "chi2_per_dof": float(np.mean(zz ** 2))}
     return summary, rows

@@ -328,10 +328,14 @@ def test_failure_paths():
         big.staging_weights(0, 0, 70, np.zeros(71 * 2))
     with pytest.raises(PimcError, match="window"):
         big.attempt_staging(0, 0, 70, np.zeros(69 * 2), [0.5])
-    # the hard-core retry cap ends a move as a rejection, not a hang
-    # (3 cells per dimension: the stencil sees every bead, all closer than a)
-    h = engine(dim=2, N=3, M=8, L=1.0, T=1.0, lam=0.5, hardcore_a=5.0, r_a=0.6, retry_cap=50,
+    # the hard-core retry cap ends a move as a rejection, not a hang: with
+    # zero normals every retry proposes the bridge's mean, here particle 0's
+    # own start, where particle 1 sits
+    h = engine(dim=2, N=3, M=8, L=1.0, T=1.0, lam=0.5, hardcore_a=0.3, r_a=0.6, retry_cap=50,
                seed=12, interactions=True, pair_g=0.0, pair_sigma=0.3)
+    x = np.zeros((2, 3, 8))
+    x[:, 2, :] = 0.7
+    h.set_beads(x)
     r, _ = h.attempt_staging(0, 0, 4, np.zeros(3 * 2 * 60), [0.5])
     assert r == 3
 

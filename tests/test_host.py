@@ -223,3 +223,30 @@ def test_generate_V_forms():
     assert abs(V(np.zeros(2)) - (-3.0)) < 1e-15
     c = np.mean(np.cos([0.0, math.pi / 2])); s_ = np.mean(np.sin([0.0, math.pi / 2]))
     assert abs(W(np.zeros(2)) - 2.0 * (c * c + s_ * s_)) < 1e-15
+
+
+def test_tune_cache_round_trip(tmp_path):
+    """the tuner's cache of launch shapes (pimc/tuning.py): the signature
+    follows the batch's mix of chain shapes, the device and the ABI version,
+    not the chains' order or seeds; a stored shape comes back as stored"""
+    from pimc.tuning import TuneCache, batch_signature, n_bucket
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "c4_chains.json")))
+    chains = [dict(N=n, M=m, interactions=True, semantics=0) for n, m in zip(ref["N"], ref["M"])]
+    sig = batch_signature(chains, "NVIDIA GB300", 3)
+    assert sig == batch_signature(list(reversed(chains)), "NVIDIA GB300", 3)
+    assert sig != batch_signature(chains, "NVIDIA B200", 3)
+    assert sig != batch_signature(chains, "NVIDIA GB300", 2)
+    assert sig != batch_signature(chains[:-1], "NVIDIA GB300", 3)
+    assert [n_bucket(n) for n in (8, 15, 16, 300, 512)] == [8, 8, 16, 256, 512]
+    path = str(tmp_path / "tune.json")
+    shape = dict(warp_per_chain=False, block=64, sweeps_per_launch=1, state_smem_bytes=0,
+                 split_phases=1, phase_block=[128, 64, 128], phase_warp=[0, 1, 0])
+    tc = TuneCache(path)
+    assert tc.get(sig) is None
+    tc.put(sig, shape, ms_per_sweep=35.7)
+    again = TuneCache(path)
+    assert again.get(sig) == shape
+    assert json.load(open(path))[sig]["ms_per_sweep"] == 35.7
+    # an entry missing a key (an older file) is a miss, not an error
+    again.data[sig].pop("phase_warp")
+    assert again.get(sig) is None
