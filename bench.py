@@ -56,7 +56,7 @@ PER_BEAD = {
     ("c4", "reference", "k_sweep"): {"dram_bytes": 269.7, "fp64_flops": 204.0},   # 4.82 GB, 3.65 G / 17.87 M
     # the swap launch of the split sweep (its bead updates are the swaps' 2(m-1)
     # per attempt; every attempt also reads the N heat-bath candidates)
-    ("c4", "reference", "k_sweep_swap"): {"dram_bytes": 1011.5, "fp64_flops": 522.2},  # 3.07 GB, 1.59 G / 3.037 M
+    ("c4", "reference", "k_sweep_swap"): {"dram_bytes": 1057.0, "fp64_flops": 523.0},  # 3.21 GB, 1.59 G / 3.037 M
 }
 ROOF_SWEEPS = 2  # sweeps of the per-phase timing pass
 

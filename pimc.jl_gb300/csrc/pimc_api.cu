@@ -333,13 +333,19 @@ Plan plan_smem(const Handle *h, int mode, int block, int spl, int state_cap) {
   return p;
 }
 
+// the chain descriptors to the device; the captured sweep graph is dropped,
+// since which kernels it launches depends on the chains' flags
 int upload_desc(Handle *h) {
   CK(cudaMemcpyAsync(h->d_desc, h->desc.data(), sizeof(ChainDesc) * h->nchains,
                      cudaMemcpyHostToDevice, h->stream));
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
   return PIMC_OK;
 }
 
-// cached links V and the FP32 mirror from the positions
+// cached links V and the 16-bit position mirror from the positions
 int refresh_links(Handle *h, int chain0, int nch) {
   CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, chain0, nch, h->maxNM, h->stream));
   return PIMC_OK;
@@ -610,13 +616,22 @@ int run_plain(Handle *h, long long n) {
 
 // persistent grid: every resident CTA (CTA mode) or resident warp (warp mode)
 // pulls chains from the work queue
+// 1 when every chain follows the reference's rules without a hard core or
+// a contact table: the swap phase then runs the kernel compiled for those
+// rules alone (the CUDA graph is rebuilt whenever a chain's flags change)
+int swap_spec(const Handle *h) {
+  for (const auto &d : h->desc)
+    if (d.flags & (PF_PHYS | PF_HARD | PF_CONTACT)) return 0;
+  return 1;
+}
+
 // resident CTAs (or warps) for a launch of the plan's kernel; phase >= 0
 // names a phase kernel of a split plan
 int grid_for(Handle *h, const Plan &p, int phase = -1) {
   int per_sm = 0;
   const cudaError_t e = phase >= 0
-                            ? sweep_phase_occupancy(phase, p.pwarp[phase], phase_block(p, phase),
-                                                    phase_smem(p, phase), &per_sm)
+                            ? sweep_phase_occupancy(phase, p.pwarp[phase], swap_spec(h),
+                                                    phase_block(p, phase), phase_smem(p, phase), &per_sm)
                             : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const bool warp = phase >= 0 ? p.pwarp[phase] != 0 : p.mode == 1;
@@ -631,17 +646,17 @@ int grid_for(Handle *h, const Plan &p, int phase = -1) {
 bool launch_teams(Handle *h, const Plan &p) {
   int per_sm = 0;
   if (p.mode != 0) return false;
-  const cudaError_t e = p.split ? sweep_phase_occupancy(0, 0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
+  const cudaError_t e = p.split ? sweep_phase_occupancy(0, 0, 0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
                                 : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess) return false;
   return h->nchains <= per_sm * h->num_sms;
 }
 
 // the dynamic shared-memory attribute of every kernel the plan launches
-cudaError_t plan_set_smem(const Plan &p) {
+cudaError_t plan_set_smem(const Handle *h, const Plan &p) {
   if (!p.split) return sweep_set_smem(p.mode, p.dyn_smem);
   for (int ph = 0; ph < 3; ++ph) {
-    const cudaError_t e = sweep_phase_set_smem(ph, p.pwarp[ph], phase_smem(p, ph));
+    const cudaError_t e = sweep_phase_set_smem(ph, p.pwarp[ph], swap_spec(h), phase_smem(p, ph));
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -665,8 +680,8 @@ cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long
       if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
       cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
       if (e == cudaSuccess)
-        e = launch_sweep_phase(b, ph, p.pwarp[ph], grid_for(h, p, ph), phase_block(p, ph),
-                               phase_smem(p, ph), h->stream);
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), grid_for(h, p, ph),
+                               phase_block(p, ph), phase_smem(p, ph), h->stream);
       if (e != cudaSuccess) return e;
       if (launches) *launches += 1;
     }
@@ -694,7 +709,7 @@ int build_graph(Handle *h) {
 
 int run_batched(Handle *h, long long n) {
   const Plan &p = h->bat;
-  CK(plan_set_smem(p));
+  CK(plan_set_smem(h, p));
   const int spl = std::max(1, p.spl);
   int rc = build_graph(h);
   if (rc) return rc;
@@ -1141,7 +1156,7 @@ int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
   Handle *h = H(handle);
   if (!h || !ms || n < 1) return fail(PIMC_EARG, "bad argument");
   const Plan &p = h->bat;
-  CK(plan_set_smem(p));
+  CK(plan_set_smem(h, p));
   SweepArgs a = sweep_args(h, p);
   a.order = h->d_order;
   a.queue = h->d_queue;
@@ -1160,8 +1175,8 @@ int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
         SweepArgs b = a;
         b.sweeps = 1;
         if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
-        e = launch_sweep_phase(b, ph, p.pwarp[ph], grid_for(h, p, ph), phase_block(p, ph),
-                               phase_smem(p, ph), h->stream);
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), grid_for(h, p, ph),
+                               phase_block(p, ph), phase_smem(p, ph), h->stream);
       } else {
         a.sweeps = 1;
         e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);

@@ -551,7 +551,9 @@ constexpr int PQ_CAP = 96;  // queue entries per warp (64-bit)
 // ends, added to the lane's old (so) or new (sn) sum; the caller applies the
 // link weight -tau g / 2 once per segment.  With the contact table the entry
 // is the link's pair action itself (weight 1).
-template <class Seg>
+// CT = false: the chains this code runs for have no contact table (a
+// specialised kernel), so its branch is compiled out
+template <bool CT = true, class Seg>
 __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long long e,
                                         double &so, double &sn) {
   const ChainDesc &d = *c.d;
@@ -567,7 +569,7 @@ __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long
   const int bn = j == M - 1 ? c.next[b] : b;
   const double bnx = c.X(0, bn, jn), bny = c.Xd(1, bn, jn);
   double v;
-  if (d.flags & PF_CONTACT) {
+  if (CT && (d.flags & PF_CONTACT)) {
     v = contact_link(d, ax, ay, bx, by, anx, any, bnx, bny);
   } else {
     const double r2b = mi2(d, anx, any, bnx, bny);
@@ -577,11 +579,11 @@ __device__ __forceinline__ void pq_eval(const CV &c, const Seg &s, unsigned long
 }
 
 // evaluate the first min(qn, 32) queued entries and move the rest up
-template <class Seg>
+template <bool CT = true, class Seg>
 __device__ __forceinline__ void pq_flush(const CV &c, const Seg &s, unsigned long long *q, int &qn,
                                          double &wo, double &wn, int lane) {
   const int k = qn < 32 ? qn : 32;
-  if (lane < k) pq_eval(c, s, q[lane], wo, wn);
+  if (lane < k) pq_eval<CT>(c, s, q[lane], wo, wn);
   __syncwarp();
   unsigned long long rest[3];
   const int nr = qn - k;
@@ -597,7 +599,7 @@ __device__ __forceinline__ void pq_flush(const CV &c, const Seg &s, unsigned lon
 }
 
 // the lane's sums of the links' pair exponentials, old and new configuration
-template <class Seg>
+template <bool CT = true, class Seg>
 __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
                              unsigned long long *q, double &wo, double &wn, int lane) {
   const ChainDesc &d = *c.d;
@@ -637,20 +639,20 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
       // a block of 32 particles queues up to 64 entries (old and new): drain
       // to fewer than 32 before the next block, so that the queue holds at
       // most 31 + 64 = 95 < PQ_CAP entries at any time
-      while (qn >= 32) pq_flush(c, s, q, qn, wo, wn, lane);
+      while (qn >= 32) pq_flush<CT>(c, s, q, qn, wo, wn, lane);
     }
   }
-  while (qn > 0) pq_flush(c, s, q, qn, wo, wn, lane);
+  while (qn > 0) pq_flush<CT>(c, s, q, qn, wo, wn, lane);
 }
 
 // adds the links' pair terms -tau/2 (v(r_a) + v(r_b)) of the old (wo) and the
 // new (wn) configuration; every lane of the warp calls it
-template <class Seg>
+template <bool CT = true, class Seg>
 __device__ void segment_pairs(const CV &c, const Seg &s, int t0, int t1, bool do_old, bool do_new,
                               unsigned long long *q, double &wo, double &wn, int lane) {
   double so = 0.0, sn = 0.0;
-  segment_sums(c, s, t0, t1, do_old, do_new, q, so, sn, lane);
-  if (c.d->flags & PF_CONTACT) {
+  segment_sums<CT>(c, s, t0, t1, do_old, do_new, q, so, sn, lane);
+  if (CT && (c.d->flags & PF_CONTACT)) {
     wo += so;
     wn += sn;
   } else {

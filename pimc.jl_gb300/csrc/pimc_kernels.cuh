@@ -282,11 +282,21 @@ struct HeatBath {
 // search, the bridges and the decision are the first warp's (thread 0 draws
 // the Metropolis uniform).  Returns RES_*; n2_out receives n2.
 // ---------------------------------------------------------------------------
-template <bool WARP, bool FAST, class D>
+// SPEC = SWAP_REF: every chain this code runs for follows the reference's
+// rules with the Gaussian pair (or none), no hard core and no contact table;
+// the other rules' code is compiled out, so the kernel needs fewer registers
+// and less instruction cache (the host picks it when the whole batch
+// qualifies)
+constexpr int SWAP_ANY = 0, SWAP_REF = 1;
+
+template <bool WARP, bool FAST, class D, int SPEC = SWAP_ANY>
 __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &dr,
                           SwapScratch &S, double *red, double *prop, int *n2_out) {
   using G = Group<WARP>;
   const ChainDesc &d = *c.d;
+  constexpr bool GEN = SPEC == SWAP_ANY;
+  const bool f_phys = GEN && (d.flags & PF_PHYS), f_hard = GEN && (d.flags & PF_HARD);
+  const bool f_contact = GEN && (d.flags & PF_CONTACT);
   const int N = c.N, M = c.M, dim = c.dim, lane = threadIdx.x & 31;
   const int tid = G::rank(), nt = G::size();
   const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
@@ -435,7 +445,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   }
 
   double log_ratio = 0.0;
-  if (d.flags & PF_PHYS) {
+  if (f_phys) {
     // (1/S'_1 + 1/S'_2) / (1/S_1 + 1/S_2): S_a sums the heat-bath weights
     // with a chosen first; primes after the ends of n1 and n2 are exchanged
     const HBead B = hb.bead(n2, j0);
@@ -479,7 +489,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   if (dim > 1 && fabs(s1y - f1y) > L) f1y += sgn(s1y) * (2.0 * L);
   if (fabs(s2x - f2x) > L) f2x += sgn(s2x) * (2.0 * L);
   if (dim > 1 && fabs(s2y - f2y) > L) f2y += sgn(s2y) * (2.0 * L);
-  const bool hard = (d.flags & PF_HARD) != 0;
+  const bool hard = f_hard;
   if (!hard) {
     for (int k = tid; k < 2 * (m - 1); k += nt) {
       double zz[2];
@@ -510,8 +520,8 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       for (int t = 1; t < m && !fail; ++t) {
         const double2 ab = bridge_coef(c, m, t);
         const int j = slc(t);
-        const int ea = (d.flags & PF_PHYS) ? own1(t) : (b == 0 ? n2 : n1);
-        const int eb = (d.flags & PF_PHYS) ? own2(t) : -1;
+        const int ea = f_phys ? own1(t) : (b == 0 ? n2 : n1);
+        const int eb = f_phys ? own2(t) : -1;
         int tries = 0;
         while (true) {
           if (++tries > d.ctr) { fail = 1; break; }
@@ -560,7 +570,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   }
   G::sync();
   PROF_MARK(4);
-  const bool any_pair = (d.flags & PF_PAIR) != 0, phys = (d.flags & PF_PHYS) != 0;
+  const bool any_pair = (d.flags & PF_PAIR) != 0, phys = f_phys;
   double w2[2] = {vold, 0.0};  // w_initial, w_update
   for (int k = tid; k < 2 * m; k += nt) {
     const int b = k / m, t = k % m;
@@ -572,7 +582,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   // decision and a sweep skips them (its Metropolis uniform is a pure function
   // of the move's stream).  Injected-draw attempts always evaluate them.
   bool pairs = any_pair;
-  const bool shortcuts = FAST && !(d.flags & (PF_EXACT | PF_CONTACT));
+  const bool shortcuts = FAST && !(d.flags & PF_EXACT) && !f_contact;
   int early = 0;  // 1: accepted on the pair-free sums, which are then the final sums
   // reference rules, g >= 0: dS = dS_pf + (tau g / 2)(So + Sn) with So, Sn >= 0,
   // so any lower bound of the pair sums that reaches `need` accepts the move
@@ -603,7 +613,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       const double ox = c.X(0, o1, j), oy = c.Xd(1, o1, j);
       const double r2o = mi2(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j));
       if (r2o <= d.rc2) {
-        if (d.flags & PF_CONTACT)
+        if (f_contact)
           w2[0] += contact_link(d, ox, oy, c.X(0, o2, j), c.Xd(1, o2, j), c.X(0, o1n, jn),
                                 c.Xd(1, o1n, jn), c.X(0, o2n, jn), c.Xd(1, o2n, jn));
         else
@@ -611,7 +621,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       }
       const double r2n = mi2(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t]);
       if (r2n <= d.rc2) {
-        if (d.flags & PF_CONTACT)
+        if (f_contact)
           w2[1] += contact_link(d, S.r1x[t], S.r1y[t], S.r2x[t], S.r2y[t], S.r1x[t + 1],
                                 S.r1y[t + 1], S.r2x[t + 1], S.r2y[t + 1]);
         else
@@ -636,12 +646,21 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     // once the flag is up, so without it every warp has scanned all its links
     const double gh = 0.5 * d.tau * d.g;
     volatile int *flag = S.iv + 3;
+    // the warp's lower bound is formed in FP32 (the FP64 pipe of this part
+    // is narrow, and this runs after every link): the lane's estimate minus
+    // its bounds, widened by the FP32 accumulation error as est_reduce_lanes
+    // does, summed over the warp; the FP32 rounding of these few operations
+    // and of the warp sum stays below 4e-6 of the sum of the magnitudes, which
+    // is taken off, so the bound used is never above the FP64 one and an
+    // early accept is always one the exact sums would make
     auto stop = [&](const PairEst &pe) -> bool {
       if (!monotone) return false;
       if (*flag) return true;
-      double l4[4];
-      est_reduce_lanes(pe, l4);
-      const double lb = warp_sum((l4[0] - l4[1]) + (l4[2] - l4[3]));
+      const float ro = 2.4e-7f * (float)(pe.ko + 1), rn = 2.4e-7f * (float)(pe.kn + 1);
+      const float lf = (pe.so * (1.f - ro) - pe.bo * (1.f + ro)) + (pe.sn * (1.f - rn) - pe.bn * (1.f + rn));
+      const float af = (pe.so + pe.bo) + (pe.sn + pe.bn);
+      const float slf = warp_sum(lf), saf = warp_sum(af);
+      const double lb = (double)slf - 4e-6 * (double)saf - 1e-30;
       if (gh * lb > need) {
         if (lane == 0) *flag = 1;
         return true;
@@ -680,7 +699,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       const int t0 = max(a0 - b * m, 0), t1 = min(a1 - b * m, m);
       if (t0 >= t1) continue;
       double wo = 0.0, wn = 0.0;
-      segment_pairs(c, seg_of(b), t0, t1, true, true, S.q + (size_t)warp * PQ_CAP, wo, wn, lane);
+      segment_pairs<GEN>(c, seg_of(b), t0, t1, true, true, S.q + (size_t)warp * PQ_CAP, wo, wn, lane);
       // the reference adds the new paths' pair terms to w_initial and lets
       // the old ones see the other moving path (reshape.jl:166-240)
       w2[0] += wo;

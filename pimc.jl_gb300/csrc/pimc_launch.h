@@ -100,11 +100,14 @@ cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size
 cudaError_t sweep_set_smem(int mode, size_t smem);
 // the sweep as three launches per sweep (phase 0 staging, 1 swaps, 2 the
 // rest), one CTA per chain, or for the swaps (warp = 1) one warp per chain;
-// a.sweeps must be 1
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int grid, int block,
-                               size_t smem, cudaStream_t s);
-cudaError_t sweep_phase_set_smem(int phase, int warp, size_t smem);
-cudaError_t sweep_phase_occupancy(int phase, int warp, int block, size_t smem, int *blocks_per_sm);
+// spec = 1 selects the swap kernel compiled for the reference's rules alone
+// (every chain of the launch without physical rules, hard core or contact
+// table); a.sweeps must be 1
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int grid,
+                               int block, size_t smem, cudaStream_t s);
+cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, size_t smem);
+cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int block, size_t smem,
+                                  int *blocks_per_sm);
 size_t sweep_ctl_bytes();
 cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm);
 cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s);

@@ -1,11 +1,14 @@
 // pimc_sweep.cu -- kernels of the GB300 sweep engine.
 //
-// One CTA owns one chain for the duration of a sweep (or of a block of
-// sweeps).  Chains that fit are staged in shared memory (x, V, the FP32
-// mirror and next); larger ones are updated in place in HBM/L2.  The same
-// kernel serves the plain path (one launch per chain) and the batched path
-// (persistent grid pulling chains from a device work queue in LPT order,
-// captured in a CUDA graph).
+// One CTA (or one warp) owns one chain for the duration of a sweep, of a
+// block of sweeps, or of one phase of a sweep (staging, swaps, the rest as
+// three launches).  Chains that fit are staged in shared memory (x, V, the
+// 16-bit position mirror and next); larger ones are updated in place in
+// HBM/L2.  The same kernels serve the plain path (one launch per chain) and
+// the batched path (persistent grid pulling chains from a device work queue
+// in LPT order, captured in a CUDA graph).  Also here: the layout
+// transposes, init_world, the estimators' launch, the adjoint, the contact
+// table and the FP64 throughput probe.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -152,7 +155,7 @@ __device__ void close_phase(SmemCtl &sc, double *red, int q, double (&t)[4]) {
   G::sync();
 }
 
-template <bool WARP, int PH>
+template <bool WARP, int PH, int SPEC = SWAP_ANY>
 __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *scratch,
                           int warp_scratch_d, bool teams) {
   using G = Group<WARP>;
@@ -276,7 +279,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
       const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
       const double upick = u53(r1.z, r1.w);
       GenDraws dr = gen_draws(ss);
-      const int r = swap_group<WARP, true>(c, j0, m, n1, upick, dr, S, red, nullptr, nullptr);
+      const int r = swap_group<WARP, true, GenDraws, SPEC>(c, j0, m, n1, upick, dr, S, red, nullptr,
+                                                           nullptr);
       if (tid == 0) {
         if (r == RES_SKIP) {
           tal[2] += 1.0;
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) { sweep_warp
 // in flight of a two-warp CTA per chain at the same registers per SM
 __global__ void __launch_bounds__(256, 2) k_sweep_swap_warp(SweepArgs a) { sweep_warp<SW_SWAP>(a); }
 
-template <int PH>
+template <int PH, int SPEC = SWAP_ANY>
 __device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ SmemCtl sc;
@@ -474,7 +478,8 @@ __device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
       __syncthreads();
     }
     unsigned char *scratch = smem + a.state_bytes;
-    for (int s = 0; s < a.sweeps; ++s) sweep_one<false, PH>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
+    for (int s = 0; s < a.sweeps; ++s)
+      sweep_one<false, PH, SPEC>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
     if (staged) {
       double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
       unsigned *gq = (unsigned *)(a.dpool + d.xq_off);
@@ -498,6 +503,11 @@ __global__ void __launch_bounds__(512) k_sweep(SweepArgs a) { sweep_cta<SW_ALL>(
 // the longest sum over phases, sets a sweep's time
 __global__ void __launch_bounds__(512) k_sweep_stage(SweepArgs a) { sweep_cta<SW_STAGE>(a); }
 __global__ void __launch_bounds__(512) k_sweep_swap(SweepArgs a) { sweep_cta<SW_SWAP>(a); }
+// the swap launch for batches whose every chain follows the reference's
+// rules without a hard core or a contact table (swap_group SWAP_REF)
+__global__ void __launch_bounds__(512) k_sweep_swap_ref(SweepArgs a) {
+  sweep_cta<SW_SWAP, SWAP_REF>(a);
+}
 __global__ void __launch_bounds__(512) k_sweep_rest(SweepArgs a) { sweep_cta<SW_REST>(a); }
 
 // ---------------------------------------------------------------------------
@@ -846,7 +856,7 @@ __global__ void k_init_world_hard(const ChainDesc *desc, ChainVar *var, double *
   }
 }
 
-// cached link actions V[j][n] = lnV(bead, next bead) and the FP32 mirror
+// cached link actions V[j][n] = lnV(bead, next bead) and the 16-bit mirror
 __global__ void k_links(const ChainDesc *desc, double *dpool, int *ipool, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
   CV c = make_cv(&d, dpool, ipool, nullptr);
@@ -860,7 +870,7 @@ __global__ void k_links(const ChainDesc *desc, double *dpool, int *ipool, int ch
   }
 }
 
-// the FP32 mirror alone (after verbatim state uploads)
+// the 16-bit mirror alone (after verbatim state uploads)
 __global__ void k_mirror(const ChainDesc *desc, double *dpool, int chain0) {
   const ChainDesc &d = desc[chain0 + blockIdx.y];
   CV c = make_cv(&d, dpool, nullptr, nullptr);
@@ -1282,27 +1292,34 @@ cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size
 }
 // phase kernels: 0 staging, 1 swaps, 2 the rest; warp = 1 (swaps only): one
 // warp per chain
-static const void *phase_kernel(int phase, int warp) {
-  if (phase == 1) return warp ? (const void *)k_sweep_swap_warp : (const void *)k_sweep_swap;
+// warp = 1 (swaps only): one warp per chain; spec = 1 (swaps in CTA mode):
+// the reference-rules swap kernel
+static const void *phase_kernel(int phase, int warp, int spec) {
+  if (phase == 1) {
+    if (warp) return (const void *)k_sweep_swap_warp;
+    return spec ? (const void *)k_sweep_swap_ref : (const void *)k_sweep_swap;
+  }
   return phase == 0 ? (const void *)k_sweep_stage : (const void *)k_sweep_rest;
 }
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int grid, int block,
-                               size_t smem, cudaStream_t s) {
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int grid,
+                               int block, size_t smem, cudaStream_t s) {
   if (phase == 0) k_sweep_stage<<<grid, block, smem, s>>>(a);
   else if (phase == 1 && warp) k_sweep_swap_warp<<<grid, block, smem, s>>>(a);
+  else if (phase == 1 && spec) k_sweep_swap_ref<<<grid, block, smem, s>>>(a);
   else if (phase == 1) k_sweep_swap<<<grid, block, smem, s>>>(a);
   else k_sweep_rest<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t sweep_phase_set_smem(int phase, int warp, size_t smem) {
-  return cudaFuncSetAttribute(phase_kernel(phase, warp), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem);
+cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, size_t smem) {
+  return cudaFuncSetAttribute(phase_kernel(phase, warp, spec),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-cudaError_t sweep_phase_occupancy(int phase, int warp, int block, size_t smem, int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, phase_kernel(phase, warp),
-                                                       block, smem);
+cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int block, size_t smem,
+                                  int *blocks_per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm,
+                                                       phase_kernel(phase, warp, spec), block, smem);
 }
 
 cudaError_t sweep_set_smem(int mode, size_t smem) {

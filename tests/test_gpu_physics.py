@@ -396,3 +396,40 @@ def test_bounded_decisions_equal_exact_decisions(semantics):
     assert sum(sf.accepts) > 0 and min(sf.accepts[:3]) > 0  # staging, swaps, CoM all accept
     fast.close()
     exact.close()
+
+
+def test_reference_rules_swap_kernel_equals_generic():
+    """a batch whose every chain follows the reference's rules (Gaussian pair,
+    no hard core, no contact table) runs its swaps in the kernel compiled for
+    those rules alone; the chains equal, bit for bit, the same chains swept by
+    the generic kernels (plain launches, and a batch with one physical-rules
+    chain added, which keeps the generic swap kernel)"""
+    from pimc.engine import ChainParams, Engine
+    rng = np.random.default_rng(17)
+    ps = []
+    for i in range(12):
+        N = int(rng.integers(8, 96))
+        M = int(rng.choice([16, 32]))
+        ps.append(ChainParams(dim=2, N=N, M=M, L=6.0, T=1.0 / rng.uniform(0.5, 3), lam=0.5,
+                              harmonic_omega=1.0, interactions=bool(i % 4), pair_g=float(rng.uniform(0, 2)),
+                              pair_sigma=0.5, r_a=1.5, semantics=0, seed=3000 + i, energy_capacity=8))
+    extra = ChainParams(dim=2, N=12, M=16, L=6.0, T=1.0, lam=0.5, harmonic_omega=1.0,
+                        interactions=True, pair_g=1.0, pair_sigma=0.5, r_a=1.5, semantics=1,
+                        seed=3999, energy_capacity=8)
+    engines = [Engine(ps), Engine(ps), Engine(ps + [extra])]
+    for e in engines:
+        for i, p in enumerate(ps):
+            e.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
+    engines[2].set_mix(mix(12, 16, 8, 6.0, measure_every=3), chain=len(ps))
+    for e in (engines[0], engines[2]):
+        e.set_launch(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
+                     phase_block=[128, 64, 128])
+        e.run_batched(8)
+    engines[1].run_plain(8)
+    for c in range(len(ps)):
+        for e in engines[1:]:
+            np.testing.assert_array_equal(engines[0].get_beads(c), e.get_beads(c))
+            np.testing.assert_array_equal(engines[0].get_next(c), e.get_next(c))
+    assert engines[0].total_stats().accepts[1] > 0
+    for e in engines:
+        e.close()
