@@ -277,6 +277,12 @@ struct CV {
     if (dim > 1) X(1, n, j) = py;
     xq[(size_t)j * ldn + n] = qpos(*d, px, py);
   }
+  // the same with the mirror word already computed (qpos of px, py)
+  __device__ __forceinline__ void set_pos_q(int n, int j, double px, double py, unsigned q) const {
+    X(0, n, j) = px;
+    if (dim > 1) X(1, n, j) = py;
+    xq[(size_t)j * ldn + n] = q;
+  }
   // exchange the beads of particles a and b at slice j, mirror included
   __device__ __forceinline__ void exchange(int a, int b, int j) const {
     for (int k = 0; k < dim; ++k) {

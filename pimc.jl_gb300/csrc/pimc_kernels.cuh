@@ -333,6 +333,17 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   W *Sw = reinterpret_cast<W *>(S.w);
   const int chunk = (N + 31) / 32;
   const int i0 = min(N, lane * chunk), i1 = min(N, i0 + chunk);
+  // the bridges' normals depend on the move's stream alone: draw them first,
+  // so that their arithmetic overlaps the heat bath's memory reads
+  const bool early_normals = FAST && !f_hard;
+  if (early_normals) {
+    for (int k = tid; k < 2 * (m - 1); k += nt) {
+      double zz[2];
+      dr.bead_normals(k, dim, zz);
+      S.z[2 * k] = zz[0];
+      S.z[2 * k + 1] = dim > 1 ? zz[1] : 0.0;
+    }
+  }
   W wm[1] = {W(-INFINITY)};
   if (FAST) {
     // four candidates per thread at a time: their next[] and mirror words are
@@ -358,9 +369,9 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
         const int i = i0 + u * nt;
         if (i < N) {
           const float s2 = (float)qdist2(A.q, qe[u]) + (float)qdist2(qa[u], E1.q);
-          const W v = (W)(-s2 * hb.inv_denf);
-          Sw[i] = v;
-          wm[0] = v > wm[0] ? v : wm[0];
+          // the weight itself: exp of a non-positive exponent, unshifted (a
+          // batch whose every weight underflows takes the shifted form below)
+          Sw[i] = __expf((float)(W)(-s2 * hb.inv_denf));
         }
       }
     }
@@ -371,19 +382,41 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       wm[0] = v > wm[0] ? v : wm[0];
     }
   }
-  G::template max<1>(wm, red);
+  if (!FAST) G::template max<1>(wm, red);
   G::sync();
   PROF_MARK(0);
-  const W wmax = wm[0];
+  W wmax = FAST ? W(0) : wm[0];
   W ssum = W(0);
   if (lead) {
     W ls = W(0);
-    for (int i = i0; i < i1; ++i) {
-      const W e = hb.ex_(Sw[i] - wmax);
-      Sw[i] = e;
-      ls += e;
+    if (FAST) {
+      for (int i = i0; i < i1; ++i) ls += Sw[i];
+      ssum = warp_sum(ls);
+      if (!(ssum > W(0))) {
+        // every weight underflowed: exponents shifted by their largest
+        W mx = W(-INFINITY);
+        for (int i = i0; i < i1; ++i) {
+          const W v = hb.expo(i, A, E1);
+          Sw[i] = v;
+          mx = v > mx ? v : mx;
+        }
+        wmax = warp_max(mx);
+        ls = W(0);
+        for (int i = i0; i < i1; ++i) {
+          const W e = hb.ex_(Sw[i] - wmax);
+          Sw[i] = e;
+          ls += e;
+        }
+        ssum = warp_sum(ls);
+      }
+    } else {
+      for (int i = i0; i < i1; ++i) {
+        const W e = hb.ex_(Sw[i] - wmax);
+        Sw[i] = e;
+        ls += e;
+      }
+      ssum = warp_sum(ls);
     }
-    ssum = warp_sum(ls);
     W lq = ls, target;
     if (FAST) {
       // sweeps search the unnormalised weights against u times their sum
@@ -491,15 +524,52 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   if (dim > 1 && fabs(s2y - f2y) > L) f2y += sgn(s2y) * (2.0 * L);
   const bool hard = f_hard;
   if (!hard) {
-    for (int k = tid; k < 2 * (m - 1); k += nt) {
-      double zz[2];
-      dr.bead_normals(k, dim, zz);
-      S.z[2 * k] = zz[0];
-      S.z[2 * k + 1] = dim > 1 ? zz[1] : 0.0;
-    }
+    if (!early_normals)
+      for (int k = tid; k < 2 * (m - 1); k += nt) {
+        double zz[2];
+        dr.bead_normals(k, dim, zz);
+        S.z[2 * k] = zz[0];
+        S.z[2 * k + 1] = dim > 1 ? zz[1] : 0.0;
+      }
     dr.consumed(2 * (m - 1) * dim);
     G::sync();
-    if (lead && lane < 2 * dim) {
+    if (FAST) {
+      // sweeps: each bridge coordinate p_t = a_t p_(t-1) + b_t, b_t = (1 -
+      // a_t) e + z_t sigma_t, as a prefix scan of affine maps over 32-lane
+      // chunks of t (five steps of three FP64 operations a chunk instead of
+      // one dependent step per bead on four lanes); sequence q = b dim + k
+      // (bridge b, coordinate k) goes to warp q mod nwarps, with the same
+      // arithmetic in every launch shape
+      for (int q = warp; q < 2 * dim; q += nwarps) {
+        const int b = q / dim, k = q % dim;
+        const double s0 = b == 0 ? (k == 0 ? s1x : s1y) : (k == 0 ? s2x : s2y);
+        const double e = b == 0 ? (k == 0 ? f1x : f1y) : (k == 0 ? f2x : f2y);
+        double *dst = b == 0 ? (k == 0 ? S.r1x : S.r1y) : (k == 0 ? S.r2x : S.r2y);
+        double carry = s0;
+        for (int c0 = 1; c0 < m; c0 += 32) {
+          const int t = c0 + lane;
+          const bool act = t < m;
+          double Ac = 1.0, Bc = 0.0;
+          if (act) {
+            const double2 ab = bridge_coef(c, m, t);
+            Ac = ab.x;
+            Bc = fma(1.0 - ab.x, e, S.z[2 * (b * (m - 1) + t - 1) + k] * ab.y);
+          }
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const double Ap = __shfl_up_sync(0xffffffffu, Ac, off);
+            const double Bp = __shfl_up_sync(0xffffffffu, Bc, off);
+            if (lane >= off) {
+              Bc = fma(Ac, Bp, Bc);
+              Ac *= Ap;
+            }
+          }
+          const double pv = fma(Ac, carry, Bc);
+          if (act) dst[t] = pv;
+          carry = __shfl_sync(0xffffffffu, pv, 31);
+        }
+      }
+    } else if (lead && lane < 2 * dim) {
       const int b = lane / dim, k = lane % dim;
       double p = b == 0 ? (k == 0 ? s1x : s1y) : (k == 0 ? s2x : s2y);
       const double e = b == 0 ? (k == 0 ? f1x : f1y) : (k == 0 ? f2x : f2y);
@@ -742,8 +812,13 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   auto nown2 = [&](int t) { return (j0 + t < M) ? n2 : nn2; };
   for (int t = 1 + tid; t <= m; t += nt) {
     const int j = slc(t);
-    c.set_pos(nown1(t), j, S.r1x[t], S.r1y[t]);
-    c.set_pos(nown2(t), j, S.r2x[t], S.r2y[t]);
+    if (any_pair) {  // the new beads' mirror words are at hand
+      c.set_pos_q(nown1(t), j, S.r1x[t], S.r1y[t], S.q1[t]);
+      c.set_pos_q(nown2(t), j, S.r2x[t], S.r2y[t], S.q2[t]);
+    } else {
+      c.set_pos(nown1(t), j, S.r1x[t], S.r1y[t]);
+      c.set_pos(nown2(t), j, S.r2x[t], S.r2y[t]);
+    }
   }
   for (int t = tid; t < m; t += nt) {
     const int j = slc(t);
