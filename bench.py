@@ -355,6 +355,8 @@ def run_ours(args):
     eng = Engine(chains)
     for i, m in enumerate(mixes):
         eng.set_mix(m, chain=i)
+    if args.cells is not None or args.crowding is not None:
+        eng.set_cells(1 if args.cells is None else args.cells, args.crowding)
     table = None
     if args.workload == "contact":
         t0 = time.perf_counter()
@@ -367,13 +369,16 @@ def run_ours(args):
     launch = None
     if batched and args.launch:
         f = args.launch.split(":")
+        # per phase: CTA size, "w<size>" for one warp per chain, "<size>r<regs>"
+        # for the swap kernel compiled for 170 or 255 registers
         pb = f[5].split(",") if len(f) > 5 else ["0", "0", "0"]
         eng.set_launch(block=int(f[1]), sweeps_per_launch=int(f[2]),
                        state_smem_bytes=int(f[3]) if len(f) > 3 else 0,
                        warp_per_chain=f[0] == "warp",
                        split_phases=int(f[4]) if len(f) > 4 else 0,
-                       phase_block=[int(b.lstrip("w")) for b in pb],
-                       phase_warp=[int(b.startswith("w")) for b in pb])
+                       phase_block=[int(b.lstrip("w").split("r")[0]) for b in pb],
+                       phase_warp=[int(b.startswith("w")) for b in pb],
+                       phase_regs=[int(b.split("r")[1]) if "r" in b else 0 for b in pb])
         launch = dict(eng.launch, tuned=False)
     elif batched and args.tune:
         launch = eng.tune(sweeps_per_trial=1)
@@ -423,7 +428,10 @@ def run_ours(args):
                            else f"dp{ws} (independent replicas per GPU)"),
            "l2": (f"chain state {state_bytes / 1e9:.2f} GB > 129 MB L2"
                   if state_bytes > 129e6 else f"chain state {state_bytes / 1e6:.1f} MB (L2/shared resident)"),
-           "bead_updates_per_step": beads / args.steps}
+           "bead_updates_per_step": beads / args.steps,
+           "neighbour_candidates": ({0: "slice scan", 2: "cell lists"}.get(args.cells)
+                                    or "cell lists where they pay (crowding bound "
+                                    f"{0.5 if args.crowding is None else args.crowding}), else slice scan")}
     if batched and launch:
         cfg["launch"] = dict({"tuned": True}, **launch)
     out["config"] = cfg
@@ -629,6 +637,11 @@ def main():
                     help="fixed batched launch shape instead of tuning: "
                          "cta:BLOCK:SPL:STATE_BYTES[:SPLIT[:STAGE,SWAP,REST]] or warp:BLOCK:SPL; "
                          "a phase size written wNNN runs that phase with one warp per chain")
+    ap.add_argument("--cells", type=int, default=None, choices=[0, 1, 2],
+                    help="neighbour candidates: 0 slice scan, 1 cell lists where they pay "
+                         "(the engine's default), 2 cell lists always")
+    ap.add_argument("--crowding", type=float, default=None,
+                    help="cell-list crowding bound of mode 1 (default 0.5)")
     ap.add_argument("--adjoint", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the batched adjoint timing")

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PIMC_ABI_VERSION 3
+#define PIMC_ABI_VERSION 4
 /* columns of an observable row (pimc_get_observables) */
 #define PIMC_NOBS 8
 
@@ -186,6 +186,10 @@ typedef struct {
    * of a phase_block-thread CTA its own chain, phase_block <= 256); the swap
    * phase (index 1) only */
   int phase_warp[3];
+  /* with split_phases, the swap phase (index 1) with one CTA of at most 64
+   * threads per chain: its kernel compiled for at most 170 or 255 registers
+   * a thread (6 or 4 resident CTAs per SM) instead of 128 (0 or 128) */
+  int phase_regs[3];
 } pimc_launch;
 /* time candidate launch shapes on the handle's own chains and keep the
  * fastest; the chains are restored afterwards.  chosen may be NULL. */
@@ -389,8 +393,21 @@ int pimc_last_run_launches(void *handle, long long *launches);
  * from the exact FP64 sums, without the bounded shortcuts (pair-sum
  * estimates from the position mirror, FP32 log-space Metropolis tests, the
  * reference rules' pair-free early accept).  Both ways give the same chains
- * bit for bit; the option exists to show it. */
-enum { PIMC_OPT_FORCE_WARP_WINDOW = 1, PIMC_OPT_EXACT_DECISIONS = 2 };
+ * bit for bit; the option exists to show it.
+ * PIMC_OPT_CELL_LISTS: the sweeps' neighbour queries (the cell grid of
+ * find_nns, src/nearest_neighbours.jl:26-154) take their candidates from
+ * per-slice cell lists (value 2), from a scan of the whole slice (0), or
+ * from the lists except on slices whose cells are too crowded for them to
+ * pay (1, the default): 3^dim sum over cells of n_c^2 above the crowding
+ * bound times N^2.  PIMC_OPT_CELL_CROWDING sets that bound in thousandths
+ * (default 500).  The neighbour sets are the same every way; the order in
+ * which a query sums its pairs is not, so the exact sums may differ in
+ * their last bits.  Chains whose cells would be fewer than 5 per axis
+ * always scan. */
+enum {
+  PIMC_OPT_FORCE_WARP_WINDOW = 1, PIMC_OPT_EXACT_DECISIONS = 2, PIMC_OPT_CELL_LISTS = 3,
+  PIMC_OPT_CELL_CROWDING = 4
+};
 int pimc_set_option(void *handle, int key, long long value);
 const char *pimc_last_error(void);
 int pimc_abi_version(void);

@@ -55,6 +55,7 @@ struct Plan {
   size_t psmem[3] = {0, 0, 0}; // split: dynamic shared bytes per phase
   int pwarp[3] = {0, 0, 0};    // split: 1 = that phase with one warp per chain
   int pwarp_bytes[3] = {0, 0, 0};  // ... and the scratch bytes of each warp
+  int pregs[3] = {0, 0, 0};    // split, swap phase: register variant (0, 170, 255)
 };
 
 // CTA size and dynamic shared bytes of phase ph of a plan
@@ -205,6 +206,24 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   const size_t sb = 8 * (size_t)(p.dim + 1) * nm + 4 * nm + 4 * (size_t)p.N;
   d.smem_bytes = sb > (size_t)(1 << 30) ? (1 << 30) : (int)((sb + 15) & ~(size_t)15);
   return d;
+}
+
+// cells per axis of a chain's cell lists: each cell at least as wide as the
+// largest mirror prefilter radius (pair range, hard core), no more than about
+// four cells per particle; 0 (no lists) below 5 per axis, where the block of
+// cells around a centre covers most of the box
+int cell_count(const ChainDesc &d) {
+  if (!(d.flags & (PF_PAIR | PF_HARD))) return 0;
+  unsigned lim = 0;
+  if (d.flags & PF_PAIR) lim = std::max(lim, d.q_lim_rc);
+  if (d.flags & PF_HARD) lim = std::max(lim, d.q_lim_hard);
+  unsigned long long r = (unsigned long long)std::ceil(std::sqrt((double)lim));
+  while (r * r < lim) ++r;
+  if (r < 1) r = 1;
+  long long nc = 65536 / (long long)r;
+  const long long most = d.dim == 2 ? (long long)std::floor(std::sqrt(4.0 * d.N)) : 4LL * d.N;
+  nc = std::min(nc, std::max(most, 5LL));
+  return nc >= 5 ? (int)nc : 0;
 }
 
 pimc_move_mix default_mix(const pimc_params &p) {
@@ -415,6 +434,17 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     d.eser_off = p.energy_capacity > 0 ? (long long)dp : -1;
     dp += (size_t)NOBS * p.energy_capacity;
     d.next_off = (long long)ip; ip += p.N;
+    d.cl_nc = cell_count(d);
+    d.cl_cap = std::min(p.N, std::max(32, p.N / 4));
+    d.cl_mode = 1;
+    d.cl_frac = 0.5f;
+    if (d.cl_nc > 0) {
+      const CellLayout cl = cell_layout(p.N, p.M, p.dim == 2 ? d.cl_nc * d.cl_nc : d.cl_nc, d.cl_cap);
+      d.cl_off = (long long)ip;
+      ip += (size_t)cl.total;
+    } else {
+      d.cl_off = -1;
+    }
     if (p.density_nbins > 0) {
       d.dens_off = (long long)up;
       up += p.dim == 2 ? (size_t)p.density_nbins * p.density_nbins : (size_t)p.density_nbins;
@@ -630,7 +660,7 @@ int swap_spec(const Handle *h) {
 int grid_for(Handle *h, const Plan &p, int phase = -1) {
   int per_sm = 0;
   const cudaError_t e = phase >= 0
-                            ? sweep_phase_occupancy(phase, p.pwarp[phase], swap_spec(h),
+                            ? sweep_phase_occupancy(phase, p.pwarp[phase], swap_spec(h), p.pregs[phase],
                                                     phase_block(p, phase), phase_smem(p, phase), &per_sm)
                             : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
@@ -646,7 +676,7 @@ int grid_for(Handle *h, const Plan &p, int phase = -1) {
 bool launch_teams(Handle *h, const Plan &p) {
   int per_sm = 0;
   if (p.mode != 0) return false;
-  const cudaError_t e = p.split ? sweep_phase_occupancy(0, 0, 0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
+  const cudaError_t e = p.split ? sweep_phase_occupancy(0, 0, 0, 0, phase_block(p, 0), phase_smem(p, 0), &per_sm)
                                 : sweep_occupancy(p.mode, p.block, p.dyn_smem, &per_sm);
   if (e != cudaSuccess) return false;
   return h->nchains <= per_sm * h->num_sms;
@@ -656,7 +686,7 @@ bool launch_teams(Handle *h, const Plan &p) {
 cudaError_t plan_set_smem(const Handle *h, const Plan &p) {
   if (!p.split) return sweep_set_smem(p.mode, p.dyn_smem);
   for (int ph = 0; ph < 3; ++ph) {
-    const cudaError_t e = sweep_phase_set_smem(ph, p.pwarp[ph], swap_spec(h), phase_smem(p, ph));
+    const cudaError_t e = sweep_phase_set_smem(ph, p.pwarp[ph], swap_spec(h), p.pregs[ph], phase_smem(p, ph));
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -680,7 +710,7 @@ cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long
       if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
       cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
       if (e == cudaSuccess)
-        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), grid_for(h, p, ph),
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), p.pregs[ph], grid_for(h, p, ph),
                                phase_block(p, ph), phase_smem(p, ph), h->stream);
       if (e != cudaSuccess) return e;
       if (launches) *launches += 1;
@@ -1120,7 +1150,13 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
   for (int ph = 0; ph < 3; ++ph) {
     const int b = l.phase_block[ph];
     const int w = l.phase_warp[ph];
+    const int rg = l.phase_regs[ph] == 128 ? 0 : l.phase_regs[ph];
     if (w != 0 && w != 1) return fail(PIMC_EARG, "phase_warp must be 0 or 1");
+    if (rg != 0 && rg != 170 && rg != 255) return fail(PIMC_EARG, "phase_regs must be 0, 128, 170 or 255");
+    if (rg && (!l.split_phases || ph != 1 || w || (b > 0 ? b : l.block) > 64))
+      return fail(PIMC_EARG,
+                  "phase_regs: 170 and 255 are offered for the swap phase of a split sweep in CTAs of 64 threads");
+    p.pregs[ph] = rg;
     if (w && (!l.split_phases || ph != 1))
       return fail(PIMC_EARG, "phase_warp: one warp per chain is offered for the swap phase of a split sweep");
     if (w) {
@@ -1175,7 +1211,7 @@ int pimc_batch_phase_times(void *handle, long long n, double ms[3]) {
         SweepArgs b = a;
         b.sweeps = 1;
         if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
-        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), grid_for(h, p, ph),
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), p.pregs[ph], grid_for(h, p, ph),
                                phase_block(p, ph), phase_smem(p, ph), h->stream);
       } else {
         a.sweeps = 1;
@@ -1221,6 +1257,7 @@ int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
   for (int ph = 0; ph < 3; ++ph) {
     launch->phase_block[ph] = h->bat.pblock[ph];
     launch->phase_warp[ph] = h->bat.pwarp[ph];
+    launch->phase_regs[ph] = h->bat.pregs[ph];
   }
   return PIMC_OK;
 }
@@ -1298,7 +1335,7 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
     for (int b : {64, 128, 256}) {
       pimc_launch l = keep;
       l.block = b;
-      for (int ph = 0; ph < 3; ++ph) l.phase_block[ph] = 0;
+      for (int ph = 0; ph < 3; ++ph) l.phase_block[ph] = l.phase_warp[ph] = l.phase_regs[ph] = 0;
       Plan p;
       if (check_launch(h, l, &p)) continue;
       if ((rc = pimc_batch_set_launch(h, &l))) return rc;
@@ -1310,15 +1347,13 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
           pbest[ph] = ms[ph];
           ref.phase_block[ph] = b;
           ref.phase_warp[ph] = 0;
+          ref.phase_regs[ph] = 0;
         }
     }
     // the swap phase with one warp per chain, 2 to 8 chains per CTA
     for (int b : {64, 128, 256}) {
       pimc_launch l = keep;
-      for (int ph = 0; ph < 3; ++ph) {
-        l.phase_block[ph] = 0;
-        l.phase_warp[ph] = 0;
-      }
+      for (int ph = 0; ph < 3; ++ph) l.phase_block[ph] = l.phase_warp[ph] = l.phase_regs[ph] = 0;
       l.phase_block[1] = b;
       l.phase_warp[1] = 1;
       Plan p;
@@ -1331,6 +1366,27 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
         pbest[1] = ms[1];
         ref.phase_block[1] = b;
         ref.phase_warp[1] = 1;
+        ref.phase_regs[1] = 0;
+      }
+    }
+    // the swap phase in CTAs of 64 threads with the kernels compiled for 170
+    // and 255 registers a thread (fewer spills, fewer chains per SM)
+    for (int rg : {170, 255}) {
+      pimc_launch l = keep;
+      for (int ph = 0; ph < 3; ++ph) l.phase_block[ph] = l.phase_warp[ph] = l.phase_regs[ph] = 0;
+      l.phase_block[1] = 64;
+      l.phase_regs[1] = rg;
+      Plan p;
+      if (check_launch(h, l, &p)) continue;
+      if ((rc = pimc_batch_set_launch(h, &l))) return rc;
+      double ms[3];
+      if ((rc = pimc_batch_phase_times(h, 1, ms))) return rc;  // warm
+      if ((rc = pimc_batch_phase_times(h, sweeps_per_trial, ms))) return rc;
+      if (ms[1] < pbest[1]) {
+        pbest[1] = ms[1];
+        ref.phase_block[1] = 64;
+        ref.phase_warp[1] = 0;
+        ref.phase_regs[1] = rg;
       }
     }
     Plan p;
@@ -2223,6 +2279,18 @@ int pimc_set_option(void *handle, int key, long long value) {
   if (key == PIMC_OPT_FORCE_WARP_WINDOW) {
     h->force_warp = value != 0;
     return PIMC_OK;
+  }
+  if (key == PIMC_OPT_CELL_LISTS || key == PIMC_OPT_CELL_CROWDING) {
+    if (key == PIMC_OPT_CELL_LISTS && (value < 0 || value > 2))
+      return fail(PIMC_EARG, "cell lists: 0 off, 1 auto, 2 always");
+    if (key == PIMC_OPT_CELL_CROWDING && (value < 1 || value > 1000000))
+      return fail(PIMC_EARG, "cell crowding bound in thousandths must be in [1, 1e6]");
+    for (auto &d : h->desc) {
+      if (key == PIMC_OPT_CELL_LISTS) d.cl_mode = (int)value;
+      else d.cl_frac = (float)(value / 1000.0);
+    }
+    if (upload_desc(h)) return PIMC_ECUDA;
+    return sync_check(h);
   }
   if (key == PIMC_OPT_EXACT_DECISIONS) {
     for (auto &d : h->desc) d.flags = value ? (d.flags | PF_EXACT) : (d.flags & ~PF_EXACT);

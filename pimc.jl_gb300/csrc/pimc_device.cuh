@@ -7,13 +7,16 @@
 // of one imaginary-time slice contiguous, a bead's coordinates in one 16-byte
 // unit, so that gathering a neighbour touches one sector), cached links
 // V[j][n].  Thread-per-window staging reads slices of consecutive particles
-// (coalesced), and a neighbour query at slice j is a contiguous row.  Every chain keeps a
-// 16-bit fixed-point mirror xq[j][n] of the positions (one 32-bit word per
-// bead): a warp scans the row with integer arithmetic and a bound that
-// covers the rounding, and evaluates the few candidates exactly in FP64, so
-// the neighbour set is exactly the reference's (every bead within 2L/nbins,
-// src/nearest_neighbours.jl:131-154) without a linked cell grid to chase or
-// maintain.
+// (coalesced).  Every chain keeps a 16-bit fixed-point mirror xq[j][n] of the
+// positions (one 32-bit word per bead): a neighbour query tests candidates
+// with integer arithmetic and a bound that covers the rounding, and evaluates
+// the few that pass exactly in FP64, so the neighbour set is exactly the
+// reference's (every bead within 2L/nbins, src/nearest_neighbours.jl:131-154).
+// The candidates come from per-slice cell lists (the reference's cell grid,
+// src/nearest_neighbours.jl:26-104: a counting sort of the slice's mirror
+// words, rebuilt at the start of every phase that queries, moved beads
+// tracked on the side) or, for slices whose cells are too crowded to pay,
+// from a scan of the whole slice row.
 //
 // Reference correspondence (oameye/PIMC.jl):
 //   distance / lnK / lnV / teleport      src/propagator.jl:6-32
@@ -53,8 +56,9 @@ constexpr int RES_REJECT = 0, RES_ACCEPT = 1, RES_SKIP = 2, RES_HARDCORE = 3;
 #ifndef PIMC_CHECK
 #define PIMC_CHECK 0
 #endif
-// defined here: only the kernel translation unit includes this header
-__device__ unsigned long long g_check_word;
+// one per kernel translation unit (static), read by the host through each
+// unit's accessor
+static __device__ unsigned long long g_check_word;
 
 __device__ __forceinline__ bool check_ok(bool cond, int code, const ChainDesc &d) {
 #if PIMC_CHECK
@@ -75,8 +79,8 @@ __device__ __forceinline__ bool check_ok(bool cond, int code, const ChainDesc &d
 #ifndef PIMC_PROFILE
 #define PIMC_PROFILE 0
 #endif
-// defined here: only the kernel translation unit includes this header
-__device__ unsigned long long g_prof[32];
+// one per kernel translation unit (static)
+static __device__ unsigned long long g_prof[32];
 #if PIMC_PROFILE
 #define PROF_DECL long long prof_t_ = clock64()
 #define PROF_MARK(slot)                                                              \
@@ -251,6 +255,94 @@ __device__ __forceinline__ unsigned qdist2(unsigned a, unsigned b) {
 }
 
 // ---------------------------------------------------------------------------
+// per-slice cell lists (the cell grid of src/nearest_neighbours.jl:26-104)
+//
+// A slice's particles sorted by the cell of their mirror word, nc cells per
+// axis on the 16-bit periodic mirror, each at least as wide as the largest
+// prefilter radius in mirror units: a particle that passes a prefilter
+// around a centre lies in the 3 x 3 block of cells (3 in 1D) around the
+// centre's cell.  The lists are built (a stable counting sort: the particles
+// of a cell in index order) at the start of every phase that queries them;
+// a particle whose bead moves afterwards is flagged in items (bit 15: its
+// cell is stale, queries skip the entry) and appended to the slice's list of
+// moved particles, which every query of the slice takes in full.  Each
+// slice's moves are marked by one thread in a fixed order, so the lists, and
+// with them the order in which a query visits candidates, are a function of
+// the chain's history.  A slice whose moved list overflows, or whose build
+// found the cells too crowded to pay (dn = kCellOff), is scanned row-wise.
+// ---------------------------------------------------------------------------
+constexpr int kCellOff = 1 << 30;
+
+struct CellLists {
+  int N, nc, ncq, cap, nw;
+  int *end;              // end[j*(ncq+1) + c]: end of cell c's entries (begin: end[c-1], or 0)
+  int *dn;               // dn[j]: moved particles since the build (kCellOff: row scan)
+  unsigned *moved;       // moved[j*nw + w]: bitmask of the moved particles
+  unsigned short *items; // items[j*N + k]: particles in cell order; bit 15 = moved
+  unsigned short *pos;   // pos[j*N + n]: the index of particle n in items
+  unsigned short *dl;    // dl[j*cap + k]: moved particles, in the order of their first move
+  __device__ __forceinline__ void bind(const ChainDesc &d, int *ipool) {
+    N = d.N;
+    nc = d.cl_nc;
+    ncq = d.dim > 1 ? nc * nc : nc;
+    cap = d.cl_cap;
+    nw = (d.N + 31) >> 5;
+    const CellLayout l = cell_layout(d.N, d.M, ncq, cap);
+    int *b = ipool + d.cl_off;
+    end = b + l.end;
+    dn = b + l.dn;
+    moved = (unsigned *)(b + l.moved);
+    items = (unsigned short *)(b + l.items);
+    pos = (unsigned short *)(b + l.pos);
+    dl = (unsigned short *)(b + l.dl);
+  }
+  __device__ __forceinline__ int cx(unsigned q) const {
+    return (int)(((q & 0xffffu) * (unsigned)nc) >> 16);
+  }
+  __device__ __forceinline__ int cy(unsigned q) const {
+    return ncq == nc ? 0 : (int)(((q >> 16) * (unsigned)nc) >> 16);
+  }
+  __device__ __forceinline__ int cell(unsigned q) const { return cx(q) + nc * cy(q); }
+  // particle n's bead at slice j has moved since the build.  The marks of a
+  // slice within one move come from one thread (plain loads and stores: the
+  // three reads are independent, one round trip)
+  __device__ __forceinline__ void mark(int n, int j) const {
+    unsigned *w = moved + (size_t)j * nw + (n >> 5);
+    const unsigned bit = 1u << (n & 31);
+    const unsigned old = *w;
+    const int k = dn[j];
+    const unsigned short p = pos[(size_t)j * N + n];
+    if (old & bit) return;
+    *w = old | bit;
+    dn[j] = k + 1;
+    if (k < cap) {
+      items[(size_t)j * N + p] = (unsigned short)(n | 0x8000);  // the entry of n, flagged
+      dl[(size_t)j * cap + k] = (unsigned short)n;
+    }
+  }
+  // particles a and b trade their beads at slice j.  When neither has moved
+  // since the build the lists stay exact by trading the two entries (the
+  // set of positions is unchanged); otherwise both are marked.
+  __device__ __forceinline__ void trade(int a, int b, int j) const {
+    const unsigned *mw = moved + (size_t)j * nw;
+    const unsigned wa = mw[a >> 5], wb = mw[b >> 5];
+    unsigned short *it = items + (size_t)j * N, *ps = pos + (size_t)j * N;
+    const unsigned short pa = ps[a], pb = ps[b];
+    if (((wa >> (a & 31)) & 1u) == 0u && ((wb >> (b & 31)) & 1u) == 0u) {
+      it[pa] = (unsigned short)b;
+      it[pb] = (unsigned short)a;
+      ps[a] = pb;
+      ps[b] = pa;
+      return;
+    }
+    mark(a, j);
+    mark(b, j);
+  }
+  // whether queries of slice j use the lists (uniform across the warp)
+  __device__ __forceinline__ bool usable(int j) const { return dn[j] <= cap; }
+};
+
+// ---------------------------------------------------------------------------
 // chain view: x/V/next/xq may live in shared or global memory (generic pointers)
 // ---------------------------------------------------------------------------
 struct CV {
@@ -262,6 +354,9 @@ struct CV {
   const double2 *tab; // (alpha, sigma)[m*wtab + t]
   unsigned long long *hist;
   double *eser;
+  // the chain's cell lists while a phase maintains them (moves mark, queries
+  // use them); nullptr: every query scans its row, moves mark nothing
+  const CellLists *cl;
   int N, M, dim, ldn;
   __device__ __forceinline__ double &X(int k, int n, int j) const {
     return x[((size_t)j * ldn + n) * dim + k];
@@ -271,17 +366,20 @@ struct CV {
     return k < dim ? X(k, n, j) : 0.0;
   }
   __device__ __forceinline__ unsigned Q(int n, int j) const { return xq[(size_t)j * ldn + n]; }
-  // every position write goes through here so that the mirror follows
+  // every position write goes through here so that the mirror and the cell
+  // lists follow; the writes of one slice within a move come from one thread
   __device__ __forceinline__ void set_pos(int n, int j, double px, double py) const {
     X(0, n, j) = px;
     if (dim > 1) X(1, n, j) = py;
     xq[(size_t)j * ldn + n] = qpos(*d, px, py);
+    if (cl) cl->mark(n, j);
   }
   // the same with the mirror word already computed (qpos of px, py)
   __device__ __forceinline__ void set_pos_q(int n, int j, double px, double py, unsigned q) const {
     X(0, n, j) = px;
     if (dim > 1) X(1, n, j) = py;
     xq[(size_t)j * ldn + n] = q;
+    if (cl) cl->mark(n, j);
   }
   // exchange the beads of particles a and b at slice j, mirror included
   __device__ __forceinline__ void exchange(int a, int b, int j) const {
@@ -294,8 +392,111 @@ struct CV {
     const unsigned t = r[a];
     r[a] = r[b];
     r[b] = t;
+    if (cl) cl->trade(a, b, j);
   }
 };
+
+// ---------------------------------------------------------------------------
+// cell-list queries.  Every lane of the warp calls them; f(b, valid, sides)
+// is called by every lane, 32 candidates at a time (valid: the lane holds
+// candidate b; sides: bit 0 the query's first centre, bit 1 its second).
+// ---------------------------------------------------------------------------
+// the candidates of slice j in the periodic block of cells [x0, x0+nx) x
+// [y0, y0+ny) (nx <= nc, ny <= min(nc, 4)), skipping moved entries, then the
+// slice's moved particles
+template <class F>
+__device__ __forceinline__ void cell_block(const CellLists &L, int j, int x0, int nx, int y0, int ny,
+                                           unsigned sides, int lane, F &&f) {
+  const int *E = L.end + (size_t)j * (L.ncq + 1);
+  // lane k < 2 ny holds segment k: row k/2, its columns up to the wrap
+  // (part 0) and past it (part 1): first entry and length
+  int st = 0, len = 0;
+  if (lane < 2 * ny) {
+    const int r = lane >> 1, part = lane & 1;
+    int y = y0 + r;
+    if (y >= L.nc) y -= L.nc;
+    const int xe = x0 + nx - 1;
+    int xa, xb;
+    if (xe < L.nc) {
+      xa = part ? 1 : x0;
+      xb = part ? 0 : xe;
+    } else {
+      xa = part ? 0 : x0;
+      xb = part ? xe - L.nc : L.nc - 1;
+    }
+    if (xa <= xb) {
+      const int c0 = y * L.nc + xa, c1 = y * L.nc + xb;
+      st = c0 ? E[c0 - 1] : 0;
+      len = E[c1] - st;
+    }
+  }
+  int incl = len;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int S = __shfl_sync(0xffffffffu, incl, 7);
+  const int excl = incl - len;
+  const int D = L.dn[j];
+  const unsigned short *items = L.items + (size_t)j * L.N, *dl = L.dl + (size_t)j * L.cap;
+  for (int f0 = 0; f0 < S + D; f0 += 32) {
+    const int fl = f0 + lane;
+    // the segment of entry fl: the last one that starts at or before it
+    int k = 0;
+#pragma unroll
+    for (int kk = 1; kk < 8; ++kk)
+      if (fl >= __shfl_sync(0xffffffffu, excl, kk)) k = kk;
+    const int sk = __shfl_sync(0xffffffffu, st, k), ek = __shfl_sync(0xffffffffu, excl, k);
+    int b = -1;
+    if (fl < S) {
+      const unsigned it = items[sk + fl - ek];
+      if (!(it & 0x8000u)) b = (int)it;
+    } else if (fl < S + D) {
+      b = (int)dl[fl - S];
+    }
+    f(b, b >= 0, sides);
+  }
+}
+
+// the cell-list candidates of a query at slice j around the mirror words qa
+// and qb (the old and the new position of a moving bead; qa == qb for one
+// centre).  Centres in the same or in adjacent cells share one block of
+// cells (sides 3 for every candidate); farther apart each has its own.
+// Returns false, having called nothing, when slice j has no usable lists.
+template <class F>
+__device__ __forceinline__ bool cell_query(const CellLists *L, int j, unsigned qa, unsigned qb,
+                                           int lane, F &&f) {
+  if (!L || !L->usable(j)) return false;
+  const int nc = L->nc, h = nc >> 1;
+  const int ax = L->cx(qa), ay = L->cy(qa), bx = L->cx(qb), by = L->cy(qb);
+  int dx = bx - ax, dy = by - ay;
+  if (dx > h) dx -= nc; else if (dx < -h) dx += nc;
+  if (dy > h) dy -= nc; else if (dy < -h) dy += nc;
+  const bool two = L->ncq != nc;
+  auto wrap = [&](int v) { return v < 0 ? v + nc : (v >= nc ? v - nc : v); };
+  const bool joint = abs(dx) <= 1 && abs(dy) <= 1;
+  // one call site: the block is inlined once
+  for (int k = 0; k < (joint ? 1 : 2); ++k) {
+    int x0, nx, y0, ny;
+    unsigned sides;
+    if (joint) {
+      x0 = wrap(min(ax, ax + dx) - 1);
+      nx = 3 + abs(dx);
+      y0 = two ? wrap(min(ay, ay + dy) - 1) : 0;
+      ny = two ? 3 + abs(dy) : 1;
+      sides = 3u;
+    } else {
+      x0 = wrap((k ? bx : ax) - 1);
+      nx = 3;
+      y0 = two ? wrap((k ? by : ay) - 1) : 0;
+      ny = two ? 3 : 1;
+      sides = k ? 2u : 1u;
+    }
+    cell_block(*L, j, x0, nx, y0, ny, sides, lane, f);
+  }
+  return true;
+}
 
 // ---------------------------------------------------------------------------
 // action pieces (src/propagator.jl)
@@ -328,7 +529,7 @@ __device__ __forceinline__ double sgn(double v) { return v > 0.0 ? 1.0 : (v < 0.
 // with phi_k = 2 pi scale (x sin a_k + y cos a_k) (+ a_k when helical),
 // S = (1/K) sum sin phi_k, C = (1/K) sum cos phi_k, I = S^2 + C^2; optionally
 // the gradient of I
-__device__ __noinline__ double beam_intensity(const ChainDesc &d, double x, double y, double *gx,
+static __device__ __noinline__ double beam_intensity(const ChainDesc &d, double x, double y, double *gx,
                                               double *gy) {
   double S = 0.0, Cc = 0.0, sx = 0.0, sy = 0.0, cx = 0.0, cy = 0.0;
   for (int k = 0; k < d.nbeam; ++k) {
@@ -407,8 +608,8 @@ __device__ __forceinline__ void grad_vext(const ChainDesc &d, double x, double y
 // against the library's longer range reduction and polynomial.  Arguments
 // below -40 (pair terms of far-away next beads) go to the library exp.
 constexpr int EXPTAB_N = 2560;
-// defined here: only the kernel translation unit includes this header
-__device__ double g_exptab[EXPTAB_N + 1];
+// one per kernel translation unit (static), both filled by the host
+static __device__ double g_exptab[EXPTAB_N + 1];
 
 __device__ __forceinline__ double exp_neg(double x) {
   if (!(x >= -40.0)) return exp(x);
@@ -510,7 +711,7 @@ __device__ __forceinline__ double contact_lnU(const ChainDesc &d, double d1x, do
 
 // contact_lnU from the four beads of a link pair (a, b at slice j; an, bn at
 // slice j+1), kept out of line: the Gaussian pair path does not carry its code
-__device__ __noinline__ double contact_link(const ChainDesc &d, double ax, double ay, double bx,
+static __device__ __noinline__ double contact_link(const ChainDesc &d, double ax, double ay, double bx,
                                             double by, double anx, double any, double bnx,
                                             double bny) {
   const bool two = d.dim > 1;
@@ -614,18 +815,13 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
   int qn = 0;
   for (int t = t0; t < t1; ++t) {
     const int j = s.slice(t);
+    const unsigned co = s.curq(0, t), cn = s.curq(1, t);
     Prefilter fo, fn;
-    fo.init_q(s.curq(0, t), d.q_lim_rc);
-    fn.init_q(s.curq(1, t), d.q_lim_rc);
+    fo.init_q(co, d.q_lim_rc);
+    fn.init_q(cn, d.q_lim_rc);
     const unsigned *row = c.xq + (size_t)j * c.ldn;
-    for (int b0 = 0; b0 < N; b0 += 32) {
-      const int b = b0 + lane;
-      bool po = false, pn = false;
-      if (b < N) {
-        const unsigned pb = row[b];
-        po = do_old && fo.pass(pb) && !s.skip(0, t, b);
-        pn = do_new && fn.pass(pb) && !s.skip(1, t, b);
-      }
+    // every lane calls push with its candidate's outcome, old and new side
+    auto push = [&](int b, bool po, bool pn) {
       const unsigned mo = __ballot_sync(0xffffffffu, po), mn = __ballot_sync(0xffffffffu, pn);
       const unsigned long long base = ((unsigned long long)(unsigned)b << 32) | ((unsigned)t << 1);
       if (po) {
@@ -642,10 +838,30 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
       if (qn > PQ_CAP) qn = PQ_CAP;
 #endif
       __syncwarp();
-      // a block of 32 particles queues up to 64 entries (old and new): drain
-      // to fewer than 32 before the next block, so that the queue holds at
-      // most 31 + 64 = 95 < PQ_CAP entries at any time
+      // a block of 32 candidates queues up to 64 entries (old and new):
+      // drain to fewer than 32 before the next block, so that the queue
+      // holds at most 31 + 64 = 95 < PQ_CAP entries at any time
       while (qn >= 32) pq_flush<CT>(c, s, q, qn, wo, wn, lane);
+    };
+    const bool listed = cell_query(c.cl, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
+      bool po = false, pn = false;
+      if (v) {
+        const unsigned pb = row[b];
+        po = (sides & 1u) && do_old && fo.pass(pb) && !s.skip(0, t, b);
+        pn = (sides & 2u) && do_new && fn.pass(pb) && !s.skip(1, t, b);
+      }
+      push(b, po, pn);
+    });
+    if (listed) continue;
+    for (int b0 = 0; b0 < N; b0 += 32) {
+      const int b = b0 + lane;
+      bool po = false, pn = false;
+      if (b < N) {
+        const unsigned pb = row[b];
+        po = do_old && fo.pass(pb) && !s.skip(0, t, b);
+        pn = do_new && fn.pass(pb) && !s.skip(1, t, b);
+      }
+      push(b, po, pn);
     }
   }
   while (qn > 0) pq_flush<CT>(c, s, q, qn, wo, wn, lane);
@@ -751,7 +967,28 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
         est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
       }
     };
-    if (!wrap) {
+    // a cell-list candidate: the sides its block serves, the word at slice
+    // j+1 read only for a pair that passes
+    const bool listed = cell_query(c.cl, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
+      if (!v) return;
+      const unsigned pb = row[b];
+      const unsigned d2o = qdist2(co, pb), d2n = qdist2(cn, pb);
+      const bool io = (sides & 1u) && d2o <= d.q_lim_hi && !s.skip(0, t, b);
+      const bool in = (sides & 2u) && d2n <= d.q_lim_hi && !s.skip(1, t, b);
+      if (!io && !in) return;
+      const unsigned pbn = rown[wrap ? c.next[b] : b];
+      bool edge;
+      if (io) {
+        const unsigned d2b = qdist2_w(no, pbn, edge);
+        est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
+      }
+      if (in) {
+        const unsigned d2b = qdist2_w(nn, pbn, edge);
+        est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
+      }
+    });
+    if (listed) {
+    } else if (!wrap) {
       // the words at both slices are read together, two blocks of 32
       // candidates at a time, so that one round trip to memory serves four
       // loads (the latency, not the bytes, bounds this scan); the lane's
@@ -864,6 +1101,12 @@ __device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, 
   f.init(d, x, y, d.q_lim_hard);
   const unsigned *row = c.xq + (size_t)j * c.ldn;
   bool hit = false;
+  // the cell lists serve whole warps only
+  if (lanes == 32 && cell_query(c.cl, j, f.c, f.c, lane, [&](int b, bool v, unsigned) {
+        if (!v || hit || b == e1 || b == e2 || !f.pass(row[b])) return;
+        if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;
+      }))
+    return hit;
   for (int b = lane; b < N && !hit; b += lanes) {
     if (b == e1 || b == e2 || !f.pass(row[b])) continue;
     if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;

@@ -220,6 +220,104 @@ struct Group {
   }
 };
 
+// ---------------------------------------------------------------------------
+// build of a chain's cell lists from its mirror, every slice, by the whole
+// group (warps take slices).  Per slice a stable counting sort: pass 1 counts
+// the particles of each cell 32 at a time (lanes of one cell found by
+// match_any, the lowest adds), a scan turns the counts into starts, pass 2
+// places each particle at its cell's cursor plus its rank among the lanes of
+// its cell.  After pass 2 the cursors hold each cell's end, which is what
+// end[] keeps.  The counts live in the warp's share of the shared scratch ws
+// (ws_ints ints for the group) when it has room for ncq + 1 of them, else in
+// end[] itself.  cl_mode 1: a slice whose cells hold 3^dim sum n_c^2 >
+// cl_frac N^2 pairs (the block around a particle would hold most of the
+// slice) is marked for the row scan.
+// ---------------------------------------------------------------------------
+template <bool WARP>
+__device__ void cells_build(const CV &c, const CellLists &L, int *ws, int ws_ints) {
+  const ChainDesc &d = *c.d;
+  const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
+  const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
+  const int N = c.N, M = c.M, ne = L.ncq + 1;
+  const unsigned lt = (1u << lane) - 1u;
+  const bool local = ws && ws_ints >= ne;
+  // warps that build: with shared counts, as many as the scratch holds
+  const int nb = local ? min(nwarps, ws_ints / ne) : nwarps;
+  if (warp >= nb) return;
+  int *E = local ? ws + (size_t)warp * ne : nullptr;
+  for (int j = warp; j < M; j += nb) {
+    int *Eg = L.end + (size_t)j * ne;
+    if (!local) E = Eg;
+    for (int k = lane; k < ne; k += 32) E[k] = 0;
+    for (int w = lane; w < L.nw; w += 32) L.moved[(size_t)j * L.nw + w] = 0u;
+    __syncwarp();
+    const unsigned *row = c.xq + (size_t)j * c.ldn;
+    unsigned short *items = L.items + (size_t)j * N, *pos = L.pos + (size_t)j * N;
+    double sq = 0.0;  // sum over cells of n_c^2 (the lowest lanes' shares)
+    for (int b0 = 0; b0 < N; b0 += 32) {
+      const int b = b0 + lane;
+      const bool v = b < N;
+      const int ce = v ? L.cell(row[b]) : 0;
+      const unsigned act = __ballot_sync(0xffffffffu, v);
+      if (v) {
+        const unsigned peers = __match_any_sync(act, ce);
+        if ((peers & lt) == 0) {
+          const int old = E[ce + 1], k = __popc(peers);
+          E[ce + 1] = old + k;
+          sq += (double)k * (double)(2 * old + k);
+        }
+      }
+      __syncwarp();
+    }
+    // inclusive scan of the counts E[1..ncq]: E[c] = start of cell c
+    int carry = 0;
+    for (int k0 = 1; k0 < ne; k0 += 32) {
+      const int k = k0 + lane;
+      int v = k < ne ? E[k] : 0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+      }
+      v += carry;
+      if (k < ne) E[k] = v;
+      carry = __shfl_sync(0xffffffffu, v, 31);
+    }
+    __syncwarp();
+    for (int b0 = 0; b0 < N; b0 += 32) {
+      const int b = b0 + lane;
+      const bool v = b < N;
+      const int ce = v ? L.cell(row[b]) : 0;
+      const unsigned act = __ballot_sync(0xffffffffu, v);
+      int base = 0, rank = 0, k = 0;
+      if (v) {
+        const unsigned peers = __match_any_sync(act, ce);
+        rank = __popc(peers & lt);
+        k = __popc(peers);
+        base = E[ce];
+      }
+      __syncwarp();
+      if (v) {
+        const int p = base + rank;
+        if (check_ok(p >= 0 && p < N, DERR_INDEX, d)) {
+          items[p] = (unsigned short)b;
+          pos[b] = (unsigned short)p;
+        }
+        if (rank == 0) E[ce] = base + k;
+      }
+      __syncwarp();
+    }
+    if (local)
+      for (int k = lane; k < ne; k += 32) Eg[k] = E[k];
+    sq = warp_sum(sq);
+    if (lane == 0) {
+      const double pairs = (L.ncq == L.nc ? 3.0 : 9.0) * sq;
+      L.dn[j] = (d.cl_mode == 1 && pairs > (double)d.cl_frac * N * N) ? kCellOff : 0;
+    }
+    __syncwarp();
+  }
+}
+
 // heat-bath exponent -(|s - E|^2 + |x_i(j0) - f|^2) / (4 lambda m tau) with
 // E the end bead of particle i's path (or an explicit end): FP64 as the
 // reference (attempt parity), or FP32 from the position mirror (sweeps: the
@@ -1061,17 +1159,20 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
     }
   }
   G::sync();
-  for (int k = tid; k < np * M; k += nt) {
-    const int i = pol[k / M], j = k % M;
-    double qx, qy;
-    if (!polymer) {
-      qx = q[j];
-      qy = q[M + j];
-    } else {
-      shifted(i, j, qx, qy);
+  // one thread writes a slice's beads, in cycle order (the order in which
+  // the cell lists record the moves is then fixed)
+  for (int j = tid; j < M; j += nt)
+    for (int p = 0; p < np; ++p) {
+      const int i = pol[p];
+      double qx, qy;
+      if (!polymer) {
+        qx = q[j];
+        qy = q[M + j];
+      } else {
+        shifted(i, j, qx, qy);
+      }
+      c.set_pos(i, j, qx, qy);
     }
-    c.set_pos(i, j, qx, qy);
-  }
   G::sync();
   return RES_ACCEPT;
 }
@@ -1182,9 +1283,8 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
       Prefilter f;
       f.init_q(c.Q(i, j), d.q_lim_rc);
       const unsigned *row = c.xq + (size_t)j * c.ldn;
-      for (int b0 = i + 1; b0 < N; b0 += 32) {
-        const int b = b0 + lane;
-        const bool p = b < N && f.pass(row[b]);
+      // every lane calls push with whether its candidate b passed
+      auto push = [&](int b, bool p) {
         const unsigned mk = __ballot_sync(0xffffffffu, p);
         if (p) {
           const int k = qn + __popc(mk & lt);
@@ -1197,6 +1297,14 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
 #endif
         __syncwarp();
         if (qn >= 32) flush();
+      };
+      // partners of higher index: from the cell lists, or the rest of the row
+      if (cell_query(c.cl, j, f.c, f.c, lane,
+                     [&](int b, bool v, unsigned) { push(b, v && b > i && f.pass(row[b])); }))
+        continue;
+      for (int b0 = i + 1; b0 < N; b0 += 32) {
+        const int b = b0 + lane;
+        push(b, b < N && f.pass(row[b]));
       }
     }
     while (qn > 0) flush();

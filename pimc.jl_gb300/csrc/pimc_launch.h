@@ -103,10 +103,12 @@ cudaError_t sweep_set_smem(int mode, size_t smem);
 // spec = 1 selects the swap kernel compiled for the reference's rules alone
 // (every chain of the launch without physical rules, hard core or contact
 // table); a.sweeps must be 1
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int grid,
-                               int block, size_t smem, cudaStream_t s);
-cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, size_t smem);
-cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int block, size_t smem,
+// regs (swap phase in CTA mode): 0 the 128-register kernel, 170 or 255 the
+// kernels compiled for CTAs of at most 64 threads with that many registers
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int regs,
+                               int grid, int block, size_t smem, cudaStream_t s);
+cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, int regs, size_t smem);
+cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int regs, int block, size_t smem,
                                   int *blocks_per_sm);
 size_t sweep_ctl_bytes();
 cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm);
@@ -163,6 +165,20 @@ cudaError_t launch_contact_table(double *dtab, int n, double range, double g0, d
                                  cudaStream_t s);
 // measured FP64 FMA throughput of the current device (TFLOP/s)
 cudaError_t fp64_peak(int num_sms, cudaStream_t st, double *tflops);
+// the swap-phase kernels' translation unit (pimc_swap.cu): its kernel for a
+// launch shape and its launcher
+const void *swap_kernel(int warp, int spec, int regs);
+cudaError_t launch_swap(const SweepArgs &a, int warp, int spec, int regs, int grid, int block,
+                        size_t smem, cudaStream_t s);
+// accessors of each kernel unit's device globals (swap_, fused_, attempt_)
+#define PIMC_UNIT_DECL(unit)                                                              \
+  cudaError_t unit##_upload_exp_table(const double *tab, size_t bytes);                   \
+  cudaError_t unit##_profile_take(unsigned long long *out, bool reset, cudaStream_t s);  \
+  cudaError_t unit##_check_word_take(cudaStream_t s, unsigned long long *w);
+PIMC_UNIT_DECL(swap)
+PIMC_UNIT_DECL(fused)
+PIMC_UNIT_DECL(attempt)
+#undef PIMC_UNIT_DECL
 // shared scratch of the device move routines (bytes; doubles for a window)
 size_t swap_scratch_bytes(int N, int nwarps);
 size_t com_scratch_bytes(int N, int M, int nwarps);

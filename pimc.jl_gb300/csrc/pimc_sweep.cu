@@ -14,652 +14,16 @@
 #include <atomic>
 #include <cmath>
 
-#include "pimc_kernels.cuh"
-#include "pimc_launch.h"
+#include "pimc_sweep.cuh"
 
 namespace pimc {
-
-__device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ipool,
-                                      unsigned long long *upool) {
-  CV c;
-  c.d = d;
-  c.N = d->N;
-  c.M = d->M;
-  c.dim = d->dim;
-  c.ldn = d->N;
-  c.x = dpool + d->x_off;
-  c.V = dpool + d->V_off;
-  c.xq = (unsigned *)(dpool + d->xq_off);
-  c.next = ipool + d->next_off;
-  c.tab = (const double2 *)(dpool + d->tab_off);
-  c.hist = (d->dens_off >= 0 && upool) ? upool + d->dens_off : nullptr;
-  c.eser = d->eser_off >= 0 ? dpool + d->eser_off : nullptr;
-  return c;
-}
-
-// moves whose acceptance depends on other paths at the same slice
-__device__ __forceinline__ bool chain_serial_local(const ChainDesc &d) {
-  return ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) || (d.flags & PF_HARD);
-}
-
-// next[] of a chain must be a permutation of 0..N-1: every value in range
-// (the host refuses out-of-range values before they reach the device) and no
-// value twice.  The group marks each value in a bitmap of (N + 31) / 32 words
-// of shared memory; a chain that fails gets ChainVar::err = DERR_STATE and is
-// skipped by every kernel until its state is replaced.
-template <bool WARP>
-__device__ bool next_is_permutation(const int *next, int N, unsigned *bits) {
-  const int tid = WARP ? (int)(threadIdx.x & 31) : (int)threadIdx.x;
-  const int nt = WARP ? 32 : (int)blockDim.x;
-  const int nw = (N + 31) >> 5;
-  for (int w = tid; w < nw; w += nt) bits[w] = 0u;
-  if (WARP) __syncwarp(); else __syncthreads();
-  int bad = 0;
-  for (int i = tid; i < N; i += nt) {
-    const int v = next[i];
-    if (v < 0 || v >= N) {
-      bad = 1;
-    } else {
-      const unsigned m = 1u << (v & 31);
-      if (atomicOr(&bits[v >> 5], m) & m) bad = 1;
-    }
-  }
-  return WARP ? !__any_sync(0xffffffffu, bad) : !__syncthreads_or(bad);
-}
-
-__device__ void record_measurement(const ChainDesc &d, ChainVar &v, const CV &c, const double *e,
-                                   bool density) {
-  if (c.eser && v.eser_count < (unsigned long long)d.eser_cap) {
-    for (int q = 0; q < NOBS; ++q) c.eser[v.eser_count * NOBS + q] = e[q];
-    v.eser_count++;
-  }
-  for (int q = 0; q < NOBS; ++q) {
-    v.esum[q] += e[q];
-    v.esum2[q] += e[q] * e[q];
-  }
-  v.n_meas++;
-  if (d.rdf_nb > 0) v.rdf_meas++;
-  if (density) v.ndata += d.M;
-}
-
-// adjust! (src/updates/helper.jl:22-52) from this sweep's acceptance
-__device__ void adapt_slices(int &m, double acc_ratio, int mn, int mx, double minacc,
-                             double maxacc) {
-  if (acc_ratio < minacc) m -= 1;
-  else if (acc_ratio > maxacc) m += 1;
-  m = max(mn, m);
-  m = min(mx, m);
-}
-__device__ void adapt_step(double &s, double acc_ratio, double mn, double mx, double minacc,
-                           double maxacc) {
-  if (acc_ratio < minacc) s *= 0.9;
-  else if (acc_ratio > maxacc) s *= 1.1;
-  s = fmax(mn, s);
-  s = fmin(mx, s);
-}
-
-struct SmemCtl {
-  ChainDesc d;
-  ChainVar v;
-  MixDev mix;
-  double shift[2];
-  double e4[NOBS];
-  int iflag[8];
-  int chain;
-  int scratch_bytes;  // bytes of shared scratch the group's moves may carve
-};
-
-// bytes of dynamic shared memory of the running launch
-__device__ __forceinline__ unsigned dyn_smem_bytes() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%dynamic_smem_size;" : "=r"(r));
-  return r;
-}
-
-// one sweep of one chain by a group: the whole CTA, or one warp on its own
-// the phases of a sweep; a kernel runs the ones its mask names, so that each
-// phase can run as its own launch with its own register budget
-enum : int { SW_STAGE = 1, SW_SWAP = 2, SW_REST = 4, SW_ALL = 7 };
-
-// closes one phase of move kind q: adds its tallies (attempts, accepts,
-// skips, bead updates) to the chain's counters and adapts the phase's own
-// variable (adjust!, src/updates/helper.jl:22-52) from this sweep's
-// acceptance.  Only the phase itself reads that variable, so adapting at its
-// end is the same as adapting at the end of the sweep.
-template <bool WARP>
-__device__ void close_phase(SmemCtl &sc, double *red, int q, double (&t)[4]) {
-  using G = Group<WARP>;
-  G::template sum<4>(t, red);
-  if (G::rank() == 0) {
-    ChainVar &v = sc.v;
-    const MixDev &mix = sc.mix;
-    v.att[q] += (unsigned long long)t[0];
-    v.acc[q] += (unsigned long long)t[1];
-    v.skips += (unsigned long long)t[2];
-    v.bead_updates += t[3];
-    v.beads_kind[q] += t[3];
-    // the reference divides by an empty queue (NaN) and leaves var alone
-    if (mix.adapt && t[0] > 0) {
-      const double r = t[1] / t[0];
-      if (q == MV_STAGE)
-        adapt_slices(v.stage_m, r, mix.stage_min, mix.stage_max, mix.stage_minacc, mix.stage_maxacc);
-      else if (q == MV_SWAP)
-        adapt_slices(v.swap_m, r, mix.swap_min, mix.swap_max, mix.swap_minacc, mix.swap_maxacc);
-      else if (q == MV_COM)
-        adapt_step(v.com_step, r, mix.com_minstep, mix.com_maxstep, mix.com_minacc, mix.com_maxacc);
-      else
-        adapt_step(v.pcom_step, r, mix.pcom_minstep, mix.pcom_maxstep, mix.pcom_minacc,
-                   mix.pcom_maxacc);
-    }
-  }
-  G::sync();
-}
-
-template <bool WARP, int PH, int SPEC = SWAP_ANY>
-__device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *scratch,
-                          int warp_scratch_d, bool teams) {
-  using G = Group<WARP>;
-  const ChainDesc &d = sc.d;
-  const MixDev &mix = sc.mix;
-  const int tid = G::rank(), nt = G::size(), lane = threadIdx.x & 31;
-  const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
-  const int N = c.N, M = c.M;
-  const bool serial_local = chain_serial_local(d);
-  const unsigned long long sweep = sc.v.sweep;
-  double *wsb = (double *)scratch + (size_t)warp * warp_scratch_d;
-  // every carve below must fit the group's scratch (PIMC_CHECK builds)
-  if (!check_ok((size_t)nwarps * warp_scratch_d * sizeof(double) <= (size_t)sc.scratch_bytes &&
-                    SwapScratch::bytes(N, nwarps) <= (size_t)sc.scratch_bytes &&
-                    ComScratch::bytes(N, M, nwarps) <= (size_t)sc.scratch_bytes,
-                DERR_SCRATCH, d))
-    return;
-
-  // ---- staging phases (ReshapeLinear)
-  if (PH & SW_STAGE) {
-  // per-thread tallies: attempts, accepts, skips, bead updates
-  double tal[4] = {0, 0, 0, 0};
-  for (int ph = 0; ph < mix.staging_phases; ++ph) {
-    int ell = sc.v.stage_m;
-    ell = max(2, min(ell, min(M - 1, WMAX)));
-    const int k = (M + ell - 1) / ell;
-    const Stream so = make_stream(d, sweep, PH_STAGE_OFF, (unsigned)ph);
-    const int o = min(M - 1, (int)(so.uni(0) * M));
-    const int items = N * k;
-    if (!serial_local) {
-      // every window of the phase is independent: slot s of particle n moves
-      // the beads strictly inside its slot; item order s*N + n makes
-      // neighbouring threads touch neighbouring particles of one slice
-      if (ell <= TWMAX) {
-        for (int it = tid; it < items; it += nt) {
-          const int s = it / N, n = it % N;
-          const int len = s < k - 1 ? ell : M - (k - 1) * ell;
-          if (len < 2) continue;
-          const int st = (o + s * ell) % M;
-          GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + it)));
-          const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_thread(c, n, st, m, dr, false, nullptr);
-          tal[0] += 1.0;
-          tal[1] += r;
-          tal[3] += m - 1;
-        }
-      } else {
-        for (int it = warp; it < items; it += nwarps) {
-          const int s = it / N, n = it % N;
-          const int len = s < k - 1 ? ell : M - (k - 1) * ell;
-          if (len < 2) continue;
-          const int st = (o + s * ell) % M;
-          GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + it)));
-          const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
-          if (lane == 0) {
-            tal[0] += 1.0;
-            tal[1] += r == RES_ACCEPT;
-            tal[3] += m - 1;
-          }
-        }
-      }
-    } else if (!WARP && teams && !(d.flags & PF_HARD) && 2 * k <= nwarps && k <= kMaxTeams) {
-      // fewer slots than warps: a team of T warps walks each slot, the
-      // warps splitting every window's links (named barrier 1 + team)
-      const int T = min(nwarps / k, 8), team = warp / T;
-      if (team < k) {
-        const Team tm{warp - team * T, T, 1 + team};
-        double *tb = (double *)scratch + (size_t)(team * T) * warp_scratch_d;
-        const int len = team < k - 1 ? ell : M - (k - 1) * ell;
-        const int st = (o + team * ell) % M;
-        if (len >= 2)
-          for (int n = 0; n < N; ++n) {
-            GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + team * N + n)));
-            const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-            const int r = window_team(c, tm, n, st, m, dr, tb, warp_scratch_d);
-            if (tm.w == 0 && lane == 0) {
-              tal[0] += 1.0;
-              tal[1] += r == RES_ACCEPT;
-              tal[3] += m - 1;
-            }
-          }
-      }
-    } else {
-      // windows of one slot interact through the pair action or the hard
-      // core: a warp walks the particles of its slot in order; distinct
-      // slots share only their fixed end slices and run concurrently
-      for (int s = warp; s < k; s += nwarps) {
-        const int len = s < k - 1 ? ell : M - (k - 1) * ell;
-        if (len < 2) continue;
-        const int st = (o + s * ell) % M;
-        for (int n = 0; n < N; ++n) {
-          GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + s * N + n)));
-          const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_warp(c, n, st, m, dr, false, wsb, nullptr);
-          if (lane == 0) {
-            tal[0] += 1.0;
-            tal[1] += r == RES_ACCEPT;
-            if (r != RES_HARDCORE) tal[3] += m - 1;
-          }
-        }
-      }
-    }
-    G::sync();
-  }
-  if (mix.staging_phases > 0) close_phase<WARP>(sc, red, MV_STAGE, tal);
-  }
-
-  // ---- permutation swaps (ReshapeSwapLinear), one at a time by the group
-  if ((PH & SW_SWAP) && N > 1 && mix.swaps_per_sweep > 0) {
-    double tal[4] = {0, 0, 0, 0};
-    SwapScratch S;
-    S.carve(scratch, N, nwarps);
-    const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
-    const int sm = max(2, sc.v.swap_m);
-    for (int a = 0; a < mix.swaps_per_sweep; ++a) {
-      const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
-      const uint4 r0 = ss.at(DRAW_CHOICE), r1 = ss.at(DRAW_CHOICE + 1);
-      const int j0 = min(M - 1, (int)(u53(r0.x, r0.y) * M));
-      const int m = min(mmax, 2 + (int)(u53(r0.z, r0.w) * (sm - 1)));
-      const int n1 = min(N - 1, (int)(u53(r1.x, r1.y) * N));
-      const double upick = u53(r1.z, r1.w);
-      GenDraws dr = gen_draws(ss);
-      const int r = swap_group<WARP, true, GenDraws, SPEC>(c, j0, m, n1, upick, dr, S, red, nullptr,
-                                                           nullptr);
-      if (tid == 0) {
-        if (r == RES_SKIP) {
-          tal[2] += 1.0;
-        } else {
-          tal[0] += 1.0;
-          tal[1] += r == RES_ACCEPT;
-          if (r != RES_HARDCORE) tal[3] += 2.0 * (m - 1);
-        }
-      }
-    }
-    G::sync();
-    close_phase<WARP>(sc, red, MV_SWAP, tal);
-  }
-
-  if (!(PH & SW_REST)) return;
-
-  // ---- single-path centre of mass
-  double tal[4] = {0, 0, 0, 0};
-  for (int ph = 0; ph < mix.com_phases; ++ph) {
-    const double step = sc.v.com_step;
-    if (!serial_local) {
-      for (int n = tid; n < N; n += nt) {
-        if (c.next[n] != n) continue;
-        GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_thread(c, n, step, dr);
-        tal[0] += 1.0;
-        tal[1] += r;
-        tal[3] += M;
-      }
-      G::sync();
-    } else {
-      ComScratch cs;
-      cs.carve(scratch, N, M);
-      for (int n = 0; n < N; ++n) {
-        if (c.next[n] != n) continue;
-        GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_group<WARP>(c, n, false, step, dr, cs, red, sc.shift, &sc.iflag[2], nullptr);
-        if (tid == 0) {
-          tal[0] += 1.0;
-          tal[1] += r == RES_ACCEPT;
-          if (r != RES_HARDCORE) tal[3] += M;
-        }
-        G::sync();
-      }
-    }
-  }
-
-  if (mix.com_phases > 0) close_phase<WARP>(sc, red, MV_COM, tal);
-
-  // ---- cycle centre of mass, one attempt per cycle (led by its lowest index)
-  double tlp[4] = {0, 0, 0, 0};
-  for (int ph = 0; ph < mix.polymer_com_phases; ++ph) {
-    ComScratch cs;
-    cs.carve(scratch, N, M);
-    for (int n = 0; n < N; ++n) {
-      if (tid == 0) {
-        int lead = 1, i = c.next[n], guard = 0;
-        while (i != n && guard++ <= N) {
-          if (i < n) { lead = 0; break; }
-          i = c.next[i];
-        }
-        sc.iflag[1] = lead;
-      }
-      G::sync();
-      if (!sc.iflag[1]) continue;
-      GenDraws dr = gen_draws(make_stream(d, sweep, PH_PCOM, (unsigned)(ph * N + n)));
-      const int r = com_group<WARP>(c, n, true, sc.v.pcom_step, dr, cs, red, sc.shift, &sc.iflag[2],
-                                    &sc.iflag[3]);
-      const int np = sc.iflag[3];
-      if (tid == 0) {
-        tlp[0] += 1.0;
-        tlp[1] += r == RES_ACCEPT;
-        if (r != RES_HARDCORE) tlp[3] += (double)M * np;
-      }
-      G::sync();
-    }
-  }
-  if (mix.polymer_com_phases > 0) close_phase<WARP>(sc, red, MV_PCOM, tlp);
-
-  // ---- measurement cadence (measurement_Z_sector)
-  if (mix.measure_every > 0 && ((sweep + 1) % (unsigned long long)mix.measure_every) == 0) {
-    measure_group<WARP>(c, red, sc.e4, c.hist != nullptr, (unsigned long long *)scratch);
-    if (tid == 0) record_measurement(d, sc.v, c, sc.e4, c.hist != nullptr);
-  }
-  if (tid == 0) sc.v.sweep++;
-  G::sync();
-}
-
-// warp per chain: every warp of the grid pulls chains from the queue (or
-// takes chain0 + its global warp index once) and sweeps them alone; its
-// control block and scratch live in its own slice of dynamic shared memory.
-// PH names the phases of the sweep it runs (all of them, or the swaps alone
-// as the swap launch of a split sweep).
-template <int PH>
-__device__ __forceinline__ void sweep_warp(const SweepArgs &a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const size_t ctl = (sizeof(SmemCtl) + 15) & ~(size_t)15;
-  unsigned char *mine = smem + (size_t)w * (ctl + a.warp_bytes);
-  SmemCtl &sc = *reinterpret_cast<SmemCtl *>(mine);
-  unsigned char *scratch = mine + ctl;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + w;
-  int iter = 0;
-  while (true) {
-    int ci = a.nchains;
-    if (lane == 0) {
-      if (a.queue) ci = atomicAdd(a.queue, 1);
-      else ci = iter == 0 ? gw : a.nchains;
-      if (ci < a.nchains) {
-        const int ch = a.order ? a.order[ci] : a.chain0 + ci;
-        sc.chain = ch;
-        sc.d = a.desc[ch];
-        sc.v = a.var[ch];
-        sc.mix = a.mix[ch];
-        sc.scratch_bytes = a.warp_bytes;
-      }
-    }
-    ci = __shfl_sync(0xffffffffu, ci, 0);
-    __syncwarp();
-    ++iter;
-    if (ci >= a.nchains) break;
-    CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-    // the warp's scratch (at least N doubles) holds the bitmap of the check
-    const bool ok = sc.v.err == 0 && next_is_permutation<true>(c.next, sc.d.N, (unsigned *)scratch);
-    if (!ok && lane == 0 && sc.v.err == 0) sc.v.err = DERR_STATE;
-    __syncwarp();
-    if (ok)
-      for (int s = 0; s < a.sweeps; ++s) sweep_one<true, PH>(sc, nullptr, c, scratch, a.warp_scratch_d, false);
-    if (lane == 0) a.var[sc.chain] = sc.v;
-    __syncwarp();
-  }
-}
-
-__global__ void __launch_bounds__(256, 2) k_sweep_warp(SweepArgs a) { sweep_warp<SW_ALL>(a); }
-// the swap phase of a split sweep with one warp per chain: twice the chains
-// in flight of a two-warp CTA per chain at the same registers per SM
-__global__ void __launch_bounds__(256, 2) k_sweep_swap_warp(SweepArgs a) { sweep_warp<SW_SWAP>(a); }
-
-template <int PH, int SPEC = SWAP_ANY>
-__device__ __forceinline__ void sweep_cta(const SweepArgs &a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ SmemCtl sc;
-  __shared__ double red[256];
-  const int tid = threadIdx.x, nt = blockDim.x;
-  int iter = 0;
-  while (true) {
-    if (tid == 0) {
-      int ci;
-      if (a.queue) ci = atomicAdd(a.queue, 1);
-      else ci = iter == 0 ? (int)blockIdx.x : a.nchains;
-      if (ci < a.nchains) {
-        const int ch = a.order ? a.order[ci] : a.chain0 + ci;
-        sc.chain = ch;
-        sc.d = a.desc[ch];
-        sc.v = a.var[ch];
-        sc.mix = a.mix[ch];
-        sc.scratch_bytes = (int)dyn_smem_bytes() - a.state_bytes;
-      } else {
-        sc.chain = -1;
-      }
-    }
-    __syncthreads();
-    ++iter;
-    if (sc.chain < 0) break;
-    const ChainDesc &d = sc.d;
-    CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-    {
-      __shared__ unsigned bits[(kMaxParticles + 31) / 32];
-      const bool ok = sc.v.err == 0 && next_is_permutation<false>(c.next, d.N, bits);
-      if (!ok) {
-        if (tid == 0) {
-          if (sc.v.err == 0) sc.v.err = DERR_STATE;
-          a.var[sc.chain] = sc.v;
-        }
-        __syncthreads();
-        continue;
-      }
-    }
-    const int N = d.N, M = d.M, dim = d.dim;
-    const bool staged = d.smem_bytes > 0 && d.smem_bytes <= a.state_bytes;
-    const size_t nx = (size_t)dim * M * N, nv = (size_t)M * N;
-    if (staged) {
-      double *sx = (double *)smem;
-      double *sV = sx + nx;
-      unsigned *sq = (unsigned *)(sV + nv);
-      int *snx = (int *)(sq + nv);
-      for (size_t e = tid; e < nx; e += nt) sx[e] = c.x[e];
-      for (size_t e = tid; e < nv; e += nt) sV[e] = c.V[e];
-      for (size_t e = tid; e < nv; e += nt) sq[e] = c.xq[e];
-      for (int e = tid; e < N; e += nt) snx[e] = c.next[e];
-      c.x = sx;
-      c.V = sV;
-      c.xq = sq;
-      c.next = snx;
-      __syncthreads();
-    }
-    unsigned char *scratch = smem + a.state_bytes;
-    for (int s = 0; s < a.sweeps; ++s)
-      sweep_one<false, PH, SPEC>(sc, red, c, scratch, a.warp_scratch_d, a.teams != 0);
-    if (staged) {
-      double *gx = a.dpool + d.x_off, *gV = a.dpool + d.V_off;
-      unsigned *gq = (unsigned *)(a.dpool + d.xq_off);
-      int *gn = a.ipool + d.next_off;
-      for (size_t e = tid; e < nx; e += nt) gx[e] = c.x[e];
-      for (size_t e = tid; e < nv; e += nt) gV[e] = c.V[e];
-      for (size_t e = tid; e < nv; e += nt) gq[e] = c.xq[e];
-      for (int e = tid; e < N; e += nt) gn[e] = c.next[e];
-    }
-    if (tid == 0) a.var[sc.chain] = sc.v;
-    __syncthreads();
-  }
-}
-
-// one CTA per chain, every phase of the sweep in one launch
-__global__ void __launch_bounds__(512) k_sweep(SweepArgs a) { sweep_cta<SW_ALL>(a); }
 
 // the sweep's phases as separate launches (staging, swaps, the rest), each
 // compiled and scheduled on its own: every chain of the batch finishes one
 // phase before any starts the next, so the longest chain of each phase, not
 // the longest sum over phases, sets a sweep's time
-__global__ void __launch_bounds__(512) k_sweep_stage(SweepArgs a) { sweep_cta<SW_STAGE>(a); }
-__global__ void __launch_bounds__(512) k_sweep_swap(SweepArgs a) { sweep_cta<SW_SWAP>(a); }
-// the swap launch for batches whose every chain follows the reference's
-// rules without a hard core or a contact table (swap_group SWAP_REF)
-__global__ void __launch_bounds__(512) k_sweep_swap_ref(SweepArgs a) {
-  sweep_cta<SW_SWAP, SWAP_REF>(a);
-}
-__global__ void __launch_bounds__(512) k_sweep_rest(SweepArgs a) { sweep_cta<SW_REST>(a); }
-
-// ---------------------------------------------------------------------------
-// single moves with injected draws (one CTA, state in global memory)
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_attempt(AttemptArgs a) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ SmemCtl sc;
-  __shared__ double red[256];
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    sc.d = a.desc[a.chain];
-    sc.v = a.var[a.chain];
-  }
-  __syncthreads();
-  const ChainDesc &d = sc.d;
-  CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-  InjDraws dr;
-  dr.nrm = a.normals;
-  dr.n_nrm = a.n_normals;
-  dr.pn = 0;
-  dr.uni = a.uniforms;
-  dr.n_uni = a.n_uniforms;
-  dr.pu = 0;
-  dr.exh = 0;
-  int res = 0, extra = -1;
-  const bool serial = chain_serial_local(d);
-  if (a.kind == MV_STAGE) {
-    const bool use_warp = serial || a.force_warp || a.m > TWMAX;
-    if (use_warp) {
-      if (tid < 32) res = window_warp(c, a.n, a.j0, a.m, dr, true, (double *)smem, a.prop);
-    } else {
-      if (tid == 0) res = window_thread(c, a.n, a.j0, a.m, dr, true, a.prop);
-    }
-  } else if (a.kind == MV_SWAP) {
-    if (tid < 32) {
-      SwapScratch S;
-      S.carve(smem, d.N, 1);
-      res = swap_warp<false>(c, a.j0, a.m, a.n, a.u_pick, dr, S, a.prop, &sc.iflag[4]);
-    }
-    __syncthreads();
-    extra = sc.iflag[4];
-  } else if (a.kind == MV_COM && !serial && !a.force_warp) {
-    if (tid == 0) res = com_thread(c, a.n, a.step, dr);
-  } else {
-    ComScratch cs;
-    cs.carve(smem, d.N, d.M);
-    res = com_group<false>(c, a.n, a.kind == MV_PCOM, a.step, dr, cs, red, sc.shift, &sc.iflag[2],
-                           &sc.iflag[3]);
-    extra = sc.iflag[3];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    a.out[0] = res;
-    a.out[1] = extra;
-    a.out[2] = dr.pn;
-    a.out[3] = dr.pu;
-    a.out[4] = dr.exh;
-  }
-}
-
-// ---------------------------------------------------------------------------
-// action evaluation (parity level a) and staging weights of a given window
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_eval_action(EvalArgs a) {
-  __shared__ SmemCtl sc;
-  __shared__ double red[256];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = nt >> 5;
-  if (tid == 0) sc.d = a.desc[a.chain];
-  __syncthreads();
-  const ChainDesc &d = sc.d;
-  CV c = make_cv(&sc.d, a.dpool, a.ipool, a.upool);
-  const int N = c.N, M = c.M, dim = c.dim;
-  const double den = 4.0 * d.tau * d.lambda, mhtau = -0.5 * d.tau, rc2 = d.rc * d.rc;
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int k = tid; k < N * M; k += nt) {
-    const int j = k / N, i = k % N;
-    const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-    const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
-    const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
-    s[0] += -mi2(d, ax, ay, bx, by) / den;
-    s[1] += mhtau * (vext(d, ax, ay) + vext(d, bx, by));
-    s[3] += c.Vl(i, j);
-  }
-  if (d.flags & PF_PAIR) {
-    for (int k = warp; k < N * M; k += nwarps) {
-      const int j = k / N, i = k % N;
-      const int in = j == M - 1 ? c.next[i] : i, jn = j + 1 == M ? 0 : j + 1;
-      const double ax = c.X(0, i, j), ay = c.Xd(1, i, j);
-      const double bx = c.X(0, in, jn), by = c.Xd(1, in, jn);
-      Prefilter f;
-      f.init_q(c.Q(i, j), d.q_lim_rc);
-      const unsigned *row = c.xq + (size_t)j * c.ldn;
-      for (int b = i + 1 + lane; b < N; b += 32) {
-        if (!f.pass(row[b])) continue;
-        const double r2a = mi2(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j));
-        if (r2a > rc2) continue;
-        const int bn = j == M - 1 ? c.next[b] : b;
-        if (d.flags & PF_CONTACT)
-          s[2] += contact_link(d, ax, ay, c.X(0, b, j), c.Xd(1, b, j), bx, by, c.X(0, bn, jn),
-                               c.Xd(1, bn, jn));
-        else
-          s[2] += lnU2(d, r2a, mi2(d, bx, by, c.X(0, bn, jn), c.Xd(1, bn, jn)));
-      }
-    }
-  }
-  block_sum_k<4>(s, red);
-  if (tid == 0)
-    for (int q = 0; q < 4; ++q) a.out[q] = s[q];
-}
-
-__global__ void k_eval_weights(EvalArgs a) {
-  __shared__ ChainDesc d;
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) d = a.desc[a.chain];
-  __syncthreads();
-  CV c = make_cv(&d, a.dpool, a.ipool, a.upool);
-  const int M = c.M, dim = c.dim, n = a.n, j0 = a.j0, m = a.m;
-  const int nx = c.next[n];
-  const double mhtau = -0.5 * d.tau;
-  const double *rp = a.rp;
-  auto px = [&](int t) { return rp[t * dim]; };
-  auto py = [&](int t) { return dim > 1 ? rp[t * dim + 1] : 0.0; };
-  double wi = 0.0, wu = 0.0;
-  if (lane == 0) {
-    for (int t = 0; t < m; ++t) {
-      const int ab = j0 + t;
-      wi += c.Vl(ab < M ? n : nx, ab < M ? ab : ab - M);
-    }
-    for (int t = 0; t < m; ++t) wu += mhtau * (vext(d, px(t), py(t)) + vext(d, px(t + 1), py(t + 1)));
-  }
-  if ((d.flags & PF_PAIR) && (d.flags & PF_PHYS)) {
-    __shared__ double wx[WMAX + 1], wy[WMAX + 1];
-    __shared__ unsigned wq[WMAX + 1];
-    __shared__ unsigned long long q[PQ_CAP];
-    for (int t = lane; t <= m; t += 32) {
-      wx[t] = px(t);
-      wy[t] = py(t);
-      wq[t] = qpos(d, wx[t], wy[t]);
-    }
-    __syncwarp();
-    WindowSeg seg{&c, n, nx, j0, M, wx, wy, wq};
-    segment_pairs(c, seg, 0, m, true, true, q, wi, wu, lane);
-  }
-  wi = warp_sum(wi);
-  wu = warp_sum(wu);
-  if (threadIdx.x == 0) {
-    a.out[0] = wi;
-    a.out[1] = wu;
-  }
-}
+__global__ void __launch_bounds__(512, 1) k_sweep_stage(SweepArgs a) { sweep_cta<SW_STAGE>(a); }
+__global__ void __launch_bounds__(512, 1) k_sweep_rest(SweepArgs a) { sweep_cta<SW_REST>(a); }
 
 // ---------------------------------------------------------------------------
 // state maintenance: layout transposes, init_world, cached links + mirror,
@@ -1272,81 +636,49 @@ __global__ void __launch_bounds__(256) k_adjoint_totals_b(AdjBatchArgs a) {
 // host launchers
 // ---------------------------------------------------------------------------
 
-// the exp table of exp_neg for the current device
 // scratch sizes of the device move routines, for the host's shared-memory plans
 size_t swap_scratch_bytes(int N, int nwarps) { return SwapScratch::bytes(N, nwarps); }
 size_t com_scratch_bytes(int N, int M, int nwarps) { return ComScratch::bytes(N, M, nwarps); }
 int window_scratch_doubles() { return WARP_SCRATCH_D; }
 
+// the exp table of exp_neg for the current device, in every kernel unit
 cudaError_t upload_exp_table() {
   static double tab[EXPTAB_N + 1];
   for (int k = 0; k <= EXPTAB_N; ++k) tab[k] = std::exp(-k / 64.0);
-  return cudaMemcpyToSymbol(g_exptab, tab, sizeof(tab));
+  cudaError_t e = tu_upload_exp_table(tab, sizeof(tab));
+  if (e == cudaSuccess) e = swap_upload_exp_table(tab, sizeof(tab));
+  if (e == cudaSuccess) e = fused_upload_exp_table(tab, sizeof(tab));
+  if (e == cudaSuccess) e = attempt_upload_exp_table(tab, sizeof(tab));
+  return e;
 }
 
-cudaError_t launch_sweep(const SweepArgs &a, int mode, int grid, int block, size_t smem,
-                         cudaStream_t s) {
-  if (mode == 1) k_sweep_warp<<<grid, block, smem, s>>>(a);
-  else k_sweep<<<grid, block, smem, s>>>(a);
-  return cudaGetLastError();
-}
-// phase kernels: 0 staging, 1 swaps, 2 the rest; warp = 1 (swaps only): one
-// warp per chain
-// warp = 1 (swaps only): one warp per chain; spec = 1 (swaps in CTA mode):
-// the reference-rules swap kernel
-static const void *phase_kernel(int phase, int warp, int spec) {
-  if (phase == 1) {
-    if (warp) return (const void *)k_sweep_swap_warp;
-    return spec ? (const void *)k_sweep_swap_ref : (const void *)k_sweep_swap;
-  }
+// phase kernels: 0 staging, 1 swaps (pimc_swap.cu), 2 the rest; warp = 1
+// (swaps only): one warp per chain; spec = 1 (swaps in CTA mode): the
+// reference-rules swap kernel
+static const void *phase_kernel(int phase, int warp, int spec, int regs) {
+  if (phase == 1) return swap_kernel(warp, spec, regs);
   return phase == 0 ? (const void *)k_sweep_stage : (const void *)k_sweep_rest;
 }
-cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int grid,
-                               int block, size_t smem, cudaStream_t s) {
+cudaError_t launch_sweep_phase(const SweepArgs &a, int phase, int warp, int spec, int regs,
+                               int grid, int block, size_t smem, cudaStream_t s) {
+  if (phase == 1) return launch_swap(a, warp, spec, regs, grid, block, smem, s);
   if (phase == 0) k_sweep_stage<<<grid, block, smem, s>>>(a);
-  else if (phase == 1 && warp) k_sweep_swap_warp<<<grid, block, smem, s>>>(a);
-  else if (phase == 1 && spec) k_sweep_swap_ref<<<grid, block, smem, s>>>(a);
-  else if (phase == 1) k_sweep_swap<<<grid, block, smem, s>>>(a);
   else k_sweep_rest<<<grid, block, smem, s>>>(a);
   return cudaGetLastError();
 }
 
-cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, size_t smem) {
-  return cudaFuncSetAttribute(phase_kernel(phase, warp, spec),
+cudaError_t sweep_phase_set_smem(int phase, int warp, int spec, int regs, size_t smem) {
+  return cudaFuncSetAttribute(phase_kernel(phase, warp, spec, regs),
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int block, size_t smem,
+cudaError_t sweep_phase_occupancy(int phase, int warp, int spec, int regs, int block, size_t smem,
                                   int *blocks_per_sm) {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm,
-                                                       phase_kernel(phase, warp, spec), block, smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      blocks_per_sm, phase_kernel(phase, warp, spec, regs), block, smem);
 }
 
-cudaError_t sweep_set_smem(int mode, size_t smem) {
-  if (mode == 1)
-    return cudaFuncSetAttribute(k_sweep_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  return cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
 size_t sweep_ctl_bytes() { return (sizeof(SmemCtl) + 15) & ~(size_t)15; }
-cudaError_t sweep_occupancy(int mode, int block, size_t smem, int *blocks_per_sm) {
-  if (mode == 1)
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep_warp, block, smem);
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_sweep, block, smem);
-}
-cudaError_t launch_attempt(const AttemptArgs &a, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_attempt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k_attempt<<<1, 128, smem, s>>>(a);
-  return cudaGetLastError();
-}
-cudaError_t launch_eval_action(const EvalArgs &a, cudaStream_t s) {
-  k_eval_action<<<1, 256, 0, s>>>(a);
-  return cudaGetLastError();
-}
-cudaError_t launch_eval_weights(const EvalArgs &a, cudaStream_t s) {
-  k_eval_weights<<<1, 32, 0, s>>>(a);
-  return cudaGetLastError();
-}
 cudaError_t launch_import(const ChainDesc *desc, double *dpool, const double *src, int chain0,
                           int nchains, size_t maxn, cudaStream_t s) {
   dim3 g((unsigned)std::min<size_t>((maxn + 255) / 256, 1024), nchains);
@@ -1577,17 +909,16 @@ cudaError_t adjoint_static_scratch(double **ptr) {
   return cudaSuccess;
 }
 
-// the PIMC_PROFILE build's swap counters (g_prof): read, then cleared on
-// request; cudaErrorNotSupported in other builds
+// the PIMC_PROFILE build's swap counters (g_prof of every kernel unit,
+// summed): read, then cleared on request; cudaErrorNotSupported in other
+// builds
 cudaError_t profile_take(unsigned long long *out, bool reset, cudaStream_t s) {
 #if PIMC_PROFILE
-  cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_prof, sizeof(g_prof), 0, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess && reset) {
-    static const unsigned long long z[32] = {};
-    e = cudaMemcpyToSymbolAsync(g_prof, z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  }
+  for (int k = 0; k < 32; ++k) out[k] = 0;
+  cudaError_t e = tu_profile_take(out, reset, s);
+  if (e == cudaSuccess) e = swap_profile_take(out, reset, s);
+  if (e == cudaSuccess) e = fused_profile_take(out, reset, s);
+  if (e == cudaSuccess) e = attempt_profile_take(out, reset, s);
   return e;
 #else
   (void)out;
@@ -1597,23 +928,19 @@ cudaError_t profile_take(unsigned long long *out, bool reset, cudaStream_t s) {
 #endif
 }
 
-// the PIMC_CHECK build's device check word: read and cleared (0 in the
-// default build, which has no bounds checks)
+// the PIMC_CHECK build's device check word of every kernel unit (the first
+// nonzero): read and cleared (0 in the default build, which has no bounds
+// checks)
 cudaError_t check_word_take(cudaStream_t s, unsigned long long *w) {
-  *w = 0;
-#if PIMC_CHECK
-  cudaError_t e = cudaMemcpyFromSymbolAsync(w, g_check_word, sizeof(*w), 0, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess && *w) {
-    const unsigned long long z = 0;
-    e = cudaMemcpyToSymbolAsync(g_check_word, &z, sizeof(z), 0, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaError_t (*const take[3])(cudaStream_t, unsigned long long *) = {
+      swap_check_word_take, fused_check_word_take, attempt_check_word_take};
+  cudaError_t e = tu_check_word_take(s, w);
+  for (int u = 0; u < 3 && e == cudaSuccess; ++u) {
+    unsigned long long w2 = 0;
+    e = take[u](s, &w2);
+    if (*w == 0) *w = w2;
   }
   return e;
-#else
-  (void)s;
-  return cudaSuccess;
-#endif
 }
 
 cudaError_t launch_adjoint_batch(const AdjBatchArgs &a, int maxN, cudaStream_t s) {

@@ -63,6 +63,14 @@ struct ChainDesc {
   long long next_off;   // ints: next[n]
   long long dens_off;   // u64: hist[nb^dim]
   long long eser_off;   // doubles: observable series [cap][NOBS]
+  // per-slice cell lists (ints at ipool + cl_off, cell_layout below): cl_nc
+  // cells per axis (0: no lists, every query scans its slice row), cl_cap
+  // moved particles a slice's list tracks before its queries fall back to
+  // the row scan, cl_mode 1 (a slice whose build finds its cells too crowded,
+  // 9 sum n_c^2 > cl_frac N^2 in 2D, scans its row) or 2 (lists always)
+  long long cl_off;
+  int cl_nc, cl_cap, cl_mode;
+  float cl_frac;
   int eser_cap;
   int smem_bytes;       // bytes to stage x, V, mirror, next in shared memory
   unsigned key0, key1;  // Philox key
@@ -86,6 +94,30 @@ struct ChainDesc {
   double beam_depth, beam_scale;
   double beam_sin[MAX_BEAMS], beam_cos[MAX_BEAMS];
 };
+
+// ints of a chain's cell lists: end[M][ncq+1] (end of each cell's entries in
+// items), dn[M] (moved particles per slice since its build), moved bitmask
+// [M][nw], then as 16-bit words items[M][N] (the slice's particles in cell
+// order), pos[M][N] (a particle's index in items) and dl[M][cap] (the
+// slice's moved particles)
+struct CellLayout {
+  long long end, dn, moved, items, pos, dl, total;
+};
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline CellLayout cell_layout(int N, int M, int ncq, int cap) {
+  CellLayout c;
+  const long long nw = (N + 31) / 32;
+  c.end = 0;
+  c.dn = c.end + (long long)M * (ncq + 1);
+  c.moved = c.dn + M;
+  c.items = c.moved + (long long)M * nw;
+  c.pos = c.items + ((long long)M * N + 1) / 2;
+  c.dl = c.pos + ((long long)M * N + 1) / 2;
+  c.total = c.dl + ((long long)M * cap + 1) / 2;
+  return c;
+}
 
 // move mix as seen by the device
 struct MixDev {

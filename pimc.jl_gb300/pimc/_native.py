@@ -30,7 +30,8 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE]
-SOURCES = ["pimc_sweep.cu", "pimc_api.cu", "pimc_io.cpp"]
+SOURCES = ["pimc_sweep.cu", "pimc_swap.cu", "pimc_fused.cu", "pimc_attempt.cu", "pimc_api.cu",
+           "pimc_io.cpp"]
 
 
 class PimcError(RuntimeError):
@@ -126,7 +127,7 @@ class Launch(C.Structure):
     _fields_ = [("warp_per_chain", C.c_int), ("block", C.c_int),
                 ("sweeps_per_launch", C.c_int), ("state_smem_bytes", C.c_int),
                 ("split_phases", C.c_int), ("phase_block", C.c_int * 3),
-                ("phase_warp", C.c_int * 3)]
+                ("phase_warp", C.c_int * 3), ("phase_regs", C.c_int * 3)]
 
 
 # every symbol include/pimc.h declares, with its argument types

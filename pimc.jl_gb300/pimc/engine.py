@@ -20,6 +20,8 @@ NOBS = 8  # columns of an observable row (PIMC_NOBS)
 REJECT, ACCEPT, SKIP, HARDCORE = 0, 1, 2, 3
 OPT_FORCE_WARP_WINDOW = 1
 OPT_EXACT_DECISIONS = 2
+OPT_CELL_LISTS = 3
+OPT_CELL_CROWDING = 4
 
 
 def _dp(a):
@@ -274,10 +276,12 @@ class Engine:
 
     def set_launch(self, block: int, sweeps_per_launch: int = 1,
                    state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False,
-                   split_phases: int = 0, phase_block=(0, 0, 0), phase_warp=(0, 0, 0)):
+                   split_phases: int = 0, phase_block=(0, 0, 0), phase_warp=(0, 0, 0),
+                   phase_regs=(0, 0, 0)):
         l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes,
                    int(split_phases), (C.c_int * 3)(*[int(b) for b in phase_block]),
-                   (C.c_int * 3)(*[int(w) for w in phase_warp]))
+                   (C.c_int * 3)(*[int(w) for w in phase_warp]),
+                   (C.c_int * 3)(*[int(r) for r in phase_regs]))
         check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
 
     @property
@@ -288,7 +292,7 @@ class Engine:
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
                 "split_phases": l.split_phases, "phase_block": list(l.phase_block),
-                "phase_warp": list(l.phase_warp)}
+                "phase_warp": list(l.phase_warp), "phase_regs": list(l.phase_regs)}
 
     def phase_times(self, n_sweeps: int = 2):
         """device ms of the staging, swap and remaining phases over n sweeps,
@@ -315,6 +319,14 @@ class Engine:
 
     def set_option(self, key: int, value: int):
         check(self.L.pimc_set_option(self.h, key, value))
+
+    def set_cells(self, mode: int, crowding: float | None = None):
+        """neighbour candidates from per-slice cell lists: mode 0 off (scan the
+        slice), 1 auto (lists except on slices whose 3^dim sum n_c^2 exceeds
+        crowding * N^2; default crowding 0.5), 2 always"""
+        self.set_option(OPT_CELL_LISTS, int(mode))
+        if crowding is not None:
+            self.set_option(OPT_CELL_CROWDING, int(round(crowding * 1000)))
 
     # ------------------------------------------------------------- attempts
     def attempt_staging(self, n, j0, m, normals, uniforms=()):
@@ -526,4 +538,4 @@ class Engine:
 
 __all__ = ["Engine", "ChainParams", "Mix", "EngineStats", "PimcError", "SEM_REFERENCE",
            "SEM_PHYSICAL", "REJECT", "ACCEPT", "SKIP", "HARDCORE", "OPT_FORCE_WARP_WINDOW",
-           "OPT_EXACT_DECISIONS"]
+           "OPT_EXACT_DECISIONS", "OPT_CELL_LISTS", "OPT_CELL_CROWDING"]

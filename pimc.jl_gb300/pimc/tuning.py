@@ -17,7 +17,7 @@ import os
 from collections import Counter
 
 LAUNCH_KEYS = ("warp_per_chain", "block", "sweeps_per_launch", "state_smem_bytes",
-               "split_phases", "phase_block", "phase_warp")
+               "split_phases", "phase_block", "phase_warp", "phase_regs")
 
 
 def n_bucket(N: int) -> int:
@@ -57,7 +57,7 @@ class TuneCache:
 
     def put(self, signature: str, launch: dict, ms_per_sweep: float | None = None):
         entry = {k: launch[k] for k in LAUNCH_KEYS}
-        for k in ("phase_block", "phase_warp"):
+        for k in ("phase_block", "phase_warp", "phase_regs"):
             entry[k] = [int(x) for x in entry[k]]
         if ms_per_sweep is not None:
             entry["ms_per_sweep"] = float(ms_per_sweep)

@@ -182,7 +182,12 @@ def test_batched_equals_plain_and_tuner_is_transparent():
               dict(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
                    phase_block=[128, 64, 128], phase_warp=[0, 1, 0]),
               dict(block=128, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
-                   phase_block=[128, 32, 0], phase_warp=[0, 1, 0])]
+                   phase_block=[128, 32, 0], phase_warp=[0, 1, 0]),
+              # the swap kernels compiled for 170 and 255 registers a thread
+              dict(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
+                   phase_block=[128, 64, 128], phase_regs=[0, 170, 0]),
+              dict(block=64, sweeps_per_launch=1, state_smem_bytes=32 * 1024, split_phases=1,
+                   phase_regs=[0, 255, 0])]
     b = Engine(ps)
     for i, p in enumerate(ps):
         b.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
@@ -222,7 +227,13 @@ def test_launch_shape_rejects_bad_values():
                 dict(block=64, split_phases=1, phase_warp=(1, 0, 0)),
                 dict(block=64, split_phases=0, phase_block=(0, 64, 0), phase_warp=(0, 1, 0)),
                 dict(block=64, split_phases=1, phase_block=(0, 512, 0), phase_warp=(0, 1, 0)),
-                dict(block=64, split_phases=1, phase_warp=(0, 2, 0))]:
+                dict(block=64, split_phases=1, phase_warp=(0, 2, 0)),
+                dict(block=64, split_phases=0, phase_regs=(0, 170, 0)),
+                dict(block=64, split_phases=1, phase_regs=(0, 200, 0)),
+                dict(block=64, split_phases=1, phase_regs=(170, 0, 0)),
+                dict(block=64, split_phases=1, phase_block=(0, 128, 0), phase_regs=(0, 255, 0)),
+                dict(block=64, split_phases=1, phase_block=(0, 64, 0), phase_warp=(0, 1, 0),
+                     phase_regs=(0, 170, 0))]:
         with pytest.raises(PimcError):
             e.set_launch(**bad)
     e.close()

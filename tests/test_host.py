@@ -240,7 +240,8 @@ def test_tune_cache_round_trip(tmp_path):
     assert [n_bucket(n) for n in (8, 15, 16, 300, 512)] == [8, 8, 16, 256, 512]
     path = str(tmp_path / "tune.json")
     shape = dict(warp_per_chain=False, block=64, sweeps_per_launch=1, state_smem_bytes=0,
-                 split_phases=1, phase_block=[128, 64, 128], phase_warp=[0, 1, 0])
+                 split_phases=1, phase_block=[128, 64, 128], phase_warp=[0, 1, 0],
+                 phase_regs=[0, 0, 0])
     tc = TuneCache(path)
     assert tc.get(sig) is None
     tc.put(sig, shape, ms_per_sweep=35.7)
