@@ -526,23 +526,30 @@ def run_ours(args):
     if not args.no_e2e:
         xh, keep = pinned_empty(eng.beads_all_size())
         eng.get_beads_all(xh)
+
+        # a step: the state in from pinned host memory, one sweep, the state
+        # and the estimator sums back; a batch overlaps its copies with the
+        # sweeps in chunks of chains (pimc_batch_run_io)
+        def step():
+            if batched:
+                eng.run_io(xh, 1, chunks=args.io_chunks)
+            else:
+                eng.set_beads_all(xh)
+                run(1)
+                eng.get_beads_all(xh)
+            eng.energy_sums_all()
+
         # one untimed step: the legs before this one leave other work's state
         # in the caches and the clocks
-        eng.set_beads_all(xh)
-        run(1)
-        eng.get_beads_all(xh)
-        eng.energy_sums_all()
+        step()
         e0 = eng.total_stats()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            eng.set_beads_all(xh)
-            run(1)
-            eng.get_beads_all(xh)
-            eng.energy_sums_all()
+            step()
         et = time.perf_counter() - t0
         e1 = eng.total_stats()
-        # one more step with each call timed on its own (host clock; every
-        # call returns after its device work)
+        # one more step with the three calls apart (host clock; every call
+        # returns after its device work)
         tb = []
         for f in (lambda: eng.set_beads_all(xh), lambda: run(1), lambda: eng.get_beads_all(xh),
                   eng.energy_sums_all):
@@ -553,10 +560,14 @@ def run_ours(args):
         nb = 8 * eng.beads_all_size()
         out["e2e"] = {"value": ebeads / emax, "unit": UNIT, "h2d_bytes_per_step": nb,
                       "d2h_bytes_per_step": nb + 8 * 9 * len(chains),
-                      "path": "pimc_batch_set_beads_all (pinned host) -> pimc_run -> "
-                              "pimc_batch_get_beads_all + pimc_batch_energy_sums_all",
-                      "breakdown_ms": {"set_beads_all": tb[0], "sweep": tb[1],
-                                       "get_beads_all": tb[2], "energy_sums_all": tb[3]}}
+                      "ms_per_step": emax * 1e3 / args.steps,
+                      "path": (f"pimc_batch_run_io (pinned host buffer in place, {args.io_chunks or 4} "
+                               "chunks of chains: uploads and downloads on two copy streams beside "
+                               "the sweeps) + pimc_batch_energy_sums_all") if batched else
+                              ("pimc_batch_set_beads_all (pinned host) -> pimc_run -> "
+                               "pimc_batch_get_beads_all + pimc_batch_energy_sums_all"),
+                      "calls_apart_ms": {"set_beads_all": tb[0], "sweep": tb[1],
+                                         "get_beads_all": tb[2], "energy_sums_all": tb[3]}}
     # the adjoint of every chain of the batch in one call (four launches),
     # device time by CUDA events; a step of "batched + adjoint" is one sweep
     # of every chain followed by the adjoint of every chain
@@ -649,6 +660,8 @@ def main():
                     help="skip the C4 sample's energies against the oracle's statistics")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--io-chunks", type=int, default=0,
+                    help="chunks of chains of the end-to-end step's overlapped copies (0: 4)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=6.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)

@@ -165,6 +165,16 @@ int pimc_run(void *handle, long long n_sweeps);
 int pimc_batch_run(void *handle, long long n_sweeps);
 /* the same sweeps issued as one plain launch per chain (no queue, no graph) */
 int pimc_batch_run_plain(void *handle, long long n_sweeps);
+/* pimc_batch_set_beads_all(x_in), pimc_batch_run(n_sweeps),
+ * pimc_batch_get_beads_all(x_out) as one call that overlaps the copies with
+ * the sweeps: the chains go in `chunks` contiguous groups of about equal work
+ * (chunks <= 0: 4); one group's upload or download (DMA on two copy
+ * streams; page-locked buffers make it asynchronous) runs while another
+ * sweeps.  The chains reach the same states as by the three calls.  x_in
+ * and x_out may be the same buffer.  pimc_last_run_ms gives the device time
+ * from the first upload to the last download. */
+int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long n_sweeps,
+                      int chunks);
 /* launch shape of pimc_batch_run.  warp_per_chain = 0: one CTA of `block`
  * threads per chain, the chain's state staged in shared memory when it fits
  * state_smem_bytes.  warp_per_chain = 1: every warp of a `block`-thread CTA

@@ -120,7 +120,20 @@ struct Handle {
   // the batch's 32 x 32 (particle, slice) tiles: first tile of each chain
   int *d_tile_off = nullptr;
   int ntiles = 0;
+  std::vector<int> tile_off;  // the same on the host
+  // pimc_batch_run_io: copy streams, per-chunk events, the chunks' chain
+  // ranges and work orders, made on first use for a chunk count
+  cudaStream_t s_up = nullptr, s_down = nullptr;
+  std::vector<cudaEvent_t> io_ev;
+  std::vector<int> io_cut;     // chunk k holds chains [io_cut[k], io_cut[k + 1])
+  int *d_io_order = nullptr;   // chunk k's chains longest first, at io_cut[k]
+  int *d_io_queue = nullptr;   // one work-queue counter per chunk
 };
+
+// the LPT cost of a chain (staging and CoM ~ N M, swaps ~ N^2)
+double chain_cost(const pimc_params &p) {
+  return (double)p.N * p.M * (p.interactions ? 4.0 : 1.0) + 0.5 * (double)p.N * p.N;
+}
 
 int check_params(const pimc_params &p) {
   if (p.dim < 1 || p.dim > 2) return fail(PIMC_EARG, "dim must be 1 or 2");
@@ -516,11 +529,7 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
   std::vector<int> order(nchains);
   for (int c = 0; c < nchains; ++c) order[c] = c;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    auto cost = [&](int c) {
-      const pimc_params &p = h->params[c];
-      return (double)p.N * p.M * (p.interactions ? 4.0 : 1.0) + 0.5 * (double)p.N * p.N;
-    };
-    return cost(a) > cost(b);
+    return chain_cost(h->params[a]) > chain_cost(h->params[b]);
   });
   cudaMemcpyAsync(h->d_order, order.data(), sizeof(int) * nchains, cudaMemcpyHostToDevice, h->stream);
   if (upload_desc(h)) return cleanup(PIMC_ECUDA);
@@ -657,7 +666,7 @@ int swap_spec(const Handle *h) {
 
 // resident CTAs (or warps) for a launch of the plan's kernel; phase >= 0
 // names a phase kernel of a split plan
-int grid_for(Handle *h, const Plan &p, int phase = -1) {
+int grid_for(Handle *h, const Plan &p, int phase = -1, int nch = -1) {
   int per_sm = 0;
   const cudaError_t e = phase >= 0
                             ? sweep_phase_occupancy(phase, p.pwarp[phase], swap_spec(h), p.pregs[phase],
@@ -666,7 +675,8 @@ int grid_for(Handle *h, const Plan &p, int phase = -1) {
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
   const bool warp = phase >= 0 ? p.pwarp[phase] != 0 : p.mode == 1;
   const int units_per_cta = warp ? phase_block(p, phase >= 0 ? phase : 0) / 32 : 1;
-  const int need = (h->nchains + units_per_cta - 1) / units_per_cta;
+  const int chains = nch >= 0 ? nch : h->nchains;
+  const int need = (chains + units_per_cta - 1) / units_per_cta;
   return std::max(1, std::min(need, per_sm * h->num_sms));
 }
 
@@ -695,11 +705,14 @@ cudaError_t plan_set_smem(const Handle *h, const Plan &p) {
 // n sweeps of every chain as launches on the stream: one launch of n sweeps,
 // or for a split plan n rounds of (staging, swaps, rest), each from a reset
 // work queue
+// a.queue: the work-queue counter of the launches (a.order names a.nchains
+// chains)
 cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long *launches) {
   if (!p.split) {
     a.sweeps = n;
-    cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
-    if (e == cudaSuccess) e = launch_sweep(a, p.mode, grid_for(h, p), p.block, p.dyn_smem, h->stream);
+    cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(int), h->stream);
+    if (e == cudaSuccess)
+      e = launch_sweep(a, p.mode, grid_for(h, p, -1, a.nchains), p.block, p.dyn_smem, h->stream);
     if (launches) *launches += 1;
     return e;
   }
@@ -708,9 +721,9 @@ cudaError_t issue_sweeps(Handle *h, const Plan &p, SweepArgs a, int n, long long
     for (int ph = 0; ph < 3; ++ph) {
       SweepArgs b = a;
       if (p.pwarp[ph]) b.warp_bytes = p.pwarp_bytes[ph];
-      cudaError_t e = cudaMemsetAsync(h->d_queue, 0, sizeof(int), h->stream);
+      cudaError_t e = cudaMemsetAsync(a.queue, 0, sizeof(int), h->stream);
       if (e == cudaSuccess)
-        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), p.pregs[ph], grid_for(h, p, ph),
+        e = launch_sweep_phase(b, ph, p.pwarp[ph], swap_spec(h), p.pregs[ph], grid_for(h, p, ph, a.nchains),
                                phase_block(p, ph), phase_smem(p, ph), h->stream);
       if (e != cudaSuccess) return e;
       if (launches) *launches += 1;
@@ -880,6 +893,49 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
 int pimc_fail(int code, const std::string &msg) { return fail(code, msg); }
 
 // ===================================================================== C ABI
+// pimc_batch_run_io's chunks: contiguous chain ranges of about equal LPT
+// cost, each with its own longest-first order and work-queue counter on the
+// device, and an upload and a done event per chunk
+int io_prepare(Handle *h, int chunks) {
+  if ((int)h->io_cut.size() == chunks + 1) return PIMC_OK;
+  std::vector<double> cum(h->nchains + 1, 0.0);
+  for (int c = 0; c < h->nchains; ++c) cum[c + 1] = cum[c] + chain_cost(h->params[c]);
+  std::vector<int> cut(chunks + 1, 0);
+  cut[chunks] = h->nchains;
+  for (int k = 1; k < chunks; ++k) {
+    const double target = cum[h->nchains] * k / chunks;
+    int c = (int)(std::lower_bound(cum.begin(), cum.end(), target) - cum.begin());
+    c = std::max(cut[k - 1] + 1, std::min(c, h->nchains - (chunks - k)));
+    cut[k] = c;
+  }
+  std::vector<int> order(h->nchains);
+  for (int k = 0; k < chunks; ++k) {
+    for (int c = cut[k]; c < cut[k + 1]; ++c) order[c] = c;
+    std::stable_sort(order.begin() + cut[k], order.begin() + cut[k + 1], [&](int a, int b) {
+      return chain_cost(h->params[a]) > chain_cost(h->params[b]);
+    });
+  }
+  if (!h->s_up) {
+    CK(cudaStreamCreateWithFlags(&h->s_up, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->s_down, cudaStreamNonBlocking));
+  }
+  for (cudaEvent_t e : h->io_ev) cudaEventDestroy(e);
+  h->io_ev.assign(2 * chunks + 2, nullptr);  // per chunk upload and done; start; end
+  for (auto &e : h->io_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaFree(h->d_io_order);
+  cudaFree(h->d_io_queue);
+  h->d_io_order = nullptr;
+  h->d_io_queue = nullptr;
+  h->io_cut.clear();
+  CK(cudaMalloc(&h->d_io_order, sizeof(int) * h->nchains));
+  CK(cudaMalloc(&h->d_io_queue, sizeof(int) * chunks));
+  CK(cudaMemcpyAsync(h->d_io_order, order.data(), sizeof(int) * h->nchains, cudaMemcpyHostToDevice,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->io_cut = cut;
+  return PIMC_OK;
+}
+
 extern "C" {
 
 const char *pimc_last_error(void) { return g_err.c_str(); }
@@ -909,6 +965,11 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_buf);
   cudaFree(h->d_adj);
   cudaFree(h->d_stage);
+  cudaFree(h->d_io_order);
+  cudaFree(h->d_io_queue);
+  for (cudaEvent_t e : h->io_ev) cudaEventDestroy(e);
+  if (h->s_up) cudaStreamDestroy(h->s_up);
+  if (h->s_down) cudaStreamDestroy(h->s_down);
   for (auto &t : h->ctabs) cudaFree(t.d);
   cudaFree(h->d_rdf);
   cudaFree(h->d_badj);
@@ -963,6 +1024,7 @@ static int ensure_tiles(Handle *h) {
   }
   h->d_tile_off = d;
   h->ntiles = (int)t;
+  h->tile_off = off;
   return PIMC_OK;
 }
 
@@ -993,8 +1055,8 @@ int pimc_batch_set_beads_all(void *handle, const double *x_all) {
     CK(cudaMemcpyAsync(h->d_stage, x_all, h->n_stage * 8, cudaMemcpyHostToDevice, h->stream));
     src = h->d_stage;
   }
-  CK(launch_transpose_tiles(true, h->d_desc, h->d_dpool, src, h->d_tile_off, h->nchains, h->ntiles,
-                            8 * h->num_sms, h->stream));
+  CK(launch_transpose_tiles(true, h->d_desc, h->d_dpool, src, h->d_tile_off, 0, h->nchains,
+                            h->ntiles, 8 * h->num_sms, h->stream));
   if (refresh_links(h, 0, h->nchains)) return PIMC_ECUDA;
   return sync_check(h);
 }
@@ -1005,11 +1067,86 @@ int pimc_batch_get_beads_all(void *handle, double *x_all) {
   int rc = ensure_tiles(h);
   if (rc) return rc;
   double *dst = device_view(x_all);
-  CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, dst ? dst : h->d_stage, h->d_tile_off,
+  CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, dst ? dst : h->d_stage, h->d_tile_off, 0,
                             h->nchains, h->ntiles, 8 * h->num_sms, h->stream));
   if (!dst)
     CK(cudaMemcpyAsync(x_all, h->d_stage, h->n_stage * 8, cudaMemcpyDeviceToHost, h->stream));
   return sync_check(h);
+}
+
+// upload, sweep and download the batch in chunks of chains so that the
+// copies of one chunk overlap the sweeps of another: chunk k's positions go
+// host -> staging buffer on the upload stream; on the compute stream chunk k
+// waits for them, is transposed into the device layout, has its links
+// refreshed, sweeps n times (the batched launch shape, its own work queue)
+// and is transposed back; the download stream then copies it to x_out.
+// With page-locked buffers the copies are DMA transfers that run beside the
+// sweeps.  x_in and x_out may be the same buffer.
+int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long n_sweeps, int chunks) {
+  Handle *h = H(handle);
+  if (!h || !x_in || !x_out || n_sweeps < 0) return fail(PIMC_EARG, "bad argument");
+  if (chunks <= 0) chunks = 4;
+  chunks = std::max(1, std::min(chunks, h->nchains));
+  int rc = ensure_tiles(h);
+  if (rc) return rc;
+  if ((rc = io_prepare(h, chunks))) return rc;
+  const Plan &p = h->bat;
+  CK(plan_set_smem(h, p));
+  CK(cudaEventRecord(h->ev0, h->stream));
+  cudaEvent_t start = h->io_ev[2 * chunks];
+  CK(cudaEventRecord(start, h->stream));
+  CK(cudaStreamWaitEvent(h->s_up, start, 0));
+  CK(cudaStreamWaitEvent(h->s_down, start, 0));
+  long long launches = 0;
+  for (int k = 0; k < chunks; ++k) {
+    const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
+    const size_t off = (size_t)h->desc[c0].host_off;
+    const size_t n = (c1 < h->nchains ? (size_t)h->desc[c1].host_off : h->n_stage) - off;
+    CK(cudaMemcpyAsync(h->d_stage + off, x_in + off, n * sizeof(double), cudaMemcpyHostToDevice,
+                       h->s_up));
+    CK(cudaEventRecord(h->io_ev[2 * k], h->s_up));
+  }
+  for (int k = 0; k < chunks; ++k) {
+    const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
+    const int nt = h->tile_off[c1] - h->tile_off[c0];
+    CK(cudaStreamWaitEvent(h->stream, h->io_ev[2 * k], 0));
+    CK(launch_transpose_tiles(true, h->d_desc, h->d_dpool, h->d_stage, h->d_tile_off, c0, c1, nt,
+                              8 * h->num_sms, h->stream));
+    CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, c0, c1 - c0, h->maxNM, h->stream));
+    launches += 2;
+    if (n_sweeps > 0) {
+      SweepArgs a = sweep_args(h, p);
+      a.order = h->d_io_order + c0;
+      a.nchains = c1 - c0;
+      a.queue = h->d_io_queue + k;
+      a.teams = launch_teams(h, p);
+      const int spl = std::max(1, p.spl);
+      for (long long done = 0; done < n_sweeps; done += spl)
+        CK(issue_sweeps(h, p, a, (int)std::min<long long>(spl, n_sweeps - done), &launches));
+    }
+    CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, h->d_stage, h->d_tile_off, c0, c1, nt,
+                              8 * h->num_sms, h->stream));
+    launches += 1;
+    CK(cudaEventRecord(h->io_ev[2 * k + 1], h->stream));
+  }
+  for (int k = 0; k < chunks; ++k) {
+    const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
+    const size_t off = (size_t)h->desc[c0].host_off;
+    const size_t n = (c1 < h->nchains ? (size_t)h->desc[c1].host_off : h->n_stage) - off;
+    CK(cudaStreamWaitEvent(h->s_down, h->io_ev[2 * k + 1], 0));
+    CK(cudaMemcpyAsync(x_out + off, h->d_stage + off, n * sizeof(double), cudaMemcpyDeviceToHost,
+                       h->s_down));
+  }
+  CK(cudaEventRecord(h->io_ev[2 * chunks + 1], h->s_down));
+  CK(cudaStreamWaitEvent(h->stream, h->io_ev[2 * chunks + 1], 0));
+  CK(cudaEventRecord(h->ev1, h->stream));
+  rc = sync_check(h);
+  if (rc) return rc;
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  h->last_ms = ms;
+  h->last_launches = launches;
+  return check_device_errors(h);
 }
 
 int pimc_batch_energy_sums_all(void *handle, double *sum, double *sumsq, unsigned long long *count) {

@@ -272,6 +272,9 @@ __device__ __forceinline__ unsigned qdist2(unsigned a, unsigned b) {
 // found the cells too crowded to pay (dn = kCellOff), is scanned row-wise.
 // ---------------------------------------------------------------------------
 constexpr int kCellOff = 1 << 30;
+// sweeps for which a chain whose build found most slices crowded scans rows
+// without building
+constexpr int kCellHold = 8;
 
 struct CellLists {
   int N, nc, ncq, cap, nw;
@@ -463,11 +466,12 @@ __device__ __forceinline__ void cell_block(const CellLists &L, int j, int x0, in
 // and qb (the old and the new position of a moving bead; qa == qb for one
 // centre).  Centres in the same or in adjacent cells share one block of
 // cells (sides 3 for every candidate); farther apart each has its own.
-// Returns false, having called nothing, when slice j has no usable lists.
+// use: L->usable(j), which callers read ahead of the query.  Returns false,
+// having called nothing, when slice j has no usable lists.
 template <class F>
-__device__ __forceinline__ bool cell_query(const CellLists *L, int j, unsigned qa, unsigned qb,
-                                           int lane, F &&f) {
-  if (!L || !L->usable(j)) return false;
+__device__ __forceinline__ bool cell_query(const CellLists *L, bool use, int j, unsigned qa,
+                                           unsigned qb, int lane, F &&f) {
+  if (!L || !use) return false;
   const int nc = L->nc, h = nc >> 1;
   const int ax = L->cx(qa), ay = L->cy(qa), bx = L->cx(qb), by = L->cy(qb);
   int dx = bx - ax, dy = by - ay;
@@ -813,7 +817,11 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
   const int N = c.N, dim = c.dim;
   const unsigned lt = (1u << lane) - 1u;
   int qn = 0;
+  const CellLists *L = c.cl;
+  bool use_next = L && t0 < t1 && L->usable(s.slice(t0));
   for (int t = t0; t < t1; ++t) {
+    const bool use = use_next;
+    if (L && t + 1 < t1) use_next = L->usable(s.slice(t + 1));
     const int j = s.slice(t);
     const unsigned co = s.curq(0, t), cn = s.curq(1, t);
     Prefilter fo, fn;
@@ -843,7 +851,7 @@ __device__ void segment_sums(const CV &c, const Seg &s, int t0, int t1, bool do_
       // holds at most 31 + 64 = 95 < PQ_CAP entries at any time
       while (qn >= 32) pq_flush<CT>(c, s, q, qn, wo, wn, lane);
     };
-    const bool listed = cell_query(c.cl, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
+    const bool listed = cell_query(L, use, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
       bool po = false, pn = false;
       if (v) {
         const unsigned pb = row[b];
@@ -946,7 +954,12 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
                                  const Stop &stop = Stop()) {
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M;
+  // whether a slice's lists are usable is read one link ahead
+  const CellLists *L = c.cl;
+  bool use_next = L && t0 < t1 && L->usable(s.slice(t0));
   for (int t = t0; t < t1; ++t) {
+    const bool use = use_next;
+    if (L && t + 1 < t1) use_next = L->usable(s.slice(t + 1));
     const int j = s.slice(t), jn = j + 1 == M ? 0 : j + 1;
     const bool wrap = j == M - 1;
     const unsigned co = s.curq(0, t), cn = s.curq(1, t);
@@ -969,7 +982,7 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
     };
     // a cell-list candidate: the sides its block serves, the word at slice
     // j+1 read only for a pair that passes
-    const bool listed = cell_query(c.cl, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
+    const bool listed = cell_query(L, use, j, co, cn, lane, [&](int b, bool v, unsigned sides) {
       if (!v) return;
       const unsigned pb = row[b];
       const unsigned d2o = qdist2(co, pb), d2n = qdist2(cn, pb);
@@ -1102,7 +1115,7 @@ __device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, 
   const unsigned *row = c.xq + (size_t)j * c.ldn;
   bool hit = false;
   // the cell lists serve whole warps only
-  if (lanes == 32 && cell_query(c.cl, j, f.c, f.c, lane, [&](int b, bool v, unsigned) {
+  if (lanes == 32 && cell_query(c.cl, c.cl && c.cl->usable(j), j, f.c, f.c, lane, [&](int b, bool v, unsigned) {
         if (!v || hit || b == e1 || b == e2 || !f.pass(row[b])) return;
         if (mi2(d, x, y, c.X(0, b, j), c.Xd(1, b, j)) < a2) hit = true;
       }))

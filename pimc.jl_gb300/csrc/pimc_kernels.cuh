@@ -231,10 +231,11 @@ struct Group {
 // (ws_ints ints for the group) when it has room for ncq + 1 of them, else in
 // end[] itself.  cl_mode 1: a slice whose cells hold 3^dim sum n_c^2 >
 // cl_frac N^2 pairs (the block around a particle would hold most of the
-// slice) is marked for the row scan.
+// slice) is marked for the row scan.  nusable (shared) counts the slices
+// whose lists are usable.
 // ---------------------------------------------------------------------------
 template <bool WARP>
-__device__ void cells_build(const CV &c, const CellLists &L, int *ws, int ws_ints) {
+__device__ void cells_build(const CV &c, const CellLists &L, int *ws, int ws_ints, int *nusable) {
   const ChainDesc &d = *c.d;
   const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
   const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
@@ -312,7 +313,9 @@ __device__ void cells_build(const CV &c, const CellLists &L, int *ws, int ws_int
     sq = warp_sum(sq);
     if (lane == 0) {
       const double pairs = (L.ncq == L.nc ? 3.0 : 9.0) * sq;
-      L.dn[j] = (d.cl_mode == 1 && pairs > (double)d.cl_frac * N * N) ? kCellOff : 0;
+      const bool crowded = d.cl_mode == 1 && pairs > (double)d.cl_frac * N * N;
+      L.dn[j] = crowded ? kCellOff : 0;
+      if (!crowded) atomicAdd(nusable, 1);
     }
     __syncwarp();
   }
@@ -1299,7 +1302,7 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
         if (qn >= 32) flush();
       };
       // partners of higher index: from the cell lists, or the rest of the row
-      if (cell_query(c.cl, j, f.c, f.c, lane,
+      if (cell_query(c.cl, c.cl && c.cl->usable(j), j, f.c, f.c, lane,
                      [&](int b, bool v, unsigned) { push(b, v && b > i && f.pass(row[b])); }))
         continue;
       for (int b0 = i + 1; b0 < N; b0 += 32) {

@@ -129,12 +129,13 @@ cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *ds
                           int nchains, size_t maxn, cudaStream_t s);
 cudaError_t launch_mirror(const ChainDesc *desc, double *dpool, int chain0, int nchains, int maxNM,
                           cudaStream_t s);
-// every chain's positions between the host layout (at desc.host_off of
-// `host`, which may be pinned host memory the GPU reaches directly) and the
-// device layout, in 32 x 32 tiles; tile_off[nchains + 1] on the device
+// the positions of chains [c_lo, c_hi) between the host layout (at
+// desc.host_off of `host`, which may be pinned host memory the GPU reaches
+// directly) and the device layout, in 32 x 32 tiles; tile_off[nchains + 1]
+// on the device, ntiles the range's tile count
 cudaError_t launch_transpose_tiles(bool import, const ChainDesc *desc, double *dpool,
-                                   double *host, const int *tile_off, int nchains, int ntiles,
-                                   int grid, cudaStream_t s);
+                                   double *host, const int *tile_off, int c_lo, int c_hi,
+                                   int ntiles, int grid, cudaStream_t s);
 cudaError_t launch_measure(const ChainDesc *desc, ChainVar *var, double *dpool, int *ipool,
                            unsigned long long *upool, int chain0, int nchains, cudaStream_t s);
 cudaError_t launch_adjoint(const AdjArgs &a, int nbeads, cudaStream_t s);

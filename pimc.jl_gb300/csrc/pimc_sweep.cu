@@ -65,8 +65,8 @@ __global__ void k_export(const ChainDesc *desc, const double *dpool, double *dst
 // which the GPU reads and writes directly over the coherent CPU-GPU link
 // (Grace-Blackwell NVLink-C2C): the copy and the transpose are one pass.
 // Persistent grid; each block walks tiles t = blockIdx.x, += gridDim.x.
-__device__ __forceinline__ int tile_chain(const int *tile_off, int nchains, int t) {
-  int lo = 0, hi = nchains;  // tile_off[lo] <= t < tile_off[hi]
+__device__ __forceinline__ int tile_chain(const int *tile_off, int c_lo, int c_hi, int t) {
+  int lo = c_lo, hi = c_hi;  // tile_off[lo] <= t < tile_off[hi]
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
     if (tile_off[mid] <= t) lo = mid; else hi = mid;
@@ -77,12 +77,12 @@ __device__ __forceinline__ int tile_chain(const int *tile_off, int nchains, int 
 template <bool IMPORT>
 __global__ void __launch_bounds__(256) k_transpose_tiles(const ChainDesc *desc, double *dpool,
                                                           double *host, const int *tile_off,
-                                                          int nchains) {
+                                                          int c_lo, int c_hi) {
   __shared__ double tile[2][32][33];
-  const int ntiles = tile_off[nchains];
+  const int t_end = tile_off[c_hi];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int c = tile_chain(tile_off, nchains, t);
+  for (int t = tile_off[c_lo] + blockIdx.x; t < t_end; t += gridDim.x) {
+    const int c = tile_chain(tile_off, c_lo, c_hi, t);
     const ChainDesc &d = desc[c];
     const int N = d.N, M = d.M, dim = d.dim;
     const int tj = (M + 31) >> 5, lt = t - tile_off[c];
@@ -692,11 +692,11 @@ cudaError_t launch_export(const ChainDesc *desc, const double *dpool, double *ds
   return cudaGetLastError();
 }
 cudaError_t launch_transpose_tiles(bool import, const ChainDesc *desc, double *dpool,
-                                   double *host, const int *tile_off, int nchains, int ntiles,
-                                   int grid, cudaStream_t s) {
+                                   double *host, const int *tile_off, int c_lo, int c_hi,
+                                   int ntiles, int grid, cudaStream_t s) {
   const int g = std::max(1, std::min(grid, ntiles));
-  if (import) k_transpose_tiles<true><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, nchains);
-  else k_transpose_tiles<false><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, nchains);
+  if (import) k_transpose_tiles<true><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, c_lo, c_hi);
+  else k_transpose_tiles<false><<<g, 256, 0, s>>>(desc, dpool, host, tile_off, c_lo, c_hi);
   return cudaGetLastError();
 }
 cudaError_t launch_init_world(const ChainDesc *desc, double *dpool, int *ipool, int chain0,

@@ -168,6 +168,21 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
   // that do not query run on c, whose moves mark nothing
   CV cq = c;
   cq.cl = d.cl_nc > 0 && d.cl_mode > 0 ? &sc.cl : nullptr;
+  // builds the lists for a phase that queries (every thread calls it); false
+  // (row scans, no marks) while the chain is held off, or when fewer than
+  // half of its slices have usable lists, which holds it off for the next
+  // kCellHold sweeps
+  auto build_lists = [&]() -> bool {
+    if (!cq.cl || sc.v.cl_hold > 0) return false;
+    if (tid == 0) sc.iflag[5] = 0;
+    G::sync();
+    cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4, &sc.iflag[5]);
+    G::sync();
+    const bool use = 2 * sc.iflag[5] >= M;
+    G::sync();
+    if (!use && tid == 0) sc.v.cl_hold = kCellHold;
+    return use;
+  };
   double *wsb = (double *)scratch + (size_t)warp * warp_scratch_d;
   // every carve below must fit the group's scratch (PIMC_CHECK builds)
   if (!check_ok((size_t)nwarps * warp_scratch_d * sizeof(double) <= (size_t)sc.scratch_bytes &&
@@ -187,10 +202,8 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
     const Stream so = make_stream(d, sweep, PH_STAGE_OFF, (unsigned)ph);
     const int o = min(M - 1, (int)(so.uni(0) * M));
     const int items = N * k;
-    if (serial_local && cq.cl) {
-      cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4);
-      G::sync();
-    }
+    const bool lists = serial_local && build_lists();
+    const CV &cw = lists ? cq : c;
     if (!serial_local) {
       // every window of the phase is independent: slot s of particle n moves
       // the beads strictly inside its slot; item order s*N + n makes
@@ -237,7 +250,7 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
           for (int n = 0; n < N; ++n) {
             GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + team * N + n)));
             const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-            const int r = window_team(cq, tm, n, st, m, dr, tb, warp_scratch_d);
+            const int r = window_team(cw, tm, n, st, m, dr, tb, warp_scratch_d);
             if (tm.w == 0 && lane == 0) {
               tal[0] += 1.0;
               tal[1] += r == RES_ACCEPT;
@@ -256,7 +269,7 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
         for (int n = 0; n < N; ++n) {
           GenDraws dr = gen_draws(make_stream(d, sweep, PH_STAGE, (unsigned)(ph * items + s * N + n)));
           const int m = min(len, 2 + (int)(dr.s.uni(DRAW_CHOICE) * (ell - 1)));
-          const int r = window_warp(cq, n, st, m, dr, false, wsb, nullptr);
+          const int r = window_warp(cw, n, st, m, dr, false, wsb, nullptr);
           if (lane == 0) {
             tal[0] += 1.0;
             tal[1] += r == RES_ACCEPT;
@@ -277,11 +290,7 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
     S.carve(scratch, N, nwarps);
     const int mmax = max(2, min(mix.swap_max, min(M - 1, WMAX)));
     const int sm = max(2, sc.v.swap_m);
-    const bool lists = cq.cl && (d.flags & (PF_PAIR | PF_HARD));
-    if (lists) {
-      cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4);
-      G::sync();
-    }
+    const bool lists = (d.flags & (PF_PAIR | PF_HARD)) && build_lists();
     const CV &cs = lists ? cq : c;
     for (int a = 0; a < mix.swaps_per_sweep; ++a) {
       const Stream ss = make_stream(d, sweep, PH_SWAP, (unsigned)a);
@@ -326,14 +335,12 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
     } else {
       ComScratch cs;
       cs.carve(scratch, N, M);
-      if (cq.cl) {
-        cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4);
-        G::sync();
-      }
+      const bool lists = build_lists();
+      const CV &cw = lists ? cq : c;
       for (int n = 0; n < N; ++n) {
         if (c.next[n] != n) continue;
         GenDraws dr = gen_draws(make_stream(d, sweep, PH_COM, (unsigned)(ph * N + n)));
-        const int r = com_group<WARP>(cq, n, false, step, dr, cs, red, sc.shift, &sc.iflag[2], nullptr);
+        const int r = com_group<WARP>(cw, n, false, step, dr, cs, red, sc.shift, &sc.iflag[2], nullptr);
         if (tid == 0) {
           tal[0] += 1.0;
           tal[1] += r == RES_ACCEPT;
@@ -351,11 +358,7 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
   for (int ph = 0; ph < mix.polymer_com_phases; ++ph) {
     ComScratch cs;
     cs.carve(scratch, N, M);
-    const bool lists = serial_local && cq.cl;
-    if (lists) {
-      cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4);
-      G::sync();
-    }
+    const bool lists = serial_local && build_lists();
     const CV &cp = lists ? cq : c;
     for (int n = 0; n < N; ++n) {
       if (tid == 0) {
@@ -384,15 +387,14 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
 
   // ---- measurement cadence (measurement_Z_sector)
   if (mix.measure_every > 0 && ((sweep + 1) % (unsigned long long)mix.measure_every) == 0) {
-    const bool lists = cq.cl && (d.flags & PF_PAIR) && !(d.flags & PF_CONTACT);
-    if (lists) {
-      cells_build<WARP>(cq, sc.cl, (int *)scratch, sc.scratch_bytes / 4);
-      G::sync();
-    }
+    const bool lists = (d.flags & PF_PAIR) && !(d.flags & PF_CONTACT) && build_lists();
     measure_group<WARP>(lists ? cq : c, red, sc.e4, c.hist != nullptr, (unsigned long long *)scratch);
     if (tid == 0) record_measurement(d, sc.v, c, sc.e4, c.hist != nullptr);
   }
-  if (tid == 0) sc.v.sweep++;
+  if (tid == 0) {
+    sc.v.sweep++;
+    if (sc.v.cl_hold > 0) --sc.v.cl_hold;
+  }
   G::sync();
 }
 

@@ -146,7 +146,7 @@ struct ChainVar {
   unsigned long long n_meas, ndata, eser_count;
   double esum[NOBS], esum2[NOBS];
   int err;
-  int pad_;
+  int cl_hold;  // sweeps left during which the chain's crowded cell lists are not built
   unsigned long long rdf_meas;  // measurements in the pair-distance histogram
   double beads_kind[4];         // bead updates by move kind
 };

@@ -155,6 +155,7 @@ SIGNATURES = {
     "pimc_run": [_vp, C.c_longlong],
     "pimc_batch_run": [_vp, C.c_longlong],
     "pimc_batch_run_plain": [_vp, C.c_longlong],
+    "pimc_batch_run_io": [_vp, _dp, _dp, C.c_longlong, C.c_int],
     "pimc_batch_tune": [_vp, C.c_int, C.POINTER(Launch)],
     "pimc_batch_set_launch": [_vp, C.POINTER(Launch)],
     "pimc_batch_get_launch": [_vp, C.POINTER(Launch)],

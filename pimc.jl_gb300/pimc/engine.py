@@ -245,6 +245,18 @@ class Engine:
     def run_plain(self, n_sweeps: int):
         check(self.L.pimc_batch_run_plain(self.h, int(n_sweeps)))
 
+    def run_io(self, x_in, n_sweeps: int, x_out=None, chunks: int = 0):
+        """set_beads_all(x_in), run_batched(n_sweeps), get_beads_all(x_out) in
+        one call whose copies overlap the sweeps (chunks of chains; 0: 4);
+        x_out may be x_in (in place); returns x_out"""
+        for a in (x_in,) if x_out is None else (x_in, x_out):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous
+                    and a.size == self.beads_all_size()):
+                raise PimcError("x_in / x_out must be contiguous float64 arrays of beads_all_size()")
+        x_out = x_in if x_out is None else x_out
+        check(self.L.pimc_batch_run_io(self.h, _dp(x_in), _dp(x_out), int(n_sweeps), int(chunks)))
+        return x_out
+
     def device_name(self) -> str:
         buf = C.create_string_buffer(256)
         sms = C.c_int()

@@ -187,3 +187,47 @@ def test_init_world_hard_core():
     e.close()
     with pytest.raises(PimcError, match="creating world of 40 particles with hardspheres"):
         Engine(_pair_chain(300, N=40, M=8, L=1.0, hardcore_a=0.5, pair_g=0.0, r_a=0.6))
+
+
+def test_run_io_equals_set_run_get():
+    """pimc_batch_run_io (upload, sweep and download in overlapped chunks of
+    chains) leaves every chain as set_beads_all + run_batched + get_beads_all
+    do, bit for bit, with pinned and pageable buffers, in place or not"""
+    torch = pytest.importorskip("torch")
+    from pimc.engine import Engine
+    rng = np.random.default_rng(91)
+    ps = [_pair_chain(400 + i, N=int(rng.integers(2, 90)), M=int(rng.choice([8, 16, 33])),
+                      interactions=bool(i % 2), dim=int(1 + (i % 3 > 0))) for i in range(11)]
+
+    def fresh():
+        e = Engine(ps)
+        for c, p in enumerate(ps):
+            e.set_mix(_mix(p.N, p.M, measure_every=1), chain=c)
+        return e
+
+    a = fresh()
+    n = a.beads_all_size()
+    x0 = a.get_beads_all().copy()
+    a.set_beads_all(x0)
+    a.run_batched(3)
+    want = a.get_beads_all()
+    want_e = a.energy_sums_all()[0]
+    want_next = [a.get_next(c) for c in range(len(ps))]
+    a.close()
+    for chunks, pinned, inplace in [(1, True, False), (3, True, True), (0, False, False),
+                                    (11, False, True), (64, True, False)]:
+        b = fresh()
+        if pinned:
+            xin = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+            xout = torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+        else:
+            xin, xout = np.empty(n), np.empty(n)
+        xin[:] = x0
+        xout[:] = np.nan
+        got = b.run_io(xin, 3, x_out=None if inplace else xout, chunks=chunks)
+        np.testing.assert_array_equal(got, want)
+        np.testing.assert_array_equal(b.energy_sums_all()[0], want_e)
+        for c in range(len(ps)):
+            np.testing.assert_array_equal(b.get_next(c), want_next[c])
+        assert b.last_run_ms() > 0
+        b.close()
