@@ -382,6 +382,9 @@ def run_ours(args):
         launch = dict(eng.launch, tuned=False)
     elif batched and args.tune:
         launch = eng.tune(sweeps_per_trial=1)
+        if args.cells is not None:  # an explicit choice outranks the tuner's
+            eng.set_cells(args.cells, args.crowding)
+            launch = eng.launch
     for _ in range(args.warmup):
         run(1)
     prof = os.environ.get("PIMC_PROFILE", "0") == "1"
@@ -429,9 +432,11 @@ def run_ours(args):
            "l2": (f"chain state {state_bytes / 1e9:.2f} GB > 129 MB L2"
                   if state_bytes > 129e6 else f"chain state {state_bytes / 1e6:.1f} MB (L2/shared resident)"),
            "bead_updates_per_step": beads / args.steps,
-           "neighbour_candidates": ({0: "slice scan", 2: "cell lists"}.get(args.cells)
-                                    or "cell lists where they pay (crowding bound "
-                                    f"{0.5 if args.crowding is None else args.crowding}), else slice scan")}
+           "neighbour_candidates": {0: "slice scan", 2: "cell lists"}.get(
+               (launch["cell_lists"] - 1) if launch and launch.get("cell_lists")
+               else (1 if args.cells is None else args.cells),
+               "cell lists where they pay (crowding bound "
+               f"{0.5 if args.crowding is None else args.crowding}), else slice scan")}
     if batched and launch:
         cfg["launch"] = dict({"tuned": True}, **launch)
     out["config"] = cfg
@@ -528,8 +533,8 @@ def run_ours(args):
         eng.get_beads_all(xh)
 
         # a step: the state in from pinned host memory, one sweep, the state
-        # and the estimator sums back; a batch overlaps its copies with the
-        # sweeps in chunks of chains (pimc_batch_run_io)
+        # and the estimator sums back; a batch does the first three in one
+        # call (pimc_batch_run_io)
         def step():
             if batched:
                 eng.run_io(xh, 1, chunks=args.io_chunks)
@@ -561,9 +566,9 @@ def run_ours(args):
         out["e2e"] = {"value": ebeads / emax, "unit": UNIT, "h2d_bytes_per_step": nb,
                       "d2h_bytes_per_step": nb + 8 * 9 * len(chains),
                       "ms_per_step": emax * 1e3 / args.steps,
-                      "path": (f"pimc_batch_run_io (pinned host buffer in place, {args.io_chunks or 4} "
-                               "chunks of chains: uploads and downloads on two copy streams beside "
-                               "the sweeps) + pimc_batch_energy_sums_all") if batched else
+                      "path": ("pimc_batch_run_io (pinned host buffer in place: the layout "
+                               "transposes read and write it over the host link, one sweep of "
+                               "every chain in between) + pimc_batch_energy_sums_all") if batched else
                               ("pimc_batch_set_beads_all (pinned host) -> pimc_run -> "
                                "pimc_batch_get_beads_all + pimc_batch_energy_sums_all"),
                       "calls_apart_ms": {"set_beads_all": tb[0], "sweep": tb[1],
@@ -661,7 +666,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--io-chunks", type=int, default=0,
-                    help="chunks of chains of the end-to-end step's overlapped copies (0: 4)")
+                    help="chunks of chains of the end-to-end step's staged copies, used when "
+                         "the host buffer is not page-locked (0: 4)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=6.0)
     ap.add_argument("--ref-budget", type=float, default=8.0)

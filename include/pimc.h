@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PIMC_ABI_VERSION 4
+#define PIMC_ABI_VERSION 5
 /* columns of an observable row (pimc_get_observables) */
 #define PIMC_NOBS 8
 
@@ -166,13 +166,15 @@ int pimc_batch_run(void *handle, long long n_sweeps);
 /* the same sweeps issued as one plain launch per chain (no queue, no graph) */
 int pimc_batch_run_plain(void *handle, long long n_sweeps);
 /* pimc_batch_set_beads_all(x_in), pimc_batch_run(n_sweeps),
- * pimc_batch_get_beads_all(x_out) as one call that overlaps the copies with
- * the sweeps: the chains go in `chunks` contiguous groups of about equal work
- * (chunks <= 0: 4); one group's upload or download (DMA on two copy
- * streams; page-locked buffers make it asynchronous) runs while another
- * sweeps.  The chains reach the same states as by the three calls.  x_in
- * and x_out may be the same buffer.  pimc_last_run_ms gives the device time
- * from the first upload to the last download. */
+ * pimc_batch_get_beads_all(x_out) as one call with no host round trip in
+ * between.  When both buffers are page-locked, the layout transposes read
+ * x_in and write x_out in place over the host link (chunks is ignored).
+ * Otherwise the positions move through a staging buffer in `chunks`
+ * contiguous groups of about equal bytes (chunks <= 0: 4), one group's copy
+ * on its own copy stream while the compute stream transposes another.  All
+ * chains sweep together in between, as pimc_batch_run does.  The chains
+ * reach the same states as by the three calls.  x_in and x_out may be the
+ * same buffer.  pimc_last_run_ms gives the device time of the whole call. */
 int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long n_sweeps,
                       int chunks);
 /* launch shape of pimc_batch_run.  warp_per_chain = 0: one CTA of `block`
@@ -200,9 +202,17 @@ typedef struct {
    * threads per chain: its kernel compiled for at most 170 or 255 registers
    * a thread (6 or 4 resident CTAs per SM) instead of 128 (0 or 128) */
   int phase_regs[3];
+  /* the neighbour queries' candidates: 0 leaves PIMC_OPT_CELL_LISTS as it
+   * is; 1 + a value of it (1 off, 2 auto, 3 always) sets it for every chain.
+   * pimc_batch_get_launch reports 1 + the current value.  The chains are the
+   * same either way; only the speed differs. */
+  int cell_lists;
 } pimc_launch;
 /* time candidate launch shapes on the handle's own chains and keep the
- * fastest; the chains are restored afterwards.  chosen may be NULL. */
+ * fastest; the chains are restored afterwards.  For chains with cell lists
+ * it also times the chosen shape with the lists on (the handle's setting)
+ * and off, and keeps the faster (cell_lists of chosen).  chosen may be
+ * NULL. */
 int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen);
 int pimc_batch_set_launch(void *handle, const pimc_launch *launch);
 int pimc_batch_get_launch(void *handle, pimc_launch *launch);

@@ -121,13 +121,11 @@ struct Handle {
   int *d_tile_off = nullptr;
   int ntiles = 0;
   std::vector<int> tile_off;  // the same on the host
-  // pimc_batch_run_io: copy streams, per-chunk events, the chunks' chain
-  // ranges and work orders, made on first use for a chunk count
+  // pimc_batch_run_io: copy streams, per-chunk events and the chunks' chain
+  // ranges, made on first use for a chunk count
   cudaStream_t s_up = nullptr, s_down = nullptr;
   std::vector<cudaEvent_t> io_ev;
   std::vector<int> io_cut;     // chunk k holds chains [io_cut[k], io_cut[k + 1])
-  int *d_io_order = nullptr;   // chunk k's chains longest first, at io_cut[k]
-  int *d_io_queue = nullptr;   // one work-queue counter per chunk
 };
 
 // the LPT cost of a chain (staging and CoM ~ N M, swaps ~ N^2)
@@ -750,26 +748,34 @@ int build_graph(Handle *h) {
   return PIMC_OK;
 }
 
-int run_batched(Handle *h, long long n) {
+// n sweeps of every chain on the handle stream: replays of the captured
+// graph, the remainder issued directly; adds the kernel launches to *launches
+int issue_batched(Handle *h, long long n, long long *launches) {
   const Plan &p = h->bat;
   CK(plan_set_smem(h, p));
   const int spl = std::max(1, p.spl);
   int rc = build_graph(h);
   if (rc) return rc;
-  CK(cudaEventRecord(h->ev0, h->stream));
-  long long launches = 0;
   const long long full = n / spl, rem = n % spl;
   for (long long i = 0; i < full; ++i) {
     CK(cudaGraphLaunch(h->gexec, h->stream));
-    launches += h->graph_launches;
+    *launches += h->graph_launches;
   }
   if (rem) {
     SweepArgs a = sweep_args(h, p);
     a.order = h->d_order;
     a.queue = h->d_queue;
     a.teams = launch_teams(h, p);
-    CK(issue_sweeps(h, p, a, (int)rem, &launches));
+    CK(issue_sweeps(h, p, a, (int)rem, launches));
   }
+  return PIMC_OK;
+}
+
+int run_batched(Handle *h, long long n) {
+  CK(cudaEventRecord(h->ev0, h->stream));
+  long long launches = 0;
+  int rc = issue_batched(h, n, &launches);
+  if (rc) return rc;
   CK(cudaEventRecord(h->ev1, h->stream));
   rc = sync_check(h);
   if (rc) return rc;
@@ -893,27 +899,18 @@ int attempt_impl(Handle *h, int kind, int n, int j0, int m, double u_pick, doubl
 int pimc_fail(int code, const std::string &msg) { return fail(code, msg); }
 
 // ===================================================================== C ABI
-// pimc_batch_run_io's chunks: contiguous chain ranges of about equal LPT
-// cost, each with its own longest-first order and work-queue counter on the
-// device, and an upload and a done event per chunk
+// pimc_batch_run_io's chunks: contiguous chain ranges of about equal bytes
+// in the host layout, and an upload and a transposed-back event per chunk
 int io_prepare(Handle *h, int chunks) {
   if ((int)h->io_cut.size() == chunks + 1) return PIMC_OK;
-  std::vector<double> cum(h->nchains + 1, 0.0);
-  for (int c = 0; c < h->nchains; ++c) cum[c + 1] = cum[c] + chain_cost(h->params[c]);
   std::vector<int> cut(chunks + 1, 0);
   cut[chunks] = h->nchains;
+  const double total = (double)h->n_stage;
   for (int k = 1; k < chunks; ++k) {
-    const double target = cum[h->nchains] * k / chunks;
-    int c = (int)(std::lower_bound(cum.begin(), cum.end(), target) - cum.begin());
-    c = std::max(cut[k - 1] + 1, std::min(c, h->nchains - (chunks - k)));
+    const double target = total * k / chunks;
+    int c = cut[k - 1] + 1;
+    while (c < h->nchains - (chunks - k) && (double)h->desc[c].host_off < target) ++c;
     cut[k] = c;
-  }
-  std::vector<int> order(h->nchains);
-  for (int k = 0; k < chunks; ++k) {
-    for (int c = cut[k]; c < cut[k + 1]; ++c) order[c] = c;
-    std::stable_sort(order.begin() + cut[k], order.begin() + cut[k + 1], [&](int a, int b) {
-      return chain_cost(h->params[a]) > chain_cost(h->params[b]);
-    });
   }
   if (!h->s_up) {
     CK(cudaStreamCreateWithFlags(&h->s_up, cudaStreamNonBlocking));
@@ -922,16 +919,6 @@ int io_prepare(Handle *h, int chunks) {
   for (cudaEvent_t e : h->io_ev) cudaEventDestroy(e);
   h->io_ev.assign(2 * chunks + 2, nullptr);  // per chunk upload and done; start; end
   for (auto &e : h->io_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-  cudaFree(h->d_io_order);
-  cudaFree(h->d_io_queue);
-  h->d_io_order = nullptr;
-  h->d_io_queue = nullptr;
-  h->io_cut.clear();
-  CK(cudaMalloc(&h->d_io_order, sizeof(int) * h->nchains));
-  CK(cudaMalloc(&h->d_io_queue, sizeof(int) * chunks));
-  CK(cudaMemcpyAsync(h->d_io_order, order.data(), sizeof(int) * h->nchains, cudaMemcpyHostToDevice,
-                     h->stream));
-  CK(cudaStreamSynchronize(h->stream));
   h->io_cut = cut;
   return PIMC_OK;
 }
@@ -965,8 +952,6 @@ int pimc_destroy(void *handle) {
   cudaFree(h->d_buf);
   cudaFree(h->d_adj);
   cudaFree(h->d_stage);
-  cudaFree(h->d_io_order);
-  cudaFree(h->d_io_queue);
   for (cudaEvent_t e : h->io_ev) cudaEventDestroy(e);
   if (h->s_up) cudaStreamDestroy(h->s_up);
   if (h->s_down) cudaStreamDestroy(h->s_down);
@@ -1074,14 +1059,15 @@ int pimc_batch_get_beads_all(void *handle, double *x_all) {
   return sync_check(h);
 }
 
-// upload, sweep and download the batch in chunks of chains so that the
-// copies of one chunk overlap the sweeps of another: chunk k's positions go
-// host -> staging buffer on the upload stream; on the compute stream chunk k
-// waits for them, is transposed into the device layout, has its links
-// refreshed, sweeps n times (the batched launch shape, its own work queue)
-// and is transposed back; the download stream then copies it to x_out.
-// With page-locked buffers the copies are DMA transfers that run beside the
-// sweeps.  x_in and x_out may be the same buffer.
+// upload, sweep and download the batch with the copies in chunks of chains:
+// chunk k's positions go host -> staging buffer on the upload stream while
+// the compute stream transposes chunk k - 1 into the device layout and
+// refreshes its links; once every chunk is in, all chains sweep n times
+// together (the batched launch shape and its graph, so that the sweep keeps
+// the whole batch's load balance); then the compute stream transposes the
+// chunks back one by one and the download stream copies each to x_out as
+// soon as it is out.  With page-locked buffers the copies are DMA transfers
+// that run beside the transposes.  x_in and x_out may be the same buffer.
 int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long n_sweeps, int chunks) {
   Handle *h = H(handle);
   if (!h || !x_in || !x_out || n_sweeps < 0) return fail(PIMC_EARG, "bad argument");
@@ -1089,19 +1075,42 @@ int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long
   chunks = std::max(1, std::min(chunks, h->nchains));
   int rc = ensure_tiles(h);
   if (rc) return rc;
+  long long launches = 0;
+  double *vin = device_view(x_in), *vout = device_view(x_out);
+  if (vin && vout) {
+    // page-locked buffers: the tiled transposes read and write them in place
+    // over the host link, which beats staging copies plus device transposes
+    CK(cudaEventRecord(h->ev0, h->stream));
+    CK(launch_transpose_tiles(true, h->d_desc, h->d_dpool, vin, h->d_tile_off, 0, h->nchains,
+                              h->ntiles, 8 * h->num_sms, h->stream));
+    CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, 0, h->nchains, h->maxNM, h->stream));
+    launches += 2;
+    if (n_sweeps > 0 && (rc = issue_batched(h, n_sweeps, &launches))) return rc;
+    CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, vout, h->d_tile_off, 0, h->nchains,
+                              h->ntiles, 8 * h->num_sms, h->stream));
+    launches += 1;
+    CK(cudaEventRecord(h->ev1, h->stream));
+    rc = sync_check(h);
+    if (rc) return rc;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+    h->last_ms = ms;
+    h->last_launches = launches;
+    return check_device_errors(h);
+  }
   if ((rc = io_prepare(h, chunks))) return rc;
-  const Plan &p = h->bat;
-  CK(plan_set_smem(h, p));
   CK(cudaEventRecord(h->ev0, h->stream));
   cudaEvent_t start = h->io_ev[2 * chunks];
   CK(cudaEventRecord(start, h->stream));
   CK(cudaStreamWaitEvent(h->s_up, start, 0));
-  CK(cudaStreamWaitEvent(h->s_down, start, 0));
-  long long launches = 0;
-  for (int k = 0; k < chunks; ++k) {
+  auto span = [&](int k, size_t *off, size_t *n) {
     const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
-    const size_t off = (size_t)h->desc[c0].host_off;
-    const size_t n = (c1 < h->nchains ? (size_t)h->desc[c1].host_off : h->n_stage) - off;
+    *off = (size_t)h->desc[c0].host_off;
+    *n = (c1 < h->nchains ? (size_t)h->desc[c1].host_off : h->n_stage) - *off;
+  };
+  for (int k = 0; k < chunks; ++k) {
+    size_t off, n;
+    span(k, &off, &n);
     CK(cudaMemcpyAsync(h->d_stage + off, x_in + off, n * sizeof(double), cudaMemcpyHostToDevice,
                        h->s_up));
     CK(cudaEventRecord(h->io_ev[2 * k], h->s_up));
@@ -1114,25 +1123,17 @@ int pimc_batch_run_io(void *handle, const double *x_in, double *x_out, long long
                               8 * h->num_sms, h->stream));
     CK(launch_links(h->d_desc, h->d_dpool, h->d_ipool, c0, c1 - c0, h->maxNM, h->stream));
     launches += 2;
-    if (n_sweeps > 0) {
-      SweepArgs a = sweep_args(h, p);
-      a.order = h->d_io_order + c0;
-      a.nchains = c1 - c0;
-      a.queue = h->d_io_queue + k;
-      a.teams = launch_teams(h, p);
-      const int spl = std::max(1, p.spl);
-      for (long long done = 0; done < n_sweeps; done += spl)
-        CK(issue_sweeps(h, p, a, (int)std::min<long long>(spl, n_sweeps - done), &launches));
-    }
+  }
+  if (n_sweeps > 0 && (rc = issue_batched(h, n_sweeps, &launches))) return rc;
+  for (int k = 0; k < chunks; ++k) {
+    const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
+    const int nt = h->tile_off[c1] - h->tile_off[c0];
     CK(launch_transpose_tiles(false, h->d_desc, h->d_dpool, h->d_stage, h->d_tile_off, c0, c1, nt,
                               8 * h->num_sms, h->stream));
     launches += 1;
     CK(cudaEventRecord(h->io_ev[2 * k + 1], h->stream));
-  }
-  for (int k = 0; k < chunks; ++k) {
-    const int c0 = h->io_cut[k], c1 = h->io_cut[k + 1];
-    const size_t off = (size_t)h->desc[c0].host_off;
-    const size_t n = (c1 < h->nchains ? (size_t)h->desc[c1].host_off : h->n_stage) - off;
+    size_t off, n;
+    span(k, &off, &n);
     CK(cudaStreamWaitEvent(h->s_down, h->io_ev[2 * k + 1], 0));
     CK(cudaMemcpyAsync(x_out + off, h->d_stage + off, n * sizeof(double), cudaMemcpyDeviceToHost,
                        h->s_down));
@@ -1278,6 +1279,8 @@ int check_launch(const Handle *h, const pimc_launch &l, Plan *out) {
     return fail(PIMC_EARG, l.warp_per_chain ? "block must be a multiple of 32 in [32, 256]"
                                             : "block must be a multiple of 32 in [64, 512]");
   if (l.sweeps_per_launch < 1) return fail(PIMC_EARG, "sweeps_per_launch must be >= 1");
+  if (l.cell_lists < 0 || l.cell_lists > 3)
+    return fail(PIMC_EARG, "cell_lists must be 0 (keep), 1 (off), 2 (auto) or 3 (always)");
   if (l.state_smem_bytes < 0 || l.state_smem_bytes > 160 * 1024)
     return fail(PIMC_EARG, "state_smem_bytes must be in [0, 160 KiB]");
   if (l.split_phases < 0 || l.split_phases > 1 || (l.split_phases && l.warp_per_chain))
@@ -1380,6 +1383,7 @@ int pimc_batch_set_launch(void *handle, const pimc_launch *launch) {
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
   }
+  if (launch->cell_lists) return pimc_set_option(h, PIMC_OPT_CELL_LISTS, launch->cell_lists - 1);
   return PIMC_OK;
 }
 
@@ -1396,6 +1400,7 @@ int pimc_batch_get_launch(void *handle, pimc_launch *launch) {
     launch->phase_warp[ph] = h->bat.pwarp[ph];
     launch->phase_regs[ph] = h->bat.pregs[ph];
   }
+  launch->cell_lists = 1 + h->desc[0].cl_mode;
   return PIMC_OK;
 }
 
@@ -1537,6 +1542,24 @@ int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
       if ((rc = run_batched(h, sweeps_per_trial))) return rc;
       if (t_ref < h->last_ms) keep = ref;
     }
+  }
+  // the cell lists against the row scans on the chosen shape: the same
+  // chains either way, timed in turn, twice each
+  keep.cell_lists = 1 + h->desc[0].cl_mode;
+  bool lists = false;
+  for (const ChainDesc &d : h->desc) lists = lists || d.cl_nc > 0;
+  if (lists && keep.cell_lists != 1) {
+    double tot[2] = {0.0, 0.0};
+    pimc_launch lc[2] = {keep, keep};
+    lc[1].cell_lists = 1;
+    for (int round = 0; round < 2; ++round)
+      for (int k = 0; k < 2; ++k) {
+        if ((rc = pimc_batch_set_launch(h, &lc[k]))) return rc;
+        if ((rc = run_batched(h, lc[k].sweeps_per_launch))) return rc;
+        if ((rc = run_batched(h, sweeps_per_trial))) return rc;
+        tot[k] += h->last_ms;
+      }
+    if (tot[1] < tot[0]) keep = lc[1];
   }
   if ((rc = pimc_batch_set_launch(h, &keep))) return rc;
   if ((rc = pimc_set_state(h, snap.data(), nb))) return rc;

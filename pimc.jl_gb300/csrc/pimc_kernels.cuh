@@ -1197,9 +1197,14 @@ __device__ __forceinline__ long long bin_floor(double x, double L, double w, dou
 // out[4] W^2 = |sum over links of the minimum-image displacement|^2 (winding),
 // out[5] A_z = 1/2 sum over links (x dy - y dx) (signed area about the origin),
 // out[6] sum r^2 / M (classical moment of inertia / m), out[7] 0;
-// qbuf: one PQ_CAP-entry queue per warp (pair chains)
+// qbuf: one PQ_CAP-entry queue per warp (pair chains).
+// FAST (the sweeps' measurements): a neighbour pair's exponentials are FP32
+// expf of the FP64 squared distances (relative error about 1e-7 per term,
+// far below any Monte Carlo error), so that the FP64 pipe only forms the
+// distances, the exact cut-off test and the sums; the neighbour set is the
+// same.  Otherwise (pimc_measure) every term is FP64.
 // ---------------------------------------------------------------------------
-template <bool WARP>
+template <bool WARP, bool FAST = false>
 __device__ void measure_group(const CV &c, double *red, double *out, bool density,
                               unsigned long long *qbuf) {
   using G = Group<WARP>;
@@ -1262,13 +1267,24 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
         const double r2a = mi2(d, c.X(0, i, j), c.Xd(1, i, j), c.X(0, b, j), c.Xd(1, b, j));
         if (r2a <= rc2) {
           const int bn = j == M - 1 ? c.next[b] : b;
-          const double r2b = mi2(d, c.X(0, in, jn), c.Xd(1, in, jn), c.X(0, bn, jn), c.Xd(1, bn, jn));
           // the pair exponentials e = exp(x), x = -r^2/(2 s^2), and x e; the
           // factors g tau/2 are applied once at the end
-          const double xa = -r2a * cg, xb = -r2b * cg;
-          const double ea = exp_neg(xa), eb = exp_neg(xb);
-          s[3] += ea + eb;
-          s[4] = fma(xa, ea, fma(xb, eb, s[4]));
+          if (FAST) {
+            const float dxb = (float)mi1(c.X(0, in, jn), c.X(0, bn, jn), d.L, d.L2);
+            const float dyb = dim > 1 ? (float)mi1(c.Xd(1, in, jn), c.Xd(1, bn, jn), d.L, d.L2) : 0.f;
+            const float cgf = (float)cg;
+            const float xa = -(float)r2a * cgf, xb = -fmaf(dxb, dxb, dyb * dyb) * cgf;
+            const float ea = expf(xa), eb = expf(xb);
+            s[3] += (double)(ea + eb);
+            s[4] += (double)fmaf(xa, ea, xb * eb);
+          } else {
+            const double r2b =
+                mi2(d, c.X(0, in, jn), c.Xd(1, in, jn), c.X(0, bn, jn), c.Xd(1, bn, jn));
+            const double xa = -r2a * cg, xb = -r2b * cg;
+            const double ea = exp_neg(xa), eb = exp_neg(xb);
+            s[3] += ea + eb;
+            s[4] = fma(xa, ea, fma(xb, eb, s[4]));
+          }
         }
       }
       __syncwarp();

@@ -388,7 +388,7 @@ __device__ void sweep_one(SmemCtl &sc, double *red, const CV &c, unsigned char *
   // ---- measurement cadence (measurement_Z_sector)
   if (mix.measure_every > 0 && ((sweep + 1) % (unsigned long long)mix.measure_every) == 0) {
     const bool lists = (d.flags & PF_PAIR) && !(d.flags & PF_CONTACT) && build_lists();
-    measure_group<WARP>(lists ? cq : c, red, sc.e4, c.hist != nullptr, (unsigned long long *)scratch);
+    measure_group<WARP, true>(lists ? cq : c, red, sc.e4, c.hist != nullptr, (unsigned long long *)scratch);
     if (tid == 0) record_measurement(d, sc.v, c, sc.e4, c.hist != nullptr);
   }
   if (tid == 0) {

@@ -127,7 +127,8 @@ class Launch(C.Structure):
     _fields_ = [("warp_per_chain", C.c_int), ("block", C.c_int),
                 ("sweeps_per_launch", C.c_int), ("state_smem_bytes", C.c_int),
                 ("split_phases", C.c_int), ("phase_block", C.c_int * 3),
-                ("phase_warp", C.c_int * 3), ("phase_regs", C.c_int * 3)]
+                ("phase_warp", C.c_int * 3), ("phase_regs", C.c_int * 3),
+                ("cell_lists", C.c_int)]
 
 
 # every symbol include/pimc.h declares, with its argument types

@@ -289,11 +289,13 @@ class Engine:
     def set_launch(self, block: int, sweeps_per_launch: int = 1,
                    state_smem_bytes: int = 100 * 1024, warp_per_chain: bool = False,
                    split_phases: int = 0, phase_block=(0, 0, 0), phase_warp=(0, 0, 0),
-                   phase_regs=(0, 0, 0)):
+                   phase_regs=(0, 0, 0), cell_lists: int = 0):
+        """cell_lists: 0 keeps the cell-list option (set_cells), 1 + a mode
+        of it sets it (1 off, 2 auto, 3 always)"""
         l = Launch(int(bool(warp_per_chain)), block, sweeps_per_launch, state_smem_bytes,
                    int(split_phases), (C.c_int * 3)(*[int(b) for b in phase_block]),
                    (C.c_int * 3)(*[int(w) for w in phase_warp]),
-                   (C.c_int * 3)(*[int(r) for r in phase_regs]))
+                   (C.c_int * 3)(*[int(r) for r in phase_regs]), int(cell_lists))
         check(self.L.pimc_batch_set_launch(self.h, C.byref(l)))
 
     @property
@@ -304,7 +306,8 @@ class Engine:
         return {"warp_per_chain": bool(l.warp_per_chain), "block": l.block,
                 "sweeps_per_launch": l.sweeps_per_launch, "state_smem_bytes": l.state_smem_bytes,
                 "split_phases": l.split_phases, "phase_block": list(l.phase_block),
-                "phase_warp": list(l.phase_warp), "phase_regs": list(l.phase_regs)}
+                "phase_warp": list(l.phase_warp), "phase_regs": list(l.phase_regs),
+                "cell_lists": l.cell_lists}
 
     def phase_times(self, n_sweeps: int = 2):
         """device ms of the staging, swap and remaining phases over n sweeps,

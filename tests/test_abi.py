@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
 
 
 def test_abi_version_and_error_text(engine_lib):
-    assert engine_lib.pimc_abi_version() == 4
+    assert engine_lib.pimc_abi_version() == 5
     assert isinstance(engine_lib.pimc_last_error(), bytes)
 
 

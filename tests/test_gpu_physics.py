@@ -187,7 +187,11 @@ def test_batched_equals_plain_and_tuner_is_transparent():
               dict(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
                    phase_block=[128, 64, 128], phase_regs=[0, 170, 0]),
               dict(block=64, sweeps_per_launch=1, state_smem_bytes=32 * 1024, split_phases=1,
-                   phase_regs=[0, 255, 0])]
+                   phase_regs=[0, 255, 0]),
+              # neighbour candidates from row scans, from cell lists everywhere
+              dict(block=64, sweeps_per_launch=1, state_smem_bytes=0, split_phases=1,
+                   phase_block=[128, 64, 128], cell_lists=1),
+              dict(block=128, sweeps_per_launch=1, state_smem_bytes=0, cell_lists=3)]
     b = Engine(ps)
     for i, p in enumerate(ps):
         b.set_mix(mix(p.N, p.M, min(8, p.M // 2), 6.0, measure_every=3), chain=i)
@@ -233,7 +237,8 @@ def test_launch_shape_rejects_bad_values():
                 dict(block=64, split_phases=1, phase_regs=(170, 0, 0)),
                 dict(block=64, split_phases=1, phase_block=(0, 128, 0), phase_regs=(0, 255, 0)),
                 dict(block=64, split_phases=1, phase_block=(0, 64, 0), phase_warp=(0, 1, 0),
-                     phase_regs=(0, 170, 0))]:
+                     phase_regs=(0, 170, 0)),
+                dict(block=64, cell_lists=-1), dict(block=64, cell_lists=4)]:
         with pytest.raises(PimcError):
             e.set_launch(**bad)
     e.close()

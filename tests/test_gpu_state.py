@@ -24,8 +24,10 @@ def _pair_chain(seed, N=24, M=16, **kw):
 
 def _mix(N, M, measure_every=1):
     from pimc.engine import Mix
-    return Mix(stage_slices=8, stage_max=8, stage_minacc=0.0, stage_maxacc=1.0, swaps_per_sweep=N,
-               swap_slices=8, swap_max=8, swap_minacc=0.0, swap_maxacc=1.0, com_step=1.0,
+    ell = min(8, M - 1)
+    return Mix(stage_slices=ell, stage_max=ell, stage_minacc=0.0, stage_maxacc=1.0,
+               swaps_per_sweep=N, swap_slices=ell, swap_max=ell, swap_minacc=0.0,
+               swap_maxacc=1.0, com_step=1.0,
                com_maxstep=2.0, measure_every=measure_every)
 
 
