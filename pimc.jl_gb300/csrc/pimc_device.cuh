@@ -918,16 +918,33 @@ __device__ __forceinline__ unsigned qdist2_w(unsigned a, unsigned b, bool &edge)
   return (unsigned)(dx * dx) + (unsigned)(dy * dy);
 }
 
-__device__ __forceinline__ void est_term(const ChainDesc &d, unsigned d2a, unsigned d2b, bool edge_b,
-                                         float &sum, float &bnd, int &k) {
+// The relative error of a term exp(-y) whose end lies at squared mirror
+// distance d2 is at most  c1 (2 sqrt(d2) + kQErr) + (3 + 1.2 y) 1.2e-7 :
+// the argument error from the mirror (c1 = 1.01 u^2/(2 sigma^2) kQErr, the
+// 1.01 covering FP32 rounding) plus __expf's own.  The bound grows with d2,
+// so for the first end, which the callers take within q_lim_hi, the value at
+// q_lim_hi (eps_a) bounds every term.  For the second end, which may lie
+// anywhere, 2 sqrt(d2) <= d2 / s + s for any s > 0 (s = sqrt(q_lim_hi),
+// tight where it matters); past q_lim_hi the looser bound only touches
+// terms exp(-y) below exp(-y_hi).  Neither needs a square root per term.
+struct EstConst {
+  float c1, inv_s, s, eps_a;
+  __device__ __forceinline__ explicit EstConst(const ChainDesc &d) {
+    c1 = 1.01f * d.q_u2i * kQErr;
+    const float lim = (float)d.q_lim_hi;
+    s = sqrtf(lim);
+    inv_s = 1.f / s;
+    eps_a = c1 * (2.f * s + kQErr) + (3.f + 1.2f * (lim * d.q_u2i)) * 1.2e-7f;
+  }
+};
+
+__device__ __forceinline__ void est_term(const ChainDesc &d, const EstConst &K, unsigned d2a,
+                                         unsigned d2b, bool edge_b, float &sum, float &bnd, int &k) {
   const float ya = (float)d2a * d.q_u2i, yb = (float)d2b * d.q_u2i;
   const float ea = __expf(-ya), eb = __expf(-yb);
-  // relative error of each exponential: argument error from the mirror plus
-  // the fast exponential's own
-  const float da = 1.01f * d.q_u2i * kQErr * (2.f * sqrtf((float)d2a) + kQErr) +
-                   (3.f + 1.2f * ya) * 1.2e-7f;
-  const float db = 1.01f * d.q_u2i * kQErr * (2.f * sqrtf((float)d2b) + kQErr) +
-                   (3.f + 1.2f * yb) * 1.2e-7f;
+  // relative error of each exponential (EstConst)
+  const float da = K.eps_a;
+  const float db = fmaf(K.c1, fmaf((float)d2b, K.inv_s, K.s + kQErr), (3.f + 1.2f * yb) * 1.2e-7f);
   // an end next to the half box: anything in [0, 1]
   const float vb = edge_b ? 0.5f : eb, eb_err = edge_b ? 0.5f : eb * db;
   const float v = ea + vb, err = ea * da + eb_err + 2e-30f;
@@ -954,6 +971,7 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
                                  const Stop &stop = Stop()) {
   const ChainDesc &d = *c.d;
   const int N = c.N, M = c.M;
+  const EstConst K(d);
   // whether a slice's lists are usable is read one link ahead
   const CellLists *L = c.cl;
   bool use_next = L && t0 < t1 && L->usable(s.slice(t0));
@@ -973,11 +991,11 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
       bool edge;
       if (io) {
         const unsigned d2b = qdist2_w(no, pbn, edge);
-        est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
+        est_term(d, K, d2o, d2b, edge, e.so, e.bo, e.ko);
       }
       if (in) {
         const unsigned d2b = qdist2_w(nn, pbn, edge);
-        est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
+        est_term(d, K, d2n, d2b, edge, e.sn, e.bn, e.kn);
       }
     };
     // a cell-list candidate: the sides its block serves, the word at slice
@@ -993,11 +1011,11 @@ __device__ bool segment_estimate(const CV &c, const Seg &s, int t0, int t1, Pair
       bool edge;
       if (io) {
         const unsigned d2b = qdist2_w(no, pbn, edge);
-        est_term(d, d2o, d2b, edge, e.so, e.bo, e.ko);
+        est_term(d, K, d2o, d2b, edge, e.so, e.bo, e.ko);
       }
       if (in) {
         const unsigned d2b = qdist2_w(nn, pbn, edge);
-        est_term(d, d2n, d2b, edge, e.sn, e.bn, e.kn);
+        est_term(d, K, d2n, d2b, edge, e.sn, e.bn, e.kn);
       }
     });
     if (listed) {
