@@ -62,7 +62,9 @@ PLAN = {
     "c2_ref": ("c2_ref", "sweep", 64, 1000, 10000),
     "c2_ref_run": ("c2_ref", "run", 64, 1000, 10000),
     "c2_phys": ("c2_phys", "run", 64, 1000, 10000),
-    "c3_ref": ("c3_ref", "sweep", 32, 300, 1200),
+    # the reference's rules give C3 heavy-tailed chain means (a chain's
+    # cloud can spread far past the others for much of its run): 256 chains
+    "c3_ref": ("c3_ref", "sweep", 256, 300, 1200),
     "c3_ref_run": ("c3_ref", "run", 32, 300, 1200),
 }
 # C4 sample: name -> (schedule, semantics); replicas, thermalisation, measured

@@ -35,7 +35,12 @@ GPU_PLAN = {
     "c1_phys": (256, 2000, 20000),
     "c2_ref": (256, 1000, 10000),
     "c2_phys": (256, 1000, 10000),
-    "c3_ref": (96, 300, 1200),
+    # the reference's rules give C3 chains heavy-tailed chain means: now and
+    # then a chain's cloud spreads far past the others for much of its run
+    # (one of 96 device chains at <r^2> = 1.93 against a typical 1.38), so
+    # the device side runs enough chains (one launch holds them all) that
+    # such a chain moves the mean by less than its standard error
+    "c3_ref": (384, 300, 1200),
 }
 EXACT = {"c1_phys": GOLDEN["E_C1_primitive_M20"], "c2_phys": GOLDEN["E_C2_winding0"]}
 
