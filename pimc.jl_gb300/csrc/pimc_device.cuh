@@ -384,17 +384,28 @@ struct CV {
     xq[(size_t)j * ldn + n] = q;
     if (cl) cl->mark(n, j);
   }
-  // exchange the beads of particles a and b at slice j, mirror included
-  __device__ __forceinline__ void exchange(int a, int b, int j) const {
-    for (int k = 0; k < dim; ++k) {
-      const double t = X(k, a, j);
-      X(k, a, j) = X(k, b, j);
-      X(k, b, j) = t;
-    }
+  // exchange the beads of particles a and b at slice j, mirror and cached
+  // link included, with every load issued before the first store: the
+  // compiler cannot know that a != b, so exchanging the arrays one after
+  // another would cost one memory round trip each
+  __device__ __forceinline__ void exchange_linked(int a, int b, int j) const {
+    double *pa = &X(0, a, j), *pb = &X(0, b, j);
     unsigned *r = xq + (size_t)j * ldn;
-    const unsigned t = r[a];
-    r[a] = r[b];
-    r[b] = t;
+    double *v = V + (size_t)j * ldn;
+    const double xa = pa[0], xb = pb[0];
+    const double ya = dim > 1 ? pa[1] : 0.0, yb = dim > 1 ? pb[1] : 0.0;
+    const unsigned qa = r[a], qb = r[b];
+    const double va = v[a], vb = v[b];
+    pa[0] = xb;
+    pb[0] = xa;
+    if (dim > 1) {
+      pa[1] = yb;
+      pb[1] = ya;
+    }
+    r[a] = qb;
+    r[b] = qa;
+    v[a] = vb;
+    v[b] = va;
     if (cl) cl->trade(a, b, j);
   }
 };

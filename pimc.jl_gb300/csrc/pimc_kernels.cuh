@@ -927,12 +927,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     c.Vl(nown2(t), j) = mhtau * (S.vb2[t] + S.vb2[t + 1]);
   }
   if (j0 + m < M - 1)
-    for (int j = se + 1 + tid; j < M; j += nt) {
-      c.exchange(n1, n2, j);
-      const double v = c.Vl(n1, j);
-      c.Vl(n1, j) = c.Vl(n2, j);
-      c.Vl(n2, j) = v;
-    }
+    for (int j = se + 1 + tid; j < M; j += nt) c.exchange_linked(n1, n2, j);
   G::sync();
   if (tid == 0) {
     c.next[n1] = nn1;
