@@ -175,6 +175,7 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
   d.rc = 2.0 * p.L / d.nbins;
   d.ncell = p.dim == 2 ? d.nbins * d.nbins : d.nbins;
   d.L2 = 2.0 * d.L;
+  d.inv2L = 1.0 / (2.0 * d.L);
   d.rc2 = d.rc * d.rc;
   d.mhtau_g = -0.5 * d.tau * d.g;
   // 16-bit fixed-point mirror of the positions on the periodic box: a pair
@@ -197,6 +198,7 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
     d.q_u2i = (float)(u * u * d.inv2s2);
     d.q_lim_lo = rq > e ? (unsigned)std::floor((rq - e) * (rq - e)) : 0u;
     d.q_lim_hi = (unsigned)std::min(std::ceil((rq + e) * (rq + e)), (double)d.q_lim_rc);
+    d.hb_unit = (float)((double)d.q_unit2 / (4.0 * d.tau * d.lambda));
   }
   d.hard_a = p.hardcore_a;
   d.ctr = p.retry_cap > 0 ? p.retry_cap : 10000;

@@ -537,6 +537,17 @@ __device__ __forceinline__ double teleport(double x, double L, double inv2L) {
   return (x + L) - f * (2.0 * L) - L;
 }
 
+// teleport in the sweeps (SWEEP): a coordinate inside the box is kept as it
+// is.  The reference's (x + L) - L can only round its last bits, which no
+// statistic of a sweep sees, and skipping it spares two FP64 additions per
+// coordinate on this part's narrow FP64 pipe.  Injected-draw attempts keep
+// the reference's bits.
+template <bool SWEEP>
+__device__ __forceinline__ double teleport_s(double x, double L, double inv2L) {
+  if (SWEEP && fabs(x) < L) return x;
+  return teleport(x, L, inv2L);
+}
+
 __device__ __forceinline__ double sgn(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 0.0); }
 
 // engine-known external potential: hcoef |r|^2 + V0 sum sin^2(pi r_d / a)
@@ -1200,7 +1211,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
       !check_ok(n >= 0 && n < c.N, DERR_INDEX, d))
     return RES_REJECT;
   const int M = c.M, dim = c.dim;
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   const int nx = c.next[n];
   const int jend = j0 + m;
   const int oe = jend < M ? n : nx, je = jend < M ? jend : jend - M;
@@ -1212,15 +1223,28 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
   double px = sx, py = sy;
   bx[0] = sx;
   by[0] = sy;
+  // sweeps run the recursion relative to the end bead, p - e = a (p' - e) +
+  // z sigma, one FP64 operation fewer per coordinate than the reference's
+  // a p' + (1 - a) e + z sigma, which attempts keep
+  double rx = sx - ex, ry = sy - ey;
   for (int t = 1; t < m; ++t) {
     const double2 ab = bridge_coef(c, m, t);
     double z[2];
     dr.bead_normals(t - 1, dim, z);
-    px = ab.x * px + (1.0 - ab.x) * ex + z[0] * ab.y;
-    bx[t] = px;
-    if (dim > 1) {
-      py = ab.x * py + (1.0 - ab.x) * ey + z[1] * ab.y;
-      by[t] = py;
+    if (D::kSweep) {
+      rx = fma(ab.x, rx, z[0] * ab.y);
+      bx[t] = rx + ex;
+      if (dim > 1) {
+        ry = fma(ab.x, ry, z[1] * ab.y);
+        by[t] = ry + ey;
+      }
+    } else {
+      px = ab.x * px + (1.0 - ab.x) * ex + z[0] * ab.y;
+      bx[t] = px;
+      if (dim > 1) {
+        py = ab.x * py + (1.0 - ab.x) * ey + z[1] * ab.y;
+        by[t] = py;
+      }
     }
   }
   dr.consumed((m - 1) * dim);
@@ -1228,8 +1252,8 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
   by[m] = ey;
   double wi = 0.0, wu = 0.0, vprev = 0.0;
   for (int t = 0; t <= m; ++t) {
-    bx[t] = teleport(bx[t], L, inv2L);
-    if (dim > 1) by[t] = teleport(by[t], L, inv2L);
+    bx[t] = teleport_s<D::kSweep>(bx[t], L, inv2L);
+    if (dim > 1) by[t] = teleport_s<D::kSweep>(by[t], L, inv2L);
     const double vb = vext(d, bx[t], by[t]);
     if (t > 0) vp[t - 1] = mhtau * (vprev + vb);
     vprev = vb;
@@ -1270,7 +1294,7 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
     return RES_REJECT;
   const int lane = threadIdx.x & 31;
   const int M = c.M, dim = c.dim;
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
   const bool hard = (d.flags & PF_HARD) != 0;
   double *sx_ = sb, *sy_ = sb + (WMAX + 1), *svb = sb + 2 * (WMAX + 1);
@@ -1323,7 +1347,8 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
         }
         qx = __shfl_sync(0xffffffffu, qx, 0);
         qy = __shfl_sync(0xffffffffu, qy, 0);
-        const double tx = teleport(qx, L, inv2L), ty = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
+        const double tx = teleport_s<D::kSweep>(qx, L, inv2L);
+        const double ty = dim > 1 ? teleport_s<D::kSweep>(qy, L, inv2L) : 0.0;
         const bool hit = __any_sync(0xffffffffu, hard_hit_lanes(c, tx, ty, j, exc, -1, lane, 32));
         if (!hit) { px = qx; py = qy; break; }
       }
@@ -1338,8 +1363,8 @@ __device__ int window_warp(const CV &c, int n, int j0, int m, D &dr, bool rewrit
   for (int t = lane; t <= m; t += 32) {
     double qx = t == 0 ? sx : (t == m ? ex : sx_[t]);
     double qy = t == 0 ? sy : (t == m ? ey : sy_[t]);
-    qx = teleport(qx, L, inv2L);
-    if (dim > 1) qy = teleport(qy, L, inv2L);
+    qx = teleport_s<D::kSweep>(qx, L, inv2L);
+    if (dim > 1) qy = teleport_s<D::kSweep>(qy, L, inv2L);
     sx_[t] = qx;
     sy_[t] = qy;
     svb[t] = vext(d, qx, qy);
@@ -1430,7 +1455,7 @@ __device__ int window_team(const CV &c, const Team &tm, int n, int j0, int m, D 
   const ChainDesc &d = *c.d;
   const int lane = threadIdx.x & 31, tid = tm.w * 32 + lane, nt = tm.nw * 32;
   const int M = c.M, dim = c.dim;
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   double *b0 = sb(0);
   double *sx_ = b0, *sy_ = b0 + (WMAX + 1), *svb = b0 + 2 * (WMAX + 1);
   double *sz = b0 + 3 * (WMAX + 1);
@@ -1463,8 +1488,8 @@ __device__ int window_team(const CV &c, const Team &tm, int n, int j0, int m, D 
   for (int t = tid; t <= m; t += nt) {
     double qx = t == 0 ? sx : (t == m ? ex : sx_[t]);
     double qy = t == 0 ? sy : (t == m ? ey : sy_[t]);
-    qx = teleport(qx, L, inv2L);
-    if (dim > 1) qy = teleport(qy, L, inv2L);
+    qx = teleport_s<D::kSweep>(qx, L, inv2L);
+    if (dim > 1) qy = teleport_s<D::kSweep>(qy, L, inv2L);
     sx_[t] = qx;
     sy_[t] = qy;
     svb[t] = vext(d, qx, qy);

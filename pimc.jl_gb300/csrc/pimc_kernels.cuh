@@ -402,7 +402,7 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   const int tid = G::rank(), nt = G::size();
   const int warp = WARP ? 0 : (int)(threadIdx.x >> 5), nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
   const bool lead = warp == 0;
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   if (!check_ok(m >= 2 && m <= WMAX && m < M && j0 >= 0 && j0 < M, DERR_WINDOW, d) ||
       !check_ok(n1 >= 0 && n1 < N, DERR_INDEX, d))
     return RES_SKIP;
@@ -413,8 +413,14 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   hb.j0 = j0;
   hb.wrap = (j0 + m) >= M;
   hb.se = hb.wrap ? j0 + m - M : j0 + m;
-  hb.inv_den = 1.0 / (4.0 * (m * d.tau) * d.lambda);
-  hb.inv_denf = (float)hb.inv_den * d.q_unit2;
+  if (FAST) {
+    // sweeps weigh in FP32 alone: no FP64 division per attempt
+    hb.inv_den = 0.0;
+    hb.inv_denf = d.hb_unit / (float)m;
+  } else {
+    hb.inv_den = 1.0 / (4.0 * (m * d.tau) * d.lambda);
+    hb.inv_denf = (float)hb.inv_den * d.q_unit2;
+  }
   const int se = hb.se;
   const bool wrap = hb.wrap;
   const HBead A = hb.bead(n1, j0);
@@ -704,7 +710,8 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
           }
           qx = __shfl_sync(0xffffffffu, qx, 0);
           qy = __shfl_sync(0xffffffffu, qy, 0);
-          const double tx = teleport(qx, L, inv2L), ty = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
+          const double tx = teleport_s<D::kSweep>(qx, L, inv2L);
+          const double ty = dim > 1 ? teleport_s<D::kSweep>(qy, L, inv2L) : 0.0;
           if (!__any_sync(0xffffffffu, hard_hit_lanes(c, tx, ty, j, ea, eb, lane, 32))) {
             px = qx;
             py = qy;
@@ -732,8 +739,8 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
       qx = t == 0 ? s2x : (t == m ? f2x : S.r2x[t]);
       qy = t == 0 ? s2y : (t == m ? f2y : S.r2y[t]);
     }
-    qx = teleport(qx, L, inv2L);
-    qy = dim > 1 ? teleport(qy, L, inv2L) : 0.0;
+    qx = teleport_s<D::kSweep>(qx, L, inv2L);
+    qy = dim > 1 ? teleport_s<D::kSweep>(qy, L, inv2L) : 0.0;
     (b == 0 ? S.r1x : S.r2x)[t] = qx;
     (b == 0 ? S.r1y : S.r2y)[t] = qy;
     (b == 0 ? S.vb1 : S.vb2)[t] = vext(d, qx, qy);
@@ -961,19 +968,19 @@ template <class D>
 __device__ int com_thread(const CV &c, int n, double step, D &dr) {
   const ChainDesc &d = *c.d;
   const int M = c.M, dim = c.dim;
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   const double shx = step * 2.0 * (dr.uniform() - 0.5);
   const double shy = dim > 1 ? step * 2.0 * (dr.uniform() - 0.5) : 0.0;
   double wi = 0.0, wu = 0.0;
-  const double q0x = teleport(c.X(0, n, 0) + shx, L, inv2L);
-  const double q0y = dim > 1 ? teleport(c.X(1, n, 0) + shy, L, inv2L) : 0.0;
+  const double q0x = teleport_s<D::kSweep>(c.X(0, n, 0) + shx, L, inv2L);
+  const double q0y = dim > 1 ? teleport_s<D::kSweep>(c.X(1, n, 0) + shy, L, inv2L) : 0.0;
   const double v0 = vext(d, q0x, q0y);
   double vprev = v0;
   for (int j = 1; j <= M; ++j) {
     double vj = v0;
     if (j < M) {
-      const double qx = teleport(c.X(0, n, j) + shx, L, inv2L);
-      const double qy = dim > 1 ? teleport(c.X(1, n, j) + shy, L, inv2L) : 0.0;
+      const double qx = teleport_s<D::kSweep>(c.X(0, n, j) + shx, L, inv2L);
+      const double qy = dim > 1 ? teleport_s<D::kSweep>(c.X(1, n, j) + shy, L, inv2L) : 0.0;
       vj = vext(d, qx, qy);
     }
     wi += c.Vl(n, j - 1);
@@ -987,8 +994,8 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
     for (int j = 1; j <= M; ++j) {
       double qx = q0x, qy = q0y, vj = v0;
       if (j < M) {
-        qx = teleport(c.X(0, n, j) + shx, L, inv2L);
-        qy = dim > 1 ? teleport(c.X(1, n, j) + shy, L, inv2L) : 0.0;
+        qx = teleport_s<D::kSweep>(c.X(0, n, j) + shx, L, inv2L);
+        qy = dim > 1 ? teleport_s<D::kSweep>(c.X(1, n, j) + shy, L, inv2L) : 0.0;
         vj = vext(d, qx, qy);
       }
       c.set_pos(n, j - 1, px, py);
@@ -1022,7 +1029,7 @@ __device__ int com_group(const CV &c, int n, bool polymer, double step, D &dr, c
   const int N = c.N, M = c.M, dim = c.dim, tid = G::rank(), nt = G::size();
   const int lane = threadIdx.x & 31, warp = WARP ? 0 : (int)(threadIdx.x >> 5);
   const int nwarps = WARP ? 1 : (int)(blockDim.x >> 5);
-  const double L = d.L, inv2L = 1.0 / (2.0 * L), mhtau = -0.5 * d.tau;
+  const double L = d.L, inv2L = d.inv2L, mhtau = -0.5 * d.tau;
   const bool hard = (d.flags & PF_HARD) != 0;
   const bool phys_pair = (d.flags & PF_PAIR) && (d.flags & PF_PHYS);
   for (int i = tid; i < N; i += nt) idx[i] = -1;

@@ -43,6 +43,7 @@ struct ChainDesc {
   double g, inv2s2, rc, hard_a, mu;
   double dens_bw;
   double L2;            // 2L
+  double inv2L;         // 1 / (2L), the IEEE quotient
   double rc2;           // rc^2
   double mhtau_g;       // -tau g / 2: weight of a link's pair exponentials
   double q_scale;       // 65536 / (2L): box coordinate -> 16-bit mirror units
@@ -54,7 +55,9 @@ struct ChainDesc {
   // which it is surely beyond (kQErr units of mirror error on a distance)
   float q_u2i;
   unsigned q_lim_lo, q_lim_hi;
-  int pad2_;
+  // the sweeps' FP32 heat-bath exponent scale per window length m:
+  // hb_unit / m = (squared mirror unit) / (4 lambda m tau)
+  float hb_unit;
   long long x_off;      // doubles: x[j][n][d] (slice-major) at dpool + x_off
   long long V_off;      // doubles: V[j][n]
   long long xq_off;     // doubles: 16-bit fixed-point mirror [j][n] (x | y << 16, u32)
