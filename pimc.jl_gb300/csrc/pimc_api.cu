@@ -443,7 +443,7 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     dp = (dp + 1) & ~(size_t)1;
     d.host_off = (long long)h->n_stage;
     h->n_stage += (size_t)p.dim * NM;
-    d.tab_off = (long long)dp; dp += 2 * (size_t)d.wtab * d.wtab;
+    d.tab_off = (long long)dp; dp += 4 * (size_t)d.wtab * d.wtab;  // (alpha, sigma), then (w, k)
     d.eser_off = p.energy_capacity > 0 ? (long long)dp : -1;
     dp += (size_t)NOBS * p.energy_capacity;
     d.next_off = (long long)ip; ip += p.N;
@@ -501,17 +501,26 @@ int create_impl(const pimc_params *params, int nchains, void **out) {
     return cleanup(fail(PIMC_ENOMEM, "device allocation failed"));
   cudaMemsetAsync(h->d_dpool, 0, sizeof(double) * h->n_dpool, h->stream);
   cudaMemsetAsync(h->d_upool, 0, sizeof(unsigned long long) * h->n_upool, h->stream);
-  // bridge coefficient tables: alpha = (m-t)/(m+1-t), sigma = sqrt(2 lambda alpha tau)
+  // bridge coefficient tables: alpha = (m-t)/(m+1-t), sigma = sqrt(2 lambda
+  // alpha tau); then the sweeps' closed form of the same bridge, (w, k) =
+  // (sigma / (m-t), m-t) at t >= 1 and (1/m, m) at t = 0
   std::vector<double> tab;
   for (int c = 0; c < nchains; ++c) {
     const ChainDesc &d = h->desc[c];
-    tab.assign(2 * (size_t)d.wtab * d.wtab, 0.0);
-    for (int m = 2; m < d.wtab; ++m)
+    const size_t ww = (size_t)d.wtab * d.wtab;
+    tab.assign(4 * ww, 0.0);
+    for (int m = 2; m < d.wtab; ++m) {
+      tab[2 * (ww + (size_t)m * d.wtab)] = 1.0 / m;
+      tab[2 * (ww + (size_t)m * d.wtab) + 1] = (double)m;
       for (int t = 1; t < m; ++t) {
         const double a = (double)(m - t) / (double)(m + 1 - t);
+        const double sig = std::sqrt(2.0 * d.lambda * a * d.tau);
         tab[2 * ((size_t)m * d.wtab + t)] = a;
-        tab[2 * ((size_t)m * d.wtab + t) + 1] = std::sqrt(2.0 * d.lambda * a * d.tau);
+        tab[2 * ((size_t)m * d.wtab + t) + 1] = sig;
+        tab[2 * (ww + (size_t)m * d.wtab + t)] = sig / (m - t);
+        tab[2 * (ww + (size_t)m * d.wtab + t) + 1] = (double)(m - t);
       }
+    }
     cudaMemcpyAsync(h->d_dpool + d.tab_off, tab.data(), sizeof(double) * tab.size(),
                     cudaMemcpyHostToDevice, h->stream);
   }

@@ -355,6 +355,7 @@ struct CV {
   int *next;
   unsigned *xq;       // fixed-point mirror [j*ldn + n]
   const double2 *tab; // (alpha, sigma)[m*wtab + t]
+  const double2 *tabw; // (w, k)[m*wtab + t] of the closed form (bridge_w)
   unsigned long long *hist;
   double *eser;
   // the chain's cell lists while a phase maintains them (moves mark, queries
@@ -664,6 +665,20 @@ __device__ __forceinline__ double2 bridge_coef(const CV &c, int m, int t) {
   if (m < c.d->wtab) return c.tab[m * c.d->wtab + t];
   const double a = (double)(m - t) / (double)(m + 1 - t);
   return make_double2(a, sqrt(2.0 * c.d->lambda * a * c.d->tau));
+}
+
+// the sweeps' closed form of the same bridge.  With q_t = p_t - e and
+// a_t = (m-t)/(m+1-t), q_t = a_t q_(t-1) + sigma_t z_t becomes
+// u_t = u_(t-1) + w_t z_t for u_t = q_t / (m-t), so
+//   p_t = e + (m-t) (q_0/m + sum_(s<=t) w_s z_s),   w_t = sigma_t / (m-t):
+// a prefix sum in place of the recursion (two FP64 operations a coordinate
+// per bead, or a plain scan across lanes).  bridge_w(c, m, t) = (w_t, m-t)
+// for t >= 1 and (1/m, m) for t = 0; tabulated per chain for m < wtab
+__device__ __forceinline__ double2 bridge_w(const CV &c, int m, int t) {
+  if (m < c.d->wtab) return c.tabw[m * c.d->wtab + t];
+  if (t == 0) return make_double2(1.0 / m, (double)m);
+  const double a = (double)(m - t) / (double)(m + 1 - t);
+  return make_double2(sqrt(2.0 * c.d->lambda * a * c.d->tau) / (m - t), (double)(m - t));
 }
 
 // minimum-image difference a - b: the same magnitude as dist1 (|a-b| when it
@@ -1223,22 +1238,23 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
   double px = sx, py = sy;
   bx[0] = sx;
   by[0] = sy;
-  // sweeps run the recursion relative to the end bead, p - e = a (p' - e) +
-  // z sigma, one FP64 operation fewer per coordinate than the reference's
-  // a p' + (1 - a) e + z sigma, which attempts keep
-  double rx = sx - ex, ry = sy - ey;
+  // sweeps take the bridge's closed form (bridge_w); attempts keep the
+  // reference's recursion a p' + (1 - a) e + z sigma and its bits
+  const double inv_m = D::kSweep ? bridge_w(c, m, 0).x : 0.0;
+  double ux = (sx - ex) * inv_m, uy = (sy - ey) * inv_m;
   for (int t = 1; t < m; ++t) {
-    const double2 ab = bridge_coef(c, m, t);
     double z[2];
     dr.bead_normals(t - 1, dim, z);
     if (D::kSweep) {
-      rx = fma(ab.x, rx, z[0] * ab.y);
-      bx[t] = rx + ex;
+      const double2 wk = bridge_w(c, m, t);
+      ux = fma(z[0], wk.x, ux);
+      bx[t] = fma(wk.y, ux, ex);
       if (dim > 1) {
-        ry = fma(ab.x, ry, z[1] * ab.y);
-        by[t] = ry + ey;
+        uy = fma(z[1], wk.x, uy);
+        by[t] = fma(wk.y, uy, ey);
       }
     } else {
+      const double2 ab = bridge_coef(c, m, t);
       px = ab.x * px + (1.0 - ab.x) * ex + z[0] * ab.y;
       bx[t] = px;
       if (dim > 1) {

@@ -641,39 +641,35 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     dr.consumed(2 * (m - 1) * dim);
     G::sync();
     if (FAST) {
-      // sweeps: each bridge coordinate p_t = a_t p_(t-1) + b_t, b_t = (1 -
-      // a_t) e + z_t sigma_t, as a prefix scan of affine maps over 32-lane
-      // chunks of t (five steps of three FP64 operations a chunk instead of
-      // one dependent step per bead on four lanes); sequence q = b dim + k
-      // (bridge b, coordinate k) goes to warp q mod nwarps, with the same
-      // arithmetic in every launch shape
+      // sweeps: each bridge coordinate in the closed form (bridge_w),
+      // p_t = e + (m-t) u_t with u_t = (s - e)/m + sum_(s<=t) w_s z_s, the
+      // sum a prefix scan over 32-lane chunks of t (five FP64 additions a
+      // chunk); sequence q = b dim + k (bridge b, coordinate k) goes to warp
+      // q mod nwarps, with the same arithmetic in every launch shape
+      const double inv_m = bridge_w(c, m, 0).x;
       for (int q = warp; q < 2 * dim; q += nwarps) {
         const int b = q / dim, k = q % dim;
         const double s0 = b == 0 ? (k == 0 ? s1x : s1y) : (k == 0 ? s2x : s2y);
         const double e = b == 0 ? (k == 0 ? f1x : f1y) : (k == 0 ? f2x : f2y);
         double *dst = b == 0 ? (k == 0 ? S.r1x : S.r1y) : (k == 0 ? S.r2x : S.r2y);
-        double carry = s0;
+        double carry = (s0 - e) * inv_m;
         for (int c0 = 1; c0 < m; c0 += 32) {
           const int t = c0 + lane;
           const bool act = t < m;
-          double Ac = 1.0, Bc = 0.0;
+          double v = 0.0, kt = 0.0;
           if (act) {
-            const double2 ab = bridge_coef(c, m, t);
-            Ac = ab.x;
-            Bc = fma(1.0 - ab.x, e, S.z[2 * (b * (m - 1) + t - 1) + k] * ab.y);
+            const double2 wk = bridge_w(c, m, t);
+            v = S.z[2 * (b * (m - 1) + t - 1) + k] * wk.x;
+            kt = wk.y;
           }
 #pragma unroll
           for (int off = 1; off < 32; off <<= 1) {
-            const double Ap = __shfl_up_sync(0xffffffffu, Ac, off);
-            const double Bp = __shfl_up_sync(0xffffffffu, Bc, off);
-            if (lane >= off) {
-              Bc = fma(Ac, Bp, Bc);
-              Ac *= Ap;
-            }
+            const double vp = __shfl_up_sync(0xffffffffu, v, off);
+            if (lane >= off) v += vp;
           }
-          const double pv = fma(Ac, carry, Bc);
-          if (act) dst[t] = pv;
-          carry = __shfl_sync(0xffffffffu, pv, 31);
+          const double u = carry + v;
+          if (act) dst[t] = fma(kt, u, e);
+          carry = __shfl_sync(0xffffffffu, u, 31);
         }
       }
     } else if (lead && lane < 2 * dim) {

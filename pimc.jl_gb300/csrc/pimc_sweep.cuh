@@ -27,6 +27,7 @@ __device__ __forceinline__ CV make_cv(const ChainDesc *d, double *dpool, int *ip
   c.xq = (unsigned *)(dpool + d->xq_off);
   c.next = ipool + d->next_off;
   c.tab = (const double2 *)(dpool + d->tab_off);
+  c.tabw = c.tab + (size_t)d->wtab * d->wtab;
   c.hist = (d->dens_off >= 0 && upool) ? upool + d->dens_off : nullptr;
   c.eser = d->eser_off >= 0 ? dpool + d->eser_off : nullptr;
   c.cl = nullptr;
