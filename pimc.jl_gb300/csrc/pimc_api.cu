@@ -199,6 +199,8 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
     d.q_lim_lo = rq > e ? (unsigned)std::floor((rq - e) * (rq - e)) : 0u;
     d.q_lim_hi = (unsigned)std::min(std::ceil((rq + e) * (rq + e)), (double)d.q_lim_rc);
     d.hb_unit = (float)((double)d.q_unit2 / (4.0 * d.tau * d.lambda));
+    d.q_Lf = (float)p.L;
+    d.q_scalef = (float)d.q_scale;
   }
   d.hard_a = p.hardcore_a;
   d.ctr = p.retry_cap > 0 ? p.retry_cap : 10000;

@@ -241,8 +241,15 @@ struct InjDraws {
 // the minimum-image separation in mirror units, so a neighbour prefilter is
 // integer arithmetic on one word per bead (half the bytes of an FP32 copy).
 // ---------------------------------------------------------------------------
+// formed in FP32: the roundings of x, L, the sum, q_scale and the product
+// move the value by at most 2^-24 (4 L s + 2 L s + 2^16) = 2^-6 units (L s =
+// 2^15), so a word lies within 0.516 units of the exact position instead of
+// 0.5.  Two such words and a shifted centre differ from the exact
+// separation by at most 1.55 units per axis, 2.2 in distance, inside the
+// prefilter bounds' 4 units and the estimates' kQErr = 3.  The FP64 pipe
+// does one conversion instead of an addition, a product and a conversion
 __device__ __forceinline__ unsigned qcoord(const ChainDesc &d, double x) {
-  return (unsigned)__double2ll_rn((x + d.L) * d.q_scale) & 0xffffu;
+  return (unsigned)__float2int_rn(((float)x + d.q_Lf) * d.q_scalef) & 0xffffu;
 }
 __device__ __forceinline__ unsigned qpos(const ChainDesc &d, double x, double y) {
   return qcoord(d, x) | (d.dim > 1 ? qcoord(d, y) << 16 : 0u);

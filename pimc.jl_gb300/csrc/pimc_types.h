@@ -58,6 +58,8 @@ struct ChainDesc {
   // the sweeps' FP32 heat-bath exponent scale per window length m:
   // hb_unit / m = (squared mirror unit) / (4 lambda m tau)
   float hb_unit;
+  // L and q_scale rounded to FP32 (the mirror words are formed in FP32)
+  float q_Lf, q_scalef;
   long long x_off;      // doubles: x[j][n][d] (slice-major) at dpool + x_off
   long long V_off;      // doubles: V[j][n]
   long long xq_off;     // doubles: 16-bit fixed-point mirror [j][n] (x | y << 16, u32)
