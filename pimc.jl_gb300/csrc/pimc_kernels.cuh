@@ -1319,9 +1319,30 @@ __device__ void measure_group(const CV &c, double *red, double *out, bool densit
       if (cell_query(c.cl, c.cl && c.cl->usable(j), j, f.c, f.c, lane,
                      [&](int b, bool v, unsigned) { push(b, v && b > i && f.pass(row[b])); }))
         continue;
-      for (int b0 = i + 1; b0 < N; b0 += 32) {
-        const int b = b0 + lane;
-        push(b, b < N && f.pass(row[b]));
+      // two blocks of 32 partners at a time: both rows' words are loaded
+      // before either is tested, and the queue takes both blocks with one
+      // warp synchronisation (at most 31 + 64 = 95 < PQ_CAP entries before
+      // it drains below 32 again)
+      for (int b0 = i + 1; b0 < N; b0 += 64) {
+        const int ba = b0 + lane, bb = ba + 32;
+        const unsigned wa = ba < N ? row[ba] : 0u, wb = bb < N ? row[bb] : 0u;
+        const bool pa = ba < N && f.pass(wa), pb = bb < N && f.pass(wb);
+        const unsigned ma = __ballot_sync(0xffffffffu, pa), mb = __ballot_sync(0xffffffffu, pb);
+        const unsigned long long tag = (unsigned)kk;
+        if (pa) {
+          const int k = qn + __popc(ma & lt);
+          if (check_ok(k < PQ_CAP, DERR_QUEUE, d)) q[k] = ((unsigned long long)(unsigned)ba << 32) | tag;
+        }
+        if (pb) {
+          const int k = qn + __popc(ma) + __popc(mb & lt);
+          if (check_ok(k < PQ_CAP, DERR_QUEUE, d)) q[k] = ((unsigned long long)(unsigned)bb << 32) | tag;
+        }
+        qn += __popc(ma) + __popc(mb);
+#if PIMC_CHECK
+        if (qn > PQ_CAP) qn = PQ_CAP;
+#endif
+        __syncwarp();
+        while (qn >= 32) flush();
       }
     }
     while (qn > 0) flush();
