@@ -1427,9 +1427,28 @@ int pimc_state_size(void *handle, size_t *bytes);
 // and keep the fastest.  Smaller staging budgets trade shared-memory residency
 // of small chains for more resident CTAs per SM; warp mode trades threads per
 // chain for chains in flight.
+static int tune_impl(Handle *h, int sweeps_per_trial, pimc_launch *chosen);
+
+// The trials run with measurements off: a trial of a sweep or two that
+// happened to hold a measurement sweep (several times a plain sweep's cost
+// with the pair energy) would lose whatever shape it timed.  The chains' move
+// mixes are restored afterwards, as their states are.
 int pimc_batch_tune(void *handle, int sweeps_per_trial, pimc_launch *chosen) {
   Handle *h = H(handle);
   if (!h || sweeps_per_trial < 1) return fail(PIMC_EARG, "bad argument");
+  const std::vector<MixDev> saved = h->mix;
+  for (MixDev &m : h->mix) m.measure_every = 0;
+  CK(cudaMemcpyAsync(h->d_mix, h->mix.data(), sizeof(MixDev) * h->nchains, cudaMemcpyHostToDevice,
+                     h->stream));
+  const int rc = tune_impl(h, sweeps_per_trial, chosen);
+  h->mix = saved;
+  CK(cudaMemcpyAsync(h->d_mix, h->mix.data(), sizeof(MixDev) * h->nchains, cudaMemcpyHostToDevice,
+                     h->stream));
+  const int rs = sync_check(h);
+  return rc ? rc : rs;
+}
+
+static int tune_impl(Handle *h, int sweeps_per_trial, pimc_launch *chosen) {
   // trials advance the chains; the snapshot puts them back afterwards
   size_t nb = 0;
   int rc = pimc_state_size(h, &nb);

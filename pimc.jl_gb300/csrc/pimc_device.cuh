@@ -1278,7 +1278,8 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
     bx[t] = teleport_s<D::kSweep>(bx[t], L, inv2L);
     if (dim > 1) by[t] = teleport_s<D::kSweep>(by[t], L, inv2L);
     const double vb = vext(d, bx[t], by[t]);
-    if (t > 0) vp[t - 1] = mhtau * (vprev + vb);
+    // sweeps keep the links' sums and scale once (the write-back scales each)
+    if (t > 0) vp[t - 1] = D::kSweep ? vprev + vb : mhtau * (vprev + vb);
     vprev = vb;
   }
   for (int t = 0; t < m; ++t) {
@@ -1286,6 +1287,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
     wi += c.Vl(a < M ? n : nx, a < M ? a : a - M);
   }
   for (int t = 0; t < m; ++t) wu += vp[t];
+  if (D::kSweep) wu *= mhtau;
   if (prop)
     for (int t = 0; t <= m; ++t) {
       prop[t * dim] = bx[t];
@@ -1297,7 +1299,7 @@ __device__ int window_thread(const CV &c, int n, int j0, int m, D &dr, bool rewr
       const int a = j0 + t;
       const int o = a < M ? n : nx, j = a < M ? a : a - M;
       if (t > 0 || rewrite_start) c.set_pos(o, j, bx[t], by[t]);
-      c.Vl(o, j) = vp[t];
+      c.Vl(o, j) = D::kSweep ? mhtau * vp[t] : vp[t];
     }
   }
   return acc ? 1 : 0;

@@ -980,9 +980,12 @@ __device__ int com_thread(const CV &c, int n, double step, D &dr) {
       vj = vext(d, qx, qy);
     }
     wi += c.Vl(n, j - 1);
-    wu += mhtau * (vprev + vj);
+    // sweeps sum the links and scale once
+    if (D::kSweep) wu += vprev + vj;
+    else wu += mhtau * (vprev + vj);
     vprev = vj;
   }
+  if (D::kSweep) wu *= mhtau;
   const bool acc = metropolis(d, wu - wi, dr);
   if (acc) {
     vprev = v0;
