@@ -642,10 +642,11 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
     G::sync();
     if (FAST) {
       // sweeps: each bridge coordinate in the closed form (bridge_w),
-      // p_t = e + (m-t) u_t with u_t = (s - e)/m + sum_(s<=t) w_s z_s, the
-      // sum a prefix scan over 32-lane chunks of t (five FP64 additions a
-      // chunk); sequence q = b dim + k (bridge b, coordinate k) goes to warp
-      // q mod nwarps, with the same arithmetic in every launch shape
+      // p_t = e + (m-t) u_t with u_t = (p_0 - e)/m + the sum of w_r z_r over
+      // r <= t, that sum a prefix scan over 32-lane chunks of t (five FP64
+      // additions a chunk); sequence q = b dim + k (bridge b, coordinate k)
+      // goes to warp q mod nwarps, with the same arithmetic in every launch
+      // shape
       const double inv_m = bridge_w(c, m, 0).x;
       for (int q = warp; q < 2 * dim; q += nwarps) {
         const int b = q / dim, k = q % dim;
