@@ -1,4 +1,4 @@
-"""The adjoint at the configuration the benchmark spec names (C5) and batched.
+"""The adjoint at the differentiated configuration (C5) and batched.
 
 C5: 2D square optical lattice V0 (sin^2(pi x / a) + sin^2(pi y / a)), a = 1,
 V0 = 4, plus the trap omega = 0.1 and the Gaussian pair g = 1, sigma = 0.3;

@@ -6,7 +6,7 @@ Every case runs independent chains of the configuration on the device and
 compares each estimator, the mean over chains of each chain's mean, with the
 oracle's statistics committed in tests/golden/sweep_stats.json (made by
 tests/golden/make_sweep_stats.py).  Bar: energies within 2 sigma of the
-combined standard error (2 sigma is the north-star's tolerance; the seeds are
+combined standard error (2 sigma is the parity bar for energies; the seeds are
 fixed, so every outcome is reproducible); densities bin by bin.
 
 Physical rules: the oracle runs the reference's run! schedule and the physical
