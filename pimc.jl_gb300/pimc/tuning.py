@@ -17,7 +17,7 @@ import os
 from collections import Counter
 
 LAUNCH_KEYS = ("warp_per_chain", "block", "sweeps_per_launch", "state_smem_bytes",
-               "split_phases", "phase_block", "phase_warp", "phase_regs")
+               "split_phases", "phase_block", "phase_warp", "phase_regs", "cell_lists")
 
 
 def n_bucket(N: int) -> int:

@@ -241,7 +241,7 @@ def test_tune_cache_round_trip(tmp_path):
     path = str(tmp_path / "tune.json")
     shape = dict(warp_per_chain=False, block=64, sweeps_per_launch=1, state_smem_bytes=0,
                  split_phases=1, phase_block=[128, 64, 128], phase_warp=[0, 1, 0],
-                 phase_regs=[0, 0, 0])
+                 phase_regs=[0, 0, 0], cell_lists=1)
     tc = TuneCache(path)
     assert tc.get(sig) is None
     tc.put(sig, shape, ms_per_sweep=35.7)
@@ -250,4 +250,7 @@ def test_tune_cache_round_trip(tmp_path):
     assert json.load(open(path))[sig]["ms_per_sweep"] == 35.7
     # an entry missing a key (an older file) is a miss, not an error
     again.data[sig].pop("phase_warp")
+    assert again.get(sig) is None
+    again.put(sig, shape)
+    again.data[sig].pop("cell_lists")
     assert again.get(sig) is None
