@@ -564,19 +564,6 @@ __device__ int swap_group(const CV &c, int j0, int m, int n1, double u_pick, D &
   auto own1 = [&](int t) { return (j0 + t < M) ? n1 : nx1; };
   auto own2 = [&](int t) { return (j0 + t < M) ? n2 : nx2; };
   auto slc = [&](int t) { return (j0 + t < M) ? j0 + t : j0 + t - M; };
-  if (FAST && j0 + m < M - 1) {
-    // an accepted swap exchanges the tails past slice se (most decided
-    // swaps under the reference's rules accept): bring those rows into L1
-    // while the bridges are built
-    for (int j = se + 1 + tid; j < M; j += nt) {
-      prefetch_l1(&c.X(0, n1, j));
-      prefetch_l1(&c.X(0, n2, j));
-      prefetch_l1(&c.V[(size_t)j * c.ldn + n1]);
-      prefetch_l1(&c.V[(size_t)j * c.ldn + n2]);
-      prefetch_l1(&c.xq[(size_t)j * c.ldn + n1]);
-      prefetch_l1(&c.xq[(size_t)j * c.ldn + n2]);
-    }
-  }
   // the old paths' cached links (w_initial below), read now
   double vold = 0.0;
   for (int k = tid; k < 2 * m; k += nt) {
