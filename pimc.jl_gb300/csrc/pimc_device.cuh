@@ -1190,14 +1190,6 @@ __device__ __forceinline__ bool hard_hit_lanes(const CV &c, double x, double y, 
 }
 
 // ---------------------------------------------------------------------------
-// an L1 prefetch of a chain word in global memory (a no-op for chains staged
-// in shared memory)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void prefetch_l1(const void *p) {
-  if (__isGlobal(p)) asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
-// ---------------------------------------------------------------------------
 // warp helpers
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double warp_sum(double v) {
