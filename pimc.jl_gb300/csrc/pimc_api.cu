@@ -193,7 +193,8 @@ ChainDesc make_desc(const pimc_params &p, int chain) {
     d.q_lim_rc = lim(d.rc);
     d.q_lim_hard = lim(p.hardcore_a);
     // a mirror distance differs from the exact one by at most 3 units: two
-    // roundings per axis, plus one more for a shifted centre (cycle moves)
+    // roundings per axis (each within 0.516 units, the words being formed in
+    // FP32), plus one more for a shifted centre (cycle moves)
     const double rq = d.rc / u, e = 3.0;
     d.q_u2i = (float)(u * u * d.inv2s2);
     d.q_lim_lo = rq > e ? (unsigned)std::floor((rq - e) * (rq - e)) : 0u;
