@@ -57,7 +57,7 @@ PER_BEAD = {
     # the swap launch of the split sweep, the kernel compiled for the
     # reference's rules alone, row scans (its bead updates are the swaps'
     # 2(m-1) per attempt; every attempt also reads the N heat-bath candidates)
-    ("c4", "reference", "k_sweep_swap_ref"): {"dram_bytes": 1067.0, "fp64_flops": 332.0},  # 3.24 GB, 1.01 G / 3.037 M
+    ("c4", "reference", "k_sweep_swap_ref"): {"dram_bytes": 1036.0, "fp64_flops": 330.0},  # 3.15 GB, 1.00 G / 3.037 M
 }
 ROOF_SWEEPS = 2  # sweeps of the per-phase timing pass
 
